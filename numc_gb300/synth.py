@@ -1,0 +1,111 @@
+"""Seeded synthetic matmul inputs (splitmix64 streams).
+
+Every operand is drawn from its own splitmix64 stream, selected by
+``(seed, stream)``, so any array can be regenerated bit-for-bit on any host
+from two integers.  splitmix64 is Steele, Lea and Flood's generator
+("Fast splittable pseudorandom number generators", OOPSLA 2014), the same
+generator numc uses to seed its xoshiro256** state (src/random/kernel.h:46-51).
+
+Value maps (x is a 64-bit draw):
+  float32 uniform [lo, hi):  u = (x >> 40) * 2^-24
+  float64 uniform [lo, hi):  u = (x >> 11) * 2^-53
+  integers uniform [lo, hi]: lo + ((x >> 32) * (hi - lo + 1)) >> 32
+  normal:                    Box-Muller on two float64 uniforms
+"""
+import numpy as np
+
+GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+_STREAM = np.uint64(0xD1B54A32D192ED03)
+
+
+def _mix(z):
+    with np.errstate(over="ignore"):
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+    return z ^ (z >> np.uint64(31))
+
+
+def draws(seed, stream, n):
+    """n consecutive splitmix64 outputs of stream `stream` under `seed`."""
+    with np.errstate(over="ignore"):
+        base = _mix(np.uint64(seed) ^ (np.uint64(stream) * _STREAM))
+        idx = np.arange(1, n + 1, dtype=np.uint64)
+        return _mix(base + idx * GOLDEN)
+
+
+def uniform(seed, stream, shape, lo=-1.0, hi=1.0, dtype=np.float32):
+    n = int(np.prod(shape))
+    x = draws(seed, stream, n)
+    if np.dtype(dtype) == np.float32:
+        u = (x >> np.uint64(40)).astype(np.float64) * 2.0 ** -24
+    else:
+        u = (x >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+    return (lo + (hi - lo) * u).astype(dtype).reshape(shape)
+
+
+def integers(seed, stream, shape, lo, hi, dtype):
+    n = int(np.prod(shape))
+    x = draws(seed, stream, n)
+    span = np.uint64(hi - lo + 1)
+    with np.errstate(over="ignore"):
+        v = ((x >> np.uint64(32)) * span) >> np.uint64(32)
+    return (v.astype(np.int64) + lo).astype(dtype).reshape(shape)
+
+
+def normal(seed, stream, shape, dtype=np.float32):
+    n = int(np.prod(shape))
+    x = draws(seed, stream, 2 * n)
+    u1 = ((x[0::2] >> np.uint64(11)).astype(np.float64) + 1.0) * 2.0 ** -53
+    u2 = (x[1::2] >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+    z = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+    return z.astype(dtype).reshape(shape)
+
+
+# Value ranges of the integer-exactness workload (1024^3).
+INT_RANGES = {
+    "int8": (-128, 127), "uint8": (0, 255), "int16": (-32768, 32767),
+    "uint16": (0, 65535), "int32": (-1000, 1000), "uint32": (0, 2000),
+    "int64": (-(1 << 20), 1 << 20), "uint64": (0, 1 << 21),
+}
+
+
+def operands(kind, M, K, N, seed=42, dtype="float32"):
+    """(A, B) for one workload kind:
+
+    uniform     entries uniform in [-1, 1) (float) or INT_RANGES (integers)
+    normal      entries N(0, 1)
+    illscaled   N(0, 1) with row i of A times 10^u_i and column j of B times
+                10^v_j, u, v ~ U(-4, 4)
+    expspread   float64 uniform [-1, 1) times 2^e, e integer U(-20, 20)
+                per element
+    smallint    numc's own test fill: A[i] = (i % 7) + 1, B[i] = (i % 5) + 1
+    """
+    dt = np.dtype(dtype)
+    if kind == "smallint":
+        a = ((np.arange(M * K) % 7) + 1).astype(dt).reshape(M, K)
+        b = ((np.arange(K * N) % 5) + 1).astype(dt).reshape(K, N)
+        return a, b
+    if kind == "uniform":
+        if dt.kind == "f":
+            return (uniform(seed, 1, (M, K), dtype=dt),
+                    uniform(seed, 2, (K, N), dtype=dt))
+        lo, hi = INT_RANGES[dt.name]
+        return (integers(seed, 1, (M, K), lo, hi, dt),
+                integers(seed, 2, (K, N), lo, hi, dt))
+    if kind == "normal":
+        return normal(seed, 3, (M, K), dt), normal(seed, 4, (K, N), dt)
+    if kind == "illscaled":
+        a = normal(seed, 5, (M, K), np.float64)
+        b = normal(seed, 6, (K, N), np.float64)
+        u = uniform(seed, 7, (M, 1), -4.0, 4.0, np.float64)
+        v = uniform(seed, 8, (1, N), -4.0, 4.0, np.float64)
+        return ((a * 10.0 ** u).astype(dt), (b * 10.0 ** v).astype(dt))
+    if kind == "expspread":
+        a = uniform(seed, 9, (M, K), dtype=np.float64)
+        b = uniform(seed, 10, (K, N), dtype=np.float64)
+        ea = integers(seed, 11, (M, K), -20, 20, np.int64)
+        eb = integers(seed, 12, (K, N), -20, 20, np.int64)
+        return ((np.ldexp(a, ea)).astype(dt), (np.ldexp(b, eb)).astype(dt))
+    raise ValueError(f"unknown workload kind {kind!r}")

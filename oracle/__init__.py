@@ -1,0 +1,162 @@
+"""Oracle for numc's matmul (TEST INFRASTRUCTURE ONLY).
+
+Two checkers live here, both CPU-only:
+
+* ``matmul(a, b, profile)`` — the C restatement in ``numc_oracle.c``
+  (builds on any host; it is what GPU parity tests compare against).
+* ``ref_matmul(a, b)`` — the unmodified numc library compiled from the
+  reference sources (x86-64 hosts with the reference checkout only); used to
+  pin the restatement and to generate the golden fixtures in tests/golden/.
+
+The product library never imports this package.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+# numc's NumcDType numbering (include/numc/dtype.h:21-32)
+DTYPES = ["int8", "int16", "int32", "int64", "uint8", "uint16", "uint32",
+          "uint64", "float32", "float64"]
+DTYPE_CODE = {name: i for i, name in enumerate(DTYPES)}
+
+PROFILE_X86_AVX2 = 0
+PROFILE_ARM_NEON = 1
+PROFILE_WRAP = 2
+
+_lib = None
+_ref = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        lib = ctypes.CDLL(path)
+        i64 = ctypes.c_int64
+        vp = ctypes.c_void_p
+        lib.oracle_matmul.argtypes = [ctypes.c_int, vp, vp, vp, i64, i64, i64,
+                                      i64, i64, i64, i64, i64, i64,
+                                      ctypes.c_int, ctypes.c_int]
+        lib.oracle_matmul.restype = ctypes.c_int
+        lib.oracle_dot2_f64.argtypes = [vp, vp, i64, i64, vp, vp, i64, vp, vp]
+        lib.oracle_dot_f32_ref.argtypes = [vp, vp, i64, i64, vp, vp, i64, vp]
+        lib.oracle_num_threads.restype = ctypes.c_int
+        _lib = lib
+    return _lib
+
+
+def num_threads():
+    return _load().oracle_num_threads()
+
+
+def matmul(a, b, profile=PROFILE_X86_AVX2, nthreads=0):
+    """numc's result of a @ b for 2-D numpy arrays of one numc dtype."""
+    lib = _load()
+    assert a.dtype == b.dtype and a.ndim == 2 and b.ndim == 2
+    assert a.shape[1] == b.shape[0]
+    M, K = a.shape
+    N = b.shape[1]
+    es = a.dtype.itemsize
+    out = np.empty((M, N), dtype=a.dtype)
+    rc = lib.oracle_matmul(
+        DTYPE_CODE[a.dtype.name], a.ctypes.data, b.ctypes.data, out.ctypes.data,
+        M, K, N, a.strides[0] // es, a.strides[1] // es, b.strides[0] // es,
+        b.strides[1] // es, out.strides[0] // es, out.strides[1] // es,
+        profile, nthreads)
+    if rc != 0:
+        raise RuntimeError("oracle_matmul failed")
+    return out
+
+
+def dot2_f64(a, b, rows, cols):
+    """Double-double (Dot2) values of (a @ b)[rows, cols] for float64 a, b."""
+    lib = _load()
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    cols = np.ascontiguousarray(cols, dtype=np.int64)
+    hi = np.empty(len(rows)); lo = np.empty(len(rows))
+    lib.oracle_dot2_f64(a.ctypes.data, b.ctypes.data, a.shape[1], b.shape[1],
+                        rows.ctypes.data, cols.ctypes.data, len(rows),
+                        hi.ctypes.data, lo.ctypes.data)
+    return hi, lo
+
+
+def dot_f32_ref(a, b, rows, cols):
+    """float64-accurate values of (a @ b)[rows, cols] for float32 a, b."""
+    lib = _load()
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = np.ascontiguousarray(b, dtype=np.float32)
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    cols = np.ascontiguousarray(cols, dtype=np.int64)
+    out = np.empty(len(rows))
+    lib.oracle_dot_f32_ref(a.ctypes.data, b.ctypes.data, a.shape[1],
+                           b.shape[1], rows.ctypes.data, cols.ctypes.data,
+                           len(rows), out.ctypes.data)
+    return out
+
+
+# -- the compiled reference ------------------------------------------------
+
+def reference_available():
+    return os.path.exists(_build.REF_SO) or _build.reference_buildable()
+
+
+def _load_ref():
+    global _ref
+    if _ref is None:
+        path = _build.build_reference()
+        if path is None:
+            raise RuntimeError("numc reference library not buildable here")
+        lib = ctypes.CDLL(path)
+        vp = ctypes.c_void_p
+        lib.numc_ctx_create.restype = vp
+        lib.numc_ctx_free.argtypes = [vp]
+        lib.numc_array_create.restype = vp
+        lib.numc_array_create.argtypes = [vp, vp, ctypes.c_size_t, ctypes.c_int]
+        lib.numc_array_write.argtypes = [vp, vp]
+        lib.numc_array_data.restype = vp
+        lib.numc_array_data.argtypes = [vp]
+        lib.numc_array_transpose.argtypes = [vp, vp]
+        lib.numc_matmul.argtypes = [vp, vp, vp]
+        lib.numc_matmul.restype = ctypes.c_int
+        lib.numc_matmul_naive.argtypes = [vp, vp, vp]
+        lib.numc_matmul_naive.restype = ctypes.c_int
+        _ref = lib
+    return _ref
+
+
+def ref_matmul(a, b, naive=False):
+    """Run numc's own numc_matmul (or numc_matmul_naive) on contiguous a, b."""
+    lib = _load_ref()
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    M, K = a.shape
+    N = b.shape[1]
+    code = DTYPE_CODE[a.dtype.name]
+    ctx = lib.numc_ctx_create()
+    try:
+        def make(shape, src=None):
+            sh = (ctypes.c_size_t * 2)(*shape)
+            arr = lib.numc_array_create(ctx, sh, 2, code)
+            if not arr:
+                raise MemoryError("numc_array_create failed")
+            if src is not None:
+                lib.numc_array_write(arr, src.ctypes.data)
+            return arr
+        pa, pb, pc = make((M, K), a), make((K, N), b), make((M, N))
+        fn = lib.numc_matmul_naive if naive else lib.numc_matmul
+        if naive:  # the naive kernel accumulates into out: start from zero
+            z = np.zeros((M, N), dtype=a.dtype)
+            lib.numc_array_write(pc, z.ctypes.data)
+        rc = fn(pa, pb, pc)
+        if rc != 0:
+            raise RuntimeError(f"numc_matmul returned {rc}")
+        out = np.empty((M, N), dtype=a.dtype)
+        ctypes.memmove(out.ctypes.data, lib.numc_array_data(pc), out.nbytes)
+        return out
+    finally:
+        lib.numc_ctx_free(ctx)

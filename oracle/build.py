@@ -1,0 +1,59 @@
+"""Build recipe for the oracle (test infrastructure only).
+
+``build_oracle()`` compiles ``oracle/numc_oracle.c`` (the CPU restatement of
+numc's matmul arithmetic) into ``oracle/_build/liboracle.so``.
+``build_reference()`` compiles the unmodified numc sources from a local
+reference checkout into ``oracle/_ref/libnumc_ref.so`` through
+``oracle/Makefile.ref``; it only runs where that checkout exists and the host
+is x86-64 (the recipe pins AVX2).
+"""
+import os
+import platform
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libnumc_ref.so")
+REF_SRC = "/root/reference"
+
+
+def build_oracle(force=False):
+    src = os.path.join(HERE, "numc_oracle.c")
+    if (not force and os.path.exists(ORACLE_SO)
+            and os.path.getmtime(ORACLE_SO) >= os.path.getmtime(src)):
+        return ORACLE_SO
+    os.makedirs(os.path.dirname(ORACLE_SO), exist_ok=True)
+    flags = ["-O3", "-std=c11", "-fopenmp", "-fPIC", "-shared",
+             "-ffp-contract=off"]
+    if platform.machine() in ("x86_64", "AMD64"):
+        flags.append("-mfma")  # vector FMA for fmaf(); aarch64 has it natively
+    tmp = ORACLE_SO + ".tmp"
+    subprocess.check_call(["gcc", *flags, src, "-o", tmp, "-lm"])
+    os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+def reference_buildable():
+    return (os.path.isdir(os.path.join(REF_SRC, "src"))
+            and platform.machine() in ("x86_64", "AMD64")
+            and shutil.which("make") is not None)
+
+
+def build_reference():
+    """Returns the path of the compiled reference, or None if not buildable."""
+    if os.path.exists(REF_SO):
+        return REF_SO
+    if not reference_buildable():
+        return None
+    subprocess.check_call(
+        ["make", "-f", os.path.join("oracle", "Makefile.ref"),
+         f"-j{os.cpu_count() or 4}", f"REF={REF_SRC}"],
+        cwd=ROOT, stdout=subprocess.DEVNULL)
+    return REF_SO if os.path.exists(REF_SO) else None
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    print(build_reference())
