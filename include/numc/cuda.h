@@ -1,0 +1,110 @@
+/* CUDA backend extensions (GB300, sm_103a).  numc itself has no GPU API;
+ * these entry points are additions.  They keep numc's conventions: return 0
+ * or a negative NumcErrorCode, message via numc_get_error().
+ *
+ * Two layers:
+ *   1. Device residency for NumcArray, so chains of numc_matmul calls keep
+ *      their operands in HBM.
+ *   2. The C-ABI GEMM below numc_matmul: plain device pointers, sizes and
+ *      element strides.  It mirrors numc's per-dtype kernel table entry
+ *        void (*GemmSimdKernel)(const void *a, const void *b, void *out,
+ *                               size_t M, size_t K, size_t N, intptr_t rsa,
+ *                               intptr_t csa, intptr_t rsb, intptr_t rso)
+ *      (src/matmul/matmul.c:84-86), adding the column strides numc assumes
+ *      to be 1, an algorithm choice, scratch memory and a CUDA stream.
+ */
+#ifndef NUMC_CUDA_H
+#define NUMC_CUDA_H
+
+#include "numc/array.h"
+#include "numc/export.h"
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  NUMC_CUDA_ALGO_DEFAULT = 0,    /* process-wide choice for the dtype */
+  NUMC_CUDA_ALGO_SIMT = 1,       /* CUDA cores; every dtype.  float32/64 are
+                                    per-output FMA chains in k order */
+  NUMC_CUDA_ALGO_SPLIT_BF16 = 2, /* float32: a = hi + lo in bfloat16,
+                                    hi*hi + hi*lo + lo*hi on tcgen05 with
+                                    float32 accumulation in TMEM */
+  NUMC_CUDA_ALGO_DMMA = 3,       /* float64: mma.sync f64 tensor path */
+  NUMC_CUDA_ALGO_OZAKI = 4,      /* float64: Ozaki slicing, exact integer
+                                    slice products on tcgen05, `param` =
+                                    slice count 3..8 */
+  NUMC_CUDA_ALGO_AUTO = 5        /* float32: split-BF16 when the problem is
+                                    large enough to pay for it, else SIMT */
+} NumcCudaAlgo;
+
+/* Which numc build's int8/uint8 results to reproduce (the store rules of
+ * numc's packed integer kernels differ by ISA). */
+typedef enum {
+  NUMC_INT8_X86_AVX2 = 0, /* numc built for x86-64 AVX2 (default) */
+  NUMC_INT8_ARM_NEON = 1, /* numc built for aarch64 NEON */
+  NUMC_INT8_WRAP = 2      /* numc_matmul_naive: truncate the sum to 8 bits */
+} NumcInt8Profile;
+
+/* Number of usable CUDA devices (0 when none). */
+NUMC_API int numc_cuda_device_count(void);
+
+/* Process-wide algorithm per dtype used by numc_matmul and by
+ * NUMC_CUDA_ALGO_DEFAULT.  For float64 OZAKI, `param` is the slice count;
+ * for int8/uint8, `param` is a NumcInt8Profile.  Environment defaults:
+ * NUMC_CUDA_F32_ALGO (simt|split|auto), NUMC_CUDA_F64_ALGO (simt|dmma|
+ * ozaki[:slices]), NUMC_CUDA_INT8_PROFILE (x86|neon|wrap). */
+NUMC_API int numc_cuda_set_algo(NumcDType dtype, int algo, int param);
+NUMC_API int numc_cuda_get_algo(NumcDType dtype, int *algo, int *param);
+
+/* --- device residency --------------------------------------------------- */
+
+/* Copy the array to HBM and make the device copy authoritative: later
+ * numc_matmul calls read/write it there without host transfers. */
+NUMC_API int numc_cuda_array_to_device(NumcArray *arr);
+/* Copy a device-resident array back into its host buffer (it stays
+ * resident; both copies are valid until the next device write). */
+NUMC_API int numc_cuda_array_to_host(NumcArray *arr);
+/* Device address of the element at index 0, or NULL if not resident. */
+NUMC_API void *numc_cuda_array_device_data(const NumcArray *arr);
+NUMC_API int numc_cuda_array_is_resident(const NumcArray *arr);
+/* The context's CUDA stream (cudaStream_t) and a wait for its work. */
+NUMC_API void *numc_cuda_ctx_stream(NumcCtx *ctx);
+NUMC_API int numc_cuda_ctx_synchronize(NumcCtx *ctx);
+
+/* --- C-ABI GEMM on device pointers -------------------------------------- */
+
+/* Scratch bytes numc_cuda_gemm needs for this problem (0 for SIMT/DMMA). */
+NUMC_API size_t numc_cuda_gemm_workspace_size(NumcDType dtype, int algo,
+                                              int param, size_t M, size_t K,
+                                              size_t N);
+
+/* out[i*rso + j*cso] = sum_k a[i*rsa + k*csa] * b[k*rsb + j*csb] with numc's
+ * arithmetic for `dtype`.  a, b, out are device pointers; strides are in
+ * elements.  `workspace` may be NULL (the library then keeps a per-device
+ * scratch buffer, grown with cudaMalloc) or caller memory of at least
+ * numc_cuda_gemm_workspace_size() bytes, aligned to 256 bytes.  `stream` is
+ * a cudaStream_t (NULL = legacy default stream).  Asynchronous: returns
+ * after enqueueing; launch errors are returned, kernel-side timeouts are
+ * reported by numc_cuda_check_status(). */
+NUMC_API int numc_cuda_gemm(NumcDType dtype, int algo, int param,
+                            const void *a, const void *b, void *out,
+                            size_t M, size_t K, size_t N, intptr_t rsa,
+                            intptr_t csa, intptr_t rsb, intptr_t csb,
+                            intptr_t rso, intptr_t cso, void *workspace,
+                            size_t workspace_bytes, void *stream);
+
+/* Waits for `stream` and reports any kernel that gave up on a bounded
+ * wait (NUMC_ERR_INTERNAL); clears the flag. */
+NUMC_API int numc_cuda_check_status(void *stream);
+
+/* Number of kernels this library has launched since load (diagnostics). */
+NUMC_API uint64_t numc_cuda_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NUMC_CUDA_H */

@@ -1,0 +1,333 @@
+"""numc_gb300 — numc's matmul hot path on GB300 (sm_103a).
+
+The product is the C-ABI shared library ``libnumc_gb300.so`` (headers in
+include/numc/).  This module is a thin ctypes binding of it with the shape of
+numc's C API, used by the tests and the benchmark: ``Ctx``/``Array`` mirror
+NumcCtx/NumcArray, ``matmul`` is numc_matmul, and ``gemm`` is the
+device-pointer entry numc_cuda_gemm for torch CUDA tensors.
+
+There is no CPU fallback: if the library is not built, importing works but
+every call raises ``NumcLibraryMissing``.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnumc_gb300.so")
+
+DTYPES = ["int8", "int16", "int32", "int64", "uint8", "uint16", "uint32",
+          "uint64", "float32", "float64"]
+CODE = {n: i for i, n in enumerate(DTYPES)}
+
+# NumcErrorCode (include/numc/error.h)
+ERR_NONE, ERR_NULL, ERR_MALLOC, ERR_SHAPE = 0, -1, -2, -3
+ERR_TYPE, ERR_BOUNDS, ERR_VALUE, ERR_INTERNAL = -4, -5, -6, -99
+
+# NumcCudaAlgo (include/numc/cuda.h)
+ALGO_DEFAULT, ALGO_SIMT, ALGO_SPLIT_BF16, ALGO_DMMA, ALGO_OZAKI, ALGO_AUTO = range(6)
+INT8_X86_AVX2, INT8_ARM_NEON, INT8_WRAP = 0, 1, 2
+
+
+class NumcLibraryMissing(RuntimeError):
+    pass
+
+
+class NumcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"numc error {code}: {msg}")
+        self.code = code
+        self.msg = msg
+
+
+class _Err(ctypes.Structure):
+    _fields_ = [("code", ctypes.c_int), ("msg", ctypes.c_char_p)]
+
+
+class _Checkpoint(ctypes.Structure):
+    _fields_ = [("_block", ctypes.c_void_p), ("_index", ctypes.c_size_t)]
+
+
+class _Slice(ctypes.Structure):
+    _fields_ = [("axis", ctypes.c_size_t), ("start", ctypes.c_size_t),
+                ("stop", ctypes.c_size_t), ("step", ctypes.c_size_t)]
+
+
+_lib = None
+
+# (name, restype, argtypes) for every exported function.
+_VP, _SZ, _I, _IP = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_ssize_t
+SIGNATURES = [
+    ("numc_ctx_create", _VP, []),
+    ("numc_ctx_free", None, [_VP]),
+    ("numc_ctx_checkpoint", _Checkpoint, [_VP]),
+    ("numc_ctx_restore", None, [_VP, _Checkpoint]),
+    ("numc_array_create", _VP, [_VP, _VP, _SZ, _I]),
+    ("numc_array_zeros", _VP, [_VP, _VP, _SZ, _I]),
+    ("numc_array_fill", _VP, [_VP, _VP, _SZ, _I, _VP]),
+    ("numc_array_copy", _VP, [_VP]),
+    ("numc_array_write", None, [_VP, _VP]),
+    ("numc_array_transpose", _I, [_VP, _VP]),
+    ("numc_array_transpose_copy", _VP, [_VP, _VP]),
+    ("numc_array_slice", _VP, [_VP, ctypes.POINTER(_Slice)]),
+    ("numc_array_is_contiguous", ctypes.c_bool, [_VP]),
+    ("numc_array_contiguous", _I, [_VP]),
+    ("numc_array_size", _SZ, [_VP]),
+    ("numc_array_capacity", _SZ, [_VP]),
+    ("numc_array_elem_size", _SZ, [_VP]),
+    ("numc_array_ndim", _SZ, [_VP]),
+    ("numc_array_shape", None, [_VP, _VP]),
+    ("numc_array_strides", None, [_VP, _VP]),
+    ("numc_array_dtype", _I, [_VP]),
+    ("numc_array_data", _VP, [_VP]),
+    ("numc_matmul", _I, [_VP, _VP, _VP]),
+    ("numc_matmul_naive", _I, [_VP, _VP, _VP]),
+    ("numc_set_error", _I, [_I, ctypes.c_char_p]),
+    ("numc_get_error", _Err, []),
+    ("numc_log_error", None, [_VP]),
+    ("numc_cuda_device_count", _I, []),
+    ("numc_cuda_set_algo", _I, [_I, _I, _I]),
+    ("numc_cuda_get_algo", _I, [_I, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    ("numc_cuda_array_to_device", _I, [_VP]),
+    ("numc_cuda_array_to_host", _I, [_VP]),
+    ("numc_cuda_array_device_data", _VP, [_VP]),
+    ("numc_cuda_array_is_resident", _I, [_VP]),
+    ("numc_cuda_ctx_stream", _VP, [_VP]),
+    ("numc_cuda_ctx_synchronize", _I, [_VP]),
+    ("numc_cuda_gemm_workspace_size", _SZ, [_I, _I, _I, _SZ, _SZ, _SZ]),
+    ("numc_cuda_gemm", _I, [_I, _I, _I, _VP, _VP, _VP, _SZ, _SZ, _SZ,
+                            _IP, _IP, _IP, _IP, _IP, _IP, _VP, _SZ, _VP]),
+    ("numc_cuda_check_status", _I, [_VP]),
+    ("numc_cuda_launch_count", ctypes.c_uint64, []),
+]
+
+
+def lib():
+    """The loaded C library; raises NumcLibraryMissing if it is not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise NumcLibraryMissing(
+                f"{LIB_PATH} is not built; run `python -m numc_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error():
+    e = lib().numc_get_error()
+    return e.code, (e.msg or b"").decode(errors="replace")
+
+
+def check(rc):
+    if rc != 0:
+        code, msg = last_error()
+        raise NumcError(rc, msg)
+    return rc
+
+
+def device_count():
+    return lib().numc_cuda_device_count()
+
+
+def set_algo(dtype, algo, param=0):
+    check(lib().numc_cuda_set_algo(CODE[np.dtype(dtype).name], algo, param))
+
+
+def get_algo(dtype):
+    a, p = ctypes.c_int(), ctypes.c_int()
+    check(lib().numc_cuda_get_algo(CODE[np.dtype(dtype).name], ctypes.byref(a), ctypes.byref(p)))
+    return a.value, p.value
+
+
+def launch_count():
+    return lib().numc_cuda_launch_count()
+
+
+class Ctx:
+    """NumcCtx: owns every Array created from it."""
+
+    def __init__(self):
+        self.ptr = lib().numc_ctx_create()
+        if not self.ptr:
+            raise NumcError(*last_error())
+
+    def free(self):
+        if self.ptr:
+            lib().numc_ctx_free(self.ptr)
+            self.ptr = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.free()
+
+    def checkpoint(self):
+        return lib().numc_ctx_checkpoint(self.ptr)
+
+    def restore(self, cp):
+        lib().numc_ctx_restore(self.ptr, cp)
+
+    def stream(self):
+        return lib().numc_cuda_ctx_stream(self.ptr)
+
+    def synchronize(self):
+        check(lib().numc_cuda_ctx_synchronize(self.ptr))
+
+    def _make(self, fn, shape, dtype, *extra):
+        shape = tuple(int(s) for s in shape)
+        sh = (ctypes.c_size_t * max(1, len(shape)))(*shape)
+        p = fn(self.ptr, sh, len(shape), CODE[np.dtype(dtype).name], *extra)
+        if not p:
+            raise NumcError(*last_error())
+        return Array(p, self)
+
+    def create(self, shape, dtype):
+        return self._make(lib().numc_array_create, shape, dtype)
+
+    def zeros(self, shape, dtype):
+        return self._make(lib().numc_array_zeros, shape, dtype)
+
+    def fill(self, shape, dtype, value):
+        v = np.array(value, dtype=dtype)
+        return self._make(lib().numc_array_fill, shape, dtype, v.ctypes.data)
+
+    def from_numpy(self, x):
+        x = np.ascontiguousarray(x)
+        arr = self.create(x.shape, x.dtype)
+        arr.write(x)
+        return arr
+
+
+class Array:
+    """NumcArray handle (owned by its Ctx)."""
+
+    def __init__(self, ptr, ctx):
+        self.ptr = ptr
+        self.ctx = ctx
+
+    @property
+    def ndim(self):
+        return lib().numc_array_ndim(self.ptr)
+
+    @property
+    def shape(self):
+        n = self.ndim
+        buf = (ctypes.c_size_t * max(1, n))()
+        lib().numc_array_shape(self.ptr, buf)
+        return tuple(buf[:n])
+
+    @property
+    def strides(self):
+        n = self.ndim
+        buf = (ctypes.c_size_t * max(1, n))()
+        lib().numc_array_strides(self.ptr, buf)
+        return tuple(buf[:n])
+
+    @property
+    def dtype(self):
+        return np.dtype(DTYPES[lib().numc_array_dtype(self.ptr)])
+
+    def write(self, x):
+        x = np.ascontiguousarray(x, dtype=self.dtype)
+        assert x.size == lib().numc_array_size(self.ptr)
+        lib().numc_array_write(self.ptr, x.ctypes.data)
+
+    def numpy(self):
+        """Copy of the host data as a numpy array with this view's strides."""
+        L = lib()
+        data = L.numc_array_data(self.ptr)
+        n = L.numc_array_size(self.ptr)
+        es = self.dtype.itemsize
+        if n == 0:
+            return np.zeros(self.shape, dtype=self.dtype)
+        shape, strides = self.shape, self.strides
+        span = es + sum((s - 1) * st for s, st in zip(shape, strides))
+        raw = (ctypes.c_char * span).from_address(data)
+        base = np.frombuffer(raw, dtype=np.uint8)
+        view = np.lib.stride_tricks.as_strided(base.view(self.dtype) if span % es == 0
+                                               else base[: span - span % es].view(self.dtype),
+                                               shape=shape, strides=strides)
+        return np.array(view)
+
+    def transpose(self, axes):
+        ax = (ctypes.c_size_t * len(axes))(*axes)
+        if lib().numc_array_transpose(self.ptr, ax) != 0:
+            raise NumcError(*last_error())
+        return self
+
+    def slice(self, axis, start=0, stop=0, step=1):
+        s = _Slice(axis, start, stop, step)
+        p = lib().numc_array_slice(self.ptr, ctypes.byref(s))
+        if not p:
+            raise NumcError(*last_error())
+        return Array(p, self.ctx)
+
+    def copy(self):
+        p = lib().numc_array_copy(self.ptr)
+        if not p:
+            raise NumcError(*last_error())
+        return Array(p, self.ctx)
+
+    def is_contiguous(self):
+        return lib().numc_array_is_contiguous(self.ptr)
+
+    def to_device(self):
+        check(lib().numc_cuda_array_to_device(self.ptr))
+        return self
+
+    def to_host(self):
+        check(lib().numc_cuda_array_to_host(self.ptr))
+        return self
+
+    def is_resident(self):
+        return bool(lib().numc_cuda_array_is_resident(self.ptr))
+
+    def device_ptr(self):
+        return lib().numc_cuda_array_device_data(self.ptr)
+
+
+def matmul(a, b, out):
+    """numc_matmul(a, b, out); raises NumcError on a nonzero return."""
+    return check(lib().numc_matmul(a.ptr if a else None, b.ptr if b else None,
+                                   out.ptr if out else None))
+
+
+def matmul_naive(a, b, out):
+    return check(lib().numc_matmul_naive(a.ptr, b.ptr, out.ptr))
+
+
+def workspace_size(dtype, algo, param, M, K, N):
+    return lib().numc_cuda_gemm_workspace_size(CODE[np.dtype(dtype).name], algo, param, M, K, N)
+
+
+def gemm(a, b, out, algo=ALGO_DEFAULT, param=-1, workspace=None, stream=None):
+    """numc_cuda_gemm on 2-D torch CUDA tensors (any element strides).
+
+    `workspace` is an optional torch uint8 CUDA tensor; `stream` a
+    torch.cuda.Stream (default: the current stream)."""
+    import torch
+    dt = CODE[str(a.dtype).replace("torch.", "")]
+    M, K = a.shape
+    N = b.shape[1]
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    ws_ptr, ws_bytes = (workspace.data_ptr(), workspace.numel()) if workspace is not None else (None, 0)
+    rc = lib().numc_cuda_gemm(dt, algo, param, a.data_ptr(), b.data_ptr(), out.data_ptr(),
+                              M, K, N, a.stride(0), a.stride(1), b.stride(0), b.stride(1),
+                              out.stride(0), out.stride(1), ws_ptr, ws_bytes,
+                              stream.cuda_stream)
+    return check(rc)
+
+
+def check_status(stream=None):
+    import torch
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return check(lib().numc_cuda_check_status(stream.cuda_stream))

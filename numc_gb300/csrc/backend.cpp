@@ -1,0 +1,499 @@
+// CUDA backend: numc_matmul dispatch, device residency, the device-pointer
+// C-ABI (numc_cuda_gemm) and algorithm selection.
+//
+// numc_matmul keeps numc's contract (src/matmul/matmul.c:347-389,
+// src/matmul/dispatch.h:20-59): validation order and error codes are the
+// same, inputs are const, out is caller-allocated, and the call returns when
+// the result is in `out`.  Where numc picks an ISA kernel from a dtype
+// table, this backend picks a CUDA kernel; there is no CPU fallback: without
+// a usable GPU the call fails with NUMC_ERR_INTERNAL.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "kernels.h"
+#include "runtime.h"
+
+using namespace numc_rt;
+
+namespace {
+
+// ---- process-wide algorithm choice ----------------------------------------
+
+struct AlgoChoice {
+  std::atomic<int> algo;
+  std::atomic<int> param;
+};
+AlgoChoice g_algo[NUMC_DTYPE_COUNT];
+std::once_flag g_algo_once;
+
+void init_algos_from_env() {
+  for (int d = 0; d < NUMC_DTYPE_COUNT; d++) {
+    g_algo[d].algo = NUMC_CUDA_ALGO_SIMT;
+    g_algo[d].param = 0;
+  }
+  g_algo[NUMC_DTYPE_INT8].param = NUMC_INT8_X86_AVX2;
+  g_algo[NUMC_DTYPE_UINT8].param = NUMC_INT8_X86_AVX2;
+  if (const char *e = getenv("NUMC_CUDA_F32_ALGO")) {
+    std::string v(e);
+    if (v == "split") g_algo[NUMC_DTYPE_FLOAT32].algo = NUMC_CUDA_ALGO_SPLIT_BF16;
+    else if (v == "auto") g_algo[NUMC_DTYPE_FLOAT32].algo = NUMC_CUDA_ALGO_AUTO;
+  }
+  if (const char *e = getenv("NUMC_CUDA_F64_ALGO")) {
+    std::string v(e);
+    if (v == "dmma") g_algo[NUMC_DTYPE_FLOAT64].algo = NUMC_CUDA_ALGO_DMMA;
+    if (v.rfind("ozaki", 0) == 0) {
+      g_algo[NUMC_DTYPE_FLOAT64].algo = NUMC_CUDA_ALGO_OZAKI;
+      int s = v.size() > 6 ? atoi(v.c_str() + 6) : 7;
+      g_algo[NUMC_DTYPE_FLOAT64].param = s;
+    }
+  }
+  if (const char *e = getenv("NUMC_CUDA_INT8_PROFILE")) {
+    std::string v(e);
+    int p = v == "neon" ? NUMC_INT8_ARM_NEON : v == "wrap" ? NUMC_INT8_WRAP : NUMC_INT8_X86_AVX2;
+    g_algo[NUMC_DTYPE_INT8].param = p;
+    g_algo[NUMC_DTYPE_UINT8].param = p;
+  }
+}
+
+void ensure_algos() { std::call_once(g_algo_once, init_algos_from_env); }
+
+// ---- device discovery -----------------------------------------------------
+
+int g_device_count = -1;
+std::once_flag g_dev_once;
+
+int device_count() {
+  std::call_once(g_dev_once, [] {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+      n = 0;
+      cudaGetLastError();
+    }
+    g_device_count = n;
+  });
+  return g_device_count;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  int code = (e == cudaErrorMemoryAllocation) ? NUMC_ERR_MALLOC : NUMC_ERR_INTERNAL;
+  cudaGetLastError();
+  return NUMC_SET_ERROR(code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CU(call, what)                         \
+  do {                                         \
+    cudaError_t e_ = (call);                   \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+// ---- library-managed per-device workspace for numc_cuda_gemm(NULL ws) -----
+
+std::mutex g_ws_mu;
+void *g_ws[64] = {nullptr};
+size_t g_ws_bytes[64] = {0};
+
+int library_workspace(size_t bytes, cudaStream_t s, void **out) {
+  int dev = 0;
+  CU(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev < 0 || dev >= 64) return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "device index %d", dev);
+  std::lock_guard<std::mutex> lock(g_ws_mu);
+  if (g_ws_bytes[dev] < bytes) {
+    if (g_ws[dev]) {
+      // Work queued on any stream may still use the old buffer.
+      CU(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+      cudaFree(g_ws[dev]);
+      g_ws[dev] = nullptr;
+      g_ws_bytes[dev] = 0;
+    }
+    size_t grow = bytes + bytes / 4;
+    CU(cudaMalloc(&g_ws[dev], grow), "cudaMalloc(workspace)");
+    g_ws_bytes[dev] = grow;
+  }
+  (void)s;
+  *out = g_ws[dev];
+  return 0;
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// ---- algorithm resolution -------------------------------------------------
+
+struct Plan {
+  int algo;     // concrete algorithm
+  int param;    // rule8 for int8/uint8, slices for Ozaki
+};
+
+int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Plan *p) {
+  ensure_algos();
+  if (algo == NUMC_CUDA_ALGO_DEFAULT) {
+    algo = g_algo[dt].algo.load();
+    if (param < 0) param = g_algo[dt].param.load();
+  }
+  if (param < 0) param = 0;   // 0 = x86 profile for int8/uint8, default slices
+  if (algo == NUMC_CUDA_ALGO_AUTO) {
+    if (dt != NUMC_DTYPE_FLOAT32)
+      return NUMC_SET_ERROR(NUMC_ERR_VALUE, "AUTO algorithm is float32 only");
+    // Split-BF16 pays for its split pass once each output sums enough terms
+    // and the grid fills the GPU.
+    algo = ((uint64_t)M * N >= (1u << 16) && K >= 128) ? NUMC_CUDA_ALGO_SPLIT_BF16
+                                                      : NUMC_CUDA_ALGO_SIMT;
+  }
+  switch (algo) {
+  case NUMC_CUDA_ALGO_SIMT: break;
+  case NUMC_CUDA_ALGO_SPLIT_BF16:
+    if (dt != NUMC_DTYPE_FLOAT32)
+      return NUMC_SET_ERROR(NUMC_ERR_TYPE, "split-BF16 GEMM is float32 only");
+    break;
+  case NUMC_CUDA_ALGO_DMMA:
+    if (dt != NUMC_DTYPE_FLOAT64)
+      return NUMC_SET_ERROR(NUMC_ERR_TYPE, "DMMA GEMM is float64 only");
+    break;
+  case NUMC_CUDA_ALGO_OZAKI:
+    if (dt != NUMC_DTYPE_FLOAT64)
+      return NUMC_SET_ERROR(NUMC_ERR_TYPE, "Ozaki GEMM is float64 only");
+    if (param == 0) param = 7;
+    if (param < 3 || param > 8)
+      return NUMC_SET_ERROR(NUMC_ERR_VALUE, "Ozaki slice count %d outside 3..8", param);
+    break;
+  default:
+    return NUMC_SET_ERROR(NUMC_ERR_VALUE, "unknown algorithm %d", algo);
+  }
+  p->algo = algo;
+  p->param = param;
+  if (dt == NUMC_DTYPE_INT8 || dt == NUMC_DTYPE_UINT8) {
+    int profile = param;
+    if (profile == NUMC_INT8_ARM_NEON) p->param = numc_k::kRuleNeon;
+    else if (profile == NUMC_INT8_WRAP) p->param = numc_k::kRuleWrap;
+    else if (profile == NUMC_INT8_X86_AVX2)
+      // numc's x86 build sends M*K*N <= 192^3 to its unpacked kernels, which
+      // truncate (src/matmul/matmul.c:241-256, gemmsup_avx2.h:744-756).
+      p->param = ((uint64_t)M * K * N <= 192ull * 192 * 192) ? numc_k::kRuleWrap
+                                                             : numc_k::kRuleX86Packed;
+    else return NUMC_SET_ERROR(NUMC_ERR_VALUE, "unknown int8 profile %d", profile);
+  }
+  return 0;
+}
+
+size_t plan_workspace(const Plan &p, size_t M, size_t K, size_t N) {
+  if (p.algo == NUMC_CUDA_ALGO_SPLIT_BF16) return numc_k::split_bf16_workspace(M, K, N);
+  if (p.algo == NUMC_CUDA_ALGO_OZAKI) return numc_k::ozaki_workspace(M, K, N, p.param);
+  return 0;
+}
+
+int run_plan(NumcDType dt, const Plan &p, const numc_k::Gemm &g, void *ws,
+             size_t ws_bytes, cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  switch (p.algo) {
+  case NUMC_CUDA_ALGO_SIMT: e = numc_k::launch_simt(dt, g, p.param, s); break;
+  case NUMC_CUDA_ALGO_DMMA: e = numc_k::launch_dmma(g, s); break;
+  case NUMC_CUDA_ALGO_SPLIT_BF16: e = numc_k::launch_split_bf16(g, ws, ws_bytes, s); break;
+  case NUMC_CUDA_ALGO_OZAKI: e = numc_k::launch_ozaki(g, p.param, ws, ws_bytes, s); break;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  return 0;
+}
+
+// ---- context stream and scratch ------------------------------------------
+
+int ctx_stream(NumcCtx *ctx, cudaStream_t *s) {
+  if (device_count() <= 0)
+    return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "no CUDA device available (the GB300 backend has no CPU fallback)");
+  if (!ctx->stream) {
+    int dev = 0;
+    CU(cudaGetDevice(&dev), "cudaGetDevice");
+    cudaStream_t st;
+    CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    ctx->stream = st;
+    ctx->device = dev;
+  }
+  *s = (cudaStream_t)ctx->stream;
+  return 0;
+}
+
+int ctx_scratch(NumcCtx *ctx, size_t bytes, cudaStream_t s, char **out) {
+  if (ctx->scratch_bytes < bytes) {
+    if (ctx->scratch) {
+      CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+      cudaFree(ctx->scratch);
+      ctx->scratch = nullptr;
+      ctx->scratch_bytes = 0;
+    }
+    size_t grow = align_up(bytes + bytes / 4, 1 << 20);
+    CU(cudaMalloc(&ctx->scratch, grow), "cudaMalloc(scratch)");
+    ctx->scratch_bytes = grow;
+  }
+  *out = (char *)ctx->scratch;
+  return 0;
+}
+
+bool is_resident(const NumcArray *a) {
+  return a->dev_base && a->residency != kHostOnly;
+}
+
+int check_matmul(const NumcArray *a, const NumcArray *b, const NumcArray *out) {
+  if (!a || !b || !out)
+    return NUMC_SET_ERROR(NUMC_ERR_NULL, "matmul: NULL pointer (a=%p b=%p out=%p)",
+                          (const void *)a, (const void *)b, (const void *)out);
+  if (a->dtype != b->dtype || a->dtype != out->dtype)
+    return NUMC_SET_ERROR(NUMC_ERR_TYPE, "matmul: dtype mismatch (a=%d b=%d out=%d)",
+                          a->dtype, b->dtype, out->dtype);
+  if (a->dim != 2 || b->dim != 2 || out->dim != 2)
+    return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "matmul: ndim mismatch (a.dim=%zu b.dim=%zu out.dim=%zu)",
+                          a->dim, b->dim, out->dim);
+  if (a->shape[1] != b->shape[0])
+    return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "matmul: shape mismatch (a.shape[1]=%zu b.shape[0]=%zu)",
+                          a->shape[1], b->shape[0]);
+  if (out->shape[0] != a->shape[0] || out->shape[1] != b->shape[1])
+    return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "matmul: out shape (%zu, %zu) != (%zu, %zu)",
+                          out->shape[0], out->shape[1], a->shape[0], b->shape[1]);
+  return 0;
+}
+
+int matmul_impl(const NumcArray *a, const NumcArray *b, NumcArray *out, int algo, int param) {
+  int err = check_matmul(a, b, out);
+  if (err) return err;
+  const size_t M = a->shape[0], K = a->shape[1], N = b->shape[1];
+  if (M == 0 || N == 0) return 0;
+  NumcDType dt = a->dtype;
+  Plan plan;
+  if ((err = resolve(dt, algo, param, M, K, N, &plan))) return err;
+  NumcCtx *ctx = out->ctx;
+  cudaStream_t s;
+  if ((err = ctx_stream(ctx, &s))) return err;
+
+  const size_t es = a->elem_size;
+  const bool ra = is_resident(a), rb = is_resident(b), ro = is_resident(out);
+  const size_t sa = array_span_bytes(a), sb = array_span_bytes(b), so = array_span_bytes(out);
+  size_t off_a = 0, off_b = align_up(ra ? 0 : sa, 256);
+  size_t off_o = off_b + align_up(rb ? 0 : sb, 256);
+  size_t off_w = off_o + align_up(ro ? 0 : so, 256);
+  size_t ws_bytes = plan_workspace(plan, M, K, N);
+  char *scratch = nullptr;
+  if ((err = ctx_scratch(ctx, off_w + ws_bytes + 256, s, &scratch))) return err;
+
+  const char *da = ra ? a->dev_base : scratch + off_a;
+  const char *db = rb ? b->dev_base : scratch + off_b;
+  char *dout = ro ? out->dev_base : scratch + off_o;
+  if (!ra) CU(cudaMemcpyAsync((void *)da, a->data, sa, cudaMemcpyHostToDevice, s), "copy a to device");
+  if (!rb) CU(cudaMemcpyAsync((void *)db, b->data, sb, cudaMemcpyHostToDevice, s), "copy b to device");
+  // A strided `out` with gaps between rows keeps the gap bytes: stage them.
+  if (!ro && so > out->capacity)
+    CU(cudaMemcpyAsync(dout, out->data, so, cudaMemcpyHostToDevice, s), "copy out to device");
+
+  numc_k::Gemm g;
+  g.a = da; g.b = db; g.c = dout;
+  g.M = M; g.K = K; g.N = N;
+  g.rsa = a->strides[0] / es; g.csa = a->strides[1] / es;
+  g.rsb = b->strides[0] / es; g.csb = b->strides[1] / es;
+  g.rso = out->strides[0] / es; g.cso = out->strides[1] / es;
+  if ((err = run_plan(dt, plan, g, scratch + off_w, ws_bytes, s))) return err;
+
+  if (ro) {
+    out->residency = kDeviceOnly;
+    // Host operands were read by asynchronous copies: finish them before
+    // the caller may modify the host buffers.
+    if (!ra || !rb) CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  } else {
+    CU(cudaMemcpyAsync(out->data, dout, so, cudaMemcpyDeviceToHost, s), "copy out to host");
+    CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  }
+  if (plan.algo == NUMC_CUDA_ALGO_SPLIT_BF16 || plan.algo == NUMC_CUDA_ALGO_OZAKI) {
+    unsigned st = 0;
+    CU(numc_k::read_and_clear_status(&st, s), "status read");
+    if (st) return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "matmul kernel abandoned a bounded wait (code %u)", st);
+  }
+  return 0;
+}
+
+}  // namespace
+
+// ---- hooks used by the core ------------------------------------------------
+
+namespace numc_rt {
+
+bool cuda_present() { return device_count() > 0; }
+
+void *host_alloc_pinned(size_t bytes) {
+  void *p = nullptr;
+  if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+
+void host_free_pinned(void *p) { cudaFreeHost(p); }
+
+void ctx_release_device(NumcCtx *ctx, const ArenaPos *keep_upto) {
+  if (!ctx->dev_allocs) return;
+  if (ctx->stream && !ctx->dev_allocs->empty())
+    cudaStreamSynchronize((cudaStream_t)ctx->stream);
+  auto &v = *ctx->dev_allocs;
+  size_t w = 0;
+  for (size_t r = 0; r < v.size(); r++) {
+    if (!keep_upto || v[r].owner.after(*keep_upto)) cudaFree(v[r].ptr);
+    else v[w++] = v[r];
+  }
+  v.resize(w);
+  if (!keep_upto) {
+    if (ctx->scratch) {
+      if (ctx->stream) cudaStreamSynchronize((cudaStream_t)ctx->stream);
+      cudaFree(ctx->scratch);
+    }
+    ctx->scratch = nullptr;
+    ctx->scratch_bytes = 0;
+    if (ctx->stream) cudaStreamDestroy((cudaStream_t)ctx->stream);
+    ctx->stream = nullptr;
+  }
+}
+
+}  // namespace numc_rt
+
+// ---- public API ------------------------------------------------------------
+
+extern "C" int numc_matmul(const NumcArray *a, const NumcArray *b, NumcArray *out) {
+  return matmul_impl(a, b, out, NUMC_CUDA_ALGO_DEFAULT, -1);
+}
+
+extern "C" int numc_matmul_naive(const NumcArray *a, const NumcArray *b, NumcArray *out) {
+  // numc's naive kernels accumulate in the storage type (kernel.h:18-62).
+  int param = (a && (a->dtype == NUMC_DTYPE_INT8 || a->dtype == NUMC_DTYPE_UINT8))
+                  ? NUMC_INT8_WRAP : 0;
+  return matmul_impl(a, b, out, NUMC_CUDA_ALGO_SIMT, param);
+}
+
+extern "C" int numc_cuda_device_count(void) { return device_count(); }
+
+extern "C" int numc_cuda_set_algo(NumcDType dt, int algo, int param) {
+  ensure_algos();
+  if ((int)dt < 0 || (int)dt >= NUMC_DTYPE_COUNT)
+    return NUMC_SET_ERROR(NUMC_ERR_TYPE, "unknown dtype %d", (int)dt);
+  Plan p;
+  int err = resolve(dt, algo == NUMC_CUDA_ALGO_DEFAULT ? NUMC_CUDA_ALGO_SIMT : algo,
+                    param, 1024, 1024, 1024, &p);
+  if (err) return err;
+  g_algo[dt].algo = algo == NUMC_CUDA_ALGO_DEFAULT ? NUMC_CUDA_ALGO_SIMT : algo;
+  g_algo[dt].param = param;
+  return 0;
+}
+
+extern "C" int numc_cuda_get_algo(NumcDType dt, int *algo, int *param) {
+  ensure_algos();
+  if ((int)dt < 0 || (int)dt >= NUMC_DTYPE_COUNT)
+    return NUMC_SET_ERROR(NUMC_ERR_TYPE, "unknown dtype %d", (int)dt);
+  if (algo) *algo = g_algo[dt].algo.load();
+  if (param) *param = g_algo[dt].param.load();
+  return 0;
+}
+
+extern "C" int numc_cuda_array_to_device(NumcArray *arr) {
+  if (!arr) return NUMC_SET_ERROR(NUMC_ERR_NULL, "to_device: arr is NULL");
+  if (is_resident(arr)) return 0;
+  cudaStream_t s;
+  int err = ctx_stream(arr->ctx, &s);
+  if (err) return err;
+  size_t span = array_span_bytes(arr);
+  if (!arr->dev_base) {
+    void *p = nullptr;
+    CU(cudaMalloc(&p, align_up(span ? span : 1, 256)), "cudaMalloc(array)");
+    arr->ctx->dev_allocs->push_back(DeviceAlloc{p, span, arr->pos});
+    arr->dev_base = (char *)p;
+  }
+  if (span) CU(cudaMemcpyAsync(arr->dev_base, arr->data, span, cudaMemcpyHostToDevice, s), "copy to device");
+  CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  arr->residency = kBoth;
+  return 0;
+}
+
+extern "C" int numc_cuda_array_to_host(NumcArray *arr) {
+  if (!arr) return NUMC_SET_ERROR(NUMC_ERR_NULL, "to_host: arr is NULL");
+  if (arr->residency != kDeviceOnly) return 0;
+  cudaStream_t s;
+  int err = ctx_stream(arr->ctx, &s);
+  if (err) return err;
+  size_t span = array_span_bytes(arr);
+  if (span) CU(cudaMemcpyAsync(arr->data, arr->dev_base, span, cudaMemcpyDeviceToHost, s), "copy to host");
+  CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  arr->residency = kBoth;
+  return 0;
+}
+
+extern "C" void *numc_cuda_array_device_data(const NumcArray *arr) {
+  return (arr && is_resident(arr)) ? arr->dev_base : nullptr;
+}
+
+extern "C" int numc_cuda_array_is_resident(const NumcArray *arr) {
+  return arr && is_resident(arr);
+}
+
+extern "C" void *numc_cuda_ctx_stream(NumcCtx *ctx) {
+  if (!ctx) return nullptr;
+  cudaStream_t s;
+  return ctx_stream(ctx, &s) ? nullptr : (void *)s;
+}
+
+extern "C" int numc_cuda_ctx_synchronize(NumcCtx *ctx) {
+  if (!ctx) return NUMC_SET_ERROR(NUMC_ERR_NULL, "synchronize: ctx is NULL");
+  if (!ctx->stream) return 0;
+  CU(cudaStreamSynchronize((cudaStream_t)ctx->stream), "cudaStreamSynchronize");
+  return 0;
+}
+
+extern "C" size_t numc_cuda_gemm_workspace_size(NumcDType dt, int algo, int param,
+                                                size_t M, size_t K, size_t N) {
+  if ((int)dt < 0 || (int)dt >= NUMC_DTYPE_COUNT) return 0;
+  Plan p;
+  if (resolve(dt, algo, param, M, K, N, &p)) return 0;
+  return plan_workspace(p, M, K, N);
+}
+
+extern "C" int numc_cuda_gemm(NumcDType dt, int algo, int param, const void *a,
+                              const void *b, void *out, size_t M, size_t K, size_t N,
+                              intptr_t rsa, intptr_t csa, intptr_t rsb, intptr_t csb,
+                              intptr_t rso, intptr_t cso, void *workspace,
+                              size_t workspace_bytes, void *stream) {
+  if ((int)dt < 0 || (int)dt >= NUMC_DTYPE_COUNT)
+    return NUMC_SET_ERROR(NUMC_ERR_TYPE, "unknown dtype %d", (int)dt);
+  if (M == 0 || N == 0) return 0;
+  if (!out || (K > 0 && (!a || !b)))
+    return NUMC_SET_ERROR(NUMC_ERR_NULL, "gemm: NULL operand (a=%p b=%p out=%p)", a, b, out);
+  if (rsa < 0 || csa < 0 || rsb < 0 || csb < 0 || rso < 0 || cso < 0)
+    return NUMC_SET_ERROR(NUMC_ERR_VALUE, "gemm: negative stride");
+  if (device_count() <= 0)
+    return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "no CUDA device available (the GB300 backend has no CPU fallback)");
+  Plan p;
+  int err = resolve(dt, algo, param, M, K, N, &p);
+  if (err) return err;
+  cudaStream_t s = (cudaStream_t)stream;
+  size_t need = plan_workspace(p, M, K, N);
+  void *ws = workspace;
+  size_t ws_bytes = workspace_bytes;
+  if (need) {
+    if (!ws) {
+      if ((err = library_workspace(need, s, &ws))) return err;
+      ws_bytes = need;
+    } else if (ws_bytes < need || ((uintptr_t)ws & 255)) {
+      return NUMC_SET_ERROR(NUMC_ERR_VALUE, "gemm: workspace needs %zu bytes aligned to 256 (got %zu at %p)",
+                            need, ws_bytes, ws);
+    }
+  }
+  numc_k::Gemm g;
+  g.a = a; g.b = b; g.c = out;
+  g.M = M; g.K = K; g.N = N;
+  g.rsa = rsa; g.csa = csa; g.rsb = rsb; g.csb = csb; g.rso = rso; g.cso = cso;
+  return run_plan(dt, p, g, ws, ws_bytes, s);
+}
+
+extern "C" int numc_cuda_check_status(void *stream) {
+  unsigned st = 0;
+  CU(numc_k::read_and_clear_status(&st, (cudaStream_t)stream), "status read");
+  if (st) return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "a kernel abandoned a bounded wait (code %u)", st);
+  return 0;
+}
+
+extern "C" uint64_t numc_cuda_launch_count(void) { return numc_k::launches(); }

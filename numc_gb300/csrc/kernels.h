@@ -1,0 +1,51 @@
+// Launchers of the CUDA kernels (internal C++ interface of the backend).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+#include "numc/cuda.h"
+#include "numc/dtype.h"
+
+namespace numc_k {
+
+// One GEMM: c[i*rso + j*cso] = sum_k a[i*rsa + k*csa] * b[k*rsb + j*csb].
+// Element strides; device pointers.
+struct Gemm {
+  const void *a, *b;
+  void *c;
+  int64_t M, K, N;
+  int64_t rsa, csa, rsb, csb, rso, cso;
+};
+
+// int8/uint8 store rule applied by the SIMT integer kernel.
+enum Rule8 : int {
+  kRuleWrap = 0,      // truncate the full sum to 8 bits
+  kRuleX86Packed = 1, // numc x86 AVX2 packed path (K blocks of 512)
+  kRuleNeon = 2,      // numc aarch64 NEON path (one block over all K)
+};
+
+// CUDA-core kernels for every dtype.  `rule8` only matters for int8/uint8.
+cudaError_t launch_simt(NumcDType dt, const Gemm &g, int rule8, cudaStream_t s);
+// float64 on the mma.sync f64 tensor path.
+cudaError_t launch_dmma(const Gemm &g, cudaStream_t s);
+
+// float32 split-BF16 on tcgen05: workspace bytes and launcher.
+size_t split_bf16_workspace(int64_t M, int64_t K, int64_t N);
+cudaError_t launch_split_bf16(const Gemm &g, void *ws, size_t ws_bytes,
+                              cudaStream_t s);
+
+// float64 Ozaki slicing on tcgen05.
+size_t ozaki_workspace(int64_t M, int64_t K, int64_t N, int slices);
+cudaError_t launch_ozaki(const Gemm &g, int slices, void *ws, size_t ws_bytes,
+                         cudaStream_t s);
+
+// Device-side status word set by kernels that give up on a bounded wait.
+cudaError_t read_and_clear_status(unsigned *status, cudaStream_t s);
+
+// Count of kernel launches issued by this library.
+void count_launch(unsigned n = 1);
+uint64_t launches();
+
+}  // namespace numc_k

@@ -1,0 +1,124 @@
+"""Host-side behaviour of the C-ABI library (no GPU needed).
+
+The library must load, export every function include/numc/*.h declares,
+keep numc's array semantics, and return numc's error codes for invalid
+calls.  With no GPU it must refuse to compute (NUMC_ERR_INTERNAL) rather
+than fall back to the CPU.
+"""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+import numc_gb300 as nc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "numc", "*.h")):
+        text = open(h).read()
+        for m in re.finditer(r"NUMC_API\s+[^;(]*?\b(numc_\w+)\s*\(", text, re.S):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def L():
+    return nc.lib()
+
+
+def test_exports_every_declared_symbol(L):
+    names = declared_functions()
+    assert len(names) >= 40
+    for n in names:
+        assert hasattr(L, n), f"{n} declared in include/numc but not exported"
+    bound = {s[0] for s in nc.SIGNATURES}
+    assert set(names) - {"numc_set_error_v"} <= bound | {"numc_set_error_v"}
+
+
+def test_array_basics():
+    with nc.Ctx() as ctx:
+        x = np.arange(24, dtype=np.int32).reshape(4, 6)
+        a = ctx.from_numpy(x)
+        assert a.shape == (4, 6) and a.strides == (24, 4) and a.dtype == np.int32
+        np.testing.assert_array_equal(a.numpy(), x)
+        a.transpose((1, 0))
+        assert a.shape == (6, 4) and a.strides == (4, 24) and not a.is_contiguous()
+        np.testing.assert_array_equal(a.numpy(), x.T)
+        c = a.copy()
+        assert c.is_contiguous()
+        np.testing.assert_array_equal(c.numpy(), x.T)
+        s = ctx.from_numpy(x).slice(1, 1, 6, 2)
+        np.testing.assert_array_equal(s.numpy(), x[:, 1:6:2])
+        f = ctx.fill((3, 2), np.float64, 2.5)
+        assert (f.numpy() == 2.5).all()
+        z = ctx.zeros((2, 3), np.uint8)
+        assert (z.numpy() == 0).all()
+
+
+def test_checkpoint_restore():
+    with nc.Ctx() as ctx:
+        keep = ctx.from_numpy(np.ones((4, 4), np.float32))
+        cp = ctx.checkpoint()
+        for _ in range(20):
+            ctx.create((1024, 1024), np.float64)   # 8 MiB each: new blocks
+        ctx.restore(cp)
+        np.testing.assert_array_equal(keep.numpy(), np.ones((4, 4), np.float32))
+        again = ctx.create((4, 4), np.float32)
+        assert again.shape == (4, 4)
+
+
+def test_create_errors(L):
+    assert not L.numc_array_create(None, None, 1, 0)
+    assert nc.last_error()[0] == nc.ERR_NULL
+    with nc.Ctx() as ctx:
+        huge = (ctypes.c_size_t * 2)(1 << 62, 1 << 62)
+        assert not L.numc_array_create(ctx.ptr, huge, 2, 0)
+        assert nc.last_error()[0] == nc.ERR_SHAPE
+
+
+def _rc(a, b, out):
+    return nc.lib().numc_matmul(a.ptr if a else None, b.ptr if b else None,
+                                out.ptr if out else None)
+
+
+def test_matmul_validation_codes():
+    # numc's own error cases (tests/matmul/test_matmul_naive.c:164-240)
+    with nc.Ctx() as ctx:
+        a = ctx.zeros((2, 3), np.float32)
+        b = ctx.zeros((3, 2), np.float32)
+        c = ctx.zeros((2, 2), np.float32)
+        assert _rc(None, b, c) == nc.ERR_NULL
+        assert _rc(a, ctx.zeros((3, 2), np.float64), c) == nc.ERR_TYPE
+        assert _rc(a, ctx.zeros((4, 2), np.float32), c) == nc.ERR_SHAPE
+        assert _rc(a, b, ctx.zeros((3, 2), np.float32)) == nc.ERR_SHAPE
+        assert _rc(ctx.zeros((6,), np.float32), b, c) == nc.ERR_SHAPE
+        assert nc.last_error()[1]
+
+
+@pytest.mark.skipif(nc.device_count() > 0, reason="checks the no-GPU behaviour")
+def test_no_cpu_fallback():
+    with nc.Ctx() as ctx:
+        a = ctx.zeros((2, 3), np.float32)
+        b = ctx.zeros((3, 2), np.float32)
+        c = ctx.zeros((2, 2), np.float32)
+        assert _rc(a, b, c) == nc.ERR_INTERNAL
+        assert "no CUDA device" in nc.last_error()[1]
+
+
+def test_algo_settings():
+    orig = nc.get_algo("float64")
+    try:
+        nc.set_algo("float64", nc.ALGO_OZAKI, 6)
+        assert nc.get_algo("float64") == (nc.ALGO_OZAKI, 6)
+        with pytest.raises(nc.NumcError):
+            nc.set_algo("float64", nc.ALGO_OZAKI, 12)
+        with pytest.raises(nc.NumcError):
+            nc.set_algo("int32", nc.ALGO_SPLIT_BF16, 0)
+    finally:
+        nc.set_algo("float64", *orig)

@@ -1,0 +1,127 @@
+"""GPU results against numc: golden fixtures and the oracle.
+
+* Every golden case (outputs of numc's own numc_matmul on seeded inputs) is
+  recomputed by numc_matmul on the GPU: integer dtypes must reproduce the
+  SHA-256 of numc's output bit for bit, at full size (1024^3 int8, uint8,
+  int32, int64 and 300x4100x4200 int8/uint8 with numc's saturating stores).
+* Float kernels are checked against the oracle with the error bound written
+  in each test, relative to |A| @ |B|.
+* The device-pointer C-ABI (numc_cuda_gemm) is exercised with torch CUDA
+  tensors, including transposed views and a caller-provided workspace.
+"""
+import numpy as np
+import pytest
+
+import numc_gb300 as nc
+import oracle
+from numc_gb300 import synth
+
+from gpu_util import (golden, needs_gpu, rel_err_vs_scale, sha, unit_roundoff)
+
+pytestmark = [pytest.mark.gpu, needs_gpu]
+
+CASES, ARRAYS = golden()
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = nc.Ctx()
+    yield c
+    c.free()
+
+
+def _run_numc(ctx, a, b):
+    A, B = ctx.from_numpy(a), ctx.from_numpy(b)
+    C = ctx.zeros((a.shape[0], b.shape[1]), a.dtype)
+    nc.matmul(A, B, C)
+    return C.numpy()
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: c["name"])
+def test_golden_default_algorithms(ctx, case):
+    M, K, N = case["shape"]
+    dt = case["dtype"]
+    a, b = synth.operands(case["kind"], M, K, N, seed=case["seed"], dtype=dt)
+    cp = ctx.checkpoint()
+    got = _run_numc(ctx, a, b)
+    ctx.restore(cp)
+    if np.dtype(dt).kind in "iu":
+        assert sha(got) == case["sha256"], f"{dt} {M}x{K}x{N} differs from numc"
+        return
+    # SIMT float kernels are numc's per-output FMA chain: full register tiles
+    # match numc bit for bit, remainder tiles within K ulps of |A||B|.
+    if case["stored"] == "full":
+        ref = ARRAYS[case["name"]].reshape(got.shape)
+    else:
+        ref = oracle.matmul(a, b)
+        idx = ARRAYS[case["name"] + "__idx"]
+        np.testing.assert_array_equal(ref.reshape(-1)[idx], ARRAYS[case["name"]])
+    bound = (K + 2) * unit_roundoff(dt)
+    assert rel_err_vs_scale(got, ref, a, b) <= bound
+
+
+@pytest.mark.parametrize("dt", ["float32", "float64"])
+def test_simt_is_numc_fma_chain(ctx, dt):
+    # 96 x 300 x 160 sits on numc's packed path with only full 6x16 (6x8)
+    # tiles, where numc computes one FMA chain per output: bit-exact.
+    a, b = synth.operands("uniform", 96, 300, 160, dtype=dt)
+    got = _run_numc(ctx, a, b)
+    np.testing.assert_array_equal(got, oracle.matmul(a, b))
+
+
+@pytest.mark.parametrize("dt", ["int8", "uint8"])
+@pytest.mark.parametrize("profile", [nc.INT8_X86_AVX2, nc.INT8_ARM_NEON, nc.INT8_WRAP])
+def test_int8_profiles(ctx, dt, profile):
+    a, b = synth.operands("uniform", 150, 1500, 140, dtype=dt)
+    nc.set_algo(dt, nc.ALGO_SIMT, profile)
+    try:
+        got = _run_numc(ctx, a, b)
+    finally:
+        nc.set_algo(dt, nc.ALGO_SIMT, nc.INT8_X86_AVX2)
+    np.testing.assert_array_equal(got, oracle.matmul(a, b, profile))
+
+
+# ---- the device-pointer C-ABI -----------------------------------------------
+
+torch = pytest.importorskip("torch")
+
+
+def _dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+@pytest.mark.parametrize("dt", nc.DTYPES)
+def test_cabi_gemm_transposed_views(dt):
+    M, K, N = 129, 515, 67
+    a, b = synth.operands("uniform", M, K, N, dtype=dt, seed=21)
+    ta = _dev(a.T).t()                        # column-major A
+    tb = _dev(b)
+    out = torch.zeros((N, M), dtype=ta.dtype, device="cuda").t()
+    nc.gemm(ta, tb, out, algo=nc.ALGO_SIMT, param=nc.INT8_X86_AVX2)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    ref = oracle.matmul(a, b)
+    if np.dtype(dt).kind in "iu":
+        np.testing.assert_array_equal(got, ref)
+    else:
+        assert rel_err_vs_scale(got, ref, a, b) <= (K + 2) * unit_roundoff(dt)
+
+
+def test_cabi_gemm_dmma():
+    M, K, N = 200, 333, 150
+    a, b = synth.operands("expspread", M, K, N, dtype="float64")
+    out = torch.empty((M, N), dtype=torch.float64, device="cuda")
+    nc.gemm(_dev(a), _dev(b), out, algo=nc.ALGO_DMMA)
+    torch.cuda.synchronize()
+    assert rel_err_vs_scale(out.cpu().numpy(), oracle.matmul(a, b), a, b) <= (K + 2) * 2.0 ** -53
+
+
+def test_cabi_gemm_rejects_bad_args():
+    x = torch.zeros((4, 4), dtype=torch.float32, device="cuda")
+    L = nc.lib()
+    rc = L.numc_cuda_gemm(8, nc.ALGO_SIMT, 0, x.data_ptr(), None, x.data_ptr(), 4, 4, 4,
+                          4, 1, 4, 1, 4, 1, None, 0, None)
+    assert rc == nc.ERR_NULL
+    rc = L.numc_cuda_gemm(8, nc.ALGO_DMMA, 0, x.data_ptr(), x.data_ptr(), x.data_ptr(),
+                          4, 4, 4, 4, 1, 4, 1, 4, 1, None, 0, None)
+    assert rc == nc.ERR_TYPE
