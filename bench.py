@@ -1,0 +1,444 @@
+"""Benchmark of numc_matmul on GB300 (one JSON line on stdout).
+
+Headline workload: float32 M = N = K = 8192, entries N(0, 1) (seeded
+splitmix64), computed by the 3-pass split-BF16 tcgen05 kernel through the
+device-pointer C-ABI numc_cuda_gemm with operands resident in HBM.  A step is
+one full matmul (split pass + GEMM).  Inputs (2 x 256 MiB) and the split
+planes (2 x 256 MiB) exceed the 126 MiB L2, so no flush is needed between
+steps.  `value` is algorithmic TFLOP/s, 2*M*N*K / step time, summed over
+ranks (replicas: every rank computes the same product on its own GPU).
+
+Beside it, on the same run: the plain FP32-SIMT kernel on the same inputs,
+max/mean error of both against a float64-accurate oracle (compensated dot
+products), the ill-scaled variant, `e2e` through numc_matmul with host
+arrays (host<->device copies in the timed region), float64 at 4096^3 (SIMT
+and DMMA), the integer bit-exactness workload at 1024^3, and the CPU
+baseline (numc's arithmetic restated in C, OpenMP, on a row sample).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+M = N = K = 8192
+SEED = 42
+FLOPS = 2.0 * M * N * K
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="skip the side workloads")
+    return ap.parse_args()
+
+
+# ---- distributed plumbing (replicas only: no data-path collective) --------
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---- clocks during the timed region ---------------------------------------
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+    def __init__(self, gpu_id):
+        self.samples = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={gpu_id}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                self.samples.append((time.time(), float(parts[0]), float(parts[1]),
+                                     parts[3:7]))
+            except ValueError:
+                pass
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        win = [s for s in self.samples if t0 <= s[0] <= t1]
+        if not win and self.samples:   # region shorter than the sampling period
+            win = [min(self.samples, key=lambda s: abs(s[0] - (t0 + t1) / 2))]
+        if not win:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        reasons = sorted({self.NAMES[i] for s in win for i, v in enumerate(s[3])
+                          if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(s[1] for s in win),
+                "sm_max_mhz": max(s[2] for s in win), "reasons": reasons,
+                "samples": len(win)}
+
+
+def gpu_id_for_smi(dev):
+    import torch
+    try:
+        return "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
+    except Exception:
+        return str(dev)
+
+
+# ---- errors against a float64-accurate oracle -----------------------------
+
+def sample_errors(got_rows_cols, ref, absprod):
+    """max/mean elementwise relative error |c - r| / max(|r|, 2^-60 |A||B|)
+    and the largest error relative to |A||B| itself."""
+    d = np.abs(got_rows_cols.astype(np.float64) - ref)
+    rel = d / np.maximum(np.abs(ref), 2.0 ** -60 * absprod)
+    return {"max_rel": float(rel.max()), "mean_rel": float(rel.mean()),
+            "max_rel_to_absprod": float((d / absprod).max())}
+
+
+def sample_points(n_out, rows, cols, seed=7):
+    rng = np.random.default_rng(seed)
+    return rng.integers(0, rows, n_out), rng.integers(0, cols, n_out)
+
+
+# ---- CPU legs ---------------------------------------------------------------
+
+def cpu_sample_tflops(a, b, target_s, nthreads=0):
+    """Time numc's arithmetic (the oracle port, or numc itself where it was
+    compiled on this host) on the first r rows of A, r sized for ~target_s."""
+    import oracle
+    use_ref = False
+    try:
+        use_ref = oracle.reference_available() and os.path.exists(oracle._build.REF_SO)
+        if use_ref:
+            oracle._load_ref()
+    except Exception:
+        use_ref = False
+
+    def run(rows):
+        t0 = time.perf_counter()
+        if use_ref:
+            oracle.ref_matmul(a[:rows], b)
+        else:
+            oracle.matmul(a[:rows], b, nthreads=nthreads)
+        return time.perf_counter() - t0
+
+    run(8)
+    t = run(16)
+    rows = int(max(16, min(a.shape[0], 16 * target_s / max(t, 1e-6))))
+    rows = max(16, rows - rows % 16)
+    t = run(rows)
+    tflops = 2.0 * rows * b.shape[0] * b.shape[1] / t / 1e12
+    kind = "reference" if use_ref else "port"
+    cores = oracle.num_threads() if nthreads == 0 else nthreads
+    return tflops, rows, t, kind, cores
+
+
+def run_reference(args, world, rank):
+    """--impl reference: numc's CPU arithmetic on the host cores, same metric."""
+    if rank != 0:
+        return
+    from numc_gb300 import synth
+    a = synth.normal(SEED, 3, (M, K), np.float32)
+    b = synth.normal(SEED, 4, (K, N), np.float32)
+    per_step = max(0.2, 120.0 / max(1, args.steps + args.warmup))
+    # size one sample for the per-step budget, then run W + K samples
+    _, rows, _, kind, cores = cpu_sample_tflops(a, b, per_step)
+    import oracle
+    fn = (lambda: oracle.ref_matmul(a[:rows], b)) if kind == "reference" else \
+        (lambda: oracle.matmul(a[:rows], b))
+    for _ in range(args.warmup):
+        fn()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        fn()
+    dt = (time.perf_counter() - t0) / args.steps
+    value = 2.0 * rows * K * N / dt / 1e12
+    sample = f"first {rows} of {M} rows of A per step (float32 N(0,1), K=N={K})"
+    print(json.dumps({
+        "impl": "reference", "metric": "numc_matmul float32 8192^3 TFLOP/s",
+        "value": value, "unit": "TFLOP/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "f32 8192x8192x8192 N(0,1), seed 42", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+# ---- GPU legs ---------------------------------------------------------------
+
+def time_gemm(nc, torch, a, b, c, algo, param, steps, warmup, ws=None):
+    for _ in range(warmup):
+        nc.gemm(a, b, c, algo=algo, param=param, workspace=ws)
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        nc.gemm(a, b, c, algo=algo, param=param, workspace=ws)
+    e1.record(s)
+    torch.cuda.synchronize()
+    nc.check_status()
+    return e0.elapsed_time(e1) / steps
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    import torch
+    import numc_gb300 as nc
+    from numc_gb300 import synth
+    import oracle
+    if not os.path.exists(nc.LIB_PATH):
+        from numc_gb300 import build as nb
+        nb.build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+
+    # -- inputs: N(0,1) float32, generated on the host from the seed ---------
+    a_h = synth.normal(SEED, 3, (M, K), np.float32)
+    b_h = synth.normal(SEED, 4, (K, N), np.float32)
+    a = torch.from_numpy(a_h).to(dev)
+    b = torch.from_numpy(b_h).to(dev)
+    c = torch.empty((M, N), dtype=torch.float32, device=dev)
+    ws_bytes = nc.workspace_size("float32", nc.ALGO_SPLIT_BF16, 0, M, K, N)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+
+    # -- headline: split-BF16, device-resident -------------------------------
+    for _ in range(max(3, args.warmup)):
+        nc.gemm(a, b, c, algo=nc.ALGO_SPLIT_BF16, workspace=ws)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(gpu_id_for_smi(local))
+    time.sleep(0.3)
+    nc.phase_timing(True)
+    launches0 = nc.launch_count()
+    barrier(world)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t_wall0 = time.time()
+    e0.record(stream)
+    for _ in range(args.steps):
+        nc.gemm(a, b, c, algo=nc.ALGO_SPLIT_BF16, workspace=ws)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_wall1 = time.time()
+    barrier(world)
+    launches = nc.launch_count() - launches0
+    nc.check_status()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world)
+    prep_ms, gemm_ms, calls = nc.phase_times()
+    nc.phase_timing(False)
+    sampler.stop()
+    clocks = sampler.summary(t_wall0, t_wall1)
+    value = world * FLOPS / (ms * 1e-3) / 1e12
+
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    bf16_peak = peaks.get("bf16_tflops")
+    peak_src = "measured" if bf16_peak else "fallback"
+    bf16_peak = bf16_peak or 1900.0
+    gemm_avg = gemm_ms / max(1, calls)
+    tensor_flops = 3 * FLOPS   # three bf16 products per float32 product
+    achieved = tensor_flops / (gemm_avg * 1e-3) / 1e12
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak,
+                "unit": "TFLOP/s", "frac": achieved / bf16_peak,
+                "traffic": TRAFFIC_PER_LAUNCH, "kernel": "split_bf16_gemm<128,3>",
+                "kernel_ms": gemm_avg, "split_pass_ms": prep_ms / max(1, calls),
+                "peak_source": f"bf16_tflops of {peak_src}",
+                "algorithmic_flops_per_launch": tensor_flops}
+
+    result = {
+        "metric": "numc_matmul float32 8192^3 TFLOP/s (split-BF16 tcgen05 vs plain FP32-SIMT)",
+        "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded splitmix64 N(0,1))",
+        "config": {"workload": "f32 8192x8192x8192 N(0,1), seed 42, split-BF16 x3",
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs 512 MiB + split planes 512 MiB > 126 MiB L2, no flush"},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "roofline": roofline,
+    }
+
+    if not args.quick and rank == 0:
+        side = side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args)
+        result.update(side)
+        result["split_vs_plain"] = value / world / side["plain"]["value"]
+
+    if rank == 0:
+        tflops, rows, t, kind, cores = cpu_sample_tflops(a_h, b_h, 8.0)
+        result["cpu_baseline"] = {
+            "value": tflops, "unit": "TFLOP/s", "cores": cores, "kind": kind,
+            "sample": f"first {rows} of {M} rows of A ({t:.1f} s), numc float32 arithmetic"}
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+# DRAM bytes (read + write) of one split_bf16_gemm launch at 8192^3, from the
+# ncu capture summarised in profiles/split_bf16_gemm_f32_8192.md.
+TRAFFIC_PER_LAUNCH = 3.127454e9 + 0.262717e9
+
+
+def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
+    out = {}
+    # plain FP32-SIMT on the same inputs
+    plain_ms = time_gemm(nc, torch, a, b, c, nc.ALGO_SIMT, 0, steps=5, warmup=1)
+    rows, cols = sample_points(512, M, N)
+    ref = oracle.dot_f32_ref(a_h, b_h, rows, cols)
+    absprod = oracle.dot_f32_ref(np.abs(a_h), np.abs(b_h), rows, cols)
+    c_plain = c.cpu().numpy()[rows, cols]
+    nc.gemm(a, b, c, algo=nc.ALGO_SPLIT_BF16, workspace=ws)
+    torch.cuda.synchronize()
+    c_split = c.cpu().numpy()[rows, cols]
+    out["plain"] = {"value": FLOPS / (plain_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+                    "ms_per_step": plain_ms, "kernel": "simt_gemm<float,128,128,8,8,8>"}
+    out["errors_vs_fp64_oracle"] = {
+        "well_scaled": {"split_bf16": sample_errors(c_split, ref, absprod),
+                        "plain_fp32": sample_errors(c_plain, ref, absprod),
+                        "sample": "512 outputs, float64 compensated dot reference"}}
+
+    # ill-scaled: row i of A x 10^u_i, column j of B x 10^v_j
+    u, v = synth.ill_scales(SEED, M, N)
+    tu = torch.from_numpy(u).to(dev)
+    tv = torch.from_numpy(v).to(dev)
+    ai = (a.double() * tu[:, None]).float()
+    bi = (b.double() * tv[None, :]).float()
+    ai_h, bi_h = ai.cpu().numpy(), bi.cpu().numpy()
+    ref_i = oracle.dot_f32_ref(ai_h, bi_h, rows, cols)
+    abs_i = oracle.dot_f32_ref(np.abs(ai_h), np.abs(bi_h), rows, cols)
+    nc.gemm(ai, bi, c, algo=nc.ALGO_SPLIT_BF16, workspace=ws)
+    torch.cuda.synchronize()
+    s_i = c.cpu().numpy()[rows, cols]
+    nc.gemm(ai, bi, c, algo=nc.ALGO_SIMT)
+    torch.cuda.synchronize()
+    p_i = c.cpu().numpy()[rows, cols]
+    out["errors_vs_fp64_oracle"]["ill_scaled"] = {
+        "split_bf16": sample_errors(s_i, ref_i, abs_i),
+        "plain_fp32": sample_errors(p_i, ref_i, abs_i)}
+    del ai, bi
+
+    # e2e: numc_matmul with host arrays (pinned arena), copies in the region
+    nc.set_algo("float32", nc.ALGO_SPLIT_BF16)
+    with nc.Ctx() as ctx:
+        A, B, C = ctx.from_numpy(a_h), ctx.from_numpy(b_h), ctx.zeros((M, N), "float32")
+        nc.matmul(A, B, C)
+        steps = max(3, min(args.steps, 30))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            nc.matmul(A, B, C)
+        e2e_s = (time.perf_counter() - t0) / steps
+    nc.set_algo("float32", nc.ALGO_SIMT)
+    out["e2e"] = {"value": FLOPS / e2e_s / 1e12, "unit": "TFLOP/s",
+                  "h2d_bytes_per_step": 2 * M * K * 4, "d2h_bytes_per_step": M * N * 4,
+                  "ms_per_step": e2e_s * 1e3, "steps": steps,
+                  "api": "numc_matmul(NumcArray host buffers), split-BF16"}
+
+    # config 1: float32 512^3, uniform [-1, 1)
+    a1, b1 = synth.operands("uniform", 512, 512, 512, dtype="float32")
+    ta1, tb1 = torch.from_numpy(a1).to(dev), torch.from_numpy(b1).to(dev)
+    tc1 = torch.empty((512, 512), device=dev)
+    f1 = 2.0 * 512 ** 3
+    ms_p = time_gemm(nc, torch, ta1, tb1, tc1, nc.ALGO_SIMT, 0, steps=200, warmup=10)
+    ms_s = time_gemm(nc, torch, ta1, tb1, tc1, nc.ALGO_SPLIT_BF16, 0, steps=200, warmup=10)
+    out["f32_512"] = {"plain_tflops": f1 / ms_p / 1e9, "split_tflops": f1 / ms_s / 1e9,
+                      "plain_us": ms_p * 1e3, "split_us": ms_s * 1e3,
+                      "note": "L2-resident, latency-bound"}
+
+    # float64 4096^3, uniform [-1,1) x 2^e, e ~ U(-20, 20)
+    a4, b4 = synth.operands("expspread", 4096, 4096, 4096, dtype="float64")
+    ta4, tb4 = torch.from_numpy(a4).to(dev), torch.from_numpy(b4).to(dev)
+    tc4 = torch.empty((4096, 4096), dtype=torch.float64, device=dev)
+    f4 = 2.0 * 4096 ** 3
+    r4, c4 = sample_points(256, 4096, 4096)
+    hi, lo = oracle.dot2_f64(a4, b4, r4, c4)
+    abs4, _ = oracle.dot2_f64(np.abs(a4), np.abs(b4), r4, c4)
+    f64 = {}
+    for name, algo, param in [("simt", nc.ALGO_SIMT, 0), ("dmma", nc.ALGO_DMMA, 0)]:
+        ms4 = time_gemm(nc, torch, ta4, tb4, tc4, algo, param, steps=3, warmup=1)
+        got = tc4.cpu().numpy()[r4, c4]
+        d = np.abs((got - hi) - lo)
+        f64[name] = {"tflops": f4 / ms4 / 1e9, "ms": ms4,
+                     "max_rel": float((d / np.maximum(np.abs(hi), 2.0 ** -60 * abs4)).max()),
+                     "max_rel_to_absprod": float((d / abs4).max())}
+    out["f64_4096"] = f64
+
+    # integer bit-exactness workload, 1024^3, against numc's own outputs
+    import hashlib
+    gold = {cse["name"]: cse for cse in json.load(open(os.path.join(ROOT, "tests", "golden", "golden.json")))["cases"]}
+    ints = {}
+    for dt in ["int8", "uint8", "int32", "int64"]:
+        ai_, bi_ = synth.operands("uniform", 1024, 1024, 1024, dtype=dt)
+        ta_, tb_ = torch.from_numpy(ai_).to(dev), torch.from_numpy(bi_).to(dev)
+        tc_ = torch.empty((1024, 1024), dtype=ta_.dtype, device=dev)
+        ms_ = time_gemm(nc, torch, ta_, tb_, tc_, nc.ALGO_SIMT, nc.INT8_X86_AVX2, steps=20, warmup=2)
+        h = hashlib.sha256(tc_.cpu().numpy().tobytes()).hexdigest()
+        ints[dt] = {"tops": 2.0 * 1024 ** 3 / ms_ / 1e9, "ms": ms_,
+                    "bitexact_vs_numc": h == gold[f"uniform_{dt}_1024x1024x1024"]["sha256"]}
+    out["int_1024"] = ints
+    return out
+
+
+if __name__ == "__main__":
+    main()

@@ -103,6 +103,16 @@ NUMC_API int numc_cuda_check_status(void *stream);
 /* Number of kernels this library has launched since load (diagnostics). */
 NUMC_API uint64_t numc_cuda_launch_count(void);
 
+/* Per-phase timing of the tensor-core GEMMs (split-BF16, Ozaki): when
+ * enabled, each call records CUDA events on its stream around the operand
+ * preparation kernels and around the GEMM kernel.  Enabling resets the
+ * totals.  Do not enable while capturing a CUDA graph. */
+NUMC_API int numc_cuda_phase_timing(int enable);
+/* Sums since enabling, in milliseconds, over `calls` completed calls
+ * (waits for the last recorded call). */
+NUMC_API int numc_cuda_phase_times(double *prep_ms, double *gemm_ms,
+                                   uint64_t *calls);
+
 #ifdef __cplusplus
 }
 #endif

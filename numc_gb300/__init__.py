@@ -100,6 +100,9 @@ SIGNATURES = [
                             _IP, _IP, _IP, _IP, _IP, _IP, _VP, _SZ, _VP]),
     ("numc_cuda_check_status", _I, [_VP]),
     ("numc_cuda_launch_count", ctypes.c_uint64, []),
+    ("numc_cuda_phase_timing", _I, [_I]),
+    ("numc_cuda_phase_times", _I, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                   ctypes.POINTER(ctypes.c_uint64)]),
 ]
 
 
@@ -331,3 +334,14 @@ def check_status(stream=None):
     if stream is None:
         stream = torch.cuda.current_stream()
     return check(lib().numc_cuda_check_status(stream.cuda_stream))
+
+
+def phase_timing(enable):
+    check(lib().numc_cuda_phase_timing(1 if enable else 0))
+
+
+def phase_times():
+    """(prep_ms_total, gemm_ms_total, calls) since phase_timing(True)."""
+    p, g, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+    check(lib().numc_cuda_phase_times(ctypes.byref(p), ctypes.byref(g), ctypes.byref(n)))
+    return p.value, g.value, n.value

@@ -24,6 +24,7 @@
 #include <cstdint>
 
 #include "kernels.h"
+#include "phase_timing.h"
 #include "status.h"
 #include "tc_common.cuh"
 
@@ -335,6 +336,7 @@ cudaError_t launch_split_bf16(const Gemm &g, void *ws_v, size_t ws_bytes, cudaSt
   dim3 ga((unsigned)(L.Kp / 64), (unsigned)((g.M + 31) / 32));
   dim3 gb((unsigned)(L.Kp / 64), (unsigned)((g.N + 31) / 32));
   if (ga.y > 65535 || gb.y > 65535) return cudaErrorInvalidConfiguration;
+  PhaseMark mark(s);
   const unsigned long long gen = ++g_split_gen;
   auto *fa = (unsigned long long *)(ws + L.flags_a), *fbw = (unsigned long long *)(ws + L.flags_b);
   split_f32_bf16<<<ga, 256, 0, s>>>((const float *)g.a, g.rsa, g.csa, g.M, g.K, L.Kp, ahi, alo,
@@ -344,7 +346,10 @@ cudaError_t launch_split_bf16(const Gemm &g, void *ws_v, size_t ws_bytes, cudaSt
   count_launch(2);
   cudaError_t e = cudaGetLastError();
   if (e) return e;
-  return launch_gemm<128, 3>(L, ws, g, gen, s);
+  mark.split_done();
+  e = launch_gemm<128, 3>(L, ws, g, gen, s);
+  mark.gemm_done();
+  return e;
 }
 
 size_t ozaki_workspace(int64_t, int64_t, int64_t, int) { return 0; }

@@ -63,6 +63,14 @@ def normal(seed, stream, shape, dtype=np.float32):
     return z.astype(dtype).reshape(shape)
 
 
+def ill_scales(seed, M, N):
+    """Row factors 10^u_i of A and column factors 10^v_j of B, u, v ~ U(-4, 4),
+    for the ill-scaled workload (applied to the `normal` operands)."""
+    u = uniform(seed, 7, (M,), -4.0, 4.0, np.float64)
+    v = uniform(seed, 8, (N,), -4.0, 4.0, np.float64)
+    return 10.0 ** u, 10.0 ** v
+
+
 # Value ranges of the integer-exactness workload (1024^3).
 INT_RANGES = {
     "int8": (-128, 127), "uint8": (0, 255), "int16": (-32768, 32767),
@@ -76,8 +84,9 @@ def operands(kind, M, K, N, seed=42, dtype="float32"):
 
     uniform     entries uniform in [-1, 1) (float) or INT_RANGES (integers)
     normal      entries N(0, 1)
-    illscaled   N(0, 1) with row i of A times 10^u_i and column j of B times
-                10^v_j, u, v ~ U(-4, 4)
+    illscaled   the `normal` operands with row i of A times 10^u_i and column
+                j of B times 10^v_j, u, v ~ U(-4, 4) (float64 product, then
+                rounded to the dtype)
     expspread   float64 uniform [-1, 1) times 2^e, e integer U(-20, 20)
                 per element
     smallint    numc's own test fill: A[i] = (i % 7) + 1, B[i] = (i % 5) + 1
@@ -97,11 +106,10 @@ def operands(kind, M, K, N, seed=42, dtype="float32"):
     if kind == "normal":
         return normal(seed, 3, (M, K), dt), normal(seed, 4, (K, N), dt)
     if kind == "illscaled":
-        a = normal(seed, 5, (M, K), np.float64)
-        b = normal(seed, 6, (K, N), np.float64)
-        u = uniform(seed, 7, (M, 1), -4.0, 4.0, np.float64)
-        v = uniform(seed, 8, (1, N), -4.0, 4.0, np.float64)
-        return ((a * 10.0 ** u).astype(dt), (b * 10.0 ** v).astype(dt))
+        a, b = normal(seed, 3, (M, K), dt), normal(seed, 4, (K, N), dt)
+        u, v = ill_scales(seed, M, N)
+        return ((a.astype(np.float64) * u[:, None]).astype(dt),
+                (b.astype(np.float64) * v[None, :]).astype(dt))
     if kind == "expspread":
         a = uniform(seed, 9, (M, K), dtype=np.float64)
         b = uniform(seed, 10, (K, N), dtype=np.float64)
