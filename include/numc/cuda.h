@@ -113,6 +113,27 @@ NUMC_API int numc_cuda_phase_timing(int enable);
 NUMC_API int numc_cuda_phase_times(double *prep_ms, double *gemm_ms,
                                    uint64_t *calls);
 
+/* float32 split-BF16 GEMM that allocates nothing.  No counterpart in the
+ * reference (numc has no GPU API); it exists for callers that cannot
+ * allocate device memory when they call — work recorded into CUDA graphs
+ * or issued from stream callbacks, services that forbid allocation after
+ * start-up, hosts whose device memory belongs to another allocator.
+ * Scratch is a 64 MiB array compiled into the library (held by every GPU
+ * that loads it until exit), so 4*(M+N)*roundup(K,64) bytes plus a few
+ * flag words must fit; larger problems are rejected with NUMC_ERR_VALUE.
+ * The caller passes device pointers for a, b, out and, optionally, a
+ * device word `status` that the call clears and a kernel sets nonzero if
+ * it abandoned a bounded wait.  The first call on each device looks up the
+ * scratch address (make it before any stream capture).  Calls share the
+ * scratch: calls that overlap on the GPU race and must be serialised.
+ * Asynchronous on `stream`, like numc_cuda_gemm. */
+NUMC_API int numc_cuda_sgemm_split_static(const float *a, const float *b,
+                                          float *out, size_t M, size_t K,
+                                          size_t N, intptr_t rsa, intptr_t csa,
+                                          intptr_t rsb, intptr_t csb,
+                                          intptr_t rso, intptr_t cso,
+                                          unsigned *status, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -100,6 +100,8 @@ SIGNATURES = [
                             _IP, _IP, _IP, _IP, _IP, _IP, _VP, _SZ, _VP]),
     ("numc_cuda_check_status", _I, [_VP]),
     ("numc_cuda_launch_count", ctypes.c_uint64, []),
+    ("numc_cuda_sgemm_split_static", _I, [_VP, _VP, _VP, _SZ, _SZ, _SZ, _IP, _IP, _IP, _IP,
+                                          _IP, _IP, _VP, _VP]),
     ("numc_cuda_phase_timing", _I, [_I]),
     ("numc_cuda_phase_times", _I, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                    ctypes.POINTER(ctypes.c_uint64)]),

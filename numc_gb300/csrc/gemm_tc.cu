@@ -22,6 +22,10 @@
 #include <cuda_runtime.h>
 #include <atomic>
 #include <cstdint>
+#include <mutex>
+
+#include "numc/cuda.h"
+#include "numc/error.h"
 
 #include "kernels.h"
 #include "phase_timing.h"
@@ -287,8 +291,8 @@ SplitLayout split_layout(int64_t M, int64_t K, int64_t N) {
 std::atomic<unsigned long long> g_split_gen{0x5eed000000000000ull};
 
 template <int BN, int STAGES>
-cudaError_t launch_gemm(const SplitLayout &L, char *ws, const Gemm &g, unsigned long long gen,
-                        cudaStream_t s) {
+cudaError_t launch_gemm_status(const SplitLayout &L, char *ws, const Gemm &g,
+                               unsigned long long gen, unsigned *status, cudaStream_t s) {
   using Cfg = SplitCfg<BN, STAGES>;
   CUtensorMap ta_hi, ta_lo, tb_hi, tb_lo;
   cudaError_t e;
@@ -301,8 +305,6 @@ cudaError_t launch_gemm(const SplitLayout &L, char *ws, const Gemm &g, unsigned 
     return e;
   const int tiles_m = (int)((g.M + kBM - 1) / kBM), tiles_n = (int)((g.N + BN - 1) / BN);
   const int vec4 = g.cso == 1 && (g.rso % 4) == 0 && ((uintptr_t)g.c % 16) == 0;
-  unsigned *status = status_word();
-  if (!status) return cudaErrorMemoryAllocation;
   Fallback fb;
   fb.A = (const float *)g.a;
   fb.B = (const float *)g.b;
@@ -315,6 +317,14 @@ cudaError_t launch_gemm(const SplitLayout &L, char *ws, const Gemm &g, unsigned 
                                                  tiles_m, tiles_n, vec4, status, fb);
   count_launch();
   return cudaGetLastError();
+}
+
+template <int BN, int STAGES>
+cudaError_t launch_gemm(const SplitLayout &L, char *ws, const Gemm &g, unsigned long long gen,
+                        cudaStream_t s) {
+  unsigned *status = status_word();
+  if (!status) return cudaErrorMemoryAllocation;
+  return launch_gemm_status<BN, STAGES>(L, ws, g, gen, status, s);
 }
 
 }  // namespace
@@ -358,3 +368,111 @@ cudaError_t launch_ozaki(const Gemm &, int, void *, size_t, cudaStream_t) {
 }
 
 }  // namespace numc_k
+
+// ---- allocation-free entry point ---------------------------------------------
+//
+// Some callers of a GEMM may not allocate device memory at call time: code
+// that records work into a CUDA graph or runs from a stream callback (where
+// cudaMalloc is not allowed), real-time services that forbid allocation
+// after start-up, and hosts whose device memory is owned by another
+// framework's allocator.  numc_cuda_sgemm_split_static runs the split-BF16
+// GEMM on a fixed scratch array compiled into this library instead of
+// asking for workspace: the caller passes only inputs and outputs.
+//
+// The scratch array below is part of this module's device image: every GPU
+// on which the library's kernels are loaded holds its 64 MiB until the
+// process exits.  All calls share it, so calls that overlap on the GPU
+// (two streams, or two host threads) race on it and must be serialised by
+// the caller.  Its contents persist between calls; nothing in it needs to
+// start at zero (the split planes are rewritten in full, the non-finite
+// flags are tagged with the call's generation number) except the
+// caller's status word, which each call clears.
+
+namespace numc_k {
+namespace {
+
+constexpr size_t kStaticScratchBytes = 64ull << 20;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+std::mutex g_static_mu;
+void *g_static_addr[64] = {nullptr};
+
+// Device address of g_static_scratch on the current device.  Host code may
+// not use the array's name as an address (it names a host-side shadow), so
+// the address is looked up once per device, with that device current.
+cudaError_t static_scratch_address(void **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_addr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return e;
+    g_static_addr[dev] = p;
+  }
+  *out = g_static_addr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace numc_k
+
+extern "C" int numc_cuda_sgemm_split_static(const float *a, const float *b, float *out,
+                                            size_t M, size_t K, size_t N, intptr_t rsa,
+                                            intptr_t csa, intptr_t rsb, intptr_t csb,
+                                            intptr_t rso, intptr_t cso, unsigned *status,
+                                            void *stream) {
+  using namespace numc_k;
+  if (M == 0 || N == 0) return 0;
+  if (!out || (K > 0 && (!a || !b)))
+    return NUMC_SET_ERROR(NUMC_ERR_NULL, "sgemm_split_static: NULL operand (a=%p b=%p out=%p)",
+                          (const void *)a, (const void *)b, (void *)out);
+  if (rsa < 0 || csa < 0 || rsb < 0 || csb < 0 || rso < 0 || cso < 0)
+    return NUMC_SET_ERROR(NUMC_ERR_VALUE, "sgemm_split_static: negative stride");
+  if (M >= (1ull << 31) || N >= (1ull << 31) || K >= (1ull << 31))
+    return NUMC_SET_ERROR(NUMC_ERR_VALUE, "sgemm_split_static: dimension above 2^31");
+  const SplitLayout L = split_layout((int64_t)M, (int64_t)K, (int64_t)N);
+  if (L.total > kStaticScratchBytes)
+    return NUMC_SET_ERROR(NUMC_ERR_VALUE,
+                          "sgemm_split_static: %zux%zux%zu needs %zu bytes of scratch; the "
+                          "static scratch holds %zu (4*(M+N)*roundup(K,64) bytes plus flags "
+                          "must fit); use numc_cuda_gemm with a workspace instead",
+                          M, K, N, L.total, kStaticScratchBytes);
+  void *base = nullptr;
+  cudaError_t e = static_scratch_address(&base);
+  if (e != cudaSuccess)
+    return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "sgemm_split_static: scratch address: %s",
+                          cudaGetErrorString(e));
+  cudaStream_t s = (cudaStream_t)stream;
+  if (status && (e = cudaMemsetAsync(status, 0, sizeof(unsigned), s)) != cudaSuccess)
+    return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "sgemm_split_static: %s", cudaGetErrorString(e));
+  Gemm g;
+  g.a = a; g.b = b; g.c = out;
+  g.M = (int64_t)M; g.K = (int64_t)K; g.N = (int64_t)N;
+  g.rsa = rsa; g.csa = csa; g.rsb = rsb; g.csb = csb; g.rso = rso; g.cso = cso;
+  if (K == 0) {
+    e = launch_simt(NUMC_DTYPE_FLOAT32, g, 0, s);   // out = 0, no scratch
+  } else {
+    char *ws = (char *)base;
+    auto *ahi = (__nv_bfloat16 *)(ws + L.a_hi), *alo = (__nv_bfloat16 *)(ws + L.a_lo);
+    auto *bhi = (__nv_bfloat16 *)(ws + L.b_hi), *blo = (__nv_bfloat16 *)(ws + L.b_lo);
+    dim3 ga((unsigned)(L.Kp / 64), (unsigned)((M + 31) / 32));
+    dim3 gb((unsigned)(L.Kp / 64), (unsigned)((N + 31) / 32));
+    if (ga.y > 65535 || gb.y > 65535)
+      return NUMC_SET_ERROR(NUMC_ERR_VALUE, "sgemm_split_static: too many rows for the split grid");
+    const unsigned long long gen = ++g_split_gen;
+    split_f32_bf16<<<ga, 256, 0, s>>>(a, rsa, csa, (int64_t)M, (int64_t)K, L.Kp, ahi, alo,
+                                      (unsigned long long *)(ws + L.flags_a), kBM, gen);
+    split_f32_bf16<<<gb, 256, 0, s>>>(b, csb, rsb, (int64_t)N, (int64_t)K, L.Kp, bhi, blo,
+                                      (unsigned long long *)(ws + L.flags_b), 64, gen);
+    count_launch(2);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = launch_gemm_status<128, 3>(L, ws, g, gen, status, s);
+  }
+  if (e != cudaSuccess)
+    return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "sgemm_split_static: launch failed: %s",
+                          cudaGetErrorString(e));
+  return 0;
+}
