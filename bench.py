@@ -301,7 +301,7 @@ def main():
     achieved = tensor_flops / (gemm_avg * 1e-3) / 1e12
     roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak,
                 "unit": "TFLOP/s", "frac": achieved / bf16_peak,
-                "traffic": TRAFFIC_PER_LAUNCH, "kernel": "split_bf16_gemm<128,3>",
+                "traffic": TRAFFIC_PER_LAUNCH, "kernel": "split_bf16_gemm<128,3,2,8>",
                 "kernel_ms": gemm_avg, "split_pass_ms": prep_ms / max(1, calls),
                 "peak_source": f"bf16_tflops of {peak_src}",
                 "algorithmic_flops_per_launch": tensor_flops}
@@ -338,7 +338,7 @@ def main():
 
 # DRAM bytes (read + write) of one split_bf16_gemm launch at 8192^3, from the
 # ncu capture summarised in profiles/split_bf16_gemm_f32_8192.md.
-TRAFFIC_PER_LAUNCH = 3.127454e9 + 0.262717e9
+TRAFFIC_PER_LAUNCH = 3.128487e9 + 0.267226e9
 
 
 def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
@@ -354,8 +354,17 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
     c_split = c.cpu().numpy()[rows, cols]
     out["plain"] = {"value": FLOPS / (plain_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
                     "ms_per_step": plain_ms, "kernel": "simt_gemm<float,128,128,8,8,8>"}
+    # six passes (three exact bf16 planes): float32-level error
+    ws6 = torch.empty(nc.workspace_size("float32", nc.ALGO_SPLIT_BF16, 6, M, K, N),
+                      dtype=torch.uint8, device=dev)
+    s6_ms = time_gemm(nc, torch, a, b, c, nc.ALGO_SPLIT_BF16, 6, steps=20, warmup=3, ws=ws6)
+    c_split6 = c.cpu().numpy()[rows, cols]
+    out["split6"] = {"value": FLOPS / (s6_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+                     "ms_per_step": s6_ms, "kernel": "split_bf16_gemm<128,2,3,1>",
+                     "vs_plain": plain_ms / s6_ms}
     out["errors_vs_fp64_oracle"] = {
         "well_scaled": {"split_bf16": sample_errors(c_split, ref, absprod),
+                        "split_bf16_6pass": sample_errors(c_split6, ref, absprod),
                         "plain_fp32": sample_errors(c_plain, ref, absprod),
                         "sample": "512 outputs, float64 compensated dot reference"}}
 
@@ -374,8 +383,13 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
     nc.gemm(ai, bi, c, algo=nc.ALGO_SIMT)
     torch.cuda.synchronize()
     p_i = c.cpu().numpy()[rows, cols]
+    nc.gemm(ai, bi, c, algo=nc.ALGO_SPLIT_BF16, param=6, workspace=ws6)
+    torch.cuda.synchronize()
+    s6_i = c.cpu().numpy()[rows, cols]
+    del ws6
     out["errors_vs_fp64_oracle"]["ill_scaled"] = {
         "split_bf16": sample_errors(s_i, ref_i, abs_i),
+        "split_bf16_6pass": sample_errors(s6_i, ref_i, abs_i),
         "plain_fp32": sample_errors(p_i, ref_i, abs_i)}
     del ai, bi
 

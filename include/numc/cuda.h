@@ -29,9 +29,12 @@ typedef enum {
   NUMC_CUDA_ALGO_DEFAULT = 0,    /* process-wide choice for the dtype */
   NUMC_CUDA_ALGO_SIMT = 1,       /* CUDA cores; every dtype.  float32/64 are
                                     per-output FMA chains in k order */
-  NUMC_CUDA_ALGO_SPLIT_BF16 = 2, /* float32: a = hi + lo in bfloat16,
-                                    hi*hi + hi*lo + lo*hi on tcgen05 with
-                                    float32 accumulation in TMEM */
+  NUMC_CUDA_ALGO_SPLIT_BF16 = 2, /* float32 on tcgen05 from bfloat16 planes
+                                    x = x0 + x1 (+ x2), float32 accumulation
+                                    in TMEM.  `param` = passes: 3 (x0x0 +
+                                    x0x1 + x1x0, default) or 6 (all
+                                    products of order <= 2, float32-level
+                                    error) */
   NUMC_CUDA_ALGO_DMMA = 3,       /* float64: mma.sync f64 tensor path */
   NUMC_CUDA_ALGO_OZAKI = 4,      /* float64: Ozaki slicing, exact integer
                                     slice products on tcgen05, `param` =
@@ -54,7 +57,7 @@ NUMC_API int numc_cuda_device_count(void);
 /* Process-wide algorithm per dtype used by numc_matmul and by
  * NUMC_CUDA_ALGO_DEFAULT.  For float64 OZAKI, `param` is the slice count;
  * for int8/uint8, `param` is a NumcInt8Profile.  Environment defaults:
- * NUMC_CUDA_F32_ALGO (simt|split|auto), NUMC_CUDA_F64_ALGO (simt|dmma|
+ * NUMC_CUDA_F32_ALGO (simt|split|split6|auto), NUMC_CUDA_F64_ALGO (simt|dmma|
  * ozaki[:slices]), NUMC_CUDA_INT8_PROFILE (x86|neon|wrap). */
 NUMC_API int numc_cuda_set_algo(NumcDType dtype, int algo, int param);
 NUMC_API int numc_cuda_get_algo(NumcDType dtype, int *algo, int *param);

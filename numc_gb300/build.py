@@ -57,7 +57,8 @@ def build(verbose=False, extra=()):
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
         return LIB
     tmp = LIB + ".tmp"
-    cmd = [NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread", "-ldl", "-lrt"]
+    cmd = [NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread", "-ldl", "-lrt",
+           "-Xlinker", "--no-undefined"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

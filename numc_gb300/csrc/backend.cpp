@@ -40,7 +40,11 @@ void init_algos_from_env() {
   g_algo[NUMC_DTYPE_UINT8].param = NUMC_INT8_X86_AVX2;
   if (const char *e = getenv("NUMC_CUDA_F32_ALGO")) {
     std::string v(e);
-    if (v == "split") g_algo[NUMC_DTYPE_FLOAT32].algo = NUMC_CUDA_ALGO_SPLIT_BF16;
+    if (v == "split" || v == "split3") g_algo[NUMC_DTYPE_FLOAT32].algo = NUMC_CUDA_ALGO_SPLIT_BF16;
+    if (v == "split6") {
+      g_algo[NUMC_DTYPE_FLOAT32].algo = NUMC_CUDA_ALGO_SPLIT_BF16;
+      g_algo[NUMC_DTYPE_FLOAT32].param = 6;
+    }
     else if (v == "auto") g_algo[NUMC_DTYPE_FLOAT32].algo = NUMC_CUDA_ALGO_AUTO;
   }
   if (const char *e = getenv("NUMC_CUDA_F64_ALGO")) {
@@ -142,12 +146,16 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
     // and the grid fills the GPU.
     algo = ((uint64_t)M * N >= (1u << 16) && K >= 128) ? NUMC_CUDA_ALGO_SPLIT_BF16
                                                       : NUMC_CUDA_ALGO_SIMT;
+    if (param != 6) param = 0;
   }
   switch (algo) {
   case NUMC_CUDA_ALGO_SIMT: break;
   case NUMC_CUDA_ALGO_SPLIT_BF16:
     if (dt != NUMC_DTYPE_FLOAT32)
       return NUMC_SET_ERROR(NUMC_ERR_TYPE, "split-BF16 GEMM is float32 only");
+    if (param == 0) param = 3;
+    if (param != 3 && param != 6)
+      return NUMC_SET_ERROR(NUMC_ERR_VALUE, "split-BF16 pass count %d is not 3 or 6", param);
     break;
   case NUMC_CUDA_ALGO_DMMA:
     if (dt != NUMC_DTYPE_FLOAT64)
@@ -180,7 +188,7 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
 }
 
 size_t plan_workspace(const Plan &p, size_t M, size_t K, size_t N) {
-  if (p.algo == NUMC_CUDA_ALGO_SPLIT_BF16) return numc_k::split_bf16_workspace(M, K, N);
+  if (p.algo == NUMC_CUDA_ALGO_SPLIT_BF16) return numc_k::split_bf16_workspace(M, K, N, p.param);
   if (p.algo == NUMC_CUDA_ALGO_OZAKI) return numc_k::ozaki_workspace(M, K, N, p.param);
   return 0;
 }
@@ -191,7 +199,7 @@ int run_plan(NumcDType dt, const Plan &p, const numc_k::Gemm &g, void *ws,
   switch (p.algo) {
   case NUMC_CUDA_ALGO_SIMT: e = numc_k::launch_simt(dt, g, p.param, s); break;
   case NUMC_CUDA_ALGO_DMMA: e = numc_k::launch_dmma(g, s); break;
-  case NUMC_CUDA_ALGO_SPLIT_BF16: e = numc_k::launch_split_bf16(g, ws, ws_bytes, s); break;
+  case NUMC_CUDA_ALGO_SPLIT_BF16: e = numc_k::launch_split_bf16(g, p.param, ws, ws_bytes, s); break;
   case NUMC_CUDA_ALGO_OZAKI: e = numc_k::launch_ozaki(g, p.param, ws, ws_bytes, s); break;
   }
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");

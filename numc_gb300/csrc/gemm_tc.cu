@@ -1,22 +1,31 @@
-// float32 GEMM as a 3-pass split-BF16 product on the 5th-generation tensor
-// cores (tcgen05), the fast alternative to numc's FP32 FMA GEMM
+// float32 GEMM as a split-BF16 product on the 5th-generation tensor cores
+// (tcgen05), the fast alternative to numc's FP32 FMA GEMM
 // (src/intrinsics/gemm_avx2.h:852 gemm_f32_avx2).
 //
-// Every float32 x is split as x = hi + lo + r with hi = bf16(x) and
-// lo = bf16(x - hi) (|r| <= 2^-17 |x|).  C = A_hi B_hi + A_hi B_lo + A_lo B_hi
-// accumulated in FP32 in tensor memory; the dropped A_lo B_lo term is below
-// 2^-16 of each product.
+// Every float32 x is cut into bfloat16 planes by repeated rounding:
+//   x0 = bf16(x), x1 = bf16(x - x0), x2 = bf16(x - x0 - x1).
+// Each remainder is exact in float32, and x0 + x1 + x2 == x exactly for
+// normal numbers (8 + 8 + 8 significant bits).
+//   2 planes, 3 products:  A0B0 + A0B1 + A1B0           (error ~2^-16 |ab|)
+//   3 planes, 6 products:  ... + A0B2 + A1B1 + A2B0     (error ~2^-24 |ab|)
+// Products of bf16 values are exact in FP32.  Within a chunk of K slabs the
+// products are summed in a tensor-memory FP32 accumulator (smallest terms
+// first); the chunks' partial sums are added in FP32 registers with
+// round-to-nearest, because the tensor core's accumulation truncates at
+// every MMA step and loses hundreds of ulps over a K = 8192 chain.
 //
 // Pass 1 (split kernel, HBM-bound): reads A and B once with any strides and
-// writes hi/lo planes, K-major with K padded to 64 (B is transposed on the
-// way), so both operands suit a 128-byte-swizzled TMA box.
-// Pass 2 (GEMM kernel): one 128 x BN output tile per CTA.  Warp 0 lane 0
-// streams (A_hi, A_lo, B_hi, B_lo) 64-deep K slabs into a STAGES-deep
-// shared-memory ring with TMA; warp 1 lane 0 issues three
-// tcgen05.mma.kind::f16 per 16-deep K step into one FP32 TMEM accumulator
-// and releases ring slots with tcgen05.commit; then all four warps drain
-// TMEM (tcgen05.ld 32x32b) and store the tile.  Tiles are rasterised in
-// groups of 16 row-tiles so the live operand panels stay in L2.
+// writes the planes K-major with K padded to 64 (B is transposed on the
+// way), so every plane suits a 128-byte-swizzled TMA box.
+// Pass 2 (GEMM kernel): one 128 x BN output tile per CTA, ten warps.  Warp
+// 0 streams 64-deep K slabs of every plane of A and B into a STAGES-deep
+// shared-memory ring with TMA (one 3-D tensor map per operand, the plane is
+// the third coordinate); warp 1 issues the tcgen05.mma.kind::f16 products
+// of each chunk into one of four TMEM buffers and releases ring slots with
+// tcgen05.commit; warps 2-9 drain each finished buffer (tcgen05.ld 32x32b)
+// into register accumulators while the next chunk is multiplied, then
+// store the tile.  Tiles are rasterised in groups of 16 row-tiles so the live
+// operand panels stay in L2.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -24,10 +33,9 @@
 #include <cstdint>
 #include <mutex>
 
+#include "kernels.h"
 #include "numc/cuda.h"
 #include "numc/error.h"
-
-#include "kernels.h"
 #include "phase_timing.h"
 #include "status.h"
 #include "tc_common.cuh"
@@ -39,62 +47,118 @@ constexpr int kBM = 128, kBK = 64;
 
 __host__ __device__ inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
-// ---- pass 1: split float32 into bf16 hi/lo planes -------------------------
+// ---- pass 1: split float32 into bf16 planes -------------------------------
 //
-// dst(row, k) = src[row * rs_row + k * rs_k] for row < R, k < K; zero for
-// K <= k < Kp.  hi and lo are R x Kp row-major.  A 32 x 64 tile per block is
-// staged through shared memory so both the read (along whichever source
-// dimension is contiguous) and the write (along k) are coalesced.
+// dst_p(row, k) for row < R, k < Kp: plane p of src[row * rs_row + k * rs_k]
+// (zero for k >= K).  Plane p starts at planes + p * R * Kp.  A 32-row x
+// 128-k tile per block goes through shared memory; reads are float4 along
+// whichever source dimension is contiguous (scalar otherwise), writes are 4
+// bf16 (8 bytes) per thread per plane along k.
 //
-// Non-finite inputs cannot go through the split (inf * lo with lo = 0 gives
+// Non-finite inputs cannot go through the split (inf * x1 with x1 = 0 gives
 // NaN where the true product is infinite), so the block records them: the
-// flag word of the row group (row / flag_rows) is set to `gen`, the call's
-// generation number, and the GEMM recomputes the affected output tiles with
-// plain FMA chains.  Stale flags from earlier calls hold other numbers.
-__global__ void __launch_bounds__(256) split_f32_bf16(const float *__restrict__ src,
-                                                      int64_t rs_row, int64_t rs_k, int64_t R,
-                                                      int64_t K, int64_t Kp,
-                                                      __nv_bfloat16 *__restrict__ hi,
-                                                      __nv_bfloat16 *__restrict__ lo,
-                                                      unsigned long long *flags, int flag_rows,
-                                                      unsigned long long gen) {
-  __shared__ float tile[32][65];
-  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 64;
+// flag word of the row group (row / flag_rows, flag_rows a multiple of 32)
+// is set to `gen`, the call's generation number, and the GEMM recomputes
+// the affected output tiles with plain FMA chains.  Stale flags from
+// earlier calls hold other numbers, so the flags never need clearing.
+constexpr int kSplitRows = 32, kSplitK = 128;
+
+template <int PLANES>
+__global__ void __launch_bounds__(256)
+split_f32_bf16(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_t R,
+               int64_t K, int64_t Kp, __nv_bfloat16 *__restrict__ planes,
+               unsigned long long *flags, int flag_rows, unsigned long long gen, int mode) {
+  __shared__ __align__(16) float tile[kSplitRows][kSplitK + 4];
+  const int64_t r0 = (int64_t)blockIdx.y * kSplitRows, k0 = (int64_t)blockIdx.x * kSplitK;
   const int tid = threadIdx.x;
-  const bool kfast = rs_k == 1 || rs_row != 1;
+  bool bad = false;
+  if (mode == 1) {            // k contiguous, 16-byte aligned rows
 #pragma unroll
-  for (int q = 0; q < 8; q++) {
-    int e = tid + 256 * q;
-    int r = kfast ? e / 64 : e % 32;
-    int k = kfast ? e % 64 : e / 32;
-    int64_t gr = r0 + r, gk = k0 + k;
-    float x = (gr < R && gk < K) ? src[gr * rs_row + gk * rs_k] : 0.0f;
-    if (!isfinite(x)) flags[gr / flag_rows] = gen;
-    tile[r][k] = x;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int q = 0; q < 4; q++) {
-    int e = tid + 256 * q;
-    int r = e / 32, kp = e % 32;
-    int64_t gr = r0 + r;
-    if (gr >= R) continue;
-    __nv_bfloat16 h[2], l[2];
-#pragma unroll
-    for (int t = 0; t < 2; t++) {
-      float x = tile[r][2 * kp + t];
-      __nv_bfloat16 hb = __float2bfloat16_rn(x);
-      float hf = __bfloat162float(hb);
-      if (isinf(hf) && !isinf(x)) {            // rounding overflowed: truncate
-        hb = __float2bfloat16_rz(x);
-        hf = __bfloat162float(hb);
+    for (int q = 0; q < 4; q++) {
+      int e = tid + 256 * q, r = e / 32, k4 = (e % 32) * 4;
+      int64_t gr = r0 + r, gk = k0 + k4;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gr < R) {
+        const float *p = src + gr * rs_row + gk;
+        if (gk + 3 < K) v = *reinterpret_cast<const float4 *>(p);
+        else {
+          if (gk < K) v.x = p[0];
+          if (gk + 1 < K) v.y = p[1];
+          if (gk + 2 < K) v.z = p[2];
+        }
       }
-      h[t] = hb;
-      l[t] = isfinite(x) ? __float2bfloat16_rn(x - hf) : __float2bfloat16_rn(0.0f);
+      bad |= !isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z) || !isfinite(v.w);
+      *reinterpret_cast<float4 *>(&tile[r][k4]) = v;
     }
-    int64_t off = gr * Kp + k0 + 2 * kp;
-    *reinterpret_cast<__nv_bfloat162 *>(hi + off) = __halves2bfloat162(h[0], h[1]);
-    *reinterpret_cast<__nv_bfloat162 *>(lo + off) = __halves2bfloat162(l[0], l[1]);
+  } else if (mode == 2) {     // rows contiguous, 16-byte aligned columns
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      int e = tid + 256 * q, rq = (e % 8) * 4, k = e / 8;
+      int64_t gr = r0 + rq, gk = k0 + k;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gk < K) {
+        const float *p = src + gr + gk * rs_k;
+        if (gr + 3 < R) v = *reinterpret_cast<const float4 *>(p);
+        else {
+          if (gr < R) v.x = p[0];
+          if (gr + 1 < R) v.y = p[1];
+          if (gr + 2 < R) v.z = p[2];
+        }
+      }
+      bad |= !isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z) || !isfinite(v.w);
+      tile[rq][k] = v.x;
+      tile[rq + 1][k] = v.y;
+      tile[rq + 2][k] = v.z;
+      tile[rq + 3][k] = v.w;
+    }
+  } else {                    // general strides
+    const bool kfast = rs_k == 1 || rs_row != 1;
+#pragma unroll 4
+    for (int q = 0; q < 16; q++) {
+      int e = tid + 256 * q;
+      int r = kfast ? e / kSplitK : e % kSplitRows;
+      int k = kfast ? e % kSplitK : e / kSplitRows;
+      int64_t gr = r0 + r, gk = k0 + k;
+      float x = (gr < R && gk < K) ? src[gr * rs_row + gk * rs_k] : 0.0f;
+      bad |= !isfinite(x);
+      tile[r][k] = x;
+    }
+  }
+  if (__syncthreads_or(bad) && tid == 0) flags[r0 / flag_rows] = gen;
+
+  const int warp = tid >> 5, lane = tid & 31;
+  const int64_t plane_elems = R * Kp;
+#pragma unroll
+  for (int rr = 0; rr < kSplitRows / 8; rr++) {
+    const int r = warp + 8 * rr;
+    const int64_t gr = r0 + r, gk = k0 + 4 * lane;
+    if (gr >= R || gk >= Kp) continue;
+    const float4 v = *reinterpret_cast<const float4 *>(&tile[r][4 * lane]);
+    float rem[4] = {v.x, v.y, v.z, v.w};
+    __nv_bfloat16 out[PLANES][4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      const bool finite = isfinite(rem[t]);
+#pragma unroll
+      for (int p = 0; p < PLANES; p++) {
+        __nv_bfloat16 h = __float2bfloat16_rn(rem[t]);
+        float hf = __bfloat162float(h);
+        if (isinf(hf) && finite) {       // rounding overflowed: truncate
+          h = __float2bfloat16_rz(rem[t]);
+          hf = __bfloat162float(h);
+        }
+        out[p][t] = (p == 0 || finite) ? h : __float2bfloat16_rn(0.0f);
+        rem[t] = finite ? rem[t] - hf : 0.0f;
+      }
+    }
+    const int64_t off = gr * Kp + gk;
+#pragma unroll
+    for (int p = 0; p < PLANES; p++) {
+      uint2 w;
+      w.x = (uint32_t)__bfloat16_as_ushort(out[p][0]) | ((uint32_t)__bfloat16_as_ushort(out[p][1]) << 16);
+      w.y = (uint32_t)__bfloat16_as_ushort(out[p][2]) | ((uint32_t)__bfloat16_as_ushort(out[p][3]) << 16);
+      *reinterpret_cast<uint2 *>(planes + p * plane_elems + off) = w;
+    }
   }
 }
 
@@ -109,27 +173,64 @@ struct Fallback {
   unsigned long long gen;
 };
 
-template <int BN, int STAGES>
+template <int BN, int STAGES, int PLANES, int FLUSH>
 struct SplitCfg {
-  static constexpr uint32_t A_BYTES = kBM * kBK * 2;
+  static constexpr uint32_t A_BYTES = kBM * kBK * 2;   // one plane of a K slab of A
   static constexpr uint32_t B_BYTES = BN * kBK * 2;
-  static constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+  static constexpr uint32_t STAGE_BYTES = PLANES * (A_BYTES + B_BYTES);
   static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-  static constexpr uint32_t TMEM_COLS = BN;   // FP32 accumulator columns
+  static constexpr int NBUF = 512 / BN;           // FP32 accumulator buffers in TMEM
+  static constexpr uint32_t TMEM_COLS = NBUF * BN;
+  static constexpr int ACC_WARPS = 8;             // two per TMEM lane quadrant
+  static constexpr int COLS_PER_WARP = BN / 2;
+  static constexpr int THREADS = 64 + 32 * ACC_WARPS;   // producer, MMA, accumulators
+  static_assert(SMEM <= 232448, "shared memory");
+  static_assert(TMEM_COLS <= 512, "tensor memory");
 };
 
-template <int BN, int STAGES>
-__global__ void __launch_bounds__(128, 1)
-split_bf16_gemm(const __grid_constant__ CUtensorMap tAhi, const __grid_constant__ CUtensorMap tAlo,
-                const __grid_constant__ CUtensorMap tBhi, const __grid_constant__ CUtensorMap tBlo,
+// The (A plane, B plane) products summed per K step, smallest first.
+template <int PLANES> struct Products;
+template <> struct Products<2> {
+  static constexpr int n = 3;
+  __device__ static constexpr int a(int t) { return t == 0 ? 1 : 0; }
+  __device__ static constexpr int b(int t) { return t == 1 ? 1 : 0; }
+};
+template <> struct Products<3> {
+  static constexpr int n = 6;
+  // (2,0) (1,1) (0,2) (1,0) (0,1) (0,0)
+  __device__ static constexpr int a(int t) { return t == 0 ? 2 : (t == 1 || t == 3) ? 1 : 0; }
+  __device__ static constexpr int b(int t) { return t == 2 ? 2 : (t == 1 || t == 4) ? 1 : 0; }
+};
+
+// Warp roles (320 threads):
+//   warp 0, lane 0   TMA producer: fills the STAGES-deep ring of K slabs.
+//   warp 1, lane 0   MMA issuer: for chunk c (FLUSH consecutive K slabs),
+//                    accumulates all products into TMEM buffer c % NBUF
+//                    (starting from zero) and commits it to the
+//                    accumulator warps.
+//   warps 2..9       accumulator warps, two per TMEM lane quadrant, each
+//                    owning half of the tile's columns: drain each chunk's
+//                    partial sums from TMEM and add them into FP32
+//                    registers (round to nearest), then release the
+//                    buffer; finally store.
+// The tensor core's own FP32 accumulation truncates at every MMA step; a
+// chain of K/16 x passes steps loses hundreds of ulps at K = 8192, so the
+// chain in TMEM is restarted every FLUSH K slabs and the chunks are summed
+// with correctly rounded FP32 adds.
+template <int BN, int STAGES, int PLANES, int FLUSH>
+__global__ void __launch_bounds__(SplitCfg<BN, STAGES, PLANES, FLUSH>::THREADS, 1)
+split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB,
                 float *__restrict__ C, int64_t rso, int64_t cso, int M, int N, int num_kb,
                 int tiles_m, int tiles_n, int vec4, unsigned *status, Fallback fb) {
-  using Cfg = SplitCfg<BN, STAGES>;
+  using Cfg = SplitCfg<BN, STAGES, PLANES, FLUSH>;
+  using P = Products<PLANES>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *bars = (uint64_t *)(smem + STAGES * Cfg::STAGE_BYTES);
-  uint64_t *full = bars, *empty = bars + STAGES, *accum = bars + 2 * STAGES;
-  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * STAGES + 1);
+  uint64_t *full = bars, *empty = bars + STAGES;
+  constexpr int NBUF = Cfg::NBUF;
+  uint64_t *tfull = bars + 2 * STAGES, *tempty = bars + 2 * STAGES + NBUF;
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * STAGES + 2 * NBUF);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -148,12 +249,13 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tAhi, const __grid_constant_
       tc::mbar_init(tc::smem_u32(&full[s]), 1);
       tc::mbar_init(tc::smem_u32(&empty[s]), 1);
     }
-    tc::mbar_init(tc::smem_u32(accum), 1);
+    for (int b = 0; b < NBUF; b++) {
+      tc::mbar_init(tc::smem_u32(&tfull[b]), 1);
+      tc::mbar_init(tc::smem_u32(&tempty[b]), Cfg::ACC_WARPS);   // one arrive per warp
+    }
     tc::fence_barrier_init();
-    tc::tma_prefetch_desc(&tAhi);
-    tc::tma_prefetch_desc(&tAlo);
-    tc::tma_prefetch_desc(&tBhi);
-    tc::tma_prefetch_desc(&tBlo);
+    tc::tma_prefetch_desc(&tA);
+    tc::tma_prefetch_desc(&tB);
   }
   if (warp == 1) tc::tmem_alloc(tc::smem_u32(tmem_slot), Cfg::TMEM_COLS);
   tc::tc_fence_before();
@@ -161,101 +263,132 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tAhi, const __grid_constant_
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0 && lane == 0) {
-    // TMA producer
-    for (int kb = 0; kb < num_kb; kb++) {
-      const int s = kb % STAGES;
-      if (kb >= STAGES &&
-          !tc::mbar_wait_bounded(tc::smem_u32(&empty[s]), ((kb / STAGES) & 1) ^ 1, status,
-                                 kStatusTimeoutProducer))
-        break;
-      const uint32_t fbar = tc::smem_u32(&full[s]);
-      uint8_t *st = smem + s * Cfg::STAGE_BYTES;
-      tc::mbar_arrive_expect_tx(fbar, Cfg::STAGE_BYTES);
-      const int k = kb * kBK;
-      tc::tma_load_2d(tc::smem_u32(st), &tAhi, fbar, k, m0);
-      tc::tma_load_2d(tc::smem_u32(st + Cfg::A_BYTES), &tAlo, fbar, k, m0);
-      tc::tma_load_2d(tc::smem_u32(st + 2 * Cfg::A_BYTES), &tBhi, fbar, k, n0);
-      tc::tma_load_2d(tc::smem_u32(st + 2 * Cfg::A_BYTES + Cfg::B_BYTES), &tBlo, fbar, k, n0);
-    }
-  } else if (warp == 1 && lane == 0) {
-    // MMA issuer: 3 products per 16-deep K step into one accumulator.
-    constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, BN);
-    for (int kb = 0; kb < num_kb; kb++) {
-      const int s = kb % STAGES;
-      if (!tc::mbar_wait_bounded(tc::smem_u32(&full[s]), (kb / STAGES) & 1, status,
-                                 kStatusTimeoutMma))
-        break;
-      tc::tc_fence_after();
-      const uint32_t st = tc::smem_u32(smem + s * Cfg::STAGE_BYTES);
-      const uint32_t a_hi = st, a_lo = st + Cfg::A_BYTES;
-      const uint32_t b_hi = st + 2 * Cfg::A_BYTES, b_lo = b_hi + Cfg::B_BYTES;
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int kb = 0; kb < num_kb; kb++) {
+        const int s = kb % STAGES;
+        if (kb >= STAGES &&
+            !tc::mbar_wait_bounded(tc::smem_u32(&empty[s]), ((kb / STAGES) & 1) ^ 1, status,
+                                   kStatusTimeoutProducer))
+          break;
+        const uint32_t fbar = tc::smem_u32(&full[s]);
+        const uint32_t st = tc::smem_u32(smem + s * Cfg::STAGE_BYTES);
+        tc::mbar_arrive_expect_tx(fbar, Cfg::STAGE_BYTES);
+        const int k = kb * kBK;
 #pragma unroll
-      for (int kk = 0; kk < kBK / 16; kk++) {
-        const uint32_t koff = kk * 32;   // 16 bf16 = 32 bytes inside the swizzle atom
-        const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
-        tc::mma_bf16(tmem, tc::sdesc_k128(a_lo + koff), tc::sdesc_k128(b_hi + koff), idesc, acc);
-        tc::mma_bf16(tmem, tc::sdesc_k128(a_hi + koff), tc::sdesc_k128(b_lo + koff), idesc, 1u);
-        tc::mma_bf16(tmem, tc::sdesc_k128(a_hi + koff), tc::sdesc_k128(b_hi + koff), idesc, 1u);
-      }
-      tc::mma_commit(tc::smem_u32(&empty[s]));
-    }
-    tc::mma_commit(tc::smem_u32(accum));
-  }
-  __syncwarp();
-
-  // Epilogue: TMEM -> registers -> global.  Warp w owns TMEM lanes
-  // [32w, 32w + 32), i.e. tile rows m0 + 32w + lane.
-  const uint64_t limit = 2000000000ull + (uint64_t)num_kb * 20000ull;
-  const bool ok = tc::mbar_wait_bounded(tc::smem_u32(accum), 0, status, kStatusTimeoutEpilogue, limit);
-  tc::tc_fence_after();
-  bool nonfinite = fb.flags_a[m0 / kBM] == fb.gen;
-#pragma unroll 1
-  for (int c = n0 / 64; c < (n0 + BN) / 64 && c * 64 < N; c++)
-    nonfinite |= fb.flags_b[c] == fb.gen;
-  if (ok && nonfinite) {
-    // numc's arithmetic: one FMA chain per output in k order (slow path).
-    const int row = m0 + warp * 32 + lane;
-#pragma unroll 1
-    for (int c0 = 0; c0 < BN && row < M; c0 += 32) {
-      float acc[32];
-#pragma unroll
-      for (int j = 0; j < 32; j++) acc[j] = 0.0f;
-#pragma unroll 1
-      for (int64_t k = 0; k < fb.K; k++) {
-        const float av = fb.A[(int64_t)row * fb.rsa + k * fb.csa];
-        const float *brow = fb.B + k * fb.rsb;
-#pragma unroll
-        for (int j = 0; j < 32; j++) {
-          const int col = n0 + c0 + j;
-          const float bv = col < N ? brow[(int64_t)col * fb.csb] : 0.0f;
-          acc[j] = __fmaf_rn(av, bv, acc[j]);
+        for (int p = 0; p < PLANES; p++) {
+          tc::tma_load_3d(st + p * Cfg::A_BYTES, &tA, fbar, k, m0, p);
+          tc::tma_load_3d(st + PLANES * Cfg::A_BYTES + p * Cfg::B_BYTES, &tB, fbar, k, n0, p);
         }
       }
-#pragma unroll
-      for (int j = 0; j < 32; j++)
-        if (n0 + c0 + j < N) C[(int64_t)row * rso + (int64_t)(n0 + c0 + j) * cso] = acc[j];
     }
-  } else if (ok) {
-    const int row = m0 + warp * 32 + lane;
-    float *crow = C + (int64_t)row * rso;
-#pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 32) {
-      uint32_t r[32];
-      tc::tmem_ld_32x32b_x32(tmem + ((uint32_t)(warp * 32) << 16) + c0, r);
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, BN);
+      for (int kb = 0; kb < num_kb; kb++) {
+        const int s = kb % STAGES, chunk = kb / FLUSH, buf = chunk % NBUF;
+        const bool chunk_start = kb % FLUSH == 0;
+        const bool chunk_end = kb % FLUSH == FLUSH - 1 || kb == num_kb - 1;
+        if (chunk_start && chunk >= NBUF &&
+            !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / NBUF) & 1) ^ 1,
+                                   status, kStatusTimeoutMma))
+          break;
+        if (!tc::mbar_wait_bounded(tc::smem_u32(&full[s]), (kb / STAGES) & 1, status,
+                                   kStatusTimeoutMma))
+          break;
+        tc::tc_fence_after();
+        const uint32_t st = tc::smem_u32(smem + s * Cfg::STAGE_BYTES);
+        const uint32_t bbase = st + PLANES * Cfg::A_BYTES;
+        const uint32_t acc_tmem = tmem + buf * BN;
+#pragma unroll
+        for (int kk = 0; kk < kBK / 16; kk++) {
+          const uint32_t koff = kk * 32;   // 16 bf16 = 32 bytes inside the swizzle atom
+#pragma unroll
+          for (int t = 0; t < P::n; t++) {
+            const uint32_t acc = (!chunk_start || kk > 0 || t > 0) ? 1u : 0u;
+            tc::mma_bf16(acc_tmem, tc::sdesc_k128(st + P::a(t) * Cfg::A_BYTES + koff),
+                         tc::sdesc_k128(bbase + P::b(t) * Cfg::B_BYTES + koff), idesc, acc);
+          }
+        }
+        tc::mma_commit(tc::smem_u32(&empty[s]));
+        if (chunk_end) tc::mma_commit(tc::smem_u32(&tfull[buf]));
+      }
+    }
+    __syncwarp();
+  } else {
+    // Accumulator warps 2..9: warp w may read TMEM lanes 32 * (w % 4); the
+    // two warps of a quadrant split the columns.
+    constexpr int CW = Cfg::COLS_PER_WARP;
+    const int quad = warp & 3, half = (warp - 2) >> 2;
+    const int row = m0 + quad * 32 + lane;
+    const int cbase = half * CW;
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    float acc[CW];
+#pragma unroll
+    for (int j = 0; j < CW; j++) acc[j] = 0.0f;
+    bool ok = true;
+    const int num_chunks = (num_kb + FLUSH - 1) / FLUSH;
+    for (int chunk = 0; chunk < num_chunks && ok; chunk++) {
+      const int buf = chunk % NBUF;
+      ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / NBUF) & 1, status,
+                                 kStatusTimeoutEpilogue);
+      if (!ok) break;
+      tc::tc_fence_after();
+      uint32_t r[CW];
+#pragma unroll
+      for (int c0 = 0; c0 < CW; c0 += 32)
+        tc::tmem_ld_32x32b_x32(tmem + lane_off + buf * BN + cbase + c0,
+                               *reinterpret_cast<uint32_t(*)[32]>(&r[c0]));
       tc::tmem_ld_wait();
-      if (row < M) {
-        const int nb = n0 + c0;
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tempty[buf]));
+#pragma unroll
+      for (int j = 0; j < CW; j++) acc[j] = __fadd_rn(acc[j], __uint_as_float(r[j]));
+    }
+
+    bool nonfinite = fb.flags_a[m0 / kBM] == fb.gen;
+#pragma unroll 1
+    for (int c = n0 / 64; c < (n0 + BN) / 64 && c * 64 < N; c++)
+      nonfinite |= fb.flags_b[c] == fb.gen;
+    if (ok && nonfinite) {
+      // numc's arithmetic: one FMA chain per output in k order (slow path).
+#pragma unroll 1
+      for (int c0 = cbase; c0 < cbase + CW && row < M; c0 += 32) {
+        float f[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) f[j] = 0.0f;
+#pragma unroll 1
+        for (int64_t k = 0; k < fb.K; k++) {
+          const float av = fb.A[(int64_t)row * fb.rsa + k * fb.csa];
+          const float *brow = fb.B + k * fb.rsb;
+#pragma unroll
+          for (int j = 0; j < 32; j++) {
+            const int col = n0 + c0 + j;
+            const float bv = col < N ? brow[(int64_t)col * fb.csb] : 0.0f;
+            f[j] = __fmaf_rn(av, bv, f[j]);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+          if (n0 + c0 + j < N) C[(int64_t)row * rso + (int64_t)(n0 + c0 + j) * cso] = f[j];
+      }
+    } else if (ok && row < M) {
+      float *crow = C + (int64_t)row * rso;
+#pragma unroll
+      for (int c0 = 0; c0 < CW; c0 += 32) {
+        const int nb = n0 + cbase + c0;
         if (vec4 && nb + 32 <= N) {
           float4 *p = reinterpret_cast<float4 *>(crow + nb);
 #pragma unroll
           for (int j = 0; j < 8; j++)
-            p[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]),
-                               __uint_as_float(r[4 * j + 2]), __uint_as_float(r[4 * j + 3]));
+            p[j] = make_float4(acc[c0 + 4 * j], acc[c0 + 4 * j + 1], acc[c0 + 4 * j + 2],
+                               acc[c0 + 4 * j + 3]);
         } else {
 #pragma unroll
           for (int j = 0; j < 32; j++)
-            if (nb + j < N) crow[(int64_t)(nb + j) * cso] = __uint_as_float(r[j]);
+            if (nb + j < N) crow[(int64_t)(nb + j) * cso] = acc[c0 + j];
         }
       }
     }
@@ -268,20 +401,21 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tAhi, const __grid_constant_
   }
 }
 
+// Workspace: PLANES planes of A (M x Kp), PLANES planes of B^T (N x Kp),
+// then the non-finite flags.
 struct SplitLayout {
+  int planes;
   int64_t Kp;
-  size_t a_hi, a_lo, b_hi, b_lo, flags_a, flags_b, total;
+  size_t a, b, flags_a, flags_b, total;
 };
 
-SplitLayout split_layout(int64_t M, int64_t K, int64_t N) {
+SplitLayout split_layout(int64_t M, int64_t K, int64_t N, int planes) {
   SplitLayout L;
+  L.planes = planes;
   L.Kp = round_up(K > 0 ? K : 1, kBK);
-  size_t a = (size_t)round_up(M * L.Kp * 2, 256), b = (size_t)round_up(N * L.Kp * 2, 256);
-  L.a_hi = 0;
-  L.a_lo = a;
-  L.b_hi = 2 * a;
-  L.b_lo = 2 * a + b;
-  L.flags_a = 2 * a + 2 * b;
+  L.a = 0;
+  L.b = (size_t)round_up(planes * M * L.Kp * 2, 256);
+  L.flags_a = L.b + (size_t)round_up(planes * N * L.Kp * 2, 256);
   L.flags_b = L.flags_a + (size_t)round_up(((M + kBM - 1) / kBM) * 8, 256);
   L.total = L.flags_b + (size_t)round_up(((N + 63) / 64) * 8, 256);
   return L;
@@ -290,17 +424,47 @@ SplitLayout split_layout(int64_t M, int64_t K, int64_t N) {
 // Generation numbers of split calls (never 0; flags hold the last writer's).
 std::atomic<unsigned long long> g_split_gen{0x5eed000000000000ull};
 
-template <int BN, int STAGES>
+int split_mode(const float *p, int64_t rs_row, int64_t rs_k) {
+  if ((uintptr_t)p % 16) return 0;
+  if (rs_k == 1 && rs_row % 4 == 0) return 1;
+  if (rs_row == 1 && rs_k % 4 == 0) return 2;
+  return 0;
+}
+
+// Launch the split pass of both operands.
+cudaError_t launch_split_pass(const SplitLayout &L, char *ws, const Gemm &g,
+                              unsigned long long gen, cudaStream_t s) {
+  dim3 ga((unsigned)((L.Kp + kSplitK - 1) / kSplitK), (unsigned)((g.M + kSplitRows - 1) / kSplitRows));
+  dim3 gb((unsigned)((L.Kp + kSplitK - 1) / kSplitK), (unsigned)((g.N + kSplitRows - 1) / kSplitRows));
+  if (ga.y > 65535 || gb.y > 65535) return cudaErrorInvalidConfiguration;
+  auto *pa = (__nv_bfloat16 *)(ws + L.a), *pb = (__nv_bfloat16 *)(ws + L.b);
+  auto *fa = (unsigned long long *)(ws + L.flags_a), *fb = (unsigned long long *)(ws + L.flags_b);
+  const float *A = (const float *)g.a, *B = (const float *)g.b;
+  const int ma = split_mode(A, g.rsa, g.csa), mb = split_mode(B, g.csb, g.rsb);
+  if (L.planes == 3) {
+    split_f32_bf16<3><<<ga, 256, 0, s>>>(A, g.rsa, g.csa, g.M, g.K, L.Kp, pa, fa, kBM, gen, ma);
+    split_f32_bf16<3><<<gb, 256, 0, s>>>(B, g.csb, g.rsb, g.N, g.K, L.Kp, pb, fb, 64, gen, mb);
+  } else {
+    split_f32_bf16<2><<<ga, 256, 0, s>>>(A, g.rsa, g.csa, g.M, g.K, L.Kp, pa, fa, kBM, gen, ma);
+    split_f32_bf16<2><<<gb, 256, 0, s>>>(B, g.csb, g.rsb, g.N, g.K, L.Kp, pb, fb, 64, gen, mb);
+  }
+  count_launch(2);
+  return cudaGetLastError();
+}
+
+template <int BN, int STAGES, int PLANES, int FLUSH>
 cudaError_t launch_gemm_status(const SplitLayout &L, char *ws, const Gemm &g,
                                unsigned long long gen, unsigned *status, cudaStream_t s) {
-  using Cfg = SplitCfg<BN, STAGES>;
-  CUtensorMap ta_hi, ta_lo, tb_hi, tb_lo;
+  using Cfg = SplitCfg<BN, STAGES, PLANES, FLUSH>;
+  CUtensorMap ta, tb;
   cudaError_t e;
-  if ((e = make_tmap_2d(&ta_hi, ws + L.a_hi, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, g.M, L.Kp, L.Kp, kBM, kBK))) return e;
-  if ((e = make_tmap_2d(&ta_lo, ws + L.a_lo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, g.M, L.Kp, L.Kp, kBM, kBK))) return e;
-  if ((e = make_tmap_2d(&tb_hi, ws + L.b_hi, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, g.N, L.Kp, L.Kp, BN, kBK))) return e;
-  if ((e = make_tmap_2d(&tb_lo, ws + L.b_lo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, g.N, L.Kp, L.Kp, BN, kBK))) return e;
-  auto kern = split_bf16_gemm<BN, STAGES>;
+  if ((e = make_tmap_3d(&ta, ws + L.a, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, PLANES, g.M, L.Kp,
+                        L.Kp, kBM, kBK)))
+    return e;
+  if ((e = make_tmap_3d(&tb, ws + L.b, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, PLANES, g.N, L.Kp,
+                        L.Kp, BN, kBK)))
+    return e;
+  auto kern = split_bf16_gemm<BN, STAGES, PLANES, FLUSH>;
   if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM)))
     return e;
   const int tiles_m = (int)((g.M + kBM - 1) / kBM), tiles_n = (int)((g.N + BN - 1) / BN);
@@ -312,59 +476,52 @@ cudaError_t launch_gemm_status(const SplitLayout &L, char *ws, const Gemm &g,
   fb.flags_a = (const unsigned long long *)(ws + L.flags_a);
   fb.flags_b = (const unsigned long long *)(ws + L.flags_b);
   fb.gen = gen;
-  kern<<<tiles_m * tiles_n, 128, Cfg::SMEM, s>>>(ta_hi, ta_lo, tb_hi, tb_lo, (float *)g.c, g.rso,
-                                                 g.cso, (int)g.M, (int)g.N, (int)(L.Kp / kBK),
-                                                 tiles_m, tiles_n, vec4, status, fb);
+  kern<<<tiles_m * tiles_n, Cfg::THREADS, Cfg::SMEM, s>>>(ta, tb, (float *)g.c, g.rso, g.cso, (int)g.M,
+                                                 (int)g.N, (int)(L.Kp / kBK), tiles_m, tiles_n,
+                                                 vec4, status, fb);
   count_launch();
   return cudaGetLastError();
 }
 
-template <int BN, int STAGES>
+// Flush interval (K slabs per TMEM accumulation chain), measured at
+// 8192^3 on GB300 against a float64 reference (K = 4096 errors):
+//   3 passes: 1 slab 65 % of bf16 peak, 8 slabs 79 %, same error (the
+//             2^-16 split residual dominates) -> 8.
+//   6 passes: 1 slab 82 %, max error 6e-8 |A||B|; 2 slabs 87 %, 1e-7;
+//             plain FP32 FMA 2.3e-7 -> 1, the margin is the point of 6.
 cudaError_t launch_gemm(const SplitLayout &L, char *ws, const Gemm &g, unsigned long long gen,
-                        cudaStream_t s) {
-  unsigned *status = status_word();
-  if (!status) return cudaErrorMemoryAllocation;
-  return launch_gemm_status<BN, STAGES>(L, ws, g, gen, status, s);
+                        unsigned *status, cudaStream_t s) {
+  if (L.planes == 3) return launch_gemm_status<128, 2, 3, 1>(L, ws, g, gen, status, s);
+  return launch_gemm_status<128, 3, 2, 8>(L, ws, g, gen, status, s);
 }
+
+int planes_for(int passes) { return passes == 6 ? 3 : 2; }
 
 }  // namespace
 
-size_t split_bf16_workspace(int64_t M, int64_t K, int64_t N) {
-  return split_layout(M, K, N).total;
+size_t split_bf16_workspace(int64_t M, int64_t K, int64_t N, int passes) {
+  return split_layout(M, K, N, planes_for(passes)).total;
 }
 
-cudaError_t launch_split_bf16(const Gemm &g, void *ws_v, size_t ws_bytes, cudaStream_t s) {
+cudaError_t launch_split_bf16(const Gemm &g, int passes, void *ws_v, size_t ws_bytes,
+                              cudaStream_t s) {
   if (g.M == 0 || g.N == 0) return cudaSuccess;
   if (g.K == 0) return launch_simt(NUMC_DTYPE_FLOAT32, g, 0, s);   // C = 0
   if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31))
     return cudaErrorInvalidValue;
-  const SplitLayout L = split_layout(g.M, g.K, g.N);
+  const SplitLayout L = split_layout(g.M, g.K, g.N, planes_for(passes));
   if (ws_bytes < L.total || ((uintptr_t)ws_v & 255)) return cudaErrorInvalidValue;
   char *ws = (char *)ws_v;
-  auto *ahi = (__nv_bfloat16 *)(ws + L.a_hi), *alo = (__nv_bfloat16 *)(ws + L.a_lo);
-  auto *bhi = (__nv_bfloat16 *)(ws + L.b_hi), *blo = (__nv_bfloat16 *)(ws + L.b_lo);
-  dim3 ga((unsigned)(L.Kp / 64), (unsigned)((g.M + 31) / 32));
-  dim3 gb((unsigned)(L.Kp / 64), (unsigned)((g.N + 31) / 32));
-  if (ga.y > 65535 || gb.y > 65535) return cudaErrorInvalidConfiguration;
+  unsigned *status = status_word();
+  if (!status) return cudaErrorMemoryAllocation;
   PhaseMark mark(s);
   const unsigned long long gen = ++g_split_gen;
-  auto *fa = (unsigned long long *)(ws + L.flags_a), *fbw = (unsigned long long *)(ws + L.flags_b);
-  split_f32_bf16<<<ga, 256, 0, s>>>((const float *)g.a, g.rsa, g.csa, g.M, g.K, L.Kp, ahi, alo,
-                                    fa, kBM, gen);
-  split_f32_bf16<<<gb, 256, 0, s>>>((const float *)g.b, g.csb, g.rsb, g.N, g.K, L.Kp, bhi, blo,
-                                    fbw, 64, gen);
-  count_launch(2);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_split_pass(L, ws, g, gen, s);
   if (e) return e;
   mark.split_done();
-  e = launch_gemm<128, 3>(L, ws, g, gen, s);
+  e = launch_gemm(L, ws, g, gen, status, s);
   mark.gemm_done();
   return e;
-}
-
-size_t ozaki_workspace(int64_t, int64_t, int64_t, int) { return 0; }
-cudaError_t launch_ozaki(const Gemm &, int, void *, size_t, cudaStream_t) {
-  return cudaErrorNotSupported;
 }
 
 }  // namespace numc_k
@@ -433,7 +590,7 @@ extern "C" int numc_cuda_sgemm_split_static(const float *a, const float *b, floa
     return NUMC_SET_ERROR(NUMC_ERR_VALUE, "sgemm_split_static: negative stride");
   if (M >= (1ull << 31) || N >= (1ull << 31) || K >= (1ull << 31))
     return NUMC_SET_ERROR(NUMC_ERR_VALUE, "sgemm_split_static: dimension above 2^31");
-  const SplitLayout L = split_layout((int64_t)M, (int64_t)K, (int64_t)N);
+  const SplitLayout L = split_layout((int64_t)M, (int64_t)K, (int64_t)N, 2);
   if (L.total > kStaticScratchBytes)
     return NUMC_SET_ERROR(NUMC_ERR_VALUE,
                           "sgemm_split_static: %zux%zux%zu needs %zu bytes of scratch; the "
@@ -456,20 +613,9 @@ extern "C" int numc_cuda_sgemm_split_static(const float *a, const float *b, floa
     e = launch_simt(NUMC_DTYPE_FLOAT32, g, 0, s);   // out = 0, no scratch
   } else {
     char *ws = (char *)base;
-    auto *ahi = (__nv_bfloat16 *)(ws + L.a_hi), *alo = (__nv_bfloat16 *)(ws + L.a_lo);
-    auto *bhi = (__nv_bfloat16 *)(ws + L.b_hi), *blo = (__nv_bfloat16 *)(ws + L.b_lo);
-    dim3 ga((unsigned)(L.Kp / 64), (unsigned)((M + 31) / 32));
-    dim3 gb((unsigned)(L.Kp / 64), (unsigned)((N + 31) / 32));
-    if (ga.y > 65535 || gb.y > 65535)
-      return NUMC_SET_ERROR(NUMC_ERR_VALUE, "sgemm_split_static: too many rows for the split grid");
     const unsigned long long gen = ++g_split_gen;
-    split_f32_bf16<<<ga, 256, 0, s>>>(a, rsa, csa, (int64_t)M, (int64_t)K, L.Kp, ahi, alo,
-                                      (unsigned long long *)(ws + L.flags_a), kBM, gen);
-    split_f32_bf16<<<gb, 256, 0, s>>>(b, csb, rsb, (int64_t)N, (int64_t)K, L.Kp, bhi, blo,
-                                      (unsigned long long *)(ws + L.flags_b), 64, gen);
-    count_launch(2);
-    e = cudaGetLastError();
-    if (e == cudaSuccess) e = launch_gemm_status<128, 3>(L, ws, g, gen, status, s);
+    e = launch_split_pass(L, ws, g, gen, s);
+    if (e == cudaSuccess) e = launch_gemm(L, ws, g, gen, status, s);
   }
   if (e != cudaSuccess)
     return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "sgemm_split_static: launch failed: %s",

@@ -31,9 +31,10 @@ cudaError_t launch_simt(NumcDType dt, const Gemm &g, int rule8, cudaStream_t s);
 // float64 on the mma.sync f64 tensor path.
 cudaError_t launch_dmma(const Gemm &g, cudaStream_t s);
 
-// float32 split-BF16 on tcgen05: workspace bytes and launcher.
-size_t split_bf16_workspace(int64_t M, int64_t K, int64_t N);
-cudaError_t launch_split_bf16(const Gemm &g, void *ws, size_t ws_bytes,
+// float32 split-BF16 on tcgen05 with `passes` = 3 (two bf16 planes) or 6
+// (three planes): workspace bytes and launcher.
+size_t split_bf16_workspace(int64_t M, int64_t K, int64_t N, int passes);
+cudaError_t launch_split_bf16(const Gemm &g, int passes, void *ws, size_t ws_bytes,
                               cudaStream_t s);
 
 // float64 Ozaki slicing on tcgen05.

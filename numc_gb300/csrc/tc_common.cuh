@@ -33,6 +33,10 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t byt
                : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -86,6 +90,16 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *m, 
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
       " [%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
       "l"((uint64_t)m), "r"(bar), "r"(x), "r"(y)
+      : "memory");
+}
+
+// 3-D tiled load: box {x, y, 1} at (x, y, z); z selects a plane.
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *m, uint32_t bar,
+                                            int32_t x, int32_t y, int32_t z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+      "l"((uint64_t)m), "r"(bar), "r"(x), "r"(y), "r"(z)
       : "memory");
 }
 
@@ -184,5 +198,13 @@ __device__ __forceinline__ void tmem_ld_wait() {
 cudaError_t make_tmap_2d(CUtensorMap *m, const void *base, CUtensorMapDataType dtype,
                          int elem_bytes, uint64_t rows, uint64_t cols, uint64_t pitch_elems,
                          uint32_t box_rows, uint32_t box_cols);
+
+// Host: `planes` stacked row-major rows x cols matrices (plane pitch
+// rows * pitch_elems elements) as one 3-D tensor map with box
+// {box_cols, box_rows, 1} and 128-byte swizzle; out-of-range rows of a
+// plane read as zero.
+cudaError_t make_tmap_3d(CUtensorMap *m, const void *base, CUtensorMapDataType dtype,
+                         int elem_bytes, uint64_t planes, uint64_t rows, uint64_t cols,
+                         uint64_t pitch_elems, uint32_t box_rows, uint32_t box_cols);
 
 }  // namespace numc_k

@@ -21,16 +21,19 @@ pytestmark = [pytest.mark.gpu, needs_gpu]
 torch = pytest.importorskip("torch")
 
 
-def bound(K):
+def bound(K, passes=3):
+    if passes == 6:
+        # exact 3-plane split; dropped x1*y2 + x2*y1 + x2*y2 <= 3 * 2^-24 |xy|
+        return 3 * 2.0 ** -24 + 2 * (6 * K + 2) * 2.0 ** -24
     return 3 * 2.0 ** -16 + 2 * (3 * K + 2) * 2.0 ** -24
 
 
-def _split(a, b, out=None, ws=None):
+def _split(a, b, out=None, ws=None, passes=3):
     ta = torch.from_numpy(np.ascontiguousarray(a)).cuda()
     tb = torch.from_numpy(np.ascontiguousarray(b)).cuda()
     if out is None:
         out = torch.full((a.shape[0], b.shape[1]), float("nan"), device="cuda")
-    nc.gemm(ta, tb, out, algo=nc.ALGO_SPLIT_BF16, workspace=ws)
+    nc.gemm(ta, tb, out, algo=nc.ALGO_SPLIT_BF16, param=passes, workspace=ws)
     nc.check_status()
     return out.cpu().numpy()
 
@@ -51,13 +54,30 @@ def test_identity_exact():
                                    (1000, 40, 130), (64, 4096, 64)],
                          ids=lambda s: "x".join(map(str, s)))
 @pytest.mark.parametrize("kind", ["uniform", "normal", "illscaled"])
-def test_split_vs_oracle(shape, kind):
+@pytest.mark.parametrize("passes", [3, 6])
+def test_split_vs_oracle(shape, kind, passes):
     M, K, N = shape
     a, b = synth.operands(kind, M, K, N, dtype="float32", seed=3)
-    got = _split(a, b)
+    got = _split(a, b, passes=passes)
     assert np.isfinite(got).all()
     err = rel_err_vs_scale(got, oracle.matmul(a, b), a, b)
-    assert err <= bound(K), (err, bound(K))
+    assert err <= bound(K, passes), (err, bound(K, passes))
+
+
+def test_six_passes_reach_float32_accuracy():
+    # Six passes represent every float32 exactly and the slab partial sums
+    # are added with round-to-nearest, so against a float64-accurate
+    # reference the error must not exceed the plain FP32 FMA chain's, and
+    # must be well below the 3-pass error.
+    M, K, N = 256, 4096, 256
+    a, b = synth.operands("normal", M, K, N, dtype="float32", seed=8)
+    exact = a.astype(np.float64) @ b.astype(np.float64)
+    scale = np.abs(a.astype(np.float64)) @ np.abs(b.astype(np.float64))
+    e3 = np.max(np.abs(_split(a, b, passes=3) - exact) / scale)
+    e6 = np.max(np.abs(_split(a, b, passes=6) - exact) / scale)
+    e_fma = np.max(np.abs(oracle.matmul(a, b) - exact) / scale)
+    assert e6 < e3 / 4, (e6, e3)
+    assert e6 <= e_fma, (e6, e_fma)
 
 
 def test_strided_operands_and_output():
