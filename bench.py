@@ -429,13 +429,21 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
     hi, lo = oracle.dot2_f64(a4, b4, r4, c4)
     abs4, _ = oracle.dot2_f64(np.abs(a4), np.abs(b4), r4, c4)
     f64 = {}
-    for name, algo, param in [("simt", nc.ALGO_SIMT, 0), ("dmma", nc.ALGO_DMMA, 0)]:
-        ms4 = time_gemm(nc, torch, ta4, tb4, tc4, algo, param, steps=3, warmup=1)
+    runs = [("simt", nc.ALGO_SIMT, 0), ("dmma", nc.ALGO_DMMA, 0)] + \
+        [(f"ozaki_s{sl}", nc.ALGO_OZAKI, sl) for sl in (4, 5, 6, 7, 8)]
+    ws4 = torch.empty(nc.workspace_size("float64", nc.ALGO_OZAKI, 8, 4096, 4096, 4096),
+                      dtype=torch.uint8, device=dev)
+    for name, algo, param in runs:
+        ms4 = time_gemm(nc, torch, ta4, tb4, tc4, algo, param, steps=3, warmup=1,
+                        ws=ws4 if algo == nc.ALGO_OZAKI else None)
         got = tc4.cpu().numpy()[r4, c4]
         d = np.abs((got - hi) - lo)
         f64[name] = {"tflops": f4 / ms4 / 1e9, "ms": ms4,
                      "max_rel": float((d / np.maximum(np.abs(hi), 2.0 ** -60 * abs4)).max()),
                      "max_rel_to_absprod": float((d / abs4).max())}
+    f64["ozaki_s8_vs_dmma"] = f64["ozaki_s8"]["tflops"] / f64["dmma"]["tflops"]
+    f64["workload"] = "f64 4096^3, uniform [-1,1) x 2^e, e ~ U(-20,20); errors on 256 outputs vs double-double"
+    del ws4
     out["f64_4096"] = f64
 
     # integer bit-exactness workload, 1024^3, against numc's own outputs

@@ -36,9 +36,10 @@ typedef enum {
                                     products of order <= 2, float32-level
                                     error) */
   NUMC_CUDA_ALGO_DMMA = 3,       /* float64: mma.sync f64 tensor path */
-  NUMC_CUDA_ALGO_OZAKI = 4,      /* float64: Ozaki slicing, exact integer
-                                    slice products on tcgen05, `param` =
-                                    slice count 3..8 */
+  NUMC_CUDA_ALGO_OZAKI = 4,      /* float64: Ozaki slicing into 8-bit
+                                    integer slices, exact slice products on
+                                    tcgen05, integer recombination; `param`
+                                    = slice count 1..8 (default 8) */
   NUMC_CUDA_ALGO_AUTO = 5        /* float32: split-BF16 when the problem is
                                     large enough to pay for it, else SIMT */
 } NumcCudaAlgo;

@@ -52,7 +52,7 @@ void init_algos_from_env() {
     if (v == "dmma") g_algo[NUMC_DTYPE_FLOAT64].algo = NUMC_CUDA_ALGO_DMMA;
     if (v.rfind("ozaki", 0) == 0) {
       g_algo[NUMC_DTYPE_FLOAT64].algo = NUMC_CUDA_ALGO_OZAKI;
-      int s = v.size() > 6 ? atoi(v.c_str() + 6) : 7;
+      int s = v.size() > 6 ? atoi(v.c_str() + 6) : 8;
       g_algo[NUMC_DTYPE_FLOAT64].param = s;
     }
   }
@@ -164,9 +164,9 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
   case NUMC_CUDA_ALGO_OZAKI:
     if (dt != NUMC_DTYPE_FLOAT64)
       return NUMC_SET_ERROR(NUMC_ERR_TYPE, "Ozaki GEMM is float64 only");
-    if (param == 0) param = 7;
-    if (param < 3 || param > 8)
-      return NUMC_SET_ERROR(NUMC_ERR_VALUE, "Ozaki slice count %d outside 3..8", param);
+    if (param == 0) param = 8;
+    if (param < 1 || param > 8)
+      return NUMC_SET_ERROR(NUMC_ERR_VALUE, "Ozaki slice count %d outside 1..8", param);
     break;
   default:
     return NUMC_SET_ERROR(NUMC_ERR_VALUE, "unknown algorithm %d", algo);
