@@ -117,6 +117,48 @@ NUMC_API int numc_cuda_phase_timing(int enable);
 NUMC_API int numc_cuda_phase_times(double *prep_ms, double *gemm_ms,
                                    uint64_t *calls);
 
+/* --- grouped GEMM (many uneven problems, one plan) ------------------------ */
+
+/* One problem of a grouped GEMM: out = a @ b on device pointers with
+ * element strides, as in numc_cuda_gemm. */
+typedef struct {
+  const void *a, *b;
+  void *out;
+  size_t M, K, N;
+  intptr_t rsa, csa, rsb, csb, rso, cso;
+} NumcCudaGemmDesc;
+
+typedef struct NumcCudaGemmPlan NumcCudaGemmPlan;
+
+/* Plan `count` float32 problems once: each problem gets a kernel from the
+ * committed autotune table (split-BF16 with 128- or 64-column tiles, or the
+ * CUDA-core kernel for small problems; `algo` SIMT sends all to the CUDA
+ * cores), the plan allocates its workspace and uploads TMA descriptors and
+ * tile lists.  With SPLIT_BF16, `param` 128 or 64 forces that tile width on
+ * every problem (0 = table).  Pointers in `descs` are fixed from here on.  numc has no
+ * counterpart: its callers loop numc_matmul (src/matmul/matmul.c:347). */
+NUMC_API NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int algo,
+                                                      int param,
+                                                      const NumcCudaGemmDesc *descs,
+                                                      size_t count);
+/* Enqueue every problem of the plan on `stream` (a few launches, no host
+ * synchronisation, no allocation; can be captured in a CUDA graph). */
+NUMC_API int numc_cuda_gemm_plan_run(NumcCudaGemmPlan *plan, void *stream);
+/* The same as one CUDA graph, captured on first use and replayed. */
+NUMC_API int numc_cuda_gemm_plan_run_graph(NumcCudaGemmPlan *plan, void *stream);
+/* Problems per kernel variant and the plan's device bytes. */
+NUMC_API int numc_cuda_gemm_plan_info(const NumcCudaGemmPlan *plan, int *tc128,
+                                      int *tc64, int *simt,
+                                      size_t *workspace_bytes);
+NUMC_API void numc_cuda_gemm_plan_free(NumcCudaGemmPlan *plan);
+
+/* numc_matmul over n independent (a[i], b[i], out[i]) triples in one
+ * grouped launch (float32; other dtypes run one numc_matmul per triple).
+ * Same validation and host/device semantics as numc_matmul. */
+NUMC_API int numc_matmul_grouped(const NumcArray *const *a,
+                                 const NumcArray *const *b,
+                                 NumcArray *const *out, size_t n);
+
 /* float32 split-BF16 GEMM that allocates nothing.  No counterpart in the
  * reference (numc has no GPU API); it exists for callers that cannot
  * allocate device memory when they call — work recorded into CUDA graphs

@@ -100,6 +100,13 @@ SIGNATURES = [
                             _IP, _IP, _IP, _IP, _IP, _IP, _VP, _SZ, _VP]),
     ("numc_cuda_check_status", _I, [_VP]),
     ("numc_cuda_launch_count", ctypes.c_uint64, []),
+    ("numc_cuda_gemm_plan_create", _VP, [_I, _I, _I, _VP, _SZ]),
+    ("numc_cuda_gemm_plan_run", _I, [_VP, _VP]),
+    ("numc_cuda_gemm_plan_run_graph", _I, [_VP, _VP]),
+    ("numc_cuda_gemm_plan_info", _I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(_I),
+                                      ctypes.POINTER(_I), ctypes.POINTER(_SZ)]),
+    ("numc_cuda_gemm_plan_free", None, [_VP]),
+    ("numc_matmul_grouped", _I, [_VP, _VP, _VP, _SZ]),
     ("numc_cuda_sgemm_split_static", _I, [_VP, _VP, _VP, _SZ, _SZ, _SZ, _IP, _IP, _IP, _IP,
                                           _IP, _IP, _VP, _VP]),
     ("numc_cuda_phase_timing", _I, [_I]),
@@ -347,3 +354,60 @@ def phase_times():
     p, g, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
     check(lib().numc_cuda_phase_times(ctypes.byref(p), ctypes.byref(g), ctypes.byref(n)))
     return p.value, g.value, n.value
+
+
+class GemmDesc(ctypes.Structure):
+    """NumcCudaGemmDesc."""
+    _fields_ = [("a", ctypes.c_void_p), ("b", ctypes.c_void_p), ("out", ctypes.c_void_p),
+                ("M", ctypes.c_size_t), ("K", ctypes.c_size_t), ("N", ctypes.c_size_t),
+                ("rsa", ctypes.c_ssize_t), ("csa", ctypes.c_ssize_t),
+                ("rsb", ctypes.c_ssize_t), ("csb", ctypes.c_ssize_t),
+                ("rso", ctypes.c_ssize_t), ("cso", ctypes.c_ssize_t)]
+
+
+class GemmPlan:
+    """A grouped GEMM plan over torch CUDA tensors (a_i @ b_i -> out_i)."""
+
+    def __init__(self, problems, algo=ALGO_SPLIT_BF16, param=0):
+        n = len(problems)
+        self._keep = problems            # tensors must outlive the plan
+        arr = (GemmDesc * max(1, n))()
+        for i, (a, b, out) in enumerate(problems):
+            arr[i] = GemmDesc(a.data_ptr(), b.data_ptr(), out.data_ptr(), a.shape[0],
+                              a.shape[1], b.shape[1], a.stride(0), a.stride(1),
+                              b.stride(0), b.stride(1), out.stride(0), out.stride(1))
+        self.ptr = lib().numc_cuda_gemm_plan_create(CODE["float32"], algo, param, arr, n)
+        if not self.ptr:
+            raise NumcError(*last_error())
+
+    def run(self, stream=None, graph=False):
+        import torch
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        fn = lib().numc_cuda_gemm_plan_run_graph if graph else lib().numc_cuda_gemm_plan_run
+        check(fn(self.ptr, s))
+
+    def info(self):
+        a, b, c, w = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
+        check(lib().numc_cuda_gemm_plan_info(self.ptr, ctypes.byref(a), ctypes.byref(b),
+                                             ctypes.byref(c), ctypes.byref(w)))
+        return {"tc128": a.value, "tc64": b.value, "simt": c.value, "workspace_bytes": w.value}
+
+    def free(self):
+        if self.ptr:
+            lib().numc_cuda_gemm_plan_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def matmul_grouped(As, Bs, Outs):
+    """numc_matmul_grouped over lists of Array."""
+    n = len(As)
+    pa = (ctypes.c_void_p * max(1, n))(*[x.ptr for x in As])
+    pb = (ctypes.c_void_p * max(1, n))(*[x.ptr for x in Bs])
+    po = (ctypes.c_void_p * max(1, n))(*[x.ptr for x in Outs])
+    return check(lib().numc_matmul_grouped(pa, pb, po, n))

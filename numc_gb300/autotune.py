@@ -1,0 +1,67 @@
+"""Autotuner for grouped float32 GEMM plans (run on a GB300).
+
+For every size class of (M, N, K) — classes <=32, <=64, ..., <=1024 — time
+one plan of identical problems on each kernel variant (split-BF16 with
+128-column tiles, split-BF16 with 64-column tiles, CUDA-core FMA) and record
+the fastest in numc_gb300/autotune_table.txt, which plans read at creation.
+
+    python -m numc_gb300.autotune [--out PATH]
+"""
+import argparse
+import os
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPRESENTATIVE = [24, 48, 96, 192, 384, 768]        # one size per class 0..5
+VARIANTS = [(0, "split128", 2, 128), (1, "split64", 2, 64), (2, "simt", 1, 0)]
+
+
+def time_plan(nc, torch, problems, algo, param, reps=5):
+    plan = nc.GemmPlan(problems, algo, param)
+    plan.run(graph=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        plan.run(graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    plan.free()
+    return e0.elapsed_time(e1) / reps
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=os.path.join(HERE, "autotune_table.txt"))
+    args = ap.parse_args()
+    import torch
+    import numc_gb300 as nc
+    lines = ["# grouped float32 GEMM autotune table: mclass nclass kclass variant",
+             "# classes: 0 <=32, 1 <=64, 2 <=128, 3 <=256, 4 <=512, 5 <=1024",
+             "# variants: 0 split-BF16 128-column tiles, 1 split-BF16 64-column tiles,",
+             "#           2 CUDA-core FMA; times are ms per plan run (graph replay)",
+             f"# device: {torch.cuda.get_device_name()}, {time.strftime('%Y-%m-%d')}"]
+    t0 = time.time()
+    for cm, M in enumerate(REPRESENTATIVE):
+        for cn, N in enumerate(REPRESENTATIVE):
+            for ck, K in enumerate(REPRESENTATIVE):
+                count = int(np.clip(2.0 ** 32 / (2.0 * M * N * K), 8, 1024))
+                a = torch.randn(count, M, K, device="cuda")
+                b = torch.randn(count, K, N, device="cuda")
+                c = torch.empty(count, M, N, device="cuda")
+                problems = [(a[i], b[i], c[i]) for i in range(count)]
+                times = {name: time_plan(nc, torch, problems, algo, param)
+                         for _, name, algo, param in VARIANTS}
+                best = min(VARIANTS, key=lambda v: times[v[1]])
+                lines.append(f"{cm} {cn} {ck} {best[0]}   # {M}x{N}x{K} x{count}: " +
+                             " ".join(f"{k}={v:.3f}" for k, v in times.items()))
+                del a, b, c
+    with open(args.out, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    print(f"wrote {args.out} in {time.time() - t0:.0f} s")
+
+
+if __name__ == "__main__":
+    main()

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "kernels.h"
 #include "runtime.h"
@@ -373,6 +374,93 @@ extern "C" int numc_matmul_naive(const NumcArray *a, const NumcArray *b, NumcArr
   int param = (a && (a->dtype == NUMC_DTYPE_INT8 || a->dtype == NUMC_DTYPE_UINT8))
                   ? NUMC_INT8_WRAP : 0;
   return matmul_impl(a, b, out, NUMC_CUDA_ALGO_SIMT, param);
+}
+
+extern "C" int numc_matmul_grouped(const NumcArray *const *a, const NumcArray *const *b,
+                                   NumcArray *const *out, size_t n) {
+  if (n == 0) return 0;
+  if (!a || !b || !out) return NUMC_SET_ERROR(NUMC_ERR_NULL, "matmul_grouped: NULL array list");
+  for (size_t i = 0; i < n; i++) {
+    int err = check_matmul(a[i], b[i], out[i]);
+    if (err) return err;
+    if (a[i]->dtype != a[0]->dtype)
+      return NUMC_SET_ERROR(NUMC_ERR_TYPE, "matmul_grouped: problem %zu dtype differs", i);
+  }
+  if (a[0]->dtype != NUMC_DTYPE_FLOAT32) {
+    for (size_t i = 0; i < n; i++) {
+      int err = numc_matmul(a[i], b[i], out[i]);
+      if (err) return err;
+    }
+    return 0;
+  }
+  ensure_algos();
+  int algo = g_algo[NUMC_DTYPE_FLOAT32].algo.load();
+  if (algo != NUMC_CUDA_ALGO_SIMT) algo = NUMC_CUDA_ALGO_SPLIT_BF16;
+  NumcCtx *ctx = out[0]->ctx;
+  cudaStream_t s;
+  int err = ctx_stream(ctx, &s);
+  if (err) return err;
+
+  // Stage every non-resident operand in the context scratch.
+  const size_t es = 4;
+  std::vector<size_t> off(3 * n, 0);
+  size_t total = 0;
+  bool staged_input = false;
+  for (size_t i = 0; i < n; i++) {
+    const NumcArray *arrs[3] = {a[i], b[i], out[i]};
+    for (int t = 0; t < 3; t++) {
+      if (is_resident(arrs[t])) continue;
+      off[3 * i + t] = total;
+      total += align_up(array_span_bytes(arrs[t]) + 1, 256);
+      if (t < 2) staged_input = true;
+    }
+  }
+  char *scratch = nullptr;
+  if ((err = ctx_scratch(ctx, total + 256, s, &scratch))) return err;
+  std::vector<NumcCudaGemmDesc> descs(n);
+  for (size_t i = 0; i < n; i++) {
+    const NumcArray *arrs[3] = {a[i], b[i], out[i]};
+    char *dev[3];
+    for (int t = 0; t < 3; t++) {
+      if (is_resident(arrs[t])) {
+        dev[t] = arrs[t]->dev_base;
+      } else {
+        dev[t] = scratch + off[3 * i + t];
+        const size_t span = array_span_bytes(arrs[t]);
+        if (span && (t < 2 || span > arrs[t]->capacity))
+          CU(cudaMemcpyAsync(dev[t], arrs[t]->data, span, cudaMemcpyHostToDevice, s), "stage operand");
+      }
+    }
+    NumcCudaGemmDesc &d = descs[i];
+    d.a = dev[0]; d.b = dev[1]; d.out = dev[2];
+    d.M = a[i]->shape[0]; d.K = a[i]->shape[1]; d.N = b[i]->shape[1];
+    d.rsa = a[i]->strides[0] / es; d.csa = a[i]->strides[1] / es;
+    d.rsb = b[i]->strides[0] / es; d.csb = b[i]->strides[1] / es;
+    d.rso = out[i]->strides[0] / es; d.cso = out[i]->strides[1] / es;
+  }
+  NumcCudaGemmPlan *plan = numc_cuda_gemm_plan_create(NUMC_DTYPE_FLOAT32, algo, 0, descs.data(), n);
+  if (!plan) return numc_get_error().code ? numc_get_error().code : NUMC_ERR_INTERNAL;
+  err = numc_cuda_gemm_plan_run(plan, s);
+  for (size_t i = 0; i < n && !err; i++) {
+    if (is_resident(out[i])) {
+      out[i]->residency = kDeviceOnly;
+      continue;
+    }
+    const size_t span = array_span_bytes(out[i]);
+    if (span) {
+      cudaError_t e = cudaMemcpyAsync(out[i]->data, descs[i].out, span, cudaMemcpyDeviceToHost, s);
+      if (e) err = cuda_fail(e, "copy out to host");
+    }
+  }
+  cudaError_t e = cudaStreamSynchronize(s);
+  (void)staged_input;
+  numc_cuda_gemm_plan_free(plan);
+  if (err) return err;
+  if (e) return cuda_fail(e, "cudaStreamSynchronize");
+  unsigned st = 0;
+  CU(numc_k::read_and_clear_status(&st, s), "status read");
+  if (st) return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "grouped kernel abandoned a bounded wait (code %u)", st);
+  return 0;
 }
 
 extern "C" int numc_cuda_device_count(void) { return device_count(); }

@@ -1,0 +1,709 @@
+// Grouped float32 GEMM: many independent matmuls of uneven shape in a few
+// launches, capturable in a CUDA graph.  numc has no grouped entry point —
+// its callers loop numc_matmul (src/matmul/matmul.c:347) once per problem;
+// this is the batched form of that loop.
+//
+// A plan (numc_cuda_gemm_plan_create) fixes the problems, picks a kernel
+// variant per problem from the committed autotune table, lays out an owned
+// device workspace, encodes one TMA descriptor per operand per problem and
+// uploads per-variant tile lists.  Running it enqueues only:
+//   1. a memset of the non-finite flags,
+//   2. one grouped split pass over every tensor-core problem (x -> bf16
+//      planes x0, x1; a block binary-searches its problem in a prefix sum),
+//   3. one persistent split-BF16 tcgen05 kernel per tile width (128 or 64
+//      columns): each CTA walks a static share of the variant's tile list;
+//      the TMA ring, the MMA chunk stream and the TMEM buffers run on
+//      across tiles, so a tile's stores overlap the next tile's MMAs,
+//   4. one grouped CUDA-core kernel (FP32 FMA chains, numc's arithmetic)
+//      for problems too small for the tensor path, and for the plain
+//      algorithm.
+// The tile lists are ordered by K, largest first, so the static
+// round-robin finishes with short tiles.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "numc/cuda.h"
+#include "numc/error.h"
+#include "simt_common.cuh"
+#include "split_common.cuh"
+#include "status.h"
+#include "tc_common.cuh"
+
+namespace numc_k {
+namespace grouped {
+
+constexpr int kBM = 128, kBK = 64, kPlanes = 2;
+
+// Device-side description of one problem.
+struct Prob {
+  const float *A, *B;
+  float *C;
+  int64_t rsa, csa, rsb, csb, rso, cso;
+  int M, N, K, num_kb, Kp;
+  int split_mode_a, split_mode_b;
+  __nv_bfloat16 *pa, *pb;                 // planes (2 x M x Kp, 2 x N x Kp)
+  unsigned long long *flags_a, *flags_b;  // per 128 rows of A, per 64 columns of B
+};
+
+struct Tile {
+  int prob, m0, n0, pad;
+};
+
+// ---- grouped split pass --------------------------------------------------------
+
+// Block b handles split job b: prefix[p] <= b < prefix[p + 1] selects the
+// problem; within it, A tiles (ceil(M/32) x ceil(Kp/128)) come first, then
+// B tiles.
+__global__ void __launch_bounds__(256)
+grouped_split(const Prob *__restrict__ probs, const long long *__restrict__ prefix, int nprob,
+              unsigned long long gen) {
+  __shared__ __align__(16) float tile[kSplitRows][kSplitK + 4];
+  const long long b = blockIdx.x;
+  int lo = 0, hi = nprob - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  const Prob &P = probs[lo];
+  long long j = b - prefix[lo];
+  const long long kt = (P.Kp + kSplitK - 1) / kSplitK;
+  const long long a_jobs = (long long)((P.M + kSplitRows - 1) / kSplitRows) * kt;
+  if (j < a_jobs) {
+    split_tile<kPlanes>(P.A, P.rsa, P.csa, P.M, P.K, P.Kp, P.pa, P.flags_a, kBM, gen,
+                        P.split_mode_a, (j / kt) * kSplitRows, (j % kt) * kSplitK, tile);
+  } else {
+    j -= a_jobs;
+    split_tile<kPlanes>(P.B, P.csb, P.rsb, P.N, P.K, P.Kp, P.pb, P.flags_b, 64, gen,
+                        P.split_mode_b, (j / kt) * kSplitRows, (j % kt) * kSplitK, tile);
+  }
+}
+
+// ---- persistent grouped split-BF16 GEMM -------------------------------------------
+
+template <int BN, int STAGES, int FLUSH>
+struct Cfg {
+  static constexpr uint32_t A_BYTES = kBM * kBK * 2, B_BYTES = BN * kBK * 2;
+  static constexpr uint32_t STAGE_BYTES = kPlanes * (A_BYTES + B_BYTES);
+  static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024 + 256;
+  static constexpr int NBUF = 512 / BN;
+  static constexpr int ACC_WARPS = 8;
+  static constexpr int CW = BN / 2;
+  static constexpr int THREADS = 64 + 32 * ACC_WARPS;
+  static_assert(SMEM <= 232448, "shared memory");
+};
+
+template <int BN, int STAGES, int FLUSH>
+__global__ void __launch_bounds__(Cfg<BN, STAGES, FLUSH>::THREADS, 1)
+grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict__ probs,
+                   const Tile *__restrict__ tiles, int ntiles, unsigned *status,
+                   unsigned long long gen) {
+  using C_ = Cfg<BN, STAGES, FLUSH>;
+  constexpr int NBUF = C_::NBUF;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *bars = (uint64_t *)(smem + STAGES * C_::STAGE_BYTES);
+  uint64_t *full = bars, *empty = bars + STAGES;
+  uint64_t *tfull = bars + 2 * STAGES, *tempty = tfull + NBUF;
+  uint32_t *tmem_slot = (uint32_t *)(tempty + NBUF);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      tc::mbar_init(tc::smem_u32(&full[s]), 1);
+      tc::mbar_init(tc::smem_u32(&empty[s]), 1);
+    }
+    for (int b = 0; b < NBUF; b++) {
+      tc::mbar_init(tc::smem_u32(&tfull[b]), 1);
+      tc::mbar_init(tc::smem_u32(&tempty[b]), C_::ACC_WARPS);
+    }
+    tc::fence_barrier_init();
+  }
+  if (warp == 1) tc::tmem_alloc(tc::smem_u32(tmem_slot), 512);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int g = 0;
+      bool live = true;
+      for (int t = blockIdx.x; t < ntiles && live; t += gridDim.x) {
+        const Tile tl = tiles[t];
+        const int nkb = probs[tl.prob].num_kb;
+        const CUtensorMap *ta = tmaps + 2 * tl.prob, *tb = ta + 1;
+        tc::tensormap_acquire(ta);
+        tc::tensormap_acquire(tb);
+        for (int kb = 0; kb < nkb; kb++, g++) {
+          const int s = g % STAGES;
+          if (g >= STAGES &&
+              !tc::mbar_wait_bounded(tc::smem_u32(&empty[s]), ((g / STAGES) & 1) ^ 1, status,
+                                     kStatusTimeoutProducer)) {
+            live = false;
+            break;
+          }
+          const uint32_t fbar = tc::smem_u32(&full[s]);
+          const uint32_t st = tc::smem_u32(smem + s * C_::STAGE_BYTES);
+          tc::mbar_arrive_expect_tx(fbar, C_::STAGE_BYTES);
+#pragma unroll
+          for (int p = 0; p < kPlanes; p++) {
+            tc::tma_load_3d(st + p * C_::A_BYTES, ta, fbar, kb * kBK, tl.m0, p);
+            tc::tma_load_3d(st + kPlanes * C_::A_BYTES + p * C_::B_BYTES, tb, fbar, kb * kBK,
+                            tl.n0, p);
+          }
+        }
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, BN);
+      int g = 0, chunk = 0;
+      bool live = true;
+      for (int t = blockIdx.x; t < ntiles && live; t += gridDim.x) {
+        const int nkb = probs[tiles[t].prob].num_kb;
+        for (int kb = 0; kb < nkb; kb++, g++) {
+          const int s = g % STAGES, buf = chunk % NBUF;
+          const bool cstart = kb % FLUSH == 0;
+          const bool cend = kb % FLUSH == FLUSH - 1 || kb == nkb - 1;
+          if (cstart && chunk >= NBUF &&
+              !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / NBUF) & 1) ^ 1,
+                                     status, kStatusTimeoutMma)) {
+            live = false;
+            break;
+          }
+          if (!tc::mbar_wait_bounded(tc::smem_u32(&full[s]), (g / STAGES) & 1, status,
+                                     kStatusTimeoutMma)) {
+            live = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint32_t st = tc::smem_u32(smem + s * C_::STAGE_BYTES);
+          const uint32_t a0 = st, a1 = st + C_::A_BYTES;
+          const uint32_t b0 = st + kPlanes * C_::A_BYTES, b1 = b0 + C_::B_BYTES;
+#pragma unroll
+          for (int kk = 0; kk < kBK / 16; kk++) {
+            const uint32_t ko = kk * 32;
+            const uint32_t d = tmem + buf * BN;
+            tc::mma_bf16(d, tc::sdesc_k128(a1 + ko), tc::sdesc_k128(b0 + ko), idesc,
+                         (!cstart || kk > 0) ? 1u : 0u);
+            tc::mma_bf16(d, tc::sdesc_k128(a0 + ko), tc::sdesc_k128(b1 + ko), idesc, 1u);
+            tc::mma_bf16(d, tc::sdesc_k128(a0 + ko), tc::sdesc_k128(b0 + ko), idesc, 1u);
+          }
+          tc::mma_commit(tc::smem_u32(&empty[s]));
+          if (cend) {
+            tc::mma_commit(tc::smem_u32(&tfull[buf]));
+            chunk++;
+          }
+        }
+      }
+    }
+    __syncwarp();
+  } else {
+    constexpr int CW = C_::CW;
+    const int quad = warp & 3, half = (warp - 2) >> 2;
+    const int cbase = half * CW;
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    int chunk = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      const Tile tl = tiles[t];
+      const Prob &P = probs[tl.prob];
+      const int row = tl.m0 + quad * 32 + lane;
+      float acc[CW];
+#pragma unroll
+      for (int j = 0; j < CW; j++) acc[j] = 0.0f;
+      const int nchunks = (P.num_kb + FLUSH - 1) / FLUSH;
+      for (int c = 0; c < nchunks; c++, chunk++) {
+        const int buf = chunk % NBUF;
+        ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / NBUF) & 1, status,
+                                   kStatusTimeoutEpilogue);
+        ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
+        if (!ok) break;
+        tc::tc_fence_after();
+        uint32_t r[CW];
+#pragma unroll
+        for (int c0 = 0; c0 < CW; c0 += 32)
+          tc::tmem_ld_32x32b_x32(tmem + lane_off + buf * BN + cbase + c0,
+                                 *reinterpret_cast<uint32_t(*)[32]>(&r[c0]));
+        tc::tmem_ld_wait();
+        tc::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tempty[buf]));
+#pragma unroll
+        for (int j = 0; j < CW; j++) acc[j] = __fadd_rn(acc[j], __uint_as_float(r[j]));
+      }
+      if (!ok) break;
+      bool nonfinite = P.flags_a[tl.m0 / kBM] == gen;
+      for (int c = tl.n0 / 64; c < (tl.n0 + BN) / 64 && c * 64 < P.N; c++)
+        nonfinite |= P.flags_b[c] == gen;
+      if (row >= P.M) {
+        // rows past M: nothing to store
+      } else if (nonfinite) {
+#pragma unroll 1
+        for (int j = 0; j < CW; j++) {
+          const int col = tl.n0 + cbase + j;
+          if (col >= P.N) break;
+          float f = 0.0f;
+#pragma unroll 1
+          for (int k = 0; k < P.K; k++)
+            f = __fmaf_rn(P.A[(int64_t)row * P.rsa + (int64_t)k * P.csa],
+                          P.B[(int64_t)k * P.rsb + (int64_t)col * P.csb], f);
+          P.C[(int64_t)row * P.rso + (int64_t)col * P.cso] = f;
+        }
+      } else {
+        float *crow = P.C + (int64_t)row * P.rso;
+#pragma unroll
+        for (int j = 0; j < CW; j++) {
+          const int col = tl.n0 + cbase + j;
+          if (col < P.N) crow[(int64_t)col * P.cso] = acc[j];
+        }
+      }
+      __syncwarp();   // reconverge before the next tile's tcgen05.ld
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, 512);
+  }
+}
+
+// ---- grouped CUDA-core kernel ---------------------------------------------------
+
+constexpr int kSimtBM = 128, kSimtBN = 128;
+
+__global__ void __launch_bounds__(simt::kThreads)
+grouped_simt(const Prob *__restrict__ probs, const Tile *__restrict__ tiles) {
+  const Tile tl = tiles[blockIdx.x];
+  const Prob &P = probs[tl.prob];
+  Gemm g;
+  g.a = P.A; g.b = P.B; g.c = P.C;
+  g.M = P.M; g.K = P.K; g.N = P.N;
+  g.rsa = P.rsa; g.csa = P.csa; g.rsb = P.rsb; g.csb = P.csb; g.rso = P.rso; g.cso = P.cso;
+  simt::simt_tile<float, kSimtBM, kSimtBN, 8, 8, 8, simt::kFloat>(g, 0, tl.m0, tl.n0);
+}
+
+}  // namespace grouped
+}  // namespace numc_k
+
+// ---- plans ------------------------------------------------------------------------
+
+using namespace numc_k;
+using namespace numc_k::grouped;
+
+enum Variant : int { kVarTc128 = 0, kVarTc64 = 1, kVarSimt = 2, kNumVar = 3 };
+
+struct NumcCudaGemmPlan {
+  int device;
+  int algo;
+  size_t count;
+  std::vector<Prob> probs;        // host copy
+  std::vector<int> variant;       // per problem
+  char *dev;                      // owned device block
+  size_t dev_bytes;
+  CUtensorMap *d_tmaps;
+  Prob *d_probs;
+  long long *d_prefix;
+  long long split_jobs;
+  int n_split_probs;
+  Prob *d_split_probs;
+  Tile *d_tiles[kNumVar];
+  int ntiles[kNumVar];
+  unsigned long long *flags;      // all flag words (memset per run)
+  size_t flags_bytes;
+  unsigned long long gen;
+  cudaGraphExec_t graph;
+  unsigned graph_kernels;         // kernels per graph replay
+  int sms;
+};
+
+namespace {
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+int size_class(size_t x) {
+  int c = 0;
+  while (x > 32 && c < 6) {   // <=32, <=64, ..., <=1024, >1024
+    x = (x + 1) / 2;
+    c++;
+  }
+  return c;
+}
+
+// The autotune table: "mclass nclass kclass variant" per line (# comments),
+// classes as size_class(); written by numc_gb300/autotune.py on a GB300.
+struct TuneTable {
+  bool loaded = false;
+  int v[7][7][7];
+};
+TuneTable g_tune;
+std::once_flag g_tune_once;
+
+std::string library_dir() {
+  Dl_info info;
+  if (dladdr((void *)&library_dir, &info) && info.dli_fname) {
+    std::string p(info.dli_fname);
+    size_t s = p.rfind('/');
+    if (s != std::string::npos) return p.substr(0, s);
+  }
+  return ".";
+}
+
+void load_tune_table() {
+  for (auto &a : g_tune.v)
+    for (auto &b : a)
+      for (int &c : b) c = -1;
+  const char *env = getenv("NUMC_CUDA_AUTOTUNE_TABLE");
+  std::string path = env ? env : library_dir() + "/autotune_table.txt";
+  FILE *f = fopen(path.c_str(), "r");
+  if (!f) return;
+  char line[256];
+  while (fgets(line, sizeof line, f)) {
+    if (line[0] == '#') continue;
+    int a, b, c, v;
+    if (sscanf(line, "%d %d %d %d", &a, &b, &c, &v) == 4 && a >= 0 && a < 7 && b >= 0 &&
+        b < 7 && c >= 0 && c < 7 && v >= 0 && v < kNumVar) {
+      g_tune.v[a][b][c] = v;
+      g_tune.loaded = true;
+    }
+  }
+  fclose(f);
+}
+
+// Variant for one split-BF16 problem: the tuned choice, else a size rule.
+int pick_variant(size_t M, size_t N, size_t K) {
+  std::call_once(g_tune_once, load_tune_table);
+  if (K == 0) return kVarSimt;
+  const int v = g_tune.v[size_class(M)][size_class(N)][size_class(K)];
+  if (v >= 0) return v;
+  if ((double)M * N * K < (double)(1 << 18)) return kVarSimt;
+  return N <= 64 ? kVarTc64 : kVarTc128;
+}
+
+int fail(cudaError_t e, const char *what) {
+  cudaGetLastError();
+  return NUMC_SET_ERROR(e == cudaErrorMemoryAllocation ? NUMC_ERR_MALLOC : NUMC_ERR_INTERNAL,
+                        "%s: %s", what, cudaGetErrorString(e));
+}
+
+std::atomic<unsigned long long> g_plan_gen{0x9a0c000000000001ull};
+
+template <int BN, int STAGES, int FLUSH>
+cudaError_t prepare_tc() {
+  return cudaFuncSetAttribute(grouped_split_gemm<BN, STAGES, FLUSH>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              Cfg<BN, STAGES, FLUSH>::SMEM);
+}
+
+template <int BN, int STAGES, int FLUSH>
+cudaError_t launch_tc(const NumcCudaGemmPlan *p, int var, unsigned *status, cudaStream_t s) {
+  using C_ = Cfg<BN, STAGES, FLUSH>;
+  auto kern = grouped_split_gemm<BN, STAGES, FLUSH>;
+  const int grid = std::min(p->ntiles[var], p->sms);
+  kern<<<grid, C_::THREADS, C_::SMEM, s>>>(p->d_tmaps, p->d_probs, p->d_tiles[var],
+                                          p->ntiles[var], status, p->gen);
+  return cudaGetLastError();
+}
+
+// Enqueue one run; `kernels` receives the number of kernels launched.
+int plan_enqueue(NumcCudaGemmPlan *p, cudaStream_t s, unsigned *kernels) {
+  *kernels = 0;
+  unsigned *status = status_word();
+  if (!status) return NUMC_SET_ERROR(NUMC_ERR_MALLOC, "status word allocation failed");
+  cudaError_t e;
+  if (p->flags_bytes && (e = cudaMemsetAsync(p->flags, 0, p->flags_bytes, s)))
+    return fail(e, "plan flags");
+  if (p->split_jobs > 0) {
+    grouped_split<<<(unsigned)p->split_jobs, 256, 0, s>>>(p->d_split_probs, p->d_prefix,
+                                                          p->n_split_probs, p->gen);
+    if ((e = cudaGetLastError())) return fail(e, "grouped split");
+    ++*kernels;
+  }
+  if (p->ntiles[kVarTc128]) {
+    if ((e = launch_tc<128, 3, 8>(p, kVarTc128, status, s))) return fail(e, "grouped split-BF16 (128)");
+    ++*kernels;
+  }
+  if (p->ntiles[kVarTc64]) {
+    if ((e = launch_tc<64, 4, 8>(p, kVarTc64, status, s))) return fail(e, "grouped split-BF16 (64)");
+    ++*kernels;
+  }
+  if (p->ntiles[kVarSimt]) {
+    grouped_simt<<<p->ntiles[kVarSimt], simt::kThreads, 0, s>>>(p->d_probs, p->d_tiles[kVarSimt]);
+    if ((e = cudaGetLastError())) return fail(e, "grouped SIMT");
+    ++*kernels;
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int algo, int param,
+                                                        const NumcCudaGemmDesc *descs,
+                                                        size_t count) {
+  if (dtype != NUMC_DTYPE_FLOAT32) {
+    NUMC_SET_ERROR(NUMC_ERR_TYPE, "grouped GEMM plans are float32");
+    return nullptr;
+  }
+  if (algo == NUMC_CUDA_ALGO_DEFAULT || algo == NUMC_CUDA_ALGO_AUTO) algo = NUMC_CUDA_ALGO_SPLIT_BF16;
+  if (algo != NUMC_CUDA_ALGO_SPLIT_BF16 && algo != NUMC_CUDA_ALGO_SIMT) {
+    NUMC_SET_ERROR(NUMC_ERR_VALUE, "grouped GEMM algorithm %d (SIMT or SPLIT_BF16)", algo);
+    return nullptr;
+  }
+  // SPLIT_BF16 param: 0 (or 3) = per-problem choice from the autotune table,
+  // 128 / 64 = every problem on that tile width.
+  if (algo == NUMC_CUDA_ALGO_SPLIT_BF16 && param != 0 && param != 3 && param != -1 &&
+      param != 128 && param != 64) {
+    NUMC_SET_ERROR(NUMC_ERR_VALUE, "grouped split-BF16 param %d (0, 3, 64 or 128)", param);
+    return nullptr;
+  }
+  if (count > 0 && !descs) {
+    NUMC_SET_ERROR(NUMC_ERR_NULL, "plan_create: descs is NULL");
+    return nullptr;
+  }
+  NumcCudaGemmPlan *p = new (std::nothrow) NumcCudaGemmPlan();
+  if (!p) {
+    NUMC_SET_ERROR(NUMC_ERR_MALLOC, "plan allocation failed");
+    return nullptr;
+  }
+  p->algo = algo;
+  p->count = count;
+  p->dev = nullptr;
+  p->graph = nullptr;
+  p->graph_kernels = 0;
+  p->gen = ++g_plan_gen;
+  if (cudaGetDevice(&p->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess) {
+    cudaGetLastError();
+    delete p;
+    NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "plan_create: no CUDA device");
+    return nullptr;
+  }
+
+  // Problems, variants and the device layout.
+  std::vector<size_t> plane_off(count, 0), flag_off(count, 0);
+  size_t planes_bytes = 0, flags_bytes = 0;
+  p->probs.resize(count);
+  p->variant.resize(count);
+  for (size_t i = 0; i < count; i++) {
+    const NumcCudaGemmDesc &d = descs[i];
+    if (d.M >= (1u << 30) || d.N >= (1u << 30) || d.K >= (1u << 30) ||
+        (d.M && d.N && (!d.out || (d.K && (!d.a || !d.b)))) || d.rsa < 0 || d.csa < 0 ||
+        d.rsb < 0 || d.csb < 0 || d.rso < 0 || d.cso < 0) {
+      delete p;
+      NUMC_SET_ERROR(NUMC_ERR_VALUE, "plan_create: invalid problem %zu", i);
+      return nullptr;
+    }
+    Prob &P = p->probs[i];
+    memset(&P, 0, sizeof P);
+    P.A = (const float *)d.a; P.B = (const float *)d.b; P.C = (float *)d.out;
+    P.rsa = d.rsa; P.csa = d.csa; P.rsb = d.rsb; P.csb = d.csb; P.rso = d.rso; P.cso = d.cso;
+    P.M = (int)d.M; P.N = (int)d.N; P.K = (int)d.K;
+    P.Kp = (int)align_up(d.K ? d.K : 1, kBK);
+    P.num_kb = P.Kp / kBK;
+    int v = algo == NUMC_CUDA_ALGO_SIMT ? kVarSimt
+            : param == 128             ? (d.K ? kVarTc128 : kVarSimt)
+            : param == 64              ? (d.K ? kVarTc64 : kVarSimt)
+                                       : pick_variant(d.M, d.N, d.K);
+    if (d.M == 0 || d.N == 0) v = -1;
+    p->variant[i] = v;
+    if (v == kVarTc128 || v == kVarTc64) {
+      plane_off[i] = planes_bytes;
+      planes_bytes += align_up((size_t)kPlanes * P.Kp * (d.M + d.N) * 2, 256);
+      flag_off[i] = flags_bytes;
+      flags_bytes += align_up(((d.M + kBM - 1) / kBM + (d.N + 63) / 64) * 8, 256);
+      P.split_mode_a = split_mode(P.A, P.rsa, P.csa);
+      P.split_mode_b = split_mode(P.B, P.csb, P.rsb);
+    }
+  }
+  // Tile lists, problems sorted by K (largest first) within each variant.
+  std::vector<size_t> order(count);
+  for (size_t i = 0; i < count; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t x, size_t y) { return p->probs[x].K > p->probs[y].K; });
+  std::vector<Tile> tiles[kNumVar];
+  std::vector<size_t> split_idx;
+  for (size_t i : order) {
+    const int v = p->variant[i];
+    if (v < 0) continue;
+    const int bn = v == kVarTc128 ? 128 : v == kVarTc64 ? 64 : kSimtBN;
+    const int bm = v == kVarSimt ? kSimtBM : kBM;
+    for (int m0 = 0; m0 < p->probs[i].M; m0 += bm)
+      for (int n0 = 0; n0 < p->probs[i].N; n0 += bn) tiles[v].push_back(Tile{(int)i, m0, n0, 0});
+    if (v != kVarSimt) split_idx.push_back(i);
+  }
+  std::vector<long long> prefix(split_idx.size() + 1, 0);
+  for (size_t q = 0; q < split_idx.size(); q++) {
+    const Prob &P = p->probs[split_idx[q]];
+    const long long kt = (P.Kp + kSplitK - 1) / kSplitK;
+    prefix[q + 1] = prefix[q] + ((P.M + kSplitRows - 1) / kSplitRows) * kt +
+                    ((P.N + kSplitRows - 1) / kSplitRows) * kt;
+  }
+  p->split_jobs = prefix.back();
+  p->n_split_probs = (int)split_idx.size();
+  if (p->split_jobs > 0x7FFFFFFFll) {
+    delete p;
+    NUMC_SET_ERROR(NUMC_ERR_VALUE, "plan_create: too many split blocks");
+    return nullptr;
+  }
+
+  // One device block: tmaps | probs | split probs | prefix | tiles | flags | planes.
+  size_t off = 0;
+  const size_t o_tmaps = off; off = align_up(off + count * 2 * sizeof(CUtensorMap), 256);
+  const size_t o_probs = off; off = align_up(off + count * sizeof(Prob), 256);
+  const size_t o_sprobs = off; off = align_up(off + split_idx.size() * sizeof(Prob), 256);
+  const size_t o_prefix = off; off = align_up(off + prefix.size() * sizeof(long long), 256);
+  size_t o_tiles[kNumVar];
+  for (int v = 0; v < kNumVar; v++) {
+    o_tiles[v] = off;
+    off = align_up(off + tiles[v].size() * sizeof(Tile), 256);
+  }
+  const size_t o_flags = off; off = align_up(off + flags_bytes, 256);
+  const size_t o_planes = off; off += planes_bytes;
+  p->dev_bytes = off;
+  cudaError_t e = cudaMalloc(&p->dev, off ? off : 256);
+  if (e) {
+    delete p;
+    fail(e, "plan workspace");
+    return nullptr;
+  }
+  p->d_tmaps = (CUtensorMap *)(p->dev + o_tmaps);
+  p->d_probs = (Prob *)(p->dev + o_probs);
+  p->d_split_probs = (Prob *)(p->dev + o_sprobs);
+  p->d_prefix = (long long *)(p->dev + o_prefix);
+  for (int v = 0; v < kNumVar; v++) {
+    p->d_tiles[v] = (Tile *)(p->dev + o_tiles[v]);
+    p->ntiles[v] = (int)tiles[v].size();
+  }
+  p->flags = (unsigned long long *)(p->dev + o_flags);
+  p->flags_bytes = flags_bytes;
+
+  std::vector<CUtensorMap> tm(count * 2);
+  memset(tm.data(), 0, tm.size() * sizeof(CUtensorMap));
+  for (size_t i = 0; i < count; i++) {
+    Prob &P = p->probs[i];
+    const int v = p->variant[i];
+    if (v != kVarTc128 && v != kVarTc64) continue;
+    P.pa = (__nv_bfloat16 *)(p->dev + o_planes + plane_off[i]);
+    P.pb = P.pa + (size_t)kPlanes * P.M * P.Kp;
+    P.flags_a = (unsigned long long *)(p->dev + o_flags + flag_off[i]);
+    P.flags_b = P.flags_a + (P.M + kBM - 1) / kBM;
+    const uint32_t bn = v == kVarTc128 ? 128 : 64;
+    if ((e = make_tmap_3d(&tm[2 * i], P.pa, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, kPlanes, P.M,
+                          P.Kp, P.Kp, kBM, kBK)) ||
+        (e = make_tmap_3d(&tm[2 * i + 1], P.pb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, kPlanes,
+                          P.N, P.Kp, P.Kp, bn, kBK))) {
+      numc_cuda_gemm_plan_free(p);
+      fail(e, "plan tensor maps");
+      return nullptr;
+    }
+  }
+  // Kernel attributes are set here, not per run, so runs can be captured.
+  if ((e = prepare_tc<128, 3, 8>()) || (e = prepare_tc<64, 4, 8>()) || !status_word()) {
+    numc_cuda_gemm_plan_free(p);
+    fail(e ? e : cudaErrorMemoryAllocation, "plan kernel setup");
+    return nullptr;
+  }
+  std::vector<Prob> sp(split_idx.size());
+  for (size_t q = 0; q < split_idx.size(); q++) sp[q] = p->probs[split_idx[q]];
+  if ((e = cudaMemcpy(p->d_tmaps, tm.data(), tm.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(p->d_probs, p->probs.data(), count * sizeof(Prob), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(p->d_split_probs, sp.data(), sp.size() * sizeof(Prob), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(p->d_prefix, prefix.data(), prefix.size() * sizeof(long long), cudaMemcpyHostToDevice))) {
+    numc_cuda_gemm_plan_free(p);
+    fail(e, "plan upload");
+    return nullptr;
+  }
+  for (int v = 0; v < kNumVar; v++)
+    if (!tiles[v].empty() &&
+        (e = cudaMemcpy(p->d_tiles[v], tiles[v].data(), tiles[v].size() * sizeof(Tile),
+                        cudaMemcpyHostToDevice))) {
+      numc_cuda_gemm_plan_free(p);
+      fail(e, "plan upload");
+      return nullptr;
+    }
+  return p;
+}
+
+extern "C" int numc_cuda_gemm_plan_run(NumcCudaGemmPlan *p, void *stream) {
+  if (!p) return NUMC_SET_ERROR(NUMC_ERR_NULL, "plan_run: plan is NULL");
+  unsigned k = 0;
+  const int err = plan_enqueue(p, (cudaStream_t)stream, &k);
+  count_launch(k);
+  return err;
+}
+
+extern "C" int numc_cuda_gemm_plan_run_graph(NumcCudaGemmPlan *p, void *stream) {
+  if (!p) return NUMC_SET_ERROR(NUMC_ERR_NULL, "plan_run_graph: plan is NULL");
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e;
+  if (!p->graph) {
+    // Capture on a private stream so that the caller's stream may be the
+    // legacy default stream.
+    cudaStream_t cs;
+    if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking))) return fail(e, "capture stream");
+    status_word();   // allocate before capture
+    cudaGraph_t graph = nullptr;
+    int err = 0;
+    if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal))) {
+      cudaStreamDestroy(cs);
+      return fail(e, "begin capture");
+    }
+    err = plan_enqueue(p, cs, &p->graph_kernels);
+    e = cudaStreamEndCapture(cs, &graph);
+    cudaStreamDestroy(cs);
+    if (err) {
+      if (graph) cudaGraphDestroy(graph);
+      return err;
+    }
+    if (e) return fail(e, "end capture");
+    e = cudaGraphInstantiate(&p->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e) {
+      p->graph = nullptr;
+      return fail(e, "graph instantiate");
+    }
+  }
+  if ((e = cudaGraphLaunch(p->graph, s))) return fail(e, "graph launch");
+  count_launch(p->graph_kernels);
+  return 0;
+}
+
+extern "C" int numc_cuda_gemm_plan_info(const NumcCudaGemmPlan *p, int *tc128, int *tc64,
+                                        int *simt, size_t *workspace_bytes) {
+  if (!p) return NUMC_SET_ERROR(NUMC_ERR_NULL, "plan_info: plan is NULL");
+  int c[kNumVar] = {0, 0, 0};
+  for (int v : p->variant)
+    if (v >= 0) c[v]++;
+  if (tc128) *tc128 = c[kVarTc128];
+  if (tc64) *tc64 = c[kVarTc64];
+  if (simt) *simt = c[kVarSimt];
+  if (workspace_bytes) *workspace_bytes = p->dev_bytes;
+  return 0;
+}
+
+extern "C" void numc_cuda_gemm_plan_free(NumcCudaGemmPlan *p) {
+  if (!p) return;
+  if (p->graph) cudaGraphExecDestroy(p->graph);
+  if (p->dev) {
+    cudaDeviceSynchronize();   // work queued from this plan may still read it
+    cudaFree(p->dev);
+  }
+  delete p;
+}

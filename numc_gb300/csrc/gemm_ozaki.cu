@@ -321,6 +321,7 @@ ozaki_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
         const int buf = chunk % kNumBuf;
         ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / kNumBuf) & 1, status,
                                    kStatusTimeoutEpilogue);
+        ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
         if (!ok) break;
         tc::tc_fence_after();
 #pragma unroll

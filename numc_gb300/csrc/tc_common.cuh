@@ -103,6 +103,13 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *m, 
       : "memory");
 }
 
+// Order earlier writes of a tensor map in global memory (made by copies
+// before this kernel) before its use by TMA through the tensormap proxy.
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap *m) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"((uint64_t)m)
+               : "memory");
+}
+
 // ---- TMEM ---------------------------------------------------------------------
 
 // Executed by one full warp.  Writes the TMEM base address to *dst_smem.

@@ -1,0 +1,160 @@
+"""Grouped float32 GEMM plans (numc_cuda_gemm_plan_*, numc_matmul_grouped).
+
+Every problem of a plan must match the oracle: the CUDA-core variant is
+numc's FMA chain (same bound as the single-problem SIMT kernel), the
+split-BF16 variants meet the 3-pass bound of test_gpu_split.py.  Plans run
+directly, replayed as CUDA graphs with changed inputs, and captured by the
+caller (an MLP chain, two dependent plans in one graph).
+"""
+import numpy as np
+import pytest
+
+import numc_gb300 as nc
+import oracle
+from numc_gb300 import synth
+
+from gpu_util import needs_gpu, rel_err_vs_scale
+
+pytestmark = [pytest.mark.gpu, needs_gpu]
+torch = pytest.importorskip("torch")
+
+
+def split_bound(K):
+    return 3 * 2.0 ** -16 + 2 * (3 * K + 2) * 2.0 ** -24
+
+
+def simt_bound(K):
+    return (K + 2) * 2.0 ** -24
+
+
+def random_problems(n, lo=16, hi=1024, seed=0):
+    rng = np.random.default_rng(seed)
+    dims = np.exp(rng.uniform(np.log(lo), np.log(hi), (n, 3))).round().astype(int)
+    probs = []
+    for i, (M, N, K) in enumerate(dims):
+        a, b = synth.operands("uniform", M, K, N, dtype="float32", seed=1000 + i)
+        ta = torch.from_numpy(a).cuda()
+        tb = torch.from_numpy(b).cuda()
+        out = torch.full((M, N), float("nan"), device="cuda")
+        probs.append((ta, tb, out, a, b))
+    return probs
+
+
+def check_all(probs, bound):
+    for ta, tb, out, a, b in probs:
+        got = out.cpu().numpy()
+        assert np.isfinite(got).all()
+        assert rel_err_vs_scale(got, oracle.matmul(a, b), a, b) <= bound(a.shape[1])
+
+
+@pytest.mark.parametrize("param", [0, 128, 64])
+def test_split_plan_matches_oracle(param):
+    probs = random_problems(40, seed=1)
+    plan = nc.GemmPlan([(p[0], p[1], p[2]) for p in probs], nc.ALGO_SPLIT_BF16, param)
+    plan.run()
+    nc.check_status()
+    check_all(probs, lambda K: max(split_bound(K), simt_bound(K)))
+    info = plan.info()
+    assert sum(info[k] for k in ("tc128", "tc64", "simt")) == 40
+    if param == 128:
+        assert info["tc128"] == 40
+    plan.free()
+
+
+def test_simt_plan_is_numc_arithmetic():
+    probs = random_problems(30, hi=300, seed=2)
+    plan = nc.GemmPlan([(p[0], p[1], p[2]) for p in probs], nc.ALGO_SIMT)
+    plan.run()
+    torch.cuda.synchronize()
+    for ta, tb, out, a, b in probs:
+        single = torch.empty_like(out)
+        nc.gemm(ta, tb, single, algo=nc.ALGO_SIMT)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(out.cpu().numpy(), single.cpu().numpy())
+    check_all(probs, simt_bound)
+
+
+def test_graph_replay_sees_new_inputs():
+    probs = random_problems(12, seed=3)
+    plan = nc.GemmPlan([(p[0], p[1], p[2]) for p in probs], nc.ALGO_SPLIT_BF16)
+    plan.run(graph=True)
+    for ta, tb, out, a, b in probs:     # new values, same buffers
+        ta.mul_(-2.0)
+    plan.run(graph=True)
+    nc.check_status()
+    for ta, tb, out, a, b in probs:
+        got = out.cpu().numpy()
+        a2 = a * np.float32(-2.0)
+        assert rel_err_vs_scale(got, oracle.matmul(a2, b), a2, b) <= \
+            max(split_bound(a.shape[1]), simt_bound(a.shape[1]))
+
+
+def test_mlp_chains_in_one_captured_graph():
+    # 16 chains X[256,784] @ W1[784,128] -> H; H @ W2[128,10] -> Y
+    chains = []
+    for c in range(16):
+        x = synth.uniform(7, 100 + c, (256, 784))
+        w1 = (0.05 * synth.normal(7, 200 + c, (784, 128))).astype(np.float32)
+        w2 = (0.05 * synth.normal(7, 300 + c, (128, 10))).astype(np.float32)
+        t = [torch.from_numpy(v).cuda() for v in (x, w1, w2)]
+        h = torch.empty((256, 128), device="cuda")
+        y = torch.empty((256, 10), device="cuda")
+        chains.append((x, w1, w2, t, h, y))
+    p1 = nc.GemmPlan([(t[0], t[1], h) for _, _, _, t, h, _ in chains])
+    p2 = nc.GemmPlan([(h, t[2], y) for _, _, _, t, h, y in chains])
+    s = torch.cuda.Stream()
+    p1.run(stream=s)           # warm (first use loads kernels)
+    p2.run(stream=s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        p1.run(stream=s)
+        p2.run(stream=s)
+    for _, _, _, _, h, y in chains:
+        h.zero_(); y.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    nc.check_status()
+    for x, w1, w2, t, h, y in chains:
+        ref_h = oracle.matmul(x, w1)
+        assert rel_err_vs_scale(h.cpu().numpy(), ref_h, x, w1) <= split_bound(784)
+        ref_y = oracle.matmul(ref_h, w2)
+        err = np.abs(y.cpu().numpy().astype(np.float64) - ref_y)
+        assert err.max() <= 1e-4 * (np.abs(ref_h) @ np.abs(w2)).max()
+
+
+def test_numc_matmul_grouped_host_arrays():
+    rng = np.random.default_rng(4)
+    with nc.Ctx() as ctx:
+        As, Bs, Cs, refs = [], [], [], []
+        for i in range(10):
+            M, K, N = rng.integers(1, 300, 3)
+            a, b = synth.operands("uniform", M, K, N, dtype="float32", seed=i)
+            A, B = ctx.from_numpy(a), ctx.from_numpy(b)
+            if i % 3 == 0:
+                A.to_device()
+            As.append(A); Bs.append(B); Cs.append(ctx.zeros((M, N), "float32"))
+            refs.append((a, b))
+        nc.matmul_grouped(As, Bs, Cs)
+        for C, (a, b) in zip(Cs, refs):
+            K = a.shape[1]
+            assert rel_err_vs_scale(C.numpy(), oracle.matmul(a, b), a, b) <= \
+                max(split_bound(K), simt_bound(K))
+        # integer dtypes loop numc_matmul, bit-exact
+        a, b = synth.operands("uniform", 50, 600, 40, dtype="int8")
+        A, B, C = ctx.from_numpy(a), ctx.from_numpy(b), ctx.zeros((50, 40), "int8")
+        nc.matmul_grouped([A], [B], [C])
+        np.testing.assert_array_equal(C.numpy(), oracle.matmul(a, b))
+
+
+def test_empty_and_degenerate_problems():
+    z = torch.zeros((0, 5), device="cuda")
+    w = torch.ones((5, 3), device="cuda")
+    e = torch.zeros((0, 3), device="cuda")
+    a = torch.ones((4, 0), device="cuda")
+    b = torch.ones((0, 6), device="cuda")
+    o = torch.full((4, 6), 3.0, device="cuda")
+    plan = nc.GemmPlan([(z, w, e), (a, b, o)])
+    plan.run()
+    torch.cuda.synchronize()
+    assert bool((o == 0).all())
