@@ -459,7 +459,96 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
         ints[dt] = {"tops": 2.0 * 1024 ** 3 / ms_ / 1e9, "ms": ms_,
                     "bitexact_vs_numc": h == gold[f"uniform_{dt}_1024x1024x1024"]["sha256"]}
     out["int_1024"] = ints
+    out["grouped"] = grouped_workload(nc, torch, oracle, dev)
     return out
+
+
+def grouped_workload(nc, torch, oracle, dev):
+    """2048 float32 matmuls with M, N, K log-uniform in [16, 1024] (seed 42)
+    plus 256 MLP chains X[256,784] @ W1[784,128] -> H, H @ W2[128,10],
+    W ~ N(0, 0.05): one grouped plan per phase under a CUDA graph, split-BF16
+    vs plain, against one launch per problem (also graph-captured, so host
+    overhead is excluded)."""
+    rng = np.random.default_rng(SEED)
+    dims = np.exp(rng.uniform(np.log(16), np.log(1024), (2048, 3))).round().astype(int)
+    gen = torch.Generator(device=dev).manual_seed(SEED)
+    probs = []
+    for (Mi, Ni, Ki) in dims:
+        a = torch.rand((Mi, Ki), device=dev, generator=gen) * 2 - 1
+        b = torch.rand((Ki, Ni), device=dev, generator=gen) * 2 - 1
+        probs.append((a, b, torch.empty((Mi, Ni), device=dev)))
+    chains = []
+    for _ in range(256):
+        x = torch.rand((256, 784), device=dev, generator=gen) * 2 - 1
+        w1 = torch.randn((784, 128), device=dev, generator=gen) * 0.05
+        w2 = torch.randn((128, 10), device=dev, generator=gen) * 0.05
+        chains.append((x, w1, w2, torch.empty((256, 128), device=dev),
+                       torch.empty((256, 10), device=dev)))
+    flops = float(sum(2.0 * m * n * k for m, n, k in dims)) + \
+        256 * 2.0 * 256 * (784 * 128 + 128 * 10)
+
+    def timed(fn, reps=10):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    res = {"problems": 2048, "mlp_chains": 256, "flops": flops}
+    s = torch.cuda.Stream()
+    for name, algo in [("split_bf16", nc.ALGO_SPLIT_BF16), ("plain", nc.ALGO_SIMT)]:
+        p0 = nc.GemmPlan([(a, b, c) for a, b, c in probs], algo)
+        p1 = nc.GemmPlan([(x, w1, h) for x, w1, _, h, _ in chains], algo)
+        p2 = nc.GemmPlan([(h, w2, y) for _, _, w2, h, y in chains], algo)
+        with torch.cuda.stream(s):
+            for pl in (p0, p1, p2):
+                pl.run(stream=s)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            p0.run(stream=s)
+            p1.run(stream=s)
+            p2.run(stream=s)
+        ms = timed(g.replay)
+        nc.check_status()
+        res[name] = {"ms": ms, "tflops": flops / ms / 1e9, "variants": p0.info()}
+        # errors on a sample of problems against the float64-accurate oracle
+        errs = []
+        for i in range(0, 2048, 97):
+            a, b, c = probs[i]
+            ah, bh = a.cpu().numpy(), b.cpu().numpy()
+            r, cc = sample_points(64, ah.shape[0], bh.shape[1], seed=i)
+            ref = oracle.dot_f32_ref(ah, bh, r, cc)
+            absp = oracle.dot_f32_ref(np.abs(ah), np.abs(bh), r, cc)
+            errs.append(float((np.abs(c.cpu().numpy()[r, cc] - ref) / absp).max()))
+        res[name]["max_rel_to_absprod"] = max(errs)
+        del g
+        for pl in (p0, p1, p2):
+            pl.free()
+
+    # one numc_cuda_gemm launch per problem, captured in a graph
+    def launch_all():
+        for a, b, c in probs:
+            nc.gemm(a, b, c, algo=nc.ALGO_SIMT, stream=s)
+        for x, w1, w2, h, y in chains:
+            nc.gemm(x, w1, h, algo=nc.ALGO_SIMT, stream=s)
+            nc.gemm(h, w2, y, algo=nc.ALGO_SIMT, stream=s)
+    with torch.cuda.stream(s):
+        launch_all()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        launch_all()
+    ms = timed(g.replay, reps=3)
+    res["loop_per_problem_plain"] = {"ms": ms, "tflops": flops / ms / 1e9,
+                                     "launches": 2048 + 512}
+    res["split_vs_loop"] = res["loop_per_problem_plain"]["ms"] / res["split_bf16"]["ms"]
+    res["split_vs_plain_grouped"] = res["plain"]["ms"] / res["split_bf16"]["ms"]
+    return res
 
 
 if __name__ == "__main__":
