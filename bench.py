@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip the side workloads")
+    ap.add_argument("--only", choices=["f64", "int", "grouped", "plain"],
+                    help="run one side workload alone (for profiling) and print it")
     return ap.parse_args()
 
 
@@ -246,6 +248,22 @@ def main():
         from numc_gb300 import build as nb
         nb.build()
     torch.cuda.set_device(local)
+    if args.only:
+        dev = torch.device("cuda", local)
+        if args.only == "f64":
+            part = f64_workload(nc, torch, oracle, synth, dev)
+        elif args.only == "int":
+            part = int_workload(nc, torch, synth, dev)
+        elif args.only == "grouped":
+            part = grouped_workload(nc, torch, oracle, dev)
+        else:
+            a = torch.from_numpy(synth.normal(SEED, 3, (M, K), np.float32)).to(dev)
+            b = torch.from_numpy(synth.normal(SEED, 4, (K, N), np.float32)).to(dev)
+            c = torch.empty((M, N), device=dev)
+            ms = time_gemm(nc, torch, a, b, c, nc.ALGO_SIMT, 0, steps=3, warmup=1)
+            part = {"plain_fp32_8192": {"ms": ms, "tflops": FLOPS / ms / 1e9}}
+        print(json.dumps({"only": args.only, **part}), flush=True)
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
@@ -420,6 +438,13 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
                       "plain_us": ms_p * 1e3, "split_us": ms_s * 1e3,
                       "note": "L2-resident, latency-bound"}
 
+    out["f64_4096"] = f64_workload(nc, torch, oracle, synth, dev)
+    out["int_1024"] = int_workload(nc, torch, synth, dev)
+    out["grouped"] = grouped_workload(nc, torch, oracle, dev)
+    return out
+
+
+def f64_workload(nc, torch, oracle, synth, dev):
     # float64 4096^3, uniform [-1,1) x 2^e, e ~ U(-20, 20)
     a4, b4 = synth.operands("expspread", 4096, 4096, 4096, dtype="float64")
     ta4, tb4 = torch.from_numpy(a4).to(dev), torch.from_numpy(b4).to(dev)
@@ -444,8 +469,11 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
     f64["ozaki_s8_vs_dmma"] = f64["ozaki_s8"]["tflops"] / f64["dmma"]["tflops"]
     f64["workload"] = "f64 4096^3, uniform [-1,1) x 2^e, e ~ U(-20,20); errors on 256 outputs vs double-double"
     del ws4
-    out["f64_4096"] = f64
+    return f64
 
+
+
+def int_workload(nc, torch, synth, dev):
     # integer bit-exactness workload, 1024^3, against numc's own outputs
     import hashlib
     gold = {cse["name"]: cse for cse in json.load(open(os.path.join(ROOT, "tests", "golden", "golden.json")))["cases"]}
@@ -458,9 +486,7 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
         h = hashlib.sha256(tc_.cpu().numpy().tobytes()).hexdigest()
         ints[dt] = {"tops": 2.0 * 1024 ** 3 / ms_ / 1e9, "ms": ms_,
                     "bitexact_vs_numc": h == gold[f"uniform_{dt}_1024x1024x1024"]["sha256"]}
-    out["int_1024"] = ints
-    out["grouped"] = grouped_workload(nc, torch, oracle, dev)
-    return out
+    return ints
 
 
 def grouped_workload(nc, torch, oracle, dev):
