@@ -63,14 +63,25 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(x, world):
+def _reduce(x, world, op):
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(x, world):
+    import torch.distributed as dist
+    return _reduce(x, world, dist.ReduceOp.MAX if world > 1 else None)
+
+
+def sum_over_ranks(x, world):
+    import torch.distributed as dist
+    return _reduce(x, world, dist.ReduceOp.SUM if world > 1 else None)
 
 
 # ---- clocks during the timed region ---------------------------------------
@@ -482,10 +493,15 @@ def int_workload(nc, torch, synth, dev):
         ai_, bi_ = synth.operands("uniform", 1024, 1024, 1024, dtype=dt)
         ta_, tb_ = torch.from_numpy(ai_).to(dev), torch.from_numpy(bi_).to(dev)
         tc_ = torch.empty((1024, 1024), dtype=ta_.dtype, device=dev)
-        ms_ = time_gemm(nc, torch, ta_, tb_, tc_, nc.ALGO_SIMT, nc.INT8_X86_AVX2, steps=20, warmup=2)
-        h = hashlib.sha256(tc_.cpu().numpy().tobytes()).hexdigest()
-        ints[dt] = {"tops": 2.0 * 1024 ** 3 / ms_ / 1e9, "ms": ms_,
-                    "bitexact_vs_numc": h == gold[f"uniform_{dt}_1024x1024x1024"]["sha256"]}
+        want = gold[f"uniform_{dt}_1024x1024x1024"]["sha256"]
+        algos = [("simt", nc.ALGO_SIMT)]
+        if dt in ("int8", "uint8"):
+            algos.append(("tensor", nc.ALGO_TC_INT8))
+        for name, algo in algos:
+            ms_ = time_gemm(nc, torch, ta_, tb_, tc_, algo, nc.INT8_X86_AVX2, steps=20, warmup=2)
+            h = hashlib.sha256(tc_.cpu().numpy().tobytes()).hexdigest()
+            ints.setdefault(dt, {})[name] = {"tops": 2.0 * 1024 ** 3 / ms_ / 1e9, "ms": ms_,
+                                             "bitexact_vs_numc": h == want}
     return ints
 
 

@@ -40,8 +40,14 @@ typedef enum {
                                     integer slices, exact slice products on
                                     tcgen05, integer recombination; `param`
                                     = slice count 1..8 (default 8) */
-  NUMC_CUDA_ALGO_AUTO = 5        /* float32: split-BF16 when the problem is
-                                    large enough to pay for it, else SIMT */
+  NUMC_CUDA_ALGO_AUTO = 5,       /* float32: split-BF16 when the problem is
+                                    large enough to pay for it, else SIMT;
+                                    int8/uint8 (their default): TC_INT8 when
+                                    M*K*N >= 2^21, else SIMT */
+  NUMC_CUDA_ALGO_TC_INT8 = 6     /* int8/uint8 on tcgen05 (values exact in
+                                    bfloat16, exact FP32 sums per numc K
+                                    block) with numc's store rules; `param`
+                                    is a NumcInt8Profile */
 } NumcCudaAlgo;
 
 /* Which numc build's int8/uint8 results to reproduce (the store rules of

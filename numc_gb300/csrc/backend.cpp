@@ -39,6 +39,9 @@ void init_algos_from_env() {
   }
   g_algo[NUMC_DTYPE_INT8].param = NUMC_INT8_X86_AVX2;
   g_algo[NUMC_DTYPE_UINT8].param = NUMC_INT8_X86_AVX2;
+  // int8/uint8: the tensor path is bit-exact and faster beyond tiny sizes.
+  g_algo[NUMC_DTYPE_INT8].algo = NUMC_CUDA_ALGO_AUTO;
+  g_algo[NUMC_DTYPE_UINT8].algo = NUMC_CUDA_ALGO_AUTO;
   if (const char *e = getenv("NUMC_CUDA_F32_ALGO")) {
     std::string v(e);
     if (v == "split" || v == "split3") g_algo[NUMC_DTYPE_FLOAT32].algo = NUMC_CUDA_ALGO_SPLIT_BF16;
@@ -140,9 +143,11 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
     if (param < 0) param = g_algo[dt].param.load();
   }
   if (param < 0) param = 0;   // 0 = x86 profile for int8/uint8, default slices
-  if (algo == NUMC_CUDA_ALGO_AUTO) {
+  if (algo == NUMC_CUDA_ALGO_AUTO && (dt == NUMC_DTYPE_INT8 || dt == NUMC_DTYPE_UINT8)) {
+    algo = ((double)M * K * N >= (double)(1 << 21)) ? NUMC_CUDA_ALGO_TC_INT8 : NUMC_CUDA_ALGO_SIMT;
+  } else if (algo == NUMC_CUDA_ALGO_AUTO) {
     if (dt != NUMC_DTYPE_FLOAT32)
-      return NUMC_SET_ERROR(NUMC_ERR_VALUE, "AUTO algorithm is float32 only");
+      return NUMC_SET_ERROR(NUMC_ERR_VALUE, "AUTO algorithm is float32, int8 or uint8 only");
     // Split-BF16 pays for its split pass once each output sums enough terms
     // and the grid fills the GPU.
     algo = ((uint64_t)M * N >= (1u << 16) && K >= 128) ? NUMC_CUDA_ALGO_SPLIT_BF16
@@ -161,6 +166,10 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
   case NUMC_CUDA_ALGO_DMMA:
     if (dt != NUMC_DTYPE_FLOAT64)
       return NUMC_SET_ERROR(NUMC_ERR_TYPE, "DMMA GEMM is float64 only");
+    break;
+  case NUMC_CUDA_ALGO_TC_INT8:
+    if (dt != NUMC_DTYPE_INT8 && dt != NUMC_DTYPE_UINT8)
+      return NUMC_SET_ERROR(NUMC_ERR_TYPE, "the int8 tensor path is int8/uint8 only");
     break;
   case NUMC_CUDA_ALGO_OZAKI:
     if (dt != NUMC_DTYPE_FLOAT64)
@@ -191,6 +200,7 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
 size_t plan_workspace(const Plan &p, size_t M, size_t K, size_t N) {
   if (p.algo == NUMC_CUDA_ALGO_SPLIT_BF16) return numc_k::split_bf16_workspace(M, K, N, p.param);
   if (p.algo == NUMC_CUDA_ALGO_OZAKI) return numc_k::ozaki_workspace(M, K, N, p.param);
+  if (p.algo == NUMC_CUDA_ALGO_TC_INT8) return numc_k::int8_tc_workspace(M, K, N);
   return 0;
 }
 
@@ -202,6 +212,7 @@ int run_plan(NumcDType dt, const Plan &p, const numc_k::Gemm &g, void *ws,
   case NUMC_CUDA_ALGO_DMMA: e = numc_k::launch_dmma(g, s); break;
   case NUMC_CUDA_ALGO_SPLIT_BF16: e = numc_k::launch_split_bf16(g, p.param, ws, ws_bytes, s); break;
   case NUMC_CUDA_ALGO_OZAKI: e = numc_k::launch_ozaki(g, p.param, ws, ws_bytes, s); break;
+  case NUMC_CUDA_ALGO_TC_INT8: e = numc_k::launch_int8_tc(dt, g, p.param, ws, ws_bytes, s); break;
   }
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
   return 0;
@@ -311,7 +322,8 @@ int matmul_impl(const NumcArray *a, const NumcArray *b, NumcArray *out, int algo
     CU(cudaMemcpyAsync(out->data, dout, so, cudaMemcpyDeviceToHost, s), "copy out to host");
     CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   }
-  if (plan.algo == NUMC_CUDA_ALGO_SPLIT_BF16 || plan.algo == NUMC_CUDA_ALGO_OZAKI) {
+  if (plan.algo == NUMC_CUDA_ALGO_SPLIT_BF16 || plan.algo == NUMC_CUDA_ALGO_OZAKI ||
+      plan.algo == NUMC_CUDA_ALGO_TC_INT8) {
     unsigned st = 0;
     CU(numc_k::read_and_clear_status(&st, s), "status read");
     if (st) return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "matmul kernel abandoned a bounded wait (code %u)", st);

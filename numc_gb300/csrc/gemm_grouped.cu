@@ -105,6 +105,7 @@ struct Cfg {
   static constexpr int CW = BN / 2;
   static constexpr int THREADS = 64 + 32 * ACC_WARPS;
   static_assert(SMEM <= 232448, "shared memory");
+  static_assert((2 * STAGES + 2 * NBUF) * 8 + 4 <= 256, "barrier space");
 };
 
 template <int BN, int STAGES, int FLUSH>

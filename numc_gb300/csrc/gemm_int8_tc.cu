@@ -1,0 +1,292 @@
+// int8 / uint8 GEMM on the tcgen05 tensor cores with numc's store rules —
+// the tensor path for numc's gemm_i8_avx2 / gemm_u8_avx2
+// (src/intrinsics/gemm_avx2.h:2741-2880, 2983-3125) and gemm_i8_neon.
+//
+// 8-bit integers are exact in bfloat16 (|x| <= 255 needs 8 significant
+// bits), products are exact in FP32, and so is every partial sum below
+// 2^24: a 512-deep K block of int8 products stays below 512 * 128^2 = 2^23,
+// a 256-deep block of uint8 products below 256 * 255^2 < 2^24.  The MMA
+// warp therefore accumulates one numc K block (int8: 8 slabs of 64; uint8:
+// two chunks of 4 slabs) per TMEM buffer, and the accumulator warps turn
+// each block's exact sum P_b into numc's stored byte with the same rule
+// the CUDA-core kernel uses (simt::fold8: x86 packed saturation per block
+// and tile class, NEON clamp-once, or truncation).  Results are bit-exact.
+//
+// Passes: a convert kernel writes A as bf16 (M x Kp, K-major) and B^T as
+// bf16 (N x Kp), K padded to 512 with zeros; then one 128 x 64 output tile
+// per CTA with a 24 KiB TMA ring stage (8 stages), 320 threads (TMA warp,
+// MMA warp, 8 accumulator warps of 32 columns).
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "kernels.h"
+#include "phase_timing.h"
+#include "simt_common.cuh"
+#include "status.h"
+#include "tc_common.cuh"
+
+namespace numc_k {
+namespace {
+
+constexpr int kBM = 128, kBN = 64, kBK = 64, kStages = 8, kNumBuf = 8;
+constexpr int kBlockK = 512;                 // numc's int8 K block (KC)
+constexpr int kAccWarps = 8, kThreads = 64 + 32 * kAccWarps;
+
+inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+
+// dst(row, k) = bf16(src[row * rs_row + k * rs_k]) for row < R, k < K; zero
+// up to Kp.  32 rows x 128 k per block through shared memory.
+template <bool SIGNED>
+__global__ void __launch_bounds__(256)
+int8_to_bf16(const uint8_t *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_t R,
+             int64_t K, int64_t Kp, __nv_bfloat16 *__restrict__ dst) {
+  __shared__ short tile[32][129];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 128;
+  const int tid = threadIdx.x;
+  const bool kfast = rs_k == 1 || rs_row != 1;
+#pragma unroll 4
+  for (int q = 0; q < 16; q++) {
+    const int e = tid + 256 * q;
+    const int r = kfast ? e / 128 : e % 32, k = kfast ? e % 128 : e / 32;
+    const int64_t gr = r0 + r, gk = k0 + k;
+    short v = 0;
+    if (gr < R && gk < K) {
+      const uint8_t b = src[gr * rs_row + gk * rs_k];
+      v = SIGNED ? (short)(int8_t)b : (short)b;
+    }
+    tile[r][k] = v;
+  }
+  __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31;
+#pragma unroll
+  for (int rr = 0; rr < 4; rr++) {
+    const int r = warp + 8 * rr;
+    const int64_t gr = r0 + r, gk = k0 + 4 * lane;
+    if (gr >= R || gk >= Kp) continue;
+    uint2 w;
+    w.x = (uint32_t)__bfloat16_as_ushort(__int2bfloat16_rn(tile[r][4 * lane])) |
+          ((uint32_t)__bfloat16_as_ushort(__int2bfloat16_rn(tile[r][4 * lane + 1])) << 16);
+    w.y = (uint32_t)__bfloat16_as_ushort(__int2bfloat16_rn(tile[r][4 * lane + 2])) |
+          ((uint32_t)__bfloat16_as_ushort(__int2bfloat16_rn(tile[r][4 * lane + 3])) << 16);
+    *reinterpret_cast<uint2 *>(dst + gr * Kp + gk) = w;
+  }
+}
+
+template <bool SIGNED>
+__global__ void __launch_bounds__(kThreads, 1)
+int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB,
+             uint8_t *__restrict__ C, int64_t rso, int64_t cso, int M, int N, int num_kb,
+             int tiles_m, int tiles_n, int rule, unsigned *status) {
+  // slabs per TMEM chunk: a whole 512-deep block for int8, half for uint8
+  constexpr int CHUNK = SIGNED ? kBlockK / kBK : kBlockK / kBK / 2;
+  constexpr int CHUNKS_PER_BLOCK = kBlockK / kBK / CHUNK;
+  constexpr uint32_t A_BYTES = kBM * kBK * 2, B_BYTES = kBN * kBK * 2;
+  constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *bars = (uint64_t *)(smem + kStages * STAGE_BYTES);
+  uint64_t *full = bars, *empty = bars + kStages;
+  uint64_t *tfull = bars + 2 * kStages, *tempty = tfull + kNumBuf;
+  uint32_t *tmem_slot = (uint32_t *)(tempty + kNumBuf);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  const int tile = blockIdx.x;
+  constexpr int GM = 16;
+  const int group = tile / (GM * tiles_n);
+  const int first_m = group * GM;
+  const int gm = min(tiles_m - first_m, GM);
+  const int local = tile - group * GM * tiles_n;
+  const int m0 = (first_m + local % gm) * kBM;
+  const int n0 = (local / gm) * kBN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; s++) {
+      tc::mbar_init(tc::smem_u32(&full[s]), 1);
+      tc::mbar_init(tc::smem_u32(&empty[s]), 1);
+    }
+    for (int b = 0; b < kNumBuf; b++) {
+      tc::mbar_init(tc::smem_u32(&tfull[b]), 1);
+      tc::mbar_init(tc::smem_u32(&tempty[b]), kAccWarps);
+    }
+    tc::fence_barrier_init();
+    tc::tma_prefetch_desc(&tA);
+    tc::tma_prefetch_desc(&tB);
+  }
+  if (warp == 1) tc::tmem_alloc(tc::smem_u32(tmem_slot), kNumBuf * kBN);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int kb = 0; kb < num_kb; kb++) {
+        const int s = kb % kStages;
+        if (kb >= kStages &&
+            !tc::mbar_wait_bounded(tc::smem_u32(&empty[s]), ((kb / kStages) & 1) ^ 1, status,
+                                   kStatusTimeoutProducer))
+          break;
+        const uint32_t fbar = tc::smem_u32(&full[s]);
+        const uint32_t st = tc::smem_u32(smem + s * STAGE_BYTES);
+        tc::mbar_arrive_expect_tx(fbar, STAGE_BYTES);
+        tc::tma_load_2d(st, &tA, fbar, kb * kBK, m0);
+        tc::tma_load_2d(st + A_BYTES, &tB, fbar, kb * kBK, n0);
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
+      for (int kb = 0; kb < num_kb; kb++) {
+        const int s = kb % kStages, chunk = kb / CHUNK, buf = chunk % kNumBuf;
+        const bool cstart = kb % CHUNK == 0, cend = kb % CHUNK == CHUNK - 1;
+        if (cstart && chunk >= kNumBuf &&
+            !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / kNumBuf) & 1) ^ 1,
+                                   status, kStatusTimeoutMma))
+          break;
+        if (!tc::mbar_wait_bounded(tc::smem_u32(&full[s]), (kb / kStages) & 1, status,
+                                   kStatusTimeoutMma))
+          break;
+        tc::tc_fence_after();
+        const uint32_t sa = tc::smem_u32(smem + s * STAGE_BYTES), sb = sa + A_BYTES;
+#pragma unroll
+        for (int kk = 0; kk < kBK / 16; kk++)
+          tc::mma_bf16(tmem + buf * kBN, tc::sdesc_k128(sa + kk * 32),
+                       tc::sdesc_k128(sb + kk * 32), idesc, (!cstart || kk > 0) ? 1u : 0u);
+        tc::mma_commit(tc::smem_u32(&empty[s]));
+        if (cend) tc::mma_commit(tc::smem_u32(&tfull[buf]));
+      }
+    }
+    __syncwarp();
+  } else {
+    constexpr int CW = kBN / 2;
+    const int quad = warp & 3, half = (warp - 2) >> 2;
+    const int row = m0 + quad * 32 + lane;
+    const int cbase = half * CW;
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    int32_t d[CW], part[CW];
+#pragma unroll
+    for (int j = 0; j < CW; j++) d[j] = 0;
+    const int nchunks = num_kb / CHUNK;   // num_kb is a multiple of the block size
+    bool ok = true;
+    for (int chunk = 0; chunk < nchunks; chunk++) {
+      const int buf = chunk % kNumBuf;
+      ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / kNumBuf) & 1, status,
+                                 kStatusTimeoutEpilogue);
+      ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
+      if (!ok) break;
+      tc::tc_fence_after();
+      uint32_t r[32];
+      tc::tmem_ld_32x32b_x32(tmem + lane_off + buf * kBN + cbase, r);
+      tc::tmem_ld_wait();
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tempty[buf]));
+      const bool block_start = chunk % CHUNKS_PER_BLOCK == 0;
+#pragma unroll
+      for (int j = 0; j < CW; j++) {
+        const int32_t v = __float2int_rn(__uint_as_float(r[j]));   // exact
+        part[j] = block_start ? v : part[j] + v;
+      }
+      if (chunk % CHUNKS_PER_BLOCK == CHUNKS_PER_BLOCK - 1) {
+        const int b = chunk / CHUNKS_PER_BLOCK;
+        if (rule == kRuleNeon || rule == kRuleWrap) {
+          // one block over all K: accumulate the wrapped int32 sum
+#pragma unroll
+          for (int j = 0; j < CW; j++) d[j] = (int32_t)((uint32_t)d[j] + (uint32_t)part[j]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < CW; j++)
+            d[j] = simt::fold8(d[j], part[j], b == 0, rule, SIGNED, row, n0 + cbase + j, M, N);
+        }
+      }
+    }
+    if (ok && row < M) {
+#pragma unroll
+      for (int j = 0; j < CW; j++) {
+        const int col = n0 + cbase + j;
+        if (col >= N) continue;
+        int32_t v = d[j];
+        if (rule == kRuleNeon || rule == kRuleWrap) v = simt::fold8(0, v, true, rule, SIGNED, row, col, M, N);
+        C[(int64_t)row * rso + (int64_t)col * cso] = (uint8_t)v;
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, kNumBuf * kBN);
+  }
+}
+
+struct I8Layout {
+  int64_t Kp;
+  size_t a, b, total;
+};
+
+I8Layout i8_layout(int64_t M, int64_t K, int64_t N) {
+  I8Layout L;
+  L.Kp = round_up(K > 0 ? K : 1, kBlockK);
+  L.a = 0;
+  L.b = (size_t)round_up(M * L.Kp * 2, 256);
+  L.total = L.b + (size_t)round_up(N * L.Kp * 2, 256);
+  return L;
+}
+
+template <bool SIGNED>
+cudaError_t launch_i8(const Gemm &g, int rule, char *ws, const I8Layout &L, cudaStream_t s) {
+  unsigned *status = status_word();
+  if (!status) return cudaErrorMemoryAllocation;
+  PhaseMark mark(s);
+  auto *pa = (__nv_bfloat16 *)(ws + L.a), *pb = (__nv_bfloat16 *)(ws + L.b);
+  dim3 ga((unsigned)(L.Kp / 128), (unsigned)((g.M + 31) / 32));
+  dim3 gb((unsigned)(L.Kp / 128), (unsigned)((g.N + 31) / 32));
+  if (ga.y > 65535 || gb.y > 65535) return cudaErrorInvalidConfiguration;
+  int8_to_bf16<SIGNED><<<ga, 256, 0, s>>>((const uint8_t *)g.a, g.rsa, g.csa, g.M, g.K, L.Kp, pa);
+  int8_to_bf16<SIGNED><<<gb, 256, 0, s>>>((const uint8_t *)g.b, g.csb, g.rsb, g.N, g.K, L.Kp, pb);
+  count_launch(2);
+  cudaError_t e = cudaGetLastError();
+  if (e) return e;
+  mark.split_done();
+  CUtensorMap ta, tb;
+  if ((e = make_tmap_2d(&ta, pa, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, g.M, L.Kp, L.Kp, kBM, kBK)))
+    return e;
+  if ((e = make_tmap_2d(&tb, pb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, g.N, L.Kp, L.Kp, kBN, kBK)))
+    return e;
+  constexpr uint32_t kBarBytes = 512;   // 2*(kStages + kNumBuf) mbarriers + TMEM slot
+  static_assert((2 * kStages + 2 * kNumBuf) * 8 + 4 <= kBarBytes, "barrier space");
+  constexpr uint32_t SMEM = kStages * (kBM + kBN) * kBK * 2 + 1024 + kBarBytes;
+  static_assert(SMEM <= 232448, "shared memory");
+  if ((e = cudaFuncSetAttribute(int8_tc_gemm<SIGNED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                SMEM)))
+    return e;
+  const int tiles_m = (int)((g.M + kBM - 1) / kBM), tiles_n = (int)((g.N + kBN - 1) / kBN);
+  int8_tc_gemm<SIGNED><<<tiles_m * tiles_n, kThreads, SMEM, s>>>(
+      ta, tb, (uint8_t *)g.c, g.rso, g.cso, (int)g.M, (int)g.N, (int)(L.Kp / kBK), tiles_m,
+      tiles_n, rule, status);
+  count_launch();
+  e = cudaGetLastError();
+  mark.gemm_done();
+  return e;
+}
+
+}  // namespace
+
+size_t int8_tc_workspace(int64_t M, int64_t K, int64_t N) { return i8_layout(M, K, N).total; }
+
+cudaError_t launch_int8_tc(NumcDType dt, const Gemm &g, int rule, void *ws, size_t ws_bytes,
+                           cudaStream_t s) {
+  if (g.M == 0 || g.N == 0) return cudaSuccess;
+  if (g.K == 0) return launch_simt(dt, g, rule, s);   // C = 0
+  if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31)) return cudaErrorInvalidValue;
+  const I8Layout L = i8_layout(g.M, g.K, g.N);
+  if (ws_bytes < L.total || ((uintptr_t)ws & 255)) return cudaErrorInvalidValue;
+  if (dt == NUMC_DTYPE_INT8) return launch_i8<true>(g, rule, (char *)ws, L, s);
+  if (dt == NUMC_DTYPE_UINT8) return launch_i8<false>(g, rule, (char *)ws, L, s);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace numc_k

@@ -64,6 +64,23 @@ constexpr int kMaxSlices = 8;
 
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
+// Bit tests on float64 values: GB300's FP64 pipe is slow, so compares on
+// doubles are done on their IEEE bit patterns in the integer pipes.
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ bool finite_bits(unsigned long long a) {
+  return a < 0x7FF0000000000000ull;
+}
+// frexp exponent of a non-negative finite double given as bits (0 for 0):
+// x = m 2^e with m in [0.5, 1).
+__device__ __forceinline__ int frexp_exp_bits(unsigned long long a) {
+  if (a == 0) return 0;
+  const int field = (int)(a >> 52);
+  if (field) return field - 1022;
+  return (64 - __clzll((long long)a)) - 1074;   // subnormal: a * 2^-1074
+}
+
 // ---- pass 1: row maxima of |A|, column maxima of |B| -----------------------
 // out[row] = max over k of |src[row * rs_row + k * rs_k]| as IEEE bits
 // (atomicMax on the bit pattern orders non-negative doubles).  Non-finite
@@ -86,9 +103,9 @@ absmax_rows(const double *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_
     int k = kfast ? e % 128 : e / 32;
     int64_t gr = r0 + r, gk = k0 + k;
     if (gr < R && gk < K) {
-      double x = src[gr * rs_row + gk * rs_k];
-      if (!isfinite(x)) bad = true;
-      else atomicMax(&rmax[r], (unsigned long long)__double_as_longlong(fabs(x)));
+      const unsigned long long ax = abs_bits(src[gr * rs_row + gk * rs_k]);
+      if (!finite_bits(ax)) bad = true;
+      else if (ax) atomicMax(&rmax[r], ax);
     }
   }
   if (__syncthreads_or(bad) && tid == 0) flags[r0 / flag_rows] = gen;
@@ -132,7 +149,7 @@ slice_f64(const double *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_t 
     int k = kfast ? e % 64 : e / 32;
     int64_t gr = r0 + r, gk = k0 + k;
     double x = (gr < R && gk < K) ? src[gr * rs_row + gk * rs_k] : 0.0;
-    tile[r][k] = isfinite(x) ? x : 0.0;
+    tile[r][k] = finite_bits(abs_bits(x)) ? x : 0.0;
   }
   __syncthreads();
   const int64_t plane = R * Kp;
@@ -142,13 +159,11 @@ slice_f64(const double *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_t 
     const int r = warp + 8 * rr;
     const int64_t gr = r0 + r;
     if (gr >= R) continue;
-    int ex = 0;
-    const double mx = __longlong_as_double((long long)maxbits[gr]);
-    if (mx > 0.0) frexp(mx, &ex);
+    const int ex = frexp_exp_bits(maxbits[gr]);
     const int64_t gk = k0 + 2 * lane;
     const double x0 = tile[r][2 * lane], x1 = tile[r][2 * lane + 1];
     const uint64_t X0 = fixed_point(x0, ex, slices), X1 = fixed_point(x1, ex, slices);
-    const bool n0 = x0 < 0.0, n1 = x1 < 0.0;
+    const bool n0 = __double_as_longlong(x0) < 0, n1 = __double_as_longlong(x1) < 0;
     for (int p = 0; p < slices; p++) {
       const int sh = 8 * (slices - 1 - p);
       const int s0 = (int)((X0 >> sh) & 255), s1 = (int)((X1 >> sh) & 255);
@@ -170,10 +185,7 @@ struct OzParams {
 };
 
 __device__ __forceinline__ int exponent_of(unsigned long long bits) {
-  const double mx = __longlong_as_double((long long)bits);
-  int ex = 0;
-  if (mx > 0.0) frexp(mx, &ex);
-  return ex;
+  return frexp_exp_bits(bits);
 }
 
 // 320 threads: registers are granted per group of four warps, so at most 168
@@ -449,6 +461,7 @@ cudaError_t launch_ozaki(const Gemm &g, int slices, void *ws_v, size_t ws_bytes,
     return e;
   constexpr uint32_t SMEM = kStages * (kBM + kBN) * kBK * 2 + 1024 + 256;
   static_assert(SMEM <= 232448, "shared memory");
+  static_assert((2 * kStages + 2 * kNumBuf) * 8 + 4 <= 256, "barrier space");
   if ((e = cudaFuncSetAttribute(ozaki_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM)))
     return e;
   OzParams op;

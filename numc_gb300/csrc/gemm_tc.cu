@@ -83,6 +83,7 @@ struct SplitCfg {
   static constexpr int COLS_PER_WARP = BN / 2;
   static constexpr int THREADS = 64 + 32 * ACC_WARPS;   // producer, MMA, accumulators
   static_assert(SMEM <= 232448, "shared memory");
+  static_assert((2 * STAGES + 2 * NBUF) * 8 + 4 <= 256, "barrier space");
   static_assert(TMEM_COLS <= 512, "tensor memory");
 };
 

@@ -37,6 +37,11 @@ size_t split_bf16_workspace(int64_t M, int64_t K, int64_t N, int passes);
 cudaError_t launch_split_bf16(const Gemm &g, int passes, void *ws, size_t ws_bytes,
                               cudaStream_t s);
 
+// int8/uint8 on tcgen05 with numc's store rule `rule8`.
+size_t int8_tc_workspace(int64_t M, int64_t K, int64_t N);
+cudaError_t launch_int8_tc(NumcDType dt, const Gemm &g, int rule8, void *ws, size_t ws_bytes,
+                           cudaStream_t s);
+
 // float64 Ozaki slicing on tcgen05.
 size_t ozaki_workspace(int64_t M, int64_t K, int64_t N, int slices);
 cudaError_t launch_ozaki(const Gemm &g, int slices, void *ws, size_t ws_bytes,

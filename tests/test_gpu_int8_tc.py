@@ -1,0 +1,65 @@
+"""int8/uint8 on the tcgen05 tensor path: bit-exact with numc.
+
+Every stored byte must equal numc's own (golden SHA-256 at 1024^3 and
+300x4100x4200) and the oracle's for each store-rule profile, including
+shapes with remainder tiles and K not a multiple of numc's 512 block.
+"""
+import numpy as np
+import pytest
+
+import numc_gb300 as nc
+import oracle
+from numc_gb300 import synth
+
+from gpu_util import golden, needs_gpu, sha
+
+pytestmark = [pytest.mark.gpu, needs_gpu]
+torch = pytest.importorskip("torch")
+CASES, _ = golden()
+
+
+def _tc(a, b, profile):
+    ta = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    tb = torch.from_numpy(np.ascontiguousarray(b)).cuda()
+    out = torch.full((a.shape[0], b.shape[1]), 77, dtype=ta.dtype, device="cuda")
+    nc.gemm(ta, tb, out, algo=nc.ALGO_TC_INT8, param=profile)
+    nc.check_status()
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("dt", ["int8", "uint8"])
+@pytest.mark.parametrize("profile", [nc.INT8_X86_AVX2, nc.INT8_ARM_NEON, nc.INT8_WRAP])
+@pytest.mark.parametrize("shape", [(150, 1500, 140), (97, 1100, 203), (5, 3, 4),
+                                   (300, 513, 64), (128, 64, 65), (200, 4096, 300)],
+                         ids=lambda s: "x".join(map(str, s)))
+def test_profiles_vs_oracle(dt, profile, shape):
+    a, b = synth.operands("uniform", *shape, dtype=dt, seed=sum(shape))
+    np.testing.assert_array_equal(_tc(a, b, profile), oracle.matmul(a, b, profile))
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c["dtype"] in ("int8", "uint8")
+                                  and c["kind"] == "uniform"], ids=lambda c: c["name"])
+def test_golden_sha(case):
+    M, K, N = case["shape"]
+    a, b = synth.operands("uniform", M, K, N, seed=case["seed"], dtype=case["dtype"])
+    prof = nc.INT8_WRAP if M * K * N <= 192 ** 3 else nc.INT8_X86_AVX2
+    assert sha(_tc(a, b, prof)) == case["sha256"]
+
+
+def test_strided_and_through_numc_matmul():
+    a, b = synth.operands("uniform", 130, 700, 90, dtype="int8", seed=3)
+    ta = torch.from_numpy(np.ascontiguousarray(a.T)).cuda().t()
+    tb = torch.from_numpy(b).cuda()
+    out = torch.empty((90, 130), dtype=torch.int8, device="cuda").t()
+    nc.gemm(ta, tb, out, algo=nc.ALGO_TC_INT8, param=nc.INT8_X86_AVX2)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), oracle.matmul(a, b))
+    orig = nc.get_algo("int8")
+    nc.set_algo("int8", nc.ALGO_TC_INT8, nc.INT8_X86_AVX2)
+    try:
+        with nc.Ctx() as ctx:
+            A, B, C = ctx.from_numpy(a), ctx.from_numpy(b), ctx.zeros((130, 90), "int8")
+            nc.matmul(A, B, C)
+            np.testing.assert_array_equal(C.numpy(), oracle.matmul(a, b))
+    finally:
+        nc.set_algo("int8", *orig)

@@ -131,3 +131,25 @@ def test_zero_rows_and_k():
     assert (got[5] == 0).all() and (got[:, 9] == 0).all()
     z = _oz(np.zeros((4, 0)), np.zeros((0, 3)), 5)
     assert (z == 0).all()
+
+
+def test_tiny_and_subnormal_scales():
+    # rows and columns whose maxima are tiny or subnormal: exponents come
+    # from the bit patterns, slices must still reproduce the product
+    a, b = synth.operands("uniform", 70, 90, 50, dtype="float64", seed=8)
+    a[3] *= 2.0 ** -1030          # subnormal row
+    a[4] *= 2.0 ** -900           # tiny normal row
+    b[:, 7] *= 2.0 ** 600         # huge column
+    got = _oz(a, b, 8)
+    # Reference on power-of-two rescaled operands (no underflow in the
+    # compensated dot products), scaled back with one rounding.
+    ra = np.zeros(70, dtype=np.int64); ra[3], ra[4] = 1030, 900
+    cb = np.zeros(50, dtype=np.int64); cb[7] = -600
+    a_s, b_s = np.ldexp(a, ra[:, None]), np.ldexp(b, cb[None, :])
+    hi, lo = oracle.dot2_f64(a_s, b_s, *np.divmod(np.arange(70 * 50), 50))
+    ref = np.ldexp((hi + lo).reshape(70, 50), -(ra[:, None] + cb[None, :]))
+    bound = np.ldexp(_bound(a_s, b_s, 8), -(ra[:, None] + cb[None, :]))
+    # results in the subnormal range are rounded to multiples of 2^-1074
+    assert (np.abs(got - ref) <= bound + 2.0 ** -1074).all()
+    nz = ref[3] != 0
+    assert np.all(np.signbit(got[3][nz]) == np.signbit(ref[3][nz]))

@@ -73,11 +73,12 @@ def test_simt_is_numc_fma_chain(ctx, dt):
 @pytest.mark.parametrize("profile", [nc.INT8_X86_AVX2, nc.INT8_ARM_NEON, nc.INT8_WRAP])
 def test_int8_profiles(ctx, dt, profile):
     a, b = synth.operands("uniform", 150, 1500, 140, dtype=dt)
+    orig = nc.get_algo(dt)
     nc.set_algo(dt, nc.ALGO_SIMT, profile)
     try:
         got = _run_numc(ctx, a, b)
     finally:
-        nc.set_algo(dt, nc.ALGO_SIMT, nc.INT8_X86_AVX2)
+        nc.set_algo(dt, *orig)
     np.testing.assert_array_equal(got, oracle.matmul(a, b, profile))
 
 
