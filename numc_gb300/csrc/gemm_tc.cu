@@ -17,7 +17,8 @@
 // Pass 1 (split kernel, HBM-bound): reads A and B once with any strides and
 // writes the planes K-major with K padded to 64 (B is transposed on the
 // way), so every plane suits a 128-byte-swizzled TMA box.
-// Pass 2 (GEMM kernel): one 128 x BN output tile per CTA, ten warps.  Warp
+// Pass 2 (GEMM kernel): persistent, one CTA per SM walking 128 x BN output
+// tiles, ten warps.  Warp
 // 0 streams 64-deep K slabs of every plane of A and B into a STAGES-deep
 // shared-memory ring with TMA (one 3-D tensor map per operand, the plane is
 // the third coordinate); warp 1 issues the tcgen05.mma.kind::f16 products
@@ -29,6 +30,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <atomic>
 #include <cstdint>
 #include <mutex>
@@ -132,16 +134,20 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ 
   uint32_t *tmem_slot = (uint32_t *)(bars + 2 * STAGES + 2 * NBUF);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = tiles_m * tiles_n;
 
-  // Grouped rasterisation: 16 row-tiles per group sweep all column tiles.
-  const int tile = blockIdx.x;
-  constexpr int GM = 16;
-  const int group = tile / (GM * tiles_n);
-  const int first_m = group * GM;
-  const int gm = min(tiles_m - first_m, GM);
-  const int local = tile - group * GM * tiles_n;
-  const int m0 = (first_m + local % gm) * kBM;
-  const int n0 = (local / gm) * BN;
+  // Persistent: CTA b handles tiles b, b + gridDim.x, ...  Tiles are
+  // rasterised in groups of 16 row-tiles that sweep all column tiles, so
+  // the CTAs in flight share A and B panels in L2.
+  auto tile_origin = [&](int t, int &m0, int &n0) {
+    constexpr int GM = 16;
+    const int group = t / (GM * tiles_n);
+    const int first_m = group * GM;
+    const int gm = min(tiles_m - first_m, GM);
+    const int local = t - group * GM * tiles_n;
+    m0 = (first_m + local % gm) * kBM;
+    n0 = (local / gm) * BN;
+  };
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
@@ -161,23 +167,32 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ 
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  const int num_chunks = (num_kb + FLUSH - 1) / FLUSH;   // per tile
 
   if (warp == 0) {
     if (lane == 0) {
-      for (int kb = 0; kb < num_kb; kb++) {
-        const int s = kb % STAGES;
-        if (kb >= STAGES &&
-            !tc::mbar_wait_bounded(tc::smem_u32(&empty[s]), ((kb / STAGES) & 1) ^ 1, status,
-                                   kStatusTimeoutProducer))
-          break;
-        const uint32_t fbar = tc::smem_u32(&full[s]);
-        const uint32_t st = tc::smem_u32(smem + s * Cfg::STAGE_BYTES);
-        tc::mbar_arrive_expect_tx(fbar, Cfg::STAGE_BYTES);
-        const int k = kb * kBK;
+      int g = 0;   // stage counter across tiles
+      bool live = true;
+      for (int t = blockIdx.x; t < ntiles && live; t += gridDim.x) {
+        int m0, n0;
+        tile_origin(t, m0, n0);
+        for (int kb = 0; kb < num_kb; kb++, g++) {
+          const int s = g % STAGES;
+          if (g >= STAGES &&
+              !tc::mbar_wait_bounded(tc::smem_u32(&empty[s]), ((g / STAGES) & 1) ^ 1, status,
+                                     kStatusTimeoutProducer)) {
+            live = false;
+            break;
+          }
+          const uint32_t fbar = tc::smem_u32(&full[s]);
+          const uint32_t st = tc::smem_u32(smem + s * Cfg::STAGE_BYTES);
+          tc::mbar_arrive_expect_tx(fbar, Cfg::STAGE_BYTES);
+          const int k = kb * kBK;
 #pragma unroll
-        for (int p = 0; p < PLANES; p++) {
-          tc::tma_load_3d(st + p * Cfg::A_BYTES, &tA, fbar, k, m0, p);
-          tc::tma_load_3d(st + PLANES * Cfg::A_BYTES + p * Cfg::B_BYTES, &tB, fbar, k, n0, p);
+          for (int p = 0; p < PLANES; p++) {
+            tc::tma_load_3d(st + p * Cfg::A_BYTES, &tA, fbar, k, m0, p);
+            tc::tma_load_3d(st + PLANES * Cfg::A_BYTES + p * Cfg::B_BYTES, &tB, fbar, k, n0, p);
+          }
         }
       }
     }
@@ -185,33 +200,44 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ 
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, BN);
-      for (int kb = 0; kb < num_kb; kb++) {
-        const int s = kb % STAGES, chunk = kb / FLUSH, buf = chunk % NBUF;
-        const bool chunk_start = kb % FLUSH == 0;
-        const bool chunk_end = kb % FLUSH == FLUSH - 1 || kb == num_kb - 1;
-        if (chunk_start && chunk >= NBUF &&
-            !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / NBUF) & 1) ^ 1,
-                                   status, kStatusTimeoutMma))
-          break;
-        if (!tc::mbar_wait_bounded(tc::smem_u32(&full[s]), (kb / STAGES) & 1, status,
-                                   kStatusTimeoutMma))
-          break;
-        tc::tc_fence_after();
-        const uint32_t st = tc::smem_u32(smem + s * Cfg::STAGE_BYTES);
-        const uint32_t bbase = st + PLANES * Cfg::A_BYTES;
-        const uint32_t acc_tmem = tmem + buf * BN;
+      int g = 0, chunk = 0;   // stage and chunk counters across tiles
+      bool live = true;
+      for (int t = blockIdx.x; t < ntiles && live; t += gridDim.x) {
+        for (int kb = 0; kb < num_kb; kb++, g++) {
+          const int s = g % STAGES, buf = chunk % NBUF;
+          const bool chunk_start = kb % FLUSH == 0;
+          const bool chunk_end = kb % FLUSH == FLUSH - 1 || kb == num_kb - 1;
+          if (chunk_start && chunk >= NBUF &&
+              !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / NBUF) & 1) ^ 1,
+                                     status, kStatusTimeoutMma)) {
+            live = false;
+            break;
+          }
+          if (!tc::mbar_wait_bounded(tc::smem_u32(&full[s]), (g / STAGES) & 1, status,
+                                     kStatusTimeoutMma)) {
+            live = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint32_t st = tc::smem_u32(smem + s * Cfg::STAGE_BYTES);
+          const uint32_t bbase = st + PLANES * Cfg::A_BYTES;
+          const uint32_t acc_tmem = tmem + buf * BN;
 #pragma unroll
-        for (int kk = 0; kk < kBK / 16; kk++) {
-          const uint32_t koff = kk * 32;   // 16 bf16 = 32 bytes inside the swizzle atom
+          for (int kk = 0; kk < kBK / 16; kk++) {
+            const uint32_t koff = kk * 32;   // 16 bf16 = 32 bytes inside the swizzle atom
 #pragma unroll
-          for (int t = 0; t < P::n; t++) {
-            const uint32_t acc = (!chunk_start || kk > 0 || t > 0) ? 1u : 0u;
-            tc::mma_bf16(acc_tmem, tc::sdesc_k128(st + P::a(t) * Cfg::A_BYTES + koff),
-                         tc::sdesc_k128(bbase + P::b(t) * Cfg::B_BYTES + koff), idesc, acc);
+            for (int p = 0; p < P::n; p++) {
+              const uint32_t acc = (!chunk_start || kk > 0 || p > 0) ? 1u : 0u;
+              tc::mma_bf16(acc_tmem, tc::sdesc_k128(st + P::a(p) * Cfg::A_BYTES + koff),
+                           tc::sdesc_k128(bbase + P::b(p) * Cfg::B_BYTES + koff), idesc, acc);
+            }
+          }
+          tc::mma_commit(tc::smem_u32(&empty[s]));
+          if (chunk_end) {
+            tc::mma_commit(tc::smem_u32(&tfull[buf]));
+            chunk++;
           }
         }
-        tc::mma_commit(tc::smem_u32(&empty[s]));
-        if (chunk_end) tc::mma_commit(tc::smem_u32(&tfull[buf]));
       }
     }
     __syncwarp();
@@ -220,77 +246,83 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ 
     // two warps of a quadrant split the columns.
     constexpr int CW = Cfg::COLS_PER_WARP;
     const int quad = warp & 3, half = (warp - 2) >> 2;
-    const int row = m0 + quad * 32 + lane;
     const int cbase = half * CW;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
-    float acc[CW];
-#pragma unroll
-    for (int j = 0; j < CW; j++) acc[j] = 0.0f;
+    int chunk = 0;   // across tiles
     bool ok = true;
-    const int num_chunks = (num_kb + FLUSH - 1) / FLUSH;
-    for (int chunk = 0; chunk < num_chunks && ok; chunk++) {
-      const int buf = chunk % NBUF;
-      ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / NBUF) & 1, status,
-                                 kStatusTimeoutEpilogue);
-      ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
-      if (!ok) break;
-      tc::tc_fence_after();
-      uint32_t r[CW];
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      int m0, n0;
+      tile_origin(t, m0, n0);
+      const int row = m0 + quad * 32 + lane;
+      float acc[CW];
 #pragma unroll
-      for (int c0 = 0; c0 < CW; c0 += 32)
-        tc::tmem_ld_32x32b_x32(tmem + lane_off + buf * BN + cbase + c0,
-                               *reinterpret_cast<uint32_t(*)[32]>(&r[c0]));
-      tc::tmem_ld_wait();
-      tc::tc_fence_before();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tempty[buf]));
+      for (int j = 0; j < CW; j++) acc[j] = 0.0f;
+      for (int c = 0; c < num_chunks; c++, chunk++) {
+        const int buf = chunk % NBUF;
+        ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / NBUF) & 1, status,
+                                   kStatusTimeoutEpilogue);
+        ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
+        if (!ok) break;
+        tc::tc_fence_after();
+        uint32_t r[CW];
 #pragma unroll
-      for (int j = 0; j < CW; j++) acc[j] = __fadd_rn(acc[j], __uint_as_float(r[j]));
-    }
-
-    bool nonfinite = fb.flags_a[m0 / kBM] == fb.gen;
-#pragma unroll 1
-    for (int c = n0 / 64; c < (n0 + BN) / 64 && c * 64 < N; c++)
-      nonfinite |= fb.flags_b[c] == fb.gen;
-    if (ok && nonfinite) {
-      // numc's arithmetic: one FMA chain per output in k order (slow path).
-#pragma unroll 1
-      for (int c0 = cbase; c0 < cbase + CW && row < M; c0 += 32) {
-        float f[32];
+        for (int c0 = 0; c0 < CW; c0 += 32)
+          tc::tmem_ld_32x32b_x32(tmem + lane_off + buf * BN + cbase + c0,
+                                 *reinterpret_cast<uint32_t(*)[32]>(&r[c0]));
+        tc::tmem_ld_wait();
+        tc::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tempty[buf]));
 #pragma unroll
-        for (int j = 0; j < 32; j++) f[j] = 0.0f;
-#pragma unroll 1
-        for (int64_t k = 0; k < fb.K; k++) {
-          const float av = fb.A[(int64_t)row * fb.rsa + k * fb.csa];
-          const float *brow = fb.B + k * fb.rsb;
-#pragma unroll
-          for (int j = 0; j < 32; j++) {
-            const int col = n0 + c0 + j;
-            const float bv = col < N ? brow[(int64_t)col * fb.csb] : 0.0f;
-            f[j] = __fmaf_rn(av, bv, f[j]);
-          }
-        }
-#pragma unroll
-        for (int j = 0; j < 32; j++)
-          if (n0 + c0 + j < N) C[(int64_t)row * rso + (int64_t)(n0 + c0 + j) * cso] = f[j];
+        for (int j = 0; j < CW; j++) acc[j] = __fadd_rn(acc[j], __uint_as_float(r[j]));
       }
-    } else if (ok && row < M) {
-      float *crow = C + (int64_t)row * rso;
+      if (!ok) break;
+
+      bool nonfinite = fb.flags_a[m0 / kBM] == fb.gen;
+#pragma unroll 1
+      for (int c = n0 / 64; c < (n0 + BN) / 64 && c * 64 < N; c++)
+        nonfinite |= fb.flags_b[c] == fb.gen;
+      if (nonfinite) {
+        // numc's arithmetic: one FMA chain per output in k order (slow path).
+#pragma unroll 1
+        for (int c0 = cbase; c0 < cbase + CW && row < M; c0 += 32) {
+          float f[32];
 #pragma unroll
-      for (int c0 = 0; c0 < CW; c0 += 32) {
-        const int nb = n0 + cbase + c0;
-        if (vec4 && nb + 32 <= N) {
-          float4 *p = reinterpret_cast<float4 *>(crow + nb);
+          for (int j = 0; j < 32; j++) f[j] = 0.0f;
+#pragma unroll 1
+          for (int64_t k = 0; k < fb.K; k++) {
+            const float av = fb.A[(int64_t)row * fb.rsa + k * fb.csa];
+            const float *brow = fb.B + k * fb.rsb;
 #pragma unroll
-          for (int j = 0; j < 8; j++)
-            p[j] = make_float4(acc[c0 + 4 * j], acc[c0 + 4 * j + 1], acc[c0 + 4 * j + 2],
-                               acc[c0 + 4 * j + 3]);
-        } else {
+            for (int j = 0; j < 32; j++) {
+              const int col = n0 + c0 + j;
+              const float bv = col < N ? brow[(int64_t)col * fb.csb] : 0.0f;
+              f[j] = __fmaf_rn(av, bv, f[j]);
+            }
+          }
 #pragma unroll
           for (int j = 0; j < 32; j++)
-            if (nb + j < N) crow[(int64_t)(nb + j) * cso] = acc[c0 + j];
+            if (n0 + c0 + j < N) C[(int64_t)row * rso + (int64_t)(n0 + c0 + j) * cso] = f[j];
+        }
+      } else if (row < M) {
+        float *crow = C + (int64_t)row * rso;
+#pragma unroll
+        for (int c0 = 0; c0 < CW; c0 += 32) {
+          const int nb = n0 + cbase + c0;
+          if (vec4 && nb + 32 <= N) {
+            float4 *p = reinterpret_cast<float4 *>(crow + nb);
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+              p[j] = make_float4(acc[c0 + 4 * j], acc[c0 + 4 * j + 1], acc[c0 + 4 * j + 2],
+                                 acc[c0 + 4 * j + 3]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; j++)
+              if (nb + j < N) crow[(int64_t)(nb + j) * cso] = acc[c0 + j];
+          }
         }
       }
+      __syncwarp();   // reconverge before the next tile's tcgen05.ld
     }
   }
   tc::tc_fence_before();
@@ -319,6 +351,19 @@ SplitLayout split_layout(int64_t M, int64_t K, int64_t N, int planes) {
   L.flags_b = L.flags_a + (size_t)round_up(((M + kBM - 1) / kBM) * 8, 256);
   L.total = L.flags_b + (size_t)round_up(((N + 63) / 64) * 8, 256);
   return L;
+}
+
+// Streaming multiprocessors of the current device (persistent grid size).
+int sm_count() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+  if (!cached[dev]) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cached[dev] = n > 0 ? n : 148;
+  }
+  return cached[dev];
 }
 
 // Generation numbers of split calls (never 0; flags hold the last writer's).
@@ -369,7 +414,8 @@ cudaError_t launch_gemm_status(const SplitLayout &L, char *ws, const Gemm &g,
   fb.flags_a = (const unsigned long long *)(ws + L.flags_a);
   fb.flags_b = (const unsigned long long *)(ws + L.flags_b);
   fb.gen = gen;
-  kern<<<tiles_m * tiles_n, Cfg::THREADS, Cfg::SMEM, s>>>(ta, tb, (float *)g.c, g.rso, g.cso, (int)g.M,
+  const int grid = std::min(tiles_m * tiles_n, sm_count());
+  kern<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(ta, tb, (float *)g.c, g.rso, g.cso, (int)g.M,
                                                  (int)g.N, (int)(L.Kp / kBK), tiles_m, tiles_n,
                                                  vec4, status, fb);
   count_launch();
