@@ -97,33 +97,75 @@ static void scatter(void *dstv, const void *src, int64_t rows, int64_t cols,
 #define KB 256
 #define JB 128
 
-#define DEFINE_FLOAT_KERNEL(NAME, T, FMA)                                     \
+/* Float kernels: packed, register-blocked GEMM whose arithmetic is exactly
+ * numc's full-tile arithmetic — one FMA chain per output in k order from
+ * +0 — because each output's accumulator is reloaded from C between K
+ * blocks, never split.  B is packed per (column panel, K block) into
+ * NR-wide strips shared by all threads; each thread runs MR x NR register
+ * tiles over its rows. */
+#define FKC 256
+#define FNC 512
+
+/* Register-tile micro-kernels (numc_oracle_micro.c, compiled so that each
+ * vector multiply-add is one fused multiply-add). */
+void oracle_micro_f32(const float *a, int64_t lda, const float *bs, float *c,
+                      int64_t ldc, int64_t kc);
+void oracle_micro_f64(const double *a, int64_t lda, const double *bs,
+                      double *c, int64_t ldc, int64_t kc);
+
+#define DEFINE_FLOAT_KERNEL(NAME, T, MICRO, MR_, NR_)                         \
   static void NAME(const T *a, const T *b, T *c, int64_t M, int64_t K,       \
                    int64_t N) {                                               \
-    _Pragma("omp parallel for schedule(dynamic, 1)")                          \
-    for (int64_t i0 = 0; i0 < M; i0 += RB) {                                  \
-      int64_t i1 = MIN(i0 + RB, M);                                           \
-      for (int64_t i = i0; i < i1; i++)                                       \
-        for (int64_t j = 0; j < N; j++) c[i * N + j] = (T)0;                  \
-      for (int64_t k0 = 0; k0 < K; k0 += KB) {                                \
-        int64_t k1 = MIN(k0 + KB, K);                                         \
-        for (int64_t j0 = 0; j0 < N; j0 += JB) {                              \
-          int64_t j1 = MIN(j0 + JB, N);                                       \
-          for (int64_t i = i0; i < i1; i++) {                                 \
-            T *restrict ci = c + i * N;                                       \
-            for (int64_t k = k0; k < k1; k++) {                               \
-              const T aik = a[i * K + k];                                     \
-              const T *restrict bk = b + k * N;                               \
-              for (int64_t j = j0; j < j1; j++) ci[j] = FMA(aik, bk[j], ci[j]); \
+    enum { MR = MR_, NR = NR_ };                                              \
+    T *bp = (T *)malloc(sizeof(T) * FKC * (FNC + NR));                        \
+    for (int64_t i = 0; i < M * N; i++) c[i] = (T)0;                          \
+    for (int64_t jc = 0; jc < N; jc += FNC) {                                 \
+      const int64_t nc = MIN(FNC, N - jc);                                    \
+      const int64_t nstrips = (nc + NR - 1) / NR;                             \
+      for (int64_t pc = 0; pc < K; pc += FKC) {                               \
+        const int64_t kc = MIN(FKC, K - pc);                                  \
+        _Pragma("omp parallel for schedule(static)")                          \
+        for (int64_t js = 0; js < nstrips; js++)                              \
+          for (int64_t k = 0; k < kc; k++)                                    \
+            for (int j = 0; j < NR; j++) {                                    \
+              const int64_t col = jc + js * NR + j;                           \
+              bp[(js * kc + k) * NR + j] =                                    \
+                  col < N ? b[(pc + k) * N + col] : (T)0;                     \
             }                                                                 \
+        _Pragma("omp parallel for schedule(dynamic, 4)")                      \
+        for (int64_t ib = 0; ib < (M + MR - 1) / MR; ib++) {                  \
+          const int64_t i0 = ib * MR;                                         \
+          const int mr = (int)MIN(MR, M - i0);                                \
+          T ta[MR * FKC], tc[MR * NR];                                        \
+          for (int64_t js = 0; js < nstrips; js++) {                          \
+            const int64_t j0 = jc + js * NR;                                  \
+            const int nr = (int)MIN(NR, N - j0);                              \
+            const T *bs = bp + js * kc * NR;                                  \
+            if (mr == MR && nr == NR) {                                       \
+              MICRO(a + i0 * K + pc, K, bs, c + i0 * N + j0, N, kc);   \
+              continue;                                                       \
+            }                                                                 \
+            /* Ragged edge: run the same micro-kernel on zero-padded copies   \
+             * (padding never reaches a stored output). */                    \
+            for (int r = 0; r < MR; r++) {                                    \
+              for (int64_t k = 0; k < kc; k++)                                \
+                ta[r * kc + k] = r < mr ? a[(i0 + r) * K + pc + k] : (T)0;    \
+              for (int j = 0; j < NR; j++)                                    \
+                tc[r * NR + j] = (r < mr && j < nr) ? c[(i0 + r) * N + j0 + j] : (T)0; \
+            }                                                                 \
+            MICRO(ta, kc, bs, tc, NR, kc);                             \
+            for (int r = 0; r < mr; r++)                                      \
+              for (int j = 0; j < nr; j++)                                    \
+                c[(i0 + r) * N + j0 + j] = tc[r * NR + j];                    \
           }                                                                   \
         }                                                                     \
       }                                                                       \
     }                                                                         \
+    free(bp);                                                                 \
   }
 
-DEFINE_FLOAT_KERNEL(kern_f32, float, fmaf)
-DEFINE_FLOAT_KERNEL(kern_f64, double, fma)
+DEFINE_FLOAT_KERNEL(kern_f32, float, oracle_micro_f32, 6, 16)
+DEFINE_FLOAT_KERNEL(kern_f64, double, oracle_micro_f64, 6, 8)
 
 /* Outputs of the x86 AVX2 build that are not a plain FMA chain.
  *
@@ -137,40 +179,70 @@ DEFINE_FLOAT_KERNEL(kern_f64, double, fma)
  * the stored value.  The tile grid is MC x NR inside NC=4080 column panels.
  */
 #define DEFINE_FLOAT_EDGES(NAME, T, FMA, THR, NR, VW, MC)                     \
+  /* Packed-path remainder output (i, j): per-KC chains summed in order. */   \
+  static T NAME##_packed_one(const T *a, const T *b, int64_t i, int64_t j,   \
+                             int64_t K, int64_t N) {                          \
+    T d = (T)0;                                                               \
+    for (int64_t pc = 0; pc < K; pc += 256) {                                 \
+      int64_t pe = MIN(pc + 256, K);                                          \
+      T t = (T)0;                                                             \
+      for (int64_t k = pc; k < pe; k++) t = FMA(a[i * K + k], b[k * N + j], t); \
+      d = (pc == 0) ? t : d + t;                                              \
+    }                                                                         \
+    return d;                                                                 \
+  }                                                                           \
   static void NAME(const T *a, const T *b, T *c, int64_t M, int64_t K,       \
                    int64_t N) {                                               \
     int packed = (uint64_t)M * (uint64_t)K * (uint64_t)N > (THR);             \
+    if (packed) {                                                             \
+      /* Rows of a remainder row tile: every column is a remainder output;   \
+       * computed a whole row at a time (same arithmetic per output, B read  \
+       * along rows).  Other rows: only the tail columns of each panel. */   \
+      _Pragma("omp parallel")                                                 \
+      {                                                                       \
+        T *t = (T *)malloc(sizeof(T) * (size_t)(2 * N + 1)), *d = t + N;      \
+        _Pragma("omp for schedule(dynamic, 1)")                               \
+        for (int64_t i = 0; i < M; i++) {                                     \
+          int64_t ic = (i / (MC)) * (MC), mc = MIN((MC), M - ic);             \
+          int64_t ir = ((i - ic) / 6) * 6, mr = MIN(6, mc - ir);              \
+          if (mr < 6) {                                                       \
+            for (int64_t pc = 0; pc < K; pc += 256) {                         \
+              int64_t pe = MIN(pc + 256, K);                                  \
+              for (int64_t j = 0; j < N; j++) t[j] = (T)0;                    \
+              for (int64_t k = pc; k < pe; k++) {                             \
+                const T x = a[i * K + k];                                     \
+                const T *bk = b + k * N;                                      \
+                for (int64_t j = 0; j < N; j++) t[j] = FMA(x, bk[j], t[j]);   \
+              }                                                               \
+              for (int64_t j = 0; j < N; j++) d[j] = (pc == 0) ? t[j] : d[j] + t[j]; \
+            }                                                                 \
+            for (int64_t j = 0; j < N; j++) c[i * N + j] = K ? d[j] : (T)0;   \
+            continue;                                                         \
+          }                                                                   \
+          for (int64_t jc = 0; jc < N; jc += 4080) {                          \
+            int64_t nc = MIN(4080, N - jc);                                   \
+            for (int64_t j = jc + (nc / (NR)) * (NR); j < jc + nc; j++)       \
+              c[i * N + j] = NAME##_packed_one(a, b, i, j, K, N);             \
+          }                                                                   \
+        }                                                                     \
+        free(t);                                                              \
+      }                                                                       \
+      return;                                                                 \
+    }                                                                         \
     _Pragma("omp parallel for schedule(dynamic, 8)")                          \
     for (int64_t i = 0; i < M; i++) {                                         \
       for (int64_t j = 0; j < N; j++) {                                       \
-        if (!packed) {                                                        \
-          int64_t mr = MIN(6, M - (i / 6) * 6);                               \
-          int64_t nr = MIN((NR), N - (j / (NR)) * (NR));                      \
-          if (mr == 6 && nr == (NR)) continue;                                \
-          int64_t jj = j - (j / (NR)) * (NR);                                 \
-          if (jj < (nr / (VW)) * (VW)) continue; /* vector FMA: chain */      \
-          T acc = (T)0;                                                       \
-          for (int64_t k = 0; k < K; k++) {                                   \
-            T p = a[i * K + k] * b[k * N + j];                                \
-            acc = acc + p;                                                    \
-          }                                                                   \
-          c[i * N + j] = acc;                                                 \
-        } else {                                                              \
-          int64_t ic = (i / (MC)) * (MC), mc = MIN((MC), M - ic);             \
-          int64_t ir = ((i - ic) / 6) * 6, mr = MIN(6, mc - ir);              \
-          int64_t jc = (j / 4080) * 4080, nc = MIN(4080, N - jc);             \
-          int64_t jr = ((j - jc) / (NR)) * (NR), nr = MIN((NR), nc - jr);     \
-          if (mr == 6 && nr == (NR)) continue;                                \
-          T d = (T)0;                                                         \
-          for (int64_t pc = 0; pc < K; pc += 256) {                           \
-            int64_t pe = MIN(pc + 256, K);                                    \
-            T t = (T)0;                                                       \
-            for (int64_t k = pc; k < pe; k++)                                 \
-              t = FMA(a[i * K + k], b[k * N + j], t);                         \
-            d = (pc == 0) ? t : d + t;                                        \
-          }                                                                   \
-          c[i * N + j] = d;                                                   \
+        int64_t mr = MIN(6, M - (i / 6) * 6);                                 \
+        int64_t nr = MIN((NR), N - (j / (NR)) * (NR));                        \
+        if (mr == 6 && nr == (NR)) continue;                                  \
+        int64_t jj = j - (j / (NR)) * (NR);                                   \
+        if (jj < (nr / (VW)) * (VW)) continue; /* vector FMA: chain */        \
+        T acc = (T)0;                                                         \
+        for (int64_t k = 0; k < K; k++) {                                     \
+          T p = a[i * K + k] * b[k * N + j];                                  \
+          acc = acc + p;                                                      \
         }                                                                     \
+        c[i * N + j] = acc;                                                   \
       }                                                                       \
     }                                                                         \
   }
