@@ -1,16 +1,17 @@
 """Benchmark of numc_matmul on GB300 (one JSON line on stdout).
 
 Headline workload: float32 M = N = K = 8192, entries N(0, 1) (seeded
-splitmix64), computed by the 3-pass split-BF16 tcgen05 kernel through the
+splitmix64), computed as a 3-pass split product on tcgen05 from scaled
+float16 planes (NUMC_CUDA_ALGO_SPLIT_FP16: float32-level error) through the
 device-pointer C-ABI numc_cuda_gemm with operands resident in HBM.  A step is
-one full matmul (split pass + GEMM).  Inputs (2 x 256 MiB) and the split
-planes (2 x 256 MiB) exceed the 126 MiB L2, so no flush is needed between
-steps.  `value` is algorithmic TFLOP/s, 2*M*N*K / step time, summed over
-ranks (replicas: every rank computes the same product on its own GPU).
+one full matmul (scale pass + split pass + GEMM).  Inputs (2 x 256 MiB) and
+the split planes (2 x 256 MiB) exceed the 126 MiB L2, so no flush is needed
+between steps.  `value` is algorithmic TFLOP/s, 2*M*N*K / step time, summed
+over ranks (replicas: every rank computes the same product on its own GPU).
 
 Beside it, on the same run: the plain FP32-SIMT kernel on the same inputs,
-max/mean error of both against a float64-accurate oracle (compensated dot
-products), the ill-scaled variant, `e2e` through numc_matmul with host
+the 3- and 6-pass split-BF16 kernels, max/mean error of each against a
+float64-accurate oracle (compensated dot products), the ill-scaled variant, `e2e` through numc_matmul with host
 arrays (host<->device copies in the timed region), float64 at 4096^3 (SIMT
 and DMMA), the integer bit-exactness workload at 1024^3, and the CPU
 baseline (numc's arithmetic restated in C, OpenMP, on a row sample).
@@ -286,12 +287,12 @@ def main():
     a = torch.from_numpy(a_h).to(dev)
     b = torch.from_numpy(b_h).to(dev)
     c = torch.empty((M, N), dtype=torch.float32, device=dev)
-    ws_bytes = nc.workspace_size("float32", nc.ALGO_SPLIT_BF16, 0, M, K, N)
+    ws_bytes = nc.workspace_size("float32", HEAD_ALGO, 0, M, K, N)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
 
-    # -- headline: split-BF16, device-resident -------------------------------
+    # -- headline: 3-pass split from scaled float16 planes, device-resident --
     for _ in range(max(3, args.warmup)):
-        nc.gemm(a, b, c, algo=nc.ALGO_SPLIT_BF16, workspace=ws)
+        nc.gemm(a, b, c, algo=HEAD_ALGO, workspace=ws)
     torch.cuda.synchronize()
     sampler = ClockSampler(gpu_id_for_smi(local))
     time.sleep(0.3)
@@ -304,7 +305,7 @@ def main():
     t_wall0 = time.time()
     e0.record(stream)
     for _ in range(args.steps):
-        nc.gemm(a, b, c, algo=nc.ALGO_SPLIT_BF16, workspace=ws)
+        nc.gemm(a, b, c, algo=HEAD_ALGO, workspace=ws)
     e1.record(stream)
     torch.cuda.synchronize()
     t_wall1 = time.time()
@@ -323,25 +324,31 @@ def main():
     if os.path.exists(pk):
         peaks = json.load(open(pk))
     bf16_peak = peaks.get("bf16_tflops")
+    sustained = peaks.get("bf16_tflops_sustained")
     peak_src = "measured" if bf16_peak else "fallback"
     bf16_peak = bf16_peak or 1900.0
+    sustained = sustained or 1700.0
     gemm_avg = gemm_ms / max(1, calls)
-    tensor_flops = 3 * FLOPS   # three bf16 products per float32 product
+    tensor_flops = 3 * FLOPS   # three 16-bit products per float32 product
     achieved = tensor_flops / (gemm_avg * 1e-3) / 1e12
     roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak,
                 "unit": "TFLOP/s", "frac": achieved / bf16_peak,
-                "traffic": TRAFFIC_PER_LAUNCH, "kernel": "split_bf16_gemm<128,3,2,8>",
-                "kernel_ms": gemm_avg, "split_pass_ms": prep_ms / max(1, calls),
-                "peak_source": f"bf16_tflops of {peak_src}",
+                "frac_of_sustained": achieved / sustained,
+                "traffic": TRAFFIC_PER_LAUNCH, "kernel": HEAD_KERNEL,
+                "kernel_ms": gemm_avg, "scale_and_split_passes_ms": prep_ms / max(1, calls),
+                "peak_source": f"bf16_tflops (burst) and bf16_tflops_sustained of {peak_src}; "
+                               "fp16 and bf16 tcgen05 rates are equal",
                 "algorithmic_flops_per_launch": tensor_flops}
 
     result = {
-        "metric": "numc_matmul float32 8192^3 TFLOP/s (split-BF16 tcgen05 vs plain FP32-SIMT)",
+        "metric": "numc_matmul float32 8192^3 TFLOP/s (3-pass split on tcgen05 at float32-level "
+                  "error vs plain FP32-SIMT)",
         "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded splitmix64 N(0,1))",
-        "config": {"workload": "f32 8192x8192x8192 N(0,1), seed 42, split-BF16 x3",
+        "config": {"workload": "f32 8192x8192x8192 N(0,1), seed 42, 3-pass split from "
+                               "row/column-scaled float16 planes (NUMC_CUDA_ALGO_SPLIT_FP16)",
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs 512 MiB + split planes 512 MiB > 126 MiB L2, no flush"},
         "gpu_launches": int(launches),
@@ -365,8 +372,10 @@ def main():
         dist.destroy_process_group()
 
 
-# DRAM bytes (read + write) of one split_bf16_gemm launch at 8192^3, from the
-# ncu capture summarised in profiles/split_bf16_gemm_f32_8192.md.
+# The headline kernel, and its DRAM bytes (read + write) per launch at
+# 8192^3 from the ncu capture summarised in profiles/split_gemm_f32_8192.md.
+HEAD_ALGO = 7   # NUMC_CUDA_ALGO_SPLIT_FP16
+HEAD_KERNEL = "split_gemm<256,3,2,4,F16,2> (CTA pairs, 256x256 tiles)"
 TRAFFIC_PER_LAUNCH = 3.128487e9 + 0.267226e9
 
 
@@ -378,21 +387,30 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
     ref = oracle.dot_f32_ref(a_h, b_h, rows, cols)
     absprod = oracle.dot_f32_ref(np.abs(a_h), np.abs(b_h), rows, cols)
     c_plain = c.cpu().numpy()[rows, cols]
-    nc.gemm(a, b, c, algo=nc.ALGO_SPLIT_BF16, workspace=ws)
+    nc.gemm(a, b, c, algo=HEAD_ALGO, workspace=ws)
     torch.cuda.synchronize()
     c_split = c.cpu().numpy()[rows, cols]
     out["plain"] = {"value": FLOPS / (plain_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
                     "ms_per_step": plain_ms, "kernel": "simt_gemm<float,128,128,8,8,8>"}
+    # three passes from bfloat16 planes: faster, about 2^-16 error
+    ws3 = torch.empty(nc.workspace_size("float32", nc.ALGO_SPLIT_BF16, 3, M, K, N),
+                      dtype=torch.uint8, device=dev)
+    s3_ms = time_gemm(nc, torch, a, b, c, nc.ALGO_SPLIT_BF16, 3, steps=20, warmup=3, ws=ws3)
+    c_split3 = c.cpu().numpy()[rows, cols]
+    out["split_bf16"] = {"value": FLOPS / (s3_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+                         "ms_per_step": s3_ms, "kernel": "split_gemm<256,3,2,8,BF16,2>",
+                         "vs_plain": plain_ms / s3_ms}
     # six passes (three exact bf16 planes): float32-level error
     ws6 = torch.empty(nc.workspace_size("float32", nc.ALGO_SPLIT_BF16, 6, M, K, N),
                       dtype=torch.uint8, device=dev)
     s6_ms = time_gemm(nc, torch, a, b, c, nc.ALGO_SPLIT_BF16, 6, steps=20, warmup=3, ws=ws6)
     c_split6 = c.cpu().numpy()[rows, cols]
     out["split6"] = {"value": FLOPS / (s6_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
-                     "ms_per_step": s6_ms, "kernel": "split_bf16_gemm<128,2,3,1>",
+                     "ms_per_step": s6_ms, "kernel": "split_gemm<128,3,3,1,BF16,2>",
                      "vs_plain": plain_ms / s6_ms}
     out["errors_vs_fp64_oracle"] = {
-        "well_scaled": {"split_bf16": sample_errors(c_split, ref, absprod),
+        "well_scaled": {"split_fp16 (headline)": sample_errors(c_split, ref, absprod),
+                        "split_bf16": sample_errors(c_split3, ref, absprod),
                         "split_bf16_6pass": sample_errors(c_split6, ref, absprod),
                         "plain_fp32": sample_errors(c_plain, ref, absprod),
                         "sample": "512 outputs, float64 compensated dot reference"}}
@@ -406,24 +424,28 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
     ai_h, bi_h = ai.cpu().numpy(), bi.cpu().numpy()
     ref_i = oracle.dot_f32_ref(ai_h, bi_h, rows, cols)
     abs_i = oracle.dot_f32_ref(np.abs(ai_h), np.abs(bi_h), rows, cols)
-    nc.gemm(ai, bi, c, algo=nc.ALGO_SPLIT_BF16, workspace=ws)
+    nc.gemm(ai, bi, c, algo=HEAD_ALGO, workspace=ws)
     torch.cuda.synchronize()
     s_i = c.cpu().numpy()[rows, cols]
+    nc.gemm(ai, bi, c, algo=nc.ALGO_SPLIT_BF16, param=3, workspace=ws3)
+    torch.cuda.synchronize()
+    s3_i = c.cpu().numpy()[rows, cols]
     nc.gemm(ai, bi, c, algo=nc.ALGO_SIMT)
     torch.cuda.synchronize()
     p_i = c.cpu().numpy()[rows, cols]
     nc.gemm(ai, bi, c, algo=nc.ALGO_SPLIT_BF16, param=6, workspace=ws6)
     torch.cuda.synchronize()
     s6_i = c.cpu().numpy()[rows, cols]
-    del ws6
+    del ws6, ws3
     out["errors_vs_fp64_oracle"]["ill_scaled"] = {
-        "split_bf16": sample_errors(s_i, ref_i, abs_i),
+        "split_fp16 (headline)": sample_errors(s_i, ref_i, abs_i),
+        "split_bf16": sample_errors(s3_i, ref_i, abs_i),
         "split_bf16_6pass": sample_errors(s6_i, ref_i, abs_i),
         "plain_fp32": sample_errors(p_i, ref_i, abs_i)}
     del ai, bi
 
     # e2e: numc_matmul with host arrays (pinned arena), copies in the region
-    nc.set_algo("float32", nc.ALGO_SPLIT_BF16)
+    nc.set_algo("float32", HEAD_ALGO)
     with nc.Ctx() as ctx:
         A, B, C = ctx.from_numpy(a_h), ctx.from_numpy(b_h), ctx.zeros((M, N), "float32")
         nc.matmul(A, B, C)
@@ -436,7 +458,7 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
     out["e2e"] = {"value": FLOPS / e2e_s / 1e12, "unit": "TFLOP/s",
                   "h2d_bytes_per_step": 2 * M * K * 4, "d2h_bytes_per_step": M * N * 4,
                   "ms_per_step": e2e_s * 1e3, "steps": steps,
-                  "api": "numc_matmul(NumcArray host buffers), split-BF16"}
+                  "api": "numc_matmul(NumcArray host buffers), SPLIT_FP16"}
 
     # config 1: float32 512^3, uniform [-1, 1)
     a1, b1 = synth.operands("uniform", 512, 512, 512, dtype="float32")
@@ -444,7 +466,7 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
     tc1 = torch.empty((512, 512), device=dev)
     f1 = 2.0 * 512 ** 3
     ms_p = time_gemm(nc, torch, ta1, tb1, tc1, nc.ALGO_SIMT, 0, steps=200, warmup=10)
-    ms_s = time_gemm(nc, torch, ta1, tb1, tc1, nc.ALGO_SPLIT_BF16, 0, steps=200, warmup=10)
+    ms_s = time_gemm(nc, torch, ta1, tb1, tc1, HEAD_ALGO, 0, steps=200, warmup=10)
     out["f32_512"] = {"plain_tflops": f1 / ms_p / 1e9, "split_tflops": f1 / ms_s / 1e9,
                       "plain_us": ms_p * 1e3, "split_us": ms_s * 1e3,
                       "note": "L2-resident, latency-bound"}

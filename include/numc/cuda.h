@@ -40,14 +40,24 @@ typedef enum {
                                     integer slices, exact slice products on
                                     tcgen05, integer recombination; `param`
                                     = slice count 1..8 (default 8) */
-  NUMC_CUDA_ALGO_AUTO = 5,       /* float32: split-BF16 when the problem is
+  NUMC_CUDA_ALGO_AUTO = 5,       /* float32: SPLIT_FP16 when the problem is
                                     large enough to pay for it, else SIMT;
                                     int8/uint8 (their default): TC_INT8 when
                                     M*K*N >= 2^21, else SIMT */
-  NUMC_CUDA_ALGO_TC_INT8 = 6     /* int8/uint8 on tcgen05 (values exact in
+  NUMC_CUDA_ALGO_TC_INT8 = 6,    /* int8/uint8 on tcgen05 (values exact in
                                     bfloat16, exact FP32 sums per numc K
                                     block) with numc's store rules; `param`
                                     is a NumcInt8Profile */
+  NUMC_CUDA_ALGO_SPLIT_FP16 = 7  /* float32 on tcgen05 from float16 planes:
+                                    each row of A and column of B scaled by
+                                    a power of two, x 2^s = h0 + h1 (22
+                                    significant bits), h0h0 + h0h1 + h1h0
+                                    with float32 accumulation, result
+                                    scaled back exactly.  float32-level
+                                    error at the cost of 3 products.
+                                    `param` = K slabs of 64 per tensor-
+                                    memory accumulation chain: 1, 2, 4 or 8
+                                    (0 = default) */
 } NumcCudaAlgo;
 
 /* Which numc build's int8/uint8 results to reproduce (the store rules of
@@ -64,7 +74,7 @@ NUMC_API int numc_cuda_device_count(void);
 /* Process-wide algorithm per dtype used by numc_matmul and by
  * NUMC_CUDA_ALGO_DEFAULT.  For float64 OZAKI, `param` is the slice count;
  * for int8/uint8, `param` is a NumcInt8Profile.  Environment defaults:
- * NUMC_CUDA_F32_ALGO (simt|split|split6|auto), NUMC_CUDA_F64_ALGO (simt|dmma|
+ * NUMC_CUDA_F32_ALGO (simt|split|split6|split16|auto), NUMC_CUDA_F64_ALGO (simt|dmma|
  * ozaki[:slices]), NUMC_CUDA_INT8_PROFILE (x86|neon|wrap). */
 NUMC_API int numc_cuda_set_algo(NumcDType dtype, int algo, int param);
 NUMC_API int numc_cuda_get_algo(NumcDType dtype, int *algo, int *param);

@@ -26,7 +26,8 @@ ERR_NONE, ERR_NULL, ERR_MALLOC, ERR_SHAPE = 0, -1, -2, -3
 ERR_TYPE, ERR_BOUNDS, ERR_VALUE, ERR_INTERNAL = -4, -5, -6, -99
 
 # NumcCudaAlgo (include/numc/cuda.h)
-ALGO_DEFAULT, ALGO_SIMT, ALGO_SPLIT_BF16, ALGO_DMMA, ALGO_OZAKI, ALGO_AUTO, ALGO_TC_INT8 = range(7)
+(ALGO_DEFAULT, ALGO_SIMT, ALGO_SPLIT_BF16, ALGO_DMMA, ALGO_OZAKI, ALGO_AUTO, ALGO_TC_INT8,
+ ALGO_SPLIT_FP16) = range(8)
 INT8_X86_AVX2, INT8_ARM_NEON, INT8_WRAP = 0, 1, 2
 
 

@@ -49,6 +49,7 @@ void init_algos_from_env() {
       g_algo[NUMC_DTYPE_FLOAT32].algo = NUMC_CUDA_ALGO_SPLIT_BF16;
       g_algo[NUMC_DTYPE_FLOAT32].param = 6;
     }
+    else if (v == "split16") g_algo[NUMC_DTYPE_FLOAT32].algo = NUMC_CUDA_ALGO_SPLIT_FP16;
     else if (v == "auto") g_algo[NUMC_DTYPE_FLOAT32].algo = NUMC_CUDA_ALGO_AUTO;
   }
   if (const char *e = getenv("NUMC_CUDA_F64_ALGO")) {
@@ -148,11 +149,12 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
   } else if (algo == NUMC_CUDA_ALGO_AUTO) {
     if (dt != NUMC_DTYPE_FLOAT32)
       return NUMC_SET_ERROR(NUMC_ERR_VALUE, "AUTO algorithm is float32, int8 or uint8 only");
-    // Split-BF16 pays for its split pass once each output sums enough terms
-    // and the grid fills the GPU.
-    algo = ((uint64_t)M * N >= (1u << 16) && K >= 128) ? NUMC_CUDA_ALGO_SPLIT_BF16
+    // The scaled float16 split (float32-level error) pays for its scale
+    // and split passes once each output sums enough terms and the grid
+    // fills the GPU.
+    algo = ((uint64_t)M * N >= (1u << 16) && K >= 128) ? NUMC_CUDA_ALGO_SPLIT_FP16
                                                       : NUMC_CUDA_ALGO_SIMT;
-    if (param != 6) param = 0;
+    param = 0;
   }
   switch (algo) {
   case NUMC_CUDA_ALGO_SIMT: break;
@@ -162,6 +164,13 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
     if (param == 0) param = 3;
     if (param != 3 && param != 6)
       return NUMC_SET_ERROR(NUMC_ERR_VALUE, "split-BF16 pass count %d is not 3 or 6", param);
+    break;
+  case NUMC_CUDA_ALGO_SPLIT_FP16:
+    if (dt != NUMC_DTYPE_FLOAT32)
+      return NUMC_SET_ERROR(NUMC_ERR_TYPE, "split-FP16 GEMM is float32 only");
+    if (param != 0 && param != 1 && param != 2 && param != 4 && param != 8)
+      return NUMC_SET_ERROR(NUMC_ERR_VALUE, "split-FP16 flush interval %d is not 1, 2, 4 or 8",
+                            param);
     break;
   case NUMC_CUDA_ALGO_DMMA:
     if (dt != NUMC_DTYPE_FLOAT64)
@@ -199,6 +208,7 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
 
 size_t plan_workspace(const Plan &p, size_t M, size_t K, size_t N) {
   if (p.algo == NUMC_CUDA_ALGO_SPLIT_BF16) return numc_k::split_bf16_workspace(M, K, N, p.param);
+  if (p.algo == NUMC_CUDA_ALGO_SPLIT_FP16) return numc_k::split_f16_workspace(M, K, N);
   if (p.algo == NUMC_CUDA_ALGO_OZAKI) return numc_k::ozaki_workspace(M, K, N, p.param);
   if (p.algo == NUMC_CUDA_ALGO_TC_INT8) return numc_k::int8_tc_workspace(M, K, N);
   return 0;
@@ -211,6 +221,7 @@ int run_plan(NumcDType dt, const Plan &p, const numc_k::Gemm &g, void *ws,
   case NUMC_CUDA_ALGO_SIMT: e = numc_k::launch_simt(dt, g, p.param, s); break;
   case NUMC_CUDA_ALGO_DMMA: e = numc_k::launch_dmma(g, s); break;
   case NUMC_CUDA_ALGO_SPLIT_BF16: e = numc_k::launch_split_bf16(g, p.param, ws, ws_bytes, s); break;
+  case NUMC_CUDA_ALGO_SPLIT_FP16: e = numc_k::launch_split_f16(g, p.param, ws, ws_bytes, s); break;
   case NUMC_CUDA_ALGO_OZAKI: e = numc_k::launch_ozaki(g, p.param, ws, ws_bytes, s); break;
   case NUMC_CUDA_ALGO_TC_INT8: e = numc_k::launch_int8_tc(dt, g, p.param, ws, ws_bytes, s); break;
   }
@@ -322,8 +333,8 @@ int matmul_impl(const NumcArray *a, const NumcArray *b, NumcArray *out, int algo
     CU(cudaMemcpyAsync(out->data, dout, so, cudaMemcpyDeviceToHost, s), "copy out to host");
     CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   }
-  if (plan.algo == NUMC_CUDA_ALGO_SPLIT_BF16 || plan.algo == NUMC_CUDA_ALGO_OZAKI ||
-      plan.algo == NUMC_CUDA_ALGO_TC_INT8) {
+  if (plan.algo == NUMC_CUDA_ALGO_SPLIT_BF16 || plan.algo == NUMC_CUDA_ALGO_SPLIT_FP16 ||
+      plan.algo == NUMC_CUDA_ALGO_OZAKI || plan.algo == NUMC_CUDA_ALGO_TC_INT8) {
     unsigned st = 0;
     CU(numc_k::read_and_clear_status(&st, s), "status read");
     if (st) return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "matmul kernel abandoned a bounded wait (code %u)", st);

@@ -1,32 +1,39 @@
-// float32 GEMM as a split-BF16 product on the 5th-generation tensor cores
+// float32 GEMM as a split product on the 5th-generation tensor cores
 // (tcgen05), the fast alternative to numc's FP32 FMA GEMM
 // (src/intrinsics/gemm_avx2.h:852 gemm_f32_avx2).
 //
-// Every float32 x is cut into bfloat16 planes by repeated rounding:
+// Every float32 x is cut into 16-bit planes by repeated rounding.
+// bfloat16 planes:
 //   x0 = bf16(x), x1 = bf16(x - x0), x2 = bf16(x - x0 - x1).
 // Each remainder is exact in float32, and x0 + x1 + x2 == x exactly for
 // normal numbers (8 + 8 + 8 significant bits).
 //   2 planes, 3 products:  A0B0 + A0B1 + A1B0           (error ~2^-16 |ab|)
 //   3 planes, 6 products:  ... + A0B2 + A1B1 + A2B0     (error ~2^-24 |ab|)
-// Products of bf16 values are exact in FP32.  Within a chunk of K slabs the
+// Scaled float16 planes (split_common.cuh): rows of A and columns of B are
+// scaled by powers of two into [2^14, 2^15), x 2^s = h0 + h1 (11 + 11
+// bits); 3 products h1h0 + h0h1 + h0h0 give float32-level error, and the
+// epilogue multiplies by 2^-(s_row + s_col).
+// Products of 16-bit values are exact in FP32.  Within a chunk of K slabs the
 // products are summed in a tensor-memory FP32 accumulator (smallest terms
 // first); the chunks' partial sums are added in FP32 registers with
 // round-to-nearest, because the tensor core's accumulation truncates at
 // every MMA step and loses hundreds of ulps over a K = 8192 chain.
 //
-// Pass 1 (split kernel, HBM-bound): reads A and B once with any strides and
-// writes the planes K-major with K padded to 64 (B is transposed on the
-// way), so every plane suits a 128-byte-swizzled TMA box.
-// Pass 2 (GEMM kernel): persistent, one CTA per SM walking 128 x BN output
-// tiles, ten warps.  Warp
-// 0 streams 64-deep K slabs of every plane of A and B into a STAGES-deep
-// shared-memory ring with TMA (one 3-D tensor map per operand, the plane is
-// the third coordinate); warp 1 issues the tcgen05.mma.kind::f16 products
-// of each chunk into one of four TMEM buffers and releases ring slots with
-// tcgen05.commit; warps 2-9 drain each finished buffer (tcgen05.ld 32x32b)
-// into register accumulators while the next chunk is multiplied, then
-// store the tile.  Tiles are rasterised in groups of 16 row-tiles so the live
-// operand panels stay in L2.
+// Pass 1 (split kernels, HBM-bound): for float16 planes a scale pass finds
+// the row / column maxima; the split pass reads A and B once with any
+// strides and writes the planes K-major with K padded to 64 (B is
+// transposed on the way), so every plane suits a 128-byte-swizzled TMA box.
+// Pass 2 (GEMM kernel): persistent; by default clusters of two CTAs on
+// neighbouring SMs walk 256 x 256 output tiles (each CTA 128 rows, 18
+// warps).  Warp 0 streams 64-deep K slabs of every plane of A and of its
+// half of B into a STAGES-deep shared-memory ring with TMA (one 3-D tensor
+// map per operand, the plane is the third coordinate); warp 1 of the even
+// CTA issues the tcgen05.mma.cta_group::2.kind::f16 products of each chunk
+// into one of two TMEM buffers of both CTAs and releases ring slots with
+// tcgen05.commit; 16 accumulator warps per CTA drain each finished buffer
+// (tcgen05.ld 32x32b) into register accumulators while the next chunk is
+// multiplied, then store the tile.  Tiles are rasterised in groups of 2048
+// rows so the live operand panels stay in L2.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -52,14 +59,16 @@ __host__ __device__ inline int64_t round_up(int64_t x, int64_t a) { return (x + 
 
 // ---- pass 1: split float32 into bf16 planes (split_common.cuh) -------------
 
-template <int PLANES>
+template <int PLANES, bool F16>
 __global__ void __launch_bounds__(256)
-split_f32_bf16(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_t R,
-               int64_t K, int64_t Kp, __nv_bfloat16 *__restrict__ planes,
-               unsigned long long *flags, int flag_rows, unsigned long long gen, int mode) {
+split_planes(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_t R,
+               int64_t K, int64_t Kp, uint16_t *__restrict__ planes,
+               unsigned long long *flags, int flag_rows, unsigned long long gen, int mode,
+               const unsigned *maxbits) {
   __shared__ __align__(16) float tile[kSplitRows][kSplitK + 4];
-  split_tile<PLANES>(src, rs_row, rs_k, R, K, Kp, planes, flags, flag_rows, gen, mode,
-                     (int64_t)blockIdx.y * kSplitRows, (int64_t)blockIdx.x * kSplitK, tile);
+  split_tile<PLANES, F16>(src, rs_row, rs_k, R, K, Kp, planes, flags, flag_rows, gen, mode,
+                          (int64_t)blockIdx.y * kSplitRows, (int64_t)blockIdx.x * kSplitK, tile,
+                          maxbits);
 }
 
 // ---- pass 2: the tcgen05 GEMM ------------------------------------------------
@@ -71,19 +80,23 @@ struct Fallback {
   int64_t rsa, csa, rsb, csb, K;
   const unsigned long long *flags_a, *flags_b;   // per 128 rows of A, per 64 columns of B
   unsigned long long gen;
+  const unsigned *max_a, *max_b;   // scaled float16 planes: row / column maxima
 };
 
-template <int BN, int STAGES, int PLANES, int FLUSH>
+template <int BN, int STAGES, int PLANES, int FLUSH, int CTAS>
 struct SplitCfg {
+  static constexpr int BN_CTA = BN / CTAS;            // B rows (output columns) held per CTA
   static constexpr uint32_t A_BYTES = kBM * kBK * 2;   // one plane of a K slab of A
-  static constexpr uint32_t B_BYTES = BN * kBK * 2;
-  static constexpr uint32_t STAGE_BYTES = PLANES * (A_BYTES + B_BYTES);
+  static constexpr uint32_t B_BYTES = BN_CTA * kBK * 2;
+  static constexpr uint32_t STAGE_BYTES = PLANES * (A_BYTES + B_BYTES);   // per CTA
   static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
   static constexpr int NBUF = 512 / BN;           // FP32 accumulator buffers in TMEM
   static constexpr uint32_t TMEM_COLS = NBUF * BN;
-  static constexpr int ACC_WARPS = 8;             // two per TMEM lane quadrant
-  static constexpr int COLS_PER_WARP = BN / 2;
+  static constexpr int COLS_PER_WARP = 64;
+  static constexpr int ACC_WARPS = 4 * BN / COLS_PER_WARP;   // BN / 64 per TMEM lane quadrant
   static constexpr int THREADS = 64 + 32 * ACC_WARPS;   // producer, MMA, accumulators
+  static_assert(BN == 128 || BN == 256, "tile width");
+  static_assert(CTAS == 1 || CTAS == 2, "one CTA or a CTA pair");
   static_assert(SMEM <= 232448, "shared memory");
   static_assert((2 * STAGES + 2 * NBUF) * 8 + 4 <= 256, "barrier space");
   static_assert(TMEM_COLS <= 512, "tensor memory");
@@ -103,28 +116,42 @@ template <> struct Products<3> {
   __device__ static constexpr int b(int t) { return t == 2 ? 2 : (t == 1 || t == 4) ? 1 : 0; }
 };
 
-// Warp roles (320 threads):
+// Warp roles (64 + 32 * BN / 16 threads per CTA):
 //   warp 0, lane 0   TMA producer: fills the STAGES-deep ring of K slabs.
 //   warp 1, lane 0   MMA issuer: for chunk c (FLUSH consecutive K slabs),
 //                    accumulates all products into TMEM buffer c % NBUF
 //                    (starting from zero) and commits it to the
 //                    accumulator warps.
-//   warps 2..9       accumulator warps, two per TMEM lane quadrant, each
-//                    owning half of the tile's columns: drain each chunk's
-//                    partial sums from TMEM and add them into FP32
+//   warps 2..        accumulator warps, BN / 64 per TMEM lane quadrant,
+//                    each owning 64 of the tile's columns: drain each
+//                    chunk's partial sums from TMEM and add them into FP32
 //                    registers (round to nearest), then release the
 //                    buffer; finally store.
+// BN = 256 halves the MMA instructions, waits and commits per flop against
+// BN = 128; measured on GB300 with the operand loads and TMEM drains
+// switched off, the bare MMA loop reached 1478 TFLOP/s at BN = 128 and
+// 1807 at BN = 256 (flush 4).
 // The tensor core's own FP32 accumulation truncates at every MMA step; a
 // chain of K/16 x passes steps loses hundreds of ulps at K = 8192, so the
 // chain in TMEM is restarted every FLUSH K slabs and the chunks are summed
 // with correctly rounded FP32 adds.
-template <int BN, int STAGES, int PLANES, int FLUSH>
-__global__ void __launch_bounds__(SplitCfg<BN, STAGES, PLANES, FLUSH>::THREADS, 1)
-split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB,
-                float *__restrict__ C, int64_t rso, int64_t cso, int M, int N, int num_kb,
-                int tiles_m, int tiles_n, int vec4, unsigned *status, Fallback fb) {
-  using Cfg = SplitCfg<BN, STAGES, PLANES, FLUSH>;
+//
+// CTAS = 2 runs the kernel as clusters of two CTAs on neighbouring SMs
+// sharing 256 x BN output tiles: each CTA loads its own 128 rows of A and
+// BN/2 rows of B^T, the even CTA's MMA thread multiplies both halves with
+// cta_group::2 MMAs (each SM reads half of B from its own shared memory,
+// so per-SM operand traffic per flop drops by a quarter), its commits
+// arrive on the barriers of both CTAs, both producers count their bytes on
+// the even CTA's full barrier, and both CTAs' accumulator warps release
+// TMEM buffers on the even CTA's empty barrier.
+template <int BN, int STAGES, int PLANES, int FLUSH, bool F16, int CTAS>
+__global__ void __launch_bounds__(SplitCfg<BN, STAGES, PLANES, FLUSH, CTAS>::THREADS, 1)
+split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB,
+           float *__restrict__ C, int64_t rso, int64_t cso, int M, int N, int num_kb,
+           int tiles_m, int tiles_n, int vec4, unsigned *status, Fallback fb) {
+  using Cfg = SplitCfg<BN, STAGES, PLANES, FLUSH, CTAS>;
   using P = Products<PLANES>;
+  constexpr bool PAIR = CTAS == 2;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *bars = (uint64_t *)(smem + STAGES * Cfg::STAGE_BYTES);
@@ -134,18 +161,21 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ 
   uint32_t *tmem_slot = (uint32_t *)(bars + 2 * STAGES + 2 * NBUF);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntiles = tiles_m * tiles_n;
+  const int ntiles = tiles_m * tiles_n;   // tiles of CTAS * 128 rows
+  const uint32_t rank = PAIR ? tc::cluster_ctarank() : 0;
+  const bool leader = rank == 0;
+  const int first_tile = blockIdx.x / CTAS, tile_step = gridDim.x / CTAS;
 
-  // Persistent: CTA b handles tiles b, b + gridDim.x, ...  Tiles are
-  // rasterised in groups of 16 row-tiles that sweep all column tiles, so
-  // the CTAs in flight share A and B panels in L2.
+  // Persistent: CTA (pair) b handles tiles b, b + grid, ...  Tiles are
+  // rasterised in groups of 2048 rows that sweep all column tiles, so the
+  // CTAs in flight share A and B panels in L2.
   auto tile_origin = [&](int t, int &m0, int &n0) {
-    constexpr int GM = 16;
+    constexpr int GM = 16 / CTAS;
     const int group = t / (GM * tiles_n);
     const int first_m = group * GM;
     const int gm = min(tiles_m - first_m, GM);
     const int local = t - group * GM * tiles_n;
-    m0 = (first_m + local % gm) * kBM;
+    m0 = (first_m + local % gm) * (kBM * CTAS);
     n0 = (local / gm) * BN;
   };
 
@@ -156,15 +186,20 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ 
     }
     for (int b = 0; b < NBUF; b++) {
       tc::mbar_init(tc::smem_u32(&tfull[b]), 1);
-      tc::mbar_init(tc::smem_u32(&tempty[b]), Cfg::ACC_WARPS);   // one arrive per warp
+      // one arrive per accumulator warp of every CTA
+      tc::mbar_init(tc::smem_u32(&tempty[b]), Cfg::ACC_WARPS * CTAS);
     }
     tc::fence_barrier_init();
     tc::tma_prefetch_desc(&tA);
     tc::tma_prefetch_desc(&tB);
   }
-  if (warp == 1) tc::tmem_alloc(tc::smem_u32(tmem_slot), Cfg::TMEM_COLS);
+  if (warp == 1) {
+    if constexpr (PAIR) tc::tmem_alloc_pair(tc::smem_u32(tmem_slot), Cfg::TMEM_COLS);
+    else tc::tmem_alloc(tc::smem_u32(tmem_slot), Cfg::TMEM_COLS);
+  }
   tc::tc_fence_before();
   __syncthreads();
+  if constexpr (PAIR) tc::cluster_sync();   // peer barriers initialised
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const int num_chunks = (num_kb + FLUSH - 1) / FLUSH;   // per tile
@@ -173,9 +208,10 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ 
     if (lane == 0) {
       int g = 0;   // stage counter across tiles
       bool live = true;
-      for (int t = blockIdx.x; t < ntiles && live; t += gridDim.x) {
+      for (int t = first_tile; t < ntiles && live; t += tile_step) {
         int m0, n0;
         tile_origin(t, m0, n0);
+        const int ma = m0 + (int)rank * kBM, nb = n0 + (int)rank * Cfg::BN_CTA;
         for (int kb = 0; kb < num_kb; kb++, g++) {
           const int s = g % STAGES;
           if (g >= STAGES &&
@@ -186,23 +222,35 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ 
           }
           const uint32_t fbar = tc::smem_u32(&full[s]);
           const uint32_t st = tc::smem_u32(smem + s * Cfg::STAGE_BYTES);
-          tc::mbar_arrive_expect_tx(fbar, Cfg::STAGE_BYTES);
+          // The even CTA's full barrier counts the bytes of both CTAs.
+          if (leader) tc::mbar_arrive_expect_tx(fbar, CTAS * Cfg::STAGE_BYTES);
           const int k = kb * kBK;
+          if constexpr (PAIR) {
+            const uint32_t fbar_leader = tc::mapa_shared(fbar, 0);
 #pragma unroll
-          for (int p = 0; p < PLANES; p++) {
-            tc::tma_load_3d(st + p * Cfg::A_BYTES, &tA, fbar, k, m0, p);
-            tc::tma_load_3d(st + PLANES * Cfg::A_BYTES + p * Cfg::B_BYTES, &tB, fbar, k, n0, p);
+            for (int p = 0; p < PLANES; p++) {
+              tc::tma_load_3d_pair(st + p * Cfg::A_BYTES, &tA, fbar_leader, k, ma, p);
+              tc::tma_load_3d_pair(st + PLANES * Cfg::A_BYTES + p * Cfg::B_BYTES, &tB,
+                                   fbar_leader, k, nb, p);
+            }
+          } else {
+#pragma unroll
+            for (int p = 0; p < PLANES; p++) {
+              tc::tma_load_3d(st + p * Cfg::A_BYTES, &tA, fbar, k, ma, p);
+              tc::tma_load_3d(st + PLANES * Cfg::A_BYTES + p * Cfg::B_BYTES, &tB, fbar, k, nb, p);
+            }
           }
         }
       }
     }
     __syncwarp();
   } else if (warp == 1) {
-    if (lane == 0) {
-      constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, BN);
+    if (lane == 0 && leader) {
+      constexpr uint32_t idesc =
+          F16 ? tc::idesc_f16_f32(kBM * CTAS, BN) : tc::idesc_bf16_f32(kBM * CTAS, BN);
       int g = 0, chunk = 0;   // stage and chunk counters across tiles
       bool live = true;
-      for (int t = blockIdx.x; t < ntiles && live; t += gridDim.x) {
+      for (int t = first_tile; t < ntiles && live; t += tile_step) {
         for (int kb = 0; kb < num_kb; kb++, g++) {
           const int s = g % STAGES, buf = chunk % NBUF;
           const bool chunk_start = kb % FLUSH == 0;
@@ -224,36 +272,42 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ 
           const uint32_t acc_tmem = tmem + buf * BN;
 #pragma unroll
           for (int kk = 0; kk < kBK / 16; kk++) {
-            const uint32_t koff = kk * 32;   // 16 bf16 = 32 bytes inside the swizzle atom
+            const uint32_t koff = kk * 32;   // 16 elements = 32 bytes inside the swizzle atom
 #pragma unroll
             for (int p = 0; p < P::n; p++) {
               const uint32_t acc = (!chunk_start || kk > 0 || p > 0) ? 1u : 0u;
-              tc::mma_bf16(acc_tmem, tc::sdesc_k128(st + P::a(p) * Cfg::A_BYTES + koff),
-                           tc::sdesc_k128(bbase + P::b(p) * Cfg::B_BYTES + koff), idesc, acc);
+              const uint64_t ad = tc::sdesc_k128(st + P::a(p) * Cfg::A_BYTES + koff);
+              const uint64_t bd = tc::sdesc_k128(bbase + P::b(p) * Cfg::B_BYTES + koff);
+              if constexpr (PAIR) tc::mma_f16_pair(acc_tmem, ad, bd, idesc, acc);
+              else tc::mma_bf16(acc_tmem, ad, bd, idesc, acc);
             }
           }
-          tc::mma_commit(tc::smem_u32(&empty[s]));
-          if (chunk_end) {
-            tc::mma_commit(tc::smem_u32(&tfull[buf]));
-            chunk++;
+          if constexpr (PAIR) {
+            tc::mma_commit_pair(tc::smem_u32(&empty[s]), 0x3);
+            if (chunk_end) tc::mma_commit_pair(tc::smem_u32(&tfull[buf]), 0x3);
+          } else {
+            tc::mma_commit(tc::smem_u32(&empty[s]));
+            if (chunk_end) tc::mma_commit(tc::smem_u32(&tfull[buf]));
           }
+          if (chunk_end) chunk++;
         }
       }
     }
     __syncwarp();
   } else {
-    // Accumulator warps 2..9: warp w may read TMEM lanes 32 * (w % 4); the
-    // two warps of a quadrant split the columns.
+    // Accumulator warps: warp w may read TMEM lanes 32 * (w % 4); the
+    // warps of a quadrant split the columns 64 apiece.
     constexpr int CW = Cfg::COLS_PER_WARP;
-    const int quad = warp & 3, half = (warp - 2) >> 2;
-    const int cbase = half * CW;
+    const int quad = warp & 3, part = (warp - 2) >> 2;
+    const int cbase = part * CW;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     int chunk = 0;   // across tiles
     bool ok = true;
-    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    for (int t = first_tile; t < ntiles && ok; t += tile_step) {
       int m0, n0;
       tile_origin(t, m0, n0);
-      const int row = m0 + quad * 32 + lane;
+      const int mr = m0 + (int)rank * kBM;   // this CTA's 128 rows
+      const int row = mr + quad * 32 + lane;
       float acc[CW];
 #pragma unroll
       for (int j = 0; j < CW; j++) acc[j] = 0.0f;
@@ -264,21 +318,37 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ 
         ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
         if (!ok) break;
         tc::tc_fence_after();
-        uint32_t r[CW];
+        if constexpr (BN == 128) {
+          uint32_t r[CW];
 #pragma unroll
-        for (int c0 = 0; c0 < CW; c0 += 32)
-          tc::tmem_ld_32x32b_x32(tmem + lane_off + buf * BN + cbase + c0,
-                                 *reinterpret_cast<uint32_t(*)[32]>(&r[c0]));
-        tc::tmem_ld_wait();
+          for (int c0 = 0; c0 < CW; c0 += 32)
+            tc::tmem_ld_32x32b_x32(tmem + lane_off + buf * BN + cbase + c0,
+                                   *reinterpret_cast<uint32_t(*)[32]>(&r[c0]));
+          tc::tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < CW; j++) acc[j] = __fadd_rn(acc[j], __uint_as_float(r[j]));
+        } else {
+          // 18 warps leave 112 registers a thread: drain 16 columns at a time.
+#pragma unroll
+          for (int c0 = 0; c0 < CW; c0 += 16) {
+            uint32_t r[16];
+            tc::tmem_ld_32x32b_x16(tmem + lane_off + buf * BN + cbase + c0, r);
+            tc::tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 16; j++) acc[c0 + j] = __fadd_rn(acc[c0 + j], __uint_as_float(r[j]));
+          }
+        }
         tc::tc_fence_before();
         __syncwarp();
-        if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tempty[buf]));
-#pragma unroll
-        for (int j = 0; j < CW; j++) acc[j] = __fadd_rn(acc[j], __uint_as_float(r[j]));
+        if (lane == 0) {
+          if constexpr (PAIR) tc::mbar_arrive_cluster(tc::mapa_shared(tc::smem_u32(&tempty[buf]), 0));
+          else tc::mbar_arrive(tc::smem_u32(&tempty[buf]));
+        }
       }
       if (!ok) break;
 
-      bool nonfinite = fb.flags_a[m0 / kBM] == fb.gen;
+      // (a pair's odd CTA may lie wholly below the last row: no flag there)
+      bool nonfinite = mr < M && fb.flags_a[mr / kBM] == fb.gen;
 #pragma unroll 1
       for (int c = n0 / 64; c < (n0 + BN) / 64 && c * 64 < N; c++)
         nonfinite |= fb.flags_b[c] == fb.gen;
@@ -305,6 +375,35 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ 
             if (n0 + c0 + j < N) C[(int64_t)row * rso + (int64_t)(n0 + c0 + j) * cso] = f[j];
         }
       } else if (row < M) {
+        if (F16) {
+          // Undo the row and column scaling, acc * 2^-(sa + sb) correctly
+          // rounded: one multiply by a power of two when the exponent is a
+          // normal float32's (the product then rounds once, if at all),
+          // ldexpf otherwise.
+          const int sa = f16_scale_exp(fb.max_a[row]);
+          bool in_range = true;
+#pragma unroll 4
+          for (int j = 0; j < CW; j++) {
+            const int col = n0 + cbase + j;
+            const int e = -(sa + (col < N ? f16_scale_exp(fb.max_b[col]) : 0));
+            in_range &= e >= -126 && e <= 127;
+          }
+          if (in_range) {
+#pragma unroll
+            for (int j = 0; j < CW; j++) {
+              const int col = n0 + cbase + j;
+              const int e = -(sa + (col < N ? f16_scale_exp(fb.max_b[col]) : 0));
+              acc[j] *= exp2_int(e);
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < CW; j++) {
+              const int col = n0 + cbase + j;
+              const int e = -(sa + (col < N ? f16_scale_exp(fb.max_b[col]) : 0));
+              acc[j] = ldexpf(acc[j], e);
+            }
+          }
+        }
         float *crow = C + (int64_t)row * rso;
 #pragma unroll
         for (int c0 = 0; c0 < CW; c0 += 32) {
@@ -327,29 +426,41 @@ split_bf16_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ 
   }
   tc::tc_fence_before();
   __syncthreads();
+  // Neither CTA of a pair leaves while the other may still signal its
+  // barriers or read its shared memory.
+  if constexpr (PAIR) tc::cluster_sync();
   if (warp == 1) {
     tc::tc_fence_after();
-    tc::tmem_dealloc(tmem, Cfg::TMEM_COLS);
+    if constexpr (PAIR) tc::tmem_dealloc_pair(tmem, Cfg::TMEM_COLS);
+    else tc::tmem_dealloc(tmem, Cfg::TMEM_COLS);
   }
 }
 
 // Workspace: PLANES planes of A (M x Kp), PLANES planes of B^T (N x Kp),
-// then the non-finite flags.
+// the non-finite flags, and for scaled float16 planes the row maxima of A
+// and column maxima of B (float32 bits, M + N words).
 struct SplitLayout {
   int planes;
+  bool f16;
+  int flush;   // K slabs per TMEM accumulation chain
   int64_t Kp;
-  size_t a, b, flags_a, flags_b, total;
+  size_t a, b, flags_a, flags_b, max_a, max_b, total;
 };
 
-SplitLayout split_layout(int64_t M, int64_t K, int64_t N, int planes) {
+SplitLayout split_layout(int64_t M, int64_t K, int64_t N, int planes, bool f16 = false,
+                         int flush = 0) {
   SplitLayout L;
   L.planes = planes;
+  L.f16 = f16;
+  L.flush = flush;
   L.Kp = round_up(K > 0 ? K : 1, kBK);
   L.a = 0;
   L.b = (size_t)round_up(planes * M * L.Kp * 2, 256);
   L.flags_a = L.b + (size_t)round_up(planes * N * L.Kp * 2, 256);
   L.flags_b = L.flags_a + (size_t)round_up(((M + kBM - 1) / kBM) * 8, 256);
-  L.total = L.flags_b + (size_t)round_up(((N + 63) / 64) * 8, 256);
+  L.max_a = L.flags_b + (size_t)round_up(((N + 63) / 64) * 8, 256);
+  L.max_b = L.max_a + (f16 ? (size_t)round_up(M * 4, 256) : 0);
+  L.total = L.max_b + (f16 ? (size_t)round_up(N * 4, 256) : 0);
   return L;
 }
 
@@ -375,37 +486,64 @@ cudaError_t launch_split_pass(const SplitLayout &L, char *ws, const Gemm &g,
   dim3 ga((unsigned)((L.Kp + kSplitK - 1) / kSplitK), (unsigned)((g.M + kSplitRows - 1) / kSplitRows));
   dim3 gb((unsigned)((L.Kp + kSplitK - 1) / kSplitK), (unsigned)((g.N + kSplitRows - 1) / kSplitRows));
   if (ga.y > 65535 || gb.y > 65535) return cudaErrorInvalidConfiguration;
-  auto *pa = (__nv_bfloat16 *)(ws + L.a), *pb = (__nv_bfloat16 *)(ws + L.b);
+  auto *pa = (uint16_t *)(ws + L.a), *pb = (uint16_t *)(ws + L.b);
   auto *fa = (unsigned long long *)(ws + L.flags_a), *fb = (unsigned long long *)(ws + L.flags_b);
   const float *A = (const float *)g.a, *B = (const float *)g.b;
   const int ma = split_mode(A, g.rsa, g.csa), mb = split_mode(B, g.csb, g.rsb);
-  if (L.planes == 3) {
-    split_f32_bf16<3><<<ga, 256, 0, s>>>(A, g.rsa, g.csa, g.M, g.K, L.Kp, pa, fa, kBM, gen, ma);
-    split_f32_bf16<3><<<gb, 256, 0, s>>>(B, g.csb, g.rsb, g.N, g.K, L.Kp, pb, fb, 64, gen, mb);
+  if (L.f16) {
+    auto *xa = (unsigned *)(ws + L.max_a), *xb = (unsigned *)(ws + L.max_b);
+    const dim3 ra = absmax_grid(g.M, g.K, ma), rb = absmax_grid(g.N, g.K, mb);
+    if (ra.y > 65535 || rb.y > 65535) return cudaErrorInvalidConfiguration;
+    cudaError_t e = cudaMemsetAsync(xa, 0, L.total - L.max_a, s);
+    if (e != cudaSuccess) return e;
+    absmax_rows_f32<<<ra, 256, 0, s>>>(A, g.rsa, g.csa, g.M, g.K, ma, xa);
+    absmax_rows_f32<<<rb, 256, 0, s>>>(B, g.csb, g.rsb, g.N, g.K, mb, xb);
+    split_planes<2, true><<<ga, 256, 0, s>>>(A, g.rsa, g.csa, g.M, g.K, L.Kp, pa, fa, kBM, gen,
+                                               ma, xa);
+    split_planes<2, true><<<gb, 256, 0, s>>>(B, g.csb, g.rsb, g.N, g.K, L.Kp, pb, fb, 64, gen,
+                                               mb, xb);
+    count_launch(4);
+  } else if (L.planes == 3) {
+    split_planes<3, false><<<ga, 256, 0, s>>>(A, g.rsa, g.csa, g.M, g.K, L.Kp, pa, fa, kBM,
+                                                gen, ma, nullptr);
+    split_planes<3, false><<<gb, 256, 0, s>>>(B, g.csb, g.rsb, g.N, g.K, L.Kp, pb, fb, 64, gen,
+                                                mb, nullptr);
+    count_launch(2);
   } else {
-    split_f32_bf16<2><<<ga, 256, 0, s>>>(A, g.rsa, g.csa, g.M, g.K, L.Kp, pa, fa, kBM, gen, ma);
-    split_f32_bf16<2><<<gb, 256, 0, s>>>(B, g.csb, g.rsb, g.N, g.K, L.Kp, pb, fb, 64, gen, mb);
+    split_planes<2, false><<<ga, 256, 0, s>>>(A, g.rsa, g.csa, g.M, g.K, L.Kp, pa, fa, kBM,
+                                                gen, ma, nullptr);
+    split_planes<2, false><<<gb, 256, 0, s>>>(B, g.csb, g.rsb, g.N, g.K, L.Kp, pb, fb, 64, gen,
+                                                mb, nullptr);
+    count_launch(2);
   }
-  count_launch(2);
   return cudaGetLastError();
 }
 
-template <int BN, int STAGES, int PLANES, int FLUSH>
+// Co-resident clusters of `kern` launched with `cfg` (0 if the query fails).
+int max_active_clusters(const void *kern, const cudaLaunchConfig_t &cfg) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+template <int BN, int STAGES, int PLANES, int FLUSH, bool F16, int CTAS>
 cudaError_t launch_gemm_status(const SplitLayout &L, char *ws, const Gemm &g,
                                unsigned long long gen, unsigned *status, cudaStream_t s) {
-  using Cfg = SplitCfg<BN, STAGES, PLANES, FLUSH>;
+  using Cfg = SplitCfg<BN, STAGES, PLANES, FLUSH, CTAS>;
   CUtensorMap ta, tb;
   cudaError_t e;
-  if ((e = make_tmap_3d(&ta, ws + L.a, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, PLANES, g.M, L.Kp,
-                        L.Kp, kBM, kBK)))
+  const auto dtype = F16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  if ((e = make_tmap_3d(&ta, ws + L.a, dtype, 2, PLANES, g.M, L.Kp, L.Kp, kBM, kBK))) return e;
+  if ((e = make_tmap_3d(&tb, ws + L.b, dtype, 2, PLANES, g.N, L.Kp, L.Kp, Cfg::BN_CTA, kBK)))
     return e;
-  if ((e = make_tmap_3d(&tb, ws + L.b, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, PLANES, g.N, L.Kp,
-                        L.Kp, BN, kBK)))
-    return e;
-  auto kern = split_bf16_gemm<BN, STAGES, PLANES, FLUSH>;
+  auto kern = split_gemm<BN, STAGES, PLANES, FLUSH, F16, CTAS>;
   if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM)))
     return e;
-  const int tiles_m = (int)((g.M + kBM - 1) / kBM), tiles_n = (int)((g.N + BN - 1) / BN);
+  const int tiles_m = (int)((g.M + kBM * CTAS - 1) / (kBM * CTAS));
+  const int tiles_n = (int)((g.N + BN - 1) / BN);
   const int vec4 = g.cso == 1 && (g.rso % 4) == 0 && ((uintptr_t)g.c % 16) == 0;
   Fallback fb;
   fb.A = (const float *)g.a;
@@ -414,27 +552,108 @@ cudaError_t launch_gemm_status(const SplitLayout &L, char *ws, const Gemm &g,
   fb.flags_a = (const unsigned long long *)(ws + L.flags_a);
   fb.flags_b = (const unsigned long long *)(ws + L.flags_b);
   fb.gen = gen;
-  const int grid = std::min(tiles_m * tiles_n, sm_count());
-  kern<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(ta, tb, (float *)g.c, g.rso, g.cso, (int)g.M,
-                                                 (int)g.N, (int)(L.Kp / kBK), tiles_m, tiles_n,
-                                                 vec4, status, fb);
+  fb.max_a = F16 ? (const unsigned *)(ws + L.max_a) : nullptr;
+  fb.max_b = F16 ? (const unsigned *)(ws + L.max_b) : nullptr;
+  const int num_kb = (int)(L.Kp / kBK);
+  if (CTAS == 1) {
+    const int grid = std::min(tiles_m * tiles_n, sm_count());
+    kern<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(ta, tb, (float *)g.c, g.rso, g.cso, (int)g.M,
+                                               (int)g.N, num_kb, tiles_m, tiles_n, vec4, status,
+                                               fb);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CTAS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(Cfg::THREADS);
+    cfg.dynamicSmemBytes = Cfg::SMEM;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    // One pair per two SMs, capped by how many pairs fit at once.
+    cfg.gridDim = dim3((unsigned)(CTAS * std::max(1, sm_count() / CTAS)));
+    static int pairs_cached[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int pairs = (dev >= 0 && dev < 64) ? pairs_cached[dev] : 0;
+    if (!pairs) {
+      pairs = max_active_clusters((const void *)kern, cfg);
+      if (pairs <= 0) pairs = std::max(1, sm_count() / CTAS);
+      if (dev >= 0 && dev < 64) pairs_cached[dev] = pairs;
+    }
+    pairs = std::min(pairs, tiles_m * tiles_n);
+    cfg.gridDim = dim3((unsigned)(CTAS * pairs));
+    e = cudaLaunchKernelEx(&cfg, kern, ta, tb, (float *)g.c, (int64_t)g.rso, (int64_t)g.cso,
+                           (int)g.M, (int)g.N, num_kb, tiles_m, tiles_n, vec4, status, fb);
+    if (e != cudaSuccess) return e;
+  }
   count_launch();
   return cudaGetLastError();
 }
 
-// Flush interval (K slabs per TMEM accumulation chain), measured at
-// 8192^3 on GB300 against a float64 reference (K = 4096 errors):
+// Flush interval (K slabs per TMEM accumulation chain) of the bfloat16
+// planes, measured at 8192^3 on GB300 with 128 x 128 single-CTA tiles
+// against a float64 reference (K = 4096 errors):
 //   3 passes: 1 slab 65 % of bf16 peak, 8 slabs 79 %, same error (the
 //             2^-16 split residual dominates) -> 8.
 //   6 passes: 1 slab 82 %, max error 6e-8 |A||B|; 2 slabs 87 %, 1e-7;
 //             plain FP32 FMA 2.3e-7 -> 1, the margin is the point of 6.
+//   scaled float16, 3 passes: see kF16DefaultFlush.
+// Two-plane products run on 256-column tiles: as CTA pairs (256 x 256,
+// each CTA holding 128 rows of B^T, 3 stages of 64 KiB) or single CTAs
+// (128 x 256, 2 stages of 96 KiB).  Three planes need 128-column tiles to
+// fit a ring of at least two stages.
+template <int CTAS>
+cudaError_t launch_gemm_ctas(const SplitLayout &L, char *ws, const Gemm &g,
+                             unsigned long long gen, unsigned *status, cudaStream_t s) {
+  constexpr int S2 = CTAS == 2 ? 3 : 2;   // stages of the 2-plane ring
+  if (L.f16) {
+    switch (L.flush) {
+    case 1: return launch_gemm_status<256, S2, 2, 1, true, CTAS>(L, ws, g, gen, status, s);
+    case 2: return launch_gemm_status<256, S2, 2, 2, true, CTAS>(L, ws, g, gen, status, s);
+    case 4: return launch_gemm_status<256, S2, 2, 4, true, CTAS>(L, ws, g, gen, status, s);
+    default: return launch_gemm_status<256, S2, 2, 8, true, CTAS>(L, ws, g, gen, status, s);
+    }
+  }
+  if (L.planes == 3)
+    return launch_gemm_status<128, CTAS == 2 ? 3 : 2, 3, 1, false, CTAS>(L, ws, g, gen, status, s);
+  return launch_gemm_status<256, S2, 2, 8, false, CTAS>(L, ws, g, gen, status, s);
+}
+
+// CTA pairs unless NUMC_CUDA_SPLIT_CTAS=1 asks for single CTAs (for hosts
+// where clusters cannot be launched).  At 8192^3 the pairs measured 519
+// against 461 TFLOP/s (float16 planes, flush 4) and 600 against 500
+// (bfloat16, 3 passes).
+int split_ctas() {
+  static const int v = [] {
+    const char *e = getenv("NUMC_CUDA_SPLIT_CTAS");
+    return (e && atoi(e) == 1) ? 1 : 2;
+  }();
+  return v;
+}
+
 cudaError_t launch_gemm(const SplitLayout &L, char *ws, const Gemm &g, unsigned long long gen,
                         unsigned *status, cudaStream_t s) {
-  if (L.planes == 3) return launch_gemm_status<128, 2, 3, 1>(L, ws, g, gen, status, s);
-  return launch_gemm_status<128, 3, 2, 8>(L, ws, g, gen, status, s);
+  if (split_ctas() == 2) return launch_gemm_ctas<2>(L, ws, g, gen, status, s);
+  return launch_gemm_ctas<1>(L, ws, g, gen, status, s);
 }
 
 int planes_for(int passes) { return passes == 6 ? 3 : 2; }
+
+// K slabs per TMEM chain for scaled float16 planes.  Measured at 8192^3 on
+// GB300 with CTA pairs and 256 x 256 tiles (N(0,1) and row/column-scaled
+// 10^U(-4,4) inputs, 512 outputs against a float64 reference; max / mean
+// relative error; plain FP32 FMA 1.3e-3 / 5.6e-6, ill-scaled 7.5e-4 /
+// 5.6e-6; TFLOP/s of the whole call):
+//   1 slab  346 TFLOP/s   2.1e-5 / 8.2e-7
+//   2 slabs 485           1.2e-4 / 1.5e-6
+//   4 slabs 519           4.2e-4 / 3.5e-6   (ill-scaled 5.0e-4 / 3.0e-6)
+//   8 slabs 537           6.9e-4 / 5.7e-6   (ill-scaled 1.0e-3 / 6.5e-6)
+// 4 is the fastest that stays at or below the FP32 FMA chain's error on
+// both inputs.
+constexpr int kF16DefaultFlush = 4;
 
 }  // namespace
 
@@ -442,13 +661,34 @@ size_t split_bf16_workspace(int64_t M, int64_t K, int64_t N, int passes) {
   return split_layout(M, K, N, planes_for(passes)).total;
 }
 
+size_t split_f16_workspace(int64_t M, int64_t K, int64_t N) {
+  return split_layout(M, K, N, 2, true).total;
+}
+
+namespace {
+cudaError_t run_split(const Gemm &g, const SplitLayout &L, void *ws_v, size_t ws_bytes,
+                      cudaStream_t s);
+}
+
 cudaError_t launch_split_bf16(const Gemm &g, int passes, void *ws_v, size_t ws_bytes,
                               cudaStream_t s) {
+  return run_split(g, split_layout(g.M, g.K, g.N, planes_for(passes)), ws_v, ws_bytes, s);
+}
+
+cudaError_t launch_split_f16(const Gemm &g, int flush, void *ws_v, size_t ws_bytes,
+                             cudaStream_t s) {
+  if (flush == 0) flush = kF16DefaultFlush;
+  if (flush != 1 && flush != 2 && flush != 4 && flush != 8) return cudaErrorInvalidValue;
+  return run_split(g, split_layout(g.M, g.K, g.N, 2, true, flush), ws_v, ws_bytes, s);
+}
+
+namespace {
+cudaError_t run_split(const Gemm &g, const SplitLayout &L, void *ws_v, size_t ws_bytes,
+                      cudaStream_t s) {
   if (g.M == 0 || g.N == 0) return cudaSuccess;
   if (g.K == 0) return launch_simt(NUMC_DTYPE_FLOAT32, g, 0, s);   // C = 0
   if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31))
     return cudaErrorInvalidValue;
-  const SplitLayout L = split_layout(g.M, g.K, g.N, planes_for(passes));
   if (ws_bytes < L.total || ((uintptr_t)ws_v & 255)) return cudaErrorInvalidValue;
   char *ws = (char *)ws_v;
   unsigned *status = status_word();
@@ -462,6 +702,7 @@ cudaError_t launch_split_bf16(const Gemm &g, int passes, void *ws_v, size_t ws_b
   mark.gemm_done();
   return e;
 }
+}  // namespace
 
 }  // namespace numc_k
 

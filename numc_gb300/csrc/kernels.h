@@ -34,6 +34,11 @@ cudaError_t launch_dmma(const Gemm &g, cudaStream_t s);
 // float32 split-BF16 on tcgen05 with `passes` = 3 (two bf16 planes) or 6
 // (three planes): workspace bytes and launcher.
 size_t split_bf16_workspace(int64_t M, int64_t K, int64_t N, int passes);
+size_t split_f16_workspace(int64_t M, int64_t K, int64_t N);
+// float32 from scaled float16 planes (3 products); `flush` = K slabs per
+// TMEM accumulation chain (1, 2, 4, 8; 0 = default).
+cudaError_t launch_split_f16(const Gemm &g, int flush, void *ws, size_t ws_bytes,
+                             cudaStream_t s);
 cudaError_t launch_split_bf16(const Gemm &g, int passes, void *ws, size_t ws_bytes,
                               cudaStream_t s);
 

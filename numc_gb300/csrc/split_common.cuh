@@ -1,17 +1,135 @@
-// Splitting float32 operands into bfloat16 planes (shared by the single and
-// grouped split-BF16 GEMMs).
+// Splitting float32 operands into 16-bit planes (shared by the single and
+// grouped split GEMMs).
+//
+// Two plane formats:
+//  * bfloat16 (8 significant bits, float32's exponent range): x is cut by
+//    repeated rounding, x0 = bf16(x), x1 = bf16(x - x0), ...
+//  * scaled float16 (11 significant bits, exponents -24..15): each row of A
+//    and each column of B is first multiplied by a power of two 2^s that
+//    puts its largest magnitude in [2^14, 2^15), then cut the same way,
+//    h0 = f16(x 2^s), h1 = f16(x 2^s - h0).  h0 + h1 holds 22 bits of x;
+//    the GEMM multiplies the float32 sum by 2^-(s_row + s_col).
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 
 namespace numc_k {
 
-// ---- pass 1: split float32 into bf16 planes -------------------------------
+// Scale exponent of a row whose largest magnitude has float32 bits
+// `maxbits`: s with max * 2^s in [2^14, 2^15), or 0 for an all-zero or
+// non-finite row (a non-finite row is recomputed by the fallback anyway).
+__host__ __device__ inline int f16_scale_exp(unsigned maxbits) {
+  if (maxbits == 0 || maxbits >= 0x7f800000u) return 0;
+  int e;   // floor(log2(max))
+  if (maxbits >> 23) {
+    e = (int)(maxbits >> 23) - 127;
+  } else {   // subnormal: position of the leading bit
+    int lead = 31;
+    while (!((maxbits >> lead) & 1u)) lead--;
+    e = lead - 149;
+  }
+  return 14 - e;   // in [-113, 163]
+}
+
+// 2^e as a float32 for e in [-126, 127].
+__host__ __device__ inline float exp2_int(int e) {
+  union { unsigned u; float f; } v;
+  v.u = (unsigned)(e + 127) << 23;
+  return v.f;
+}
+
+// x * 2^s exactly for |x * 2^s| < 2^15 (s in [-113, 163]; two steps keep
+// each factor a normal float32).
+__device__ __forceinline__ float scale_pow2(float x, int s) {
+  const int s1 = s > 126 ? 126 : s;
+  return (x * exp2_int(s1)) * exp2_int(s - s1);
+}
+
+// Largest magnitude of each row r < R of src[r * rs_row + k * rs_k] over
+// k < K, as float32 bits, merged into maxbits[r] with atomicMax (maxbits
+// starts at zero).  A 256-thread block covers
+//   mode 1 (k contiguous):    8 rows x 1024 k, one warp per row;
+//   mode 2 (rows contiguous): 1024 rows x 64 k, 4 rows per thread;
+//   mode 0 (general):         256 rows x 64 k, one row per thread.
+constexpr int kMaxRows1 = 8, kMaxK1 = 1024, kMaxRows2 = 1024, kMaxK2 = 64, kMaxRows0 = 256,
+              kMaxK0 = 64;
+
+__device__ __forceinline__ unsigned absbits(float x) { return __float_as_uint(x) & 0x7fffffffu; }
+
+static __global__ void __launch_bounds__(256)
+absmax_rows_f32(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_t R,
+                int64_t K, int mode, unsigned *__restrict__ maxbits) {
+  const int tid = threadIdx.x;
+  if (mode == 1) {
+    const int64_t r = (int64_t)blockIdx.y * kMaxRows1 + (tid >> 5);
+    const int64_t k0 = (int64_t)blockIdx.x * kMaxK1;
+    const int lane = tid & 31;
+    unsigned m = 0;
+    if (r < R) {
+      const float *row = src + r * rs_row;
+#pragma unroll
+      for (int q = 0; q < kMaxK1 / 128; q++) {
+        const int64_t k = k0 + 128 * q + 4 * lane;
+        if (k + 3 < K) {
+          const float4 v = *reinterpret_cast<const float4 *>(row + k);
+          m = max(max(m, absbits(v.x)), max(absbits(v.y), max(absbits(v.z), absbits(v.w))));
+        } else {
+          for (int t = 0; t < 4; t++)
+            if (k + t < K) m = max(m, absbits(row[k + t]));
+        }
+      }
+    }
+    m = __reduce_max_sync(0xffffffffu, m);
+    if (lane == 0 && r < R && m) atomicMax(&maxbits[r], m);
+  } else if (mode == 2) {
+    const int64_t r = (int64_t)blockIdx.y * kMaxRows2 + 4 * tid;
+    const int64_t k0 = (int64_t)blockIdx.x * kMaxK2;
+    unsigned m[4] = {0, 0, 0, 0};
+    if (r < R) {
+      const int64_t k1 = k0 + kMaxK2 < K ? k0 + kMaxK2 : K;
+      for (int64_t k = k0; k < k1; k++) {
+        const float *p = src + r + k * rs_k;
+        if (r + 3 < R) {
+          const float4 v = *reinterpret_cast<const float4 *>(p);
+          m[0] = max(m[0], absbits(v.x));
+          m[1] = max(m[1], absbits(v.y));
+          m[2] = max(m[2], absbits(v.z));
+          m[3] = max(m[3], absbits(v.w));
+        } else {
+          for (int t = 0; t < 4; t++)
+            if (r + t < R) m[t] = max(m[t], absbits(p[t]));
+        }
+      }
+    }
+    for (int t = 0; t < 4; t++)
+      if (r + t < R && m[t]) atomicMax(&maxbits[r + t], m[t]);
+  } else {
+    const int64_t r = (int64_t)blockIdx.y * kMaxRows0 + tid;
+    const int64_t k0 = (int64_t)blockIdx.x * kMaxK0;
+    unsigned m = 0;
+    if (r < R) {
+      const int64_t k1 = k0 + kMaxK0 < K ? k0 + kMaxK0 : K;
+      for (int64_t k = k0; k < k1; k++) m = max(m, absbits(src[r * rs_row + k * rs_k]));
+    }
+    if (r < R && m) atomicMax(&maxbits[r], m);
+  }
+}
+
+// Grid of absmax_rows_f32 for R rows, K columns, read mode `mode`.
+inline dim3 absmax_grid(int64_t R, int64_t K, int mode) {
+  const int64_t kk = mode == 1 ? kMaxK1 : mode == 2 ? kMaxK2 : kMaxK0;
+  const int64_t rr = mode == 1 ? kMaxRows1 : mode == 2 ? kMaxRows2 : kMaxRows0;
+  return dim3((unsigned)((K + kk - 1) / kk), (unsigned)((R + rr - 1) / rr));
+}
+
+// ---- pass 1: split float32 into 16-bit planes -----------------------------
 //
 // dst_p(row, k) for row < R, k < Kp: plane p of src[row * rs_row + k * rs_k]
-// (zero for k >= K).  Plane p starts at planes + p * R * Kp.  A 32-row x
+// (zero for k >= K); bfloat16 planes, or with F16 scaled float16 planes
+// whose row scale comes from maxbits[row].  Plane p starts at planes + p * R * Kp.  A 32-row x
 // 128-k tile per block goes through shared memory; reads are float4 along
 // whichever source dimension is contiguous (scalar otherwise), writes are 4
 // bf16 (8 bytes) per thread per plane along k.
@@ -26,13 +144,15 @@ constexpr int kSplitRows = 32, kSplitK = 128;
 
 // One 32-row x 128-k tile at (r0, k0), executed by a 256-thread block;
 // `tile` is the block's shared staging buffer.
-template <int PLANES>
+template <int PLANES, bool F16 = false>
 __device__ __forceinline__ void split_tile(const float *__restrict__ src, int64_t rs_row,
                                            int64_t rs_k, int64_t R, int64_t K, int64_t Kp,
-                                           __nv_bfloat16 *__restrict__ planes,
+                                           void *__restrict__ planes_v,
                                            unsigned long long *flags, int flag_rows,
                                            unsigned long long gen, int mode, int64_t r0,
-                                           int64_t k0, float (*tile)[kSplitK + 4]) {
+                                           int64_t k0, float (*tile)[kSplitK + 4],
+                                           const unsigned *maxbits = nullptr) {
+  uint16_t *planes = (uint16_t *)planes_v;
   const int tid = threadIdx.x;
   bool bad = false;
   if (mode == 1) {            // k contiguous, 16-byte aligned rows
@@ -98,28 +218,43 @@ __device__ __forceinline__ void split_tile(const float *__restrict__ src, int64_
     if (gr >= R || gk >= Kp) continue;
     const float4 v = *reinterpret_cast<const float4 *>(&tile[r][4 * lane]);
     float rem[4] = {v.x, v.y, v.z, v.w};
-    __nv_bfloat16 out[PLANES][4];
+    uint16_t out[PLANES][4];
+    if (F16) {
+      const int sexp = f16_scale_exp(maxbits[gr]);
 #pragma unroll
-    for (int t = 0; t < 4; t++) {
-      const bool finite = isfinite(rem[t]);
+      for (int t = 0; t < 4; t++) {
+        const bool finite = isfinite(rem[t]);
+        float x = finite ? scale_pow2(rem[t], sexp) : 0.0f;   // |x| < 2^15
 #pragma unroll
-      for (int p = 0; p < PLANES; p++) {
-        __nv_bfloat16 h = __float2bfloat16_rn(rem[t]);
-        float hf = __bfloat162float(h);
-        if (isinf(hf) && finite) {       // rounding overflowed: truncate
-          h = __float2bfloat16_rz(rem[t]);
-          hf = __bfloat162float(h);
+        for (int p = 0; p < PLANES; p++) {
+          const __half h = __float2half_rn(x);
+          out[p][t] = __half_as_ushort(h);
+          x -= __half2float(h);   // exact
         }
-        out[p][t] = (p == 0 || finite) ? h : __float2bfloat16_rn(0.0f);
-        rem[t] = finite ? rem[t] - hf : 0.0f;
+      }
+    } else {
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        const bool finite = isfinite(rem[t]);
+#pragma unroll
+        for (int p = 0; p < PLANES; p++) {
+          __nv_bfloat16 h = __float2bfloat16_rn(rem[t]);
+          float hf = __bfloat162float(h);
+          if (isinf(hf) && finite) {       // rounding overflowed: truncate
+            h = __float2bfloat16_rz(rem[t]);
+            hf = __bfloat162float(h);
+          }
+          out[p][t] = __bfloat16_as_ushort((p == 0 || finite) ? h : __float2bfloat16_rn(0.0f));
+          rem[t] = finite ? rem[t] - hf : 0.0f;
+        }
       }
     }
     const int64_t off = gr * Kp + gk;
 #pragma unroll
     for (int p = 0; p < PLANES; p++) {
       uint2 w;
-      w.x = (uint32_t)__bfloat16_as_ushort(out[p][0]) | ((uint32_t)__bfloat16_as_ushort(out[p][1]) << 16);
-      w.y = (uint32_t)__bfloat16_as_ushort(out[p][2]) | ((uint32_t)__bfloat16_as_ushort(out[p][3]) << 16);
+      w.x = (uint32_t)out[p][0] | ((uint32_t)out[p][1] << 16);
+      w.y = (uint32_t)out[p][2] | ((uint32_t)out[p][3] << 16);
       *reinterpret_cast<uint2 *>(planes + p * plane_elems + off) = w;
     }
   }
