@@ -184,11 +184,17 @@ def cpu_sample_tflops(a, b, target_s, nthreads=0):
             oracle.matmul(a[:rows], b, nthreads=nthreads)
         return time.perf_counter() - t0
 
-    run(8)
-    t = run(16)
-    rows = int(max(16, min(a.shape[0], 16 * target_s / max(t, 1e-6))))
-    rows = max(16, rows - rows % 16)
+    run(6)
+    rows = 48
     t = run(rows)
+    # Per-call costs (packing all of B) dominate small samples, so grow the
+    # sample until it takes most of the target time.
+    for _ in range(4):
+        if t >= 0.6 * target_s or rows >= a.shape[0]:
+            break
+        rows = int(min(a.shape[0], rows * target_s / max(t, 1e-6)))
+        rows = max(48, rows - rows % 48)
+        t = run(rows)
     tflops = 2.0 * rows * b.shape[0] * b.shape[1] / t / 1e12
     kind = "reference" if use_ref else "port"
     cores = oracle.num_threads() if nthreads == 0 else nthreads

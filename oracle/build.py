@@ -22,9 +22,9 @@ REF_SRC = "/root/reference"
 def build_oracle(force=False):
     src = os.path.join(HERE, "numc_oracle.c")
     micro = os.path.join(HERE, "numc_oracle_micro.c")
+    deps = [src, micro, os.path.join(HERE, "numc_oracle_micro.h")]
     if (not force and os.path.exists(ORACLE_SO)
-            and os.path.getmtime(ORACLE_SO) >= max(os.path.getmtime(src),
-                                                   os.path.getmtime(micro))):
+            and os.path.getmtime(ORACLE_SO) >= max(os.path.getmtime(d) for d in deps)):
         return ORACLE_SO
     os.makedirs(os.path.dirname(ORACLE_SO), exist_ok=True)
     flags = ["-O3", "-std=c11", "-fPIC"]

@@ -108,10 +108,7 @@ static void scatter(void *dstv, const void *src, int64_t rows, int64_t cols,
 
 /* Register-tile micro-kernels (numc_oracle_micro.c, compiled so that each
  * vector multiply-add is one fused multiply-add). */
-void oracle_micro_f32(const float *a, int64_t lda, const float *bs, float *c,
-                      int64_t ldc, int64_t kc);
-void oracle_micro_f64(const double *a, int64_t lda, const double *bs,
-                      double *c, int64_t ldc, int64_t kc);
+#include "numc_oracle_micro.h"
 
 #define DEFINE_FLOAT_KERNEL(NAME, T, MICRO, MR_, NR_)                         \
   static void NAME(const T *a, const T *b, T *c, int64_t M, int64_t K,       \
@@ -132,17 +129,21 @@ void oracle_micro_f64(const double *a, int64_t lda, const double *bs,
               bp[(js * kc + k) * NR + j] =                                    \
                   col < N ? b[(pc + k) * N + col] : (T)0;                     \
             }                                                                 \
-        _Pragma("omp parallel for schedule(dynamic, 4)")                      \
-        for (int64_t ib = 0; ib < (M + MR - 1) / MR; ib++) {                  \
+        /* (row block, column strip) tiles shared out in contiguous runs,  \
+         * so a few row blocks still keep every thread busy. */              \
+        const int64_t nib = (M + MR - 1) / MR;                                \
+        _Pragma("omp parallel for schedule(static)")                          \
+        for (int64_t t = 0; t < nib * nstrips; t++) {                         \
+          const int64_t ib = t / nstrips, js = t % nstrips;                   \
           const int64_t i0 = ib * MR;                                         \
           const int mr = (int)MIN(MR, M - i0);                                \
           T ta[MR * FKC], tc[MR * NR];                                        \
-          for (int64_t js = 0; js < nstrips; js++) {                          \
+          {                                                                   \
             const int64_t j0 = jc + js * NR;                                  \
             const int nr = (int)MIN(NR, N - j0);                              \
             const T *bs = bp + js * kc * NR;                                  \
             if (mr == MR && nr == NR) {                                       \
-              MICRO(a + i0 * K + pc, K, bs, c + i0 * N + j0, N, kc);   \
+              MICRO(a + i0 * K + pc, K, bs, c + i0 * N + j0, N, kc);          \
               continue;                                                       \
             }                                                                 \
             /* Ragged edge: run the same micro-kernel on zero-padded copies   \
@@ -164,8 +165,8 @@ void oracle_micro_f64(const double *a, int64_t lda, const double *bs,
     free(bp);                                                                 \
   }
 
-DEFINE_FLOAT_KERNEL(kern_f32, float, oracle_micro_f32, 6, 16)
-DEFINE_FLOAT_KERNEL(kern_f64, double, oracle_micro_f64, 6, 8)
+DEFINE_FLOAT_KERNEL(kern_f32, float, oracle_micro_f32, ORACLE_MR, ORACLE_NR_F32)
+DEFINE_FLOAT_KERNEL(kern_f64, double, oracle_micro_f64, ORACLE_MR, ORACLE_NR_F64)
 
 /* Outputs of the x86 AVX2 build that are not a plain FMA chain.
  *
