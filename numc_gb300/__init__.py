@@ -369,7 +369,7 @@ class GemmDesc(ctypes.Structure):
 class GemmPlan:
     """A grouped GEMM plan over torch CUDA tensors (a_i @ b_i -> out_i)."""
 
-    def __init__(self, problems, algo=ALGO_SPLIT_BF16, param=0):
+    def __init__(self, problems, algo=ALGO_DEFAULT, param=0):
         n = len(problems)
         self._keep = problems            # tensors must outlive the plan
         arr = (GemmDesc * max(1, n))()

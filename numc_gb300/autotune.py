@@ -1,9 +1,10 @@
 """Autotuner for grouped float32 GEMM plans (run on a GB300).
 
 For every size class of (M, N, K) — classes <=32, <=64, ..., <=1024 — time
-one plan of identical problems on each kernel variant (split-BF16 with
-128-column tiles, split-BF16 with 64-column tiles, CUDA-core FMA) and record
-the fastest in numc_gb300/autotune_table.txt, which plans read at creation.
+one plan of identical problems on each kernel variant (the split GEMM from
+scaled float16 planes with 128-column tiles, the same with 64-column tiles,
+CUDA-core FMA) and record the fastest in numc_gb300/autotune_table.txt,
+which plans read at creation (for both split plane formats).
 
     python -m numc_gb300.autotune [--out PATH]
 """
@@ -15,7 +16,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPRESENTATIVE = [24, 48, 96, 192, 384, 768]        # one size per class 0..5
-VARIANTS = [(0, "split128", 2, 128), (1, "split64", 2, 64), (2, "simt", 1, 0)]
+VARIANTS = [(0, "split128", 7, 128), (1, "split64", 7, 64), (2, "simt", 1, 0)]   # 7 = SPLIT_FP16
 
 
 def time_plan(nc, torch, problems, algo, param, reps=5):

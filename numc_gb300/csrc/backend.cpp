@@ -417,8 +417,12 @@ extern "C" int numc_matmul_grouped(const NumcArray *const *a, const NumcArray *c
     return 0;
   }
   ensure_algos();
+  // The process-wide float32 choice: SIMT stays numc's FMA chains,
+  // SPLIT_BF16 keeps bfloat16 planes, AUTO and SPLIT_FP16 use scaled
+  // float16 planes.
   int algo = g_algo[NUMC_DTYPE_FLOAT32].algo.load();
-  if (algo != NUMC_CUDA_ALGO_SIMT) algo = NUMC_CUDA_ALGO_SPLIT_BF16;
+  if (algo != NUMC_CUDA_ALGO_SIMT && algo != NUMC_CUDA_ALGO_SPLIT_BF16)
+    algo = NUMC_CUDA_ALGO_SPLIT_FP16;
   NumcCtx *ctx = out[0]->ctx;
   cudaStream_t s;
   int err = ctx_stream(ctx, &s);

@@ -7,14 +7,17 @@
 // variant per problem from the committed autotune table, lays out an owned
 // device workspace, encodes one TMA descriptor per operand per problem and
 // uploads per-variant tile lists.  Running it enqueues only:
-//   1. a memset of the non-finite flags,
-//   2. one grouped split pass over every tensor-core problem (x -> bf16
-//      planes x0, x1; a block binary-searches its problem in a prefix sum),
-//   3. one persistent split-BF16 tcgen05 kernel per tile width (128 or 64
+//   1. a memset of the non-finite flags (and row / column maxima),
+//   2. for scaled float16 planes (NUMC_CUDA_ALGO_SPLIT_FP16, the default),
+//      one grouped scale pass: row maxima of every A, column maxima of
+//      every B,
+//   3. one grouped split pass over every tensor-core problem (x -> two
+//      16-bit planes; a block binary-searches its problem in a prefix sum),
+//   4. one persistent split tcgen05 kernel per tile width (128 or 64
 //      columns): each CTA walks a static share of the variant's tile list;
 //      the TMA ring, the MMA chunk stream and the TMEM buffers run on
 //      across tiles, so a tile's stores overlap the next tile's MMAs,
-//   4. one grouped CUDA-core kernel (FP32 FMA chains, numc's arithmetic)
+//   5. one grouped CUDA-core kernel (FP32 FMA chains, numc's arithmetic)
 //      for problems too small for the tensor path, and for the plain
 //      algorithm.
 // The tile lists are ordered by K, largest first, so the static
@@ -55,45 +58,78 @@ struct Prob {
   int64_t rsa, csa, rsb, csb, rso, cso;
   int M, N, K, num_kb, Kp;
   int split_mode_a, split_mode_b;
-  __nv_bfloat16 *pa, *pb;                 // planes (2 x M x Kp, 2 x N x Kp)
+  uint16_t *pa, *pb;                      // planes (2 x M x Kp, 2 x N x Kp)
   unsigned long long *flags_a, *flags_b;  // per 128 rows of A, per 64 columns of B
+  unsigned *max_a, *max_b;                // float16 planes: row / column maxima
 };
 
 struct Tile {
   int prob, m0, n0, pad;
 };
 
-// ---- grouped split pass --------------------------------------------------------
-
-// Block b handles split job b: prefix[p] <= b < prefix[p + 1] selects the
-// problem; within it, A tiles (ceil(M/32) x ceil(Kp/128)) come first, then
-// B tiles.
-__global__ void __launch_bounds__(256)
-grouped_split(const Prob *__restrict__ probs, const long long *__restrict__ prefix, int nprob,
-              unsigned long long gen) {
-  __shared__ __align__(16) float tile[kSplitRows][kSplitK + 4];
-  const long long b = blockIdx.x;
+// Problem owning job b: prefix[p] <= b < prefix[p + 1].
+__device__ __forceinline__ int find_problem(const long long *__restrict__ prefix, int nprob,
+                                            long long b) {
   int lo = 0, hi = nprob - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
     if (prefix[mid] <= b) lo = mid;
     else hi = mid - 1;
   }
-  const Prob &P = probs[lo];
-  long long j = b - prefix[lo];
-  const long long kt = (P.Kp + kSplitK - 1) / kSplitK;
-  const long long a_jobs = (long long)((P.M + kSplitRows - 1) / kSplitRows) * kt;
+  return lo;
+}
+
+// ---- grouped scale pass (float16 planes) -----------------------------------------
+
+// Block b handles scale job b of problem p = find_problem(b): the blocks of
+// absmax_grid(M, K) over A's rows, then those of absmax_grid(N, K) over B's
+// columns.
+__global__ void __launch_bounds__(256)
+grouped_absmax(const Prob *__restrict__ probs, const long long *__restrict__ prefix,
+               int nprob) {
+  const long long b = blockIdx.x;
+  const int p = find_problem(prefix, nprob, b);
+  const Prob &P = probs[p];
+  long long j = b - prefix[p];
+  const dim3 ga = absmax_grid(P.M, P.K, P.split_mode_a);
+  const long long a_jobs = (long long)ga.x * ga.y;
   if (j < a_jobs) {
-    split_tile<kPlanes>(P.A, P.rsa, P.csa, P.M, P.K, P.Kp, P.pa, P.flags_a, kBM, gen,
-                        P.split_mode_a, (j / kt) * kSplitRows, (j % kt) * kSplitK, tile);
+    absmax_block(P.A, P.rsa, P.csa, P.M, P.K, P.split_mode_a, P.max_a, j % ga.x, j / ga.x);
   } else {
     j -= a_jobs;
-    split_tile<kPlanes>(P.B, P.csb, P.rsb, P.N, P.K, P.Kp, P.pb, P.flags_b, 64, gen,
-                        P.split_mode_b, (j / kt) * kSplitRows, (j % kt) * kSplitK, tile);
+    const dim3 gb = absmax_grid(P.N, P.K, P.split_mode_b);
+    absmax_block(P.B, P.csb, P.rsb, P.N, P.K, P.split_mode_b, P.max_b, j % gb.x, j / gb.x);
   }
 }
 
-// ---- persistent grouped split-BF16 GEMM -------------------------------------------
+// ---- grouped split pass --------------------------------------------------------
+
+// Block b handles split job b of problem p = find_problem(b): A tiles
+// (ceil(M/32) x ceil(Kp/128)) come first, then B tiles.
+template <bool F16>
+__global__ void __launch_bounds__(256)
+grouped_split(const Prob *__restrict__ probs, const long long *__restrict__ prefix, int nprob,
+              unsigned long long gen) {
+  __shared__ __align__(16) float tile[kSplitRows][kSplitK + 4];
+  const long long b = blockIdx.x;
+  const int p = find_problem(prefix, nprob, b);
+  const Prob &P = probs[p];
+  long long j = b - prefix[p];
+  const long long kt = (P.Kp + kSplitK - 1) / kSplitK;
+  const long long a_jobs = (long long)((P.M + kSplitRows - 1) / kSplitRows) * kt;
+  if (j < a_jobs) {
+    split_tile<kPlanes, F16>(P.A, P.rsa, P.csa, P.M, P.K, P.Kp, P.pa, P.flags_a, kBM, gen,
+                             P.split_mode_a, (j / kt) * kSplitRows, (j % kt) * kSplitK, tile,
+                             P.max_a);
+  } else {
+    j -= a_jobs;
+    split_tile<kPlanes, F16>(P.B, P.csb, P.rsb, P.N, P.K, P.Kp, P.pb, P.flags_b, 64, gen,
+                             P.split_mode_b, (j / kt) * kSplitRows, (j % kt) * kSplitK, tile,
+                             P.max_b);
+  }
+}
+
+// ---- persistent grouped split GEMM ----------------------------------------------
 
 template <int BN, int STAGES, int FLUSH>
 struct Cfg {
@@ -108,7 +144,7 @@ struct Cfg {
   static_assert((2 * STAGES + 2 * NBUF) * 8 + 4 <= 256, "barrier space");
 };
 
-template <int BN, int STAGES, int FLUSH>
+template <int BN, int STAGES, int FLUSH, bool F16>
 __global__ void __launch_bounds__(Cfg<BN, STAGES, FLUSH>::THREADS, 1)
 grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict__ probs,
                    const Tile *__restrict__ tiles, int ntiles, unsigned *status,
@@ -173,7 +209,7 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
     __syncwarp();
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, BN);
+      constexpr uint32_t idesc = F16 ? tc::idesc_f16_f32(kBM, BN) : tc::idesc_bf16_f32(kBM, BN);
       int g = 0, chunk = 0;
       bool live = true;
       for (int t = blockIdx.x; t < ntiles && live; t += gridDim.x) {
@@ -268,6 +304,16 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
           P.C[(int64_t)row * P.rso + (int64_t)col * P.cso] = f;
         }
       } else {
+        if (F16) {
+          // acc * 2^-(s_row + s_col), correctly rounded (see gemm_tc.cu).
+          const int sa = f16_scale_exp(P.max_a[row]);
+#pragma unroll
+          for (int j = 0; j < CW; j++) {
+            const int col = tl.n0 + cbase + j;
+            const int e = -(sa + (col < P.N ? f16_scale_exp(P.max_b[col]) : 0));
+            acc[j] = (e >= -126 && e <= 127) ? acc[j] * exp2_int(e) : ldexpf(acc[j], e);
+          }
+        }
         float *crow = P.C + (int64_t)row * P.rso;
 #pragma unroll
         for (int j = 0; j < CW; j++) {
@@ -323,11 +369,14 @@ struct NumcCudaGemmPlan {
   Prob *d_probs;
   long long *d_prefix;
   long long split_jobs;
+  bool f16;                       // scaled float16 planes (else bfloat16)
+  long long *d_prefix_max;        // scale-pass job prefix (float16 planes)
+  long long max_jobs;
   int n_split_probs;
   Prob *d_split_probs;
   Tile *d_tiles[kNumVar];
   int ntiles[kNumVar];
-  unsigned long long *flags;      // all flag words (memset per run)
+  unsigned long long *flags;      // all flag words and maxima (memset per run)
   size_t flags_bytes;
   unsigned long long gen;
   cudaGraphExec_t graph;
@@ -406,17 +455,21 @@ int fail(cudaError_t e, const char *what) {
 
 std::atomic<unsigned long long> g_plan_gen{0x9a0c000000000001ull};
 
-template <int BN, int STAGES, int FLUSH>
+// K slabs per TMEM chain: bfloat16 planes 8, float16 planes 4 (the choices
+// of the single GEMM, gemm_tc.cu).
+constexpr int kFlushBf16 = 8, kFlushF16 = 4;
+
+template <int BN, int STAGES, int FLUSH, bool F16>
 cudaError_t prepare_tc() {
-  return cudaFuncSetAttribute(grouped_split_gemm<BN, STAGES, FLUSH>,
+  return cudaFuncSetAttribute(grouped_split_gemm<BN, STAGES, FLUSH, F16>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               Cfg<BN, STAGES, FLUSH>::SMEM);
 }
 
-template <int BN, int STAGES, int FLUSH>
+template <int BN, int STAGES, int FLUSH, bool F16>
 cudaError_t launch_tc(const NumcCudaGemmPlan *p, int var, unsigned *status, cudaStream_t s) {
   using C_ = Cfg<BN, STAGES, FLUSH>;
-  auto kern = grouped_split_gemm<BN, STAGES, FLUSH>;
+  auto kern = grouped_split_gemm<BN, STAGES, FLUSH, F16>;
   const int grid = std::min(p->ntiles[var], p->sms);
   kern<<<grid, C_::THREADS, C_::SMEM, s>>>(p->d_tmaps, p->d_probs, p->d_tiles[var],
                                           p->ntiles[var], status, p->gen);
@@ -431,18 +484,32 @@ int plan_enqueue(NumcCudaGemmPlan *p, cudaStream_t s, unsigned *kernels) {
   cudaError_t e;
   if (p->flags_bytes && (e = cudaMemsetAsync(p->flags, 0, p->flags_bytes, s)))
     return fail(e, "plan flags");
+  if (p->f16 && p->max_jobs > 0) {
+    grouped_absmax<<<(unsigned)p->max_jobs, 256, 0, s>>>(p->d_split_probs, p->d_prefix_max,
+                                                         p->n_split_probs);
+    if ((e = cudaGetLastError())) return fail(e, "grouped scale pass");
+    ++*kernels;
+  }
   if (p->split_jobs > 0) {
-    grouped_split<<<(unsigned)p->split_jobs, 256, 0, s>>>(p->d_split_probs, p->d_prefix,
-                                                          p->n_split_probs, p->gen);
+    if (p->f16)
+      grouped_split<true><<<(unsigned)p->split_jobs, 256, 0, s>>>(p->d_split_probs, p->d_prefix,
+                                                                  p->n_split_probs, p->gen);
+    else
+      grouped_split<false><<<(unsigned)p->split_jobs, 256, 0, s>>>(p->d_split_probs, p->d_prefix,
+                                                                   p->n_split_probs, p->gen);
     if ((e = cudaGetLastError())) return fail(e, "grouped split");
     ++*kernels;
   }
   if (p->ntiles[kVarTc128]) {
-    if ((e = launch_tc<128, 3, 8>(p, kVarTc128, status, s))) return fail(e, "grouped split-BF16 (128)");
+    e = p->f16 ? launch_tc<128, 3, kFlushF16, true>(p, kVarTc128, status, s)
+               : launch_tc<128, 3, kFlushBf16, false>(p, kVarTc128, status, s);
+    if (e) return fail(e, "grouped split GEMM (128)");
     ++*kernels;
   }
   if (p->ntiles[kVarTc64]) {
-    if ((e = launch_tc<64, 4, 8>(p, kVarTc64, status, s))) return fail(e, "grouped split-BF16 (64)");
+    e = p->f16 ? launch_tc<64, 4, kFlushF16, true>(p, kVarTc64, status, s)
+               : launch_tc<64, 4, kFlushBf16, false>(p, kVarTc64, status, s);
+    if (e) return fail(e, "grouped split GEMM (64)");
     ++*kernels;
   }
   if (p->ntiles[kVarSimt]) {
@@ -462,16 +529,18 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
     NUMC_SET_ERROR(NUMC_ERR_TYPE, "grouped GEMM plans are float32");
     return nullptr;
   }
-  if (algo == NUMC_CUDA_ALGO_DEFAULT || algo == NUMC_CUDA_ALGO_AUTO) algo = NUMC_CUDA_ALGO_SPLIT_BF16;
-  if (algo != NUMC_CUDA_ALGO_SPLIT_BF16 && algo != NUMC_CUDA_ALGO_SIMT) {
-    NUMC_SET_ERROR(NUMC_ERR_VALUE, "grouped GEMM algorithm %d (SIMT or SPLIT_BF16)", algo);
+  if (algo == NUMC_CUDA_ALGO_DEFAULT || algo == NUMC_CUDA_ALGO_AUTO) algo = NUMC_CUDA_ALGO_SPLIT_FP16;
+  if (algo != NUMC_CUDA_ALGO_SPLIT_FP16 && algo != NUMC_CUDA_ALGO_SPLIT_BF16 &&
+      algo != NUMC_CUDA_ALGO_SIMT) {
+    NUMC_SET_ERROR(NUMC_ERR_VALUE, "grouped GEMM algorithm %d (SIMT, SPLIT_BF16 or SPLIT_FP16)",
+                   algo);
     return nullptr;
   }
-  // SPLIT_BF16 param: 0 (or 3) = per-problem choice from the autotune table,
-  // 128 / 64 = every problem on that tile width.
-  if (algo == NUMC_CUDA_ALGO_SPLIT_BF16 && param != 0 && param != 3 && param != -1 &&
-      param != 128 && param != 64) {
-    NUMC_SET_ERROR(NUMC_ERR_VALUE, "grouped split-BF16 param %d (0, 3, 64 or 128)", param);
+  // Split param: 0 (or 3 for SPLIT_BF16) = per-problem choice from the
+  // autotune table, 128 / 64 = every problem on that tile width.
+  if (algo != NUMC_CUDA_ALGO_SIMT && param != 0 && param != 3 && param != -1 && param != 128 &&
+      param != 64) {
+    NUMC_SET_ERROR(NUMC_ERR_VALUE, "grouped split param %d (0, 3, 64 or 128)", param);
     return nullptr;
   }
   if (count > 0 && !descs) {
@@ -484,6 +553,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
     return nullptr;
   }
   p->algo = algo;
+  p->f16 = algo == NUMC_CUDA_ALGO_SPLIT_FP16;
   p->count = count;
   p->dev = nullptr;
   p->graph = nullptr;
@@ -529,6 +599,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
       planes_bytes += align_up((size_t)kPlanes * P.Kp * (d.M + d.N) * 2, 256);
       flag_off[i] = flags_bytes;
       flags_bytes += align_up(((d.M + kBM - 1) / kBM + (d.N + 63) / 64) * 8, 256);
+      if (p->f16) flags_bytes += align_up((d.M + d.N) * 4, 256);   // row / column maxima
       P.split_mode_a = split_mode(P.A, P.rsa, P.csa);
       P.split_mode_b = split_mode(P.B, P.csb, P.rsb);
     }
@@ -558,7 +629,14 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   }
   p->split_jobs = prefix.back();
   p->n_split_probs = (int)split_idx.size();
-  if (p->split_jobs > 0x7FFFFFFFll) {
+  std::vector<long long> prefix_max(split_idx.size() + 1, 0);
+  for (size_t q = 0; q < split_idx.size() && p->f16; q++) {
+    const Prob &P = p->probs[split_idx[q]];
+    const dim3 ga = absmax_grid(P.M, P.K, P.split_mode_a), gb = absmax_grid(P.N, P.K, P.split_mode_b);
+    prefix_max[q + 1] = prefix_max[q] + (long long)ga.x * ga.y + (long long)gb.x * gb.y;
+  }
+  p->max_jobs = p->f16 ? prefix_max.back() : 0;
+  if (p->split_jobs > 0x7FFFFFFFll || p->max_jobs > 0x7FFFFFFFll) {
     delete p;
     NUMC_SET_ERROR(NUMC_ERR_VALUE, "plan_create: too many split blocks");
     return nullptr;
@@ -570,6 +648,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   const size_t o_probs = off; off = align_up(off + count * sizeof(Prob), 256);
   const size_t o_sprobs = off; off = align_up(off + split_idx.size() * sizeof(Prob), 256);
   const size_t o_prefix = off; off = align_up(off + prefix.size() * sizeof(long long), 256);
+  const size_t o_prefix_max = off; off = align_up(off + prefix_max.size() * sizeof(long long), 256);
   size_t o_tiles[kNumVar];
   for (int v = 0; v < kNumVar; v++) {
     o_tiles[v] = off;
@@ -588,6 +667,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   p->d_probs = (Prob *)(p->dev + o_probs);
   p->d_split_probs = (Prob *)(p->dev + o_sprobs);
   p->d_prefix = (long long *)(p->dev + o_prefix);
+  p->d_prefix_max = (long long *)(p->dev + o_prefix_max);
   for (int v = 0; v < kNumVar; v++) {
     p->d_tiles[v] = (Tile *)(p->dev + o_tiles[v]);
     p->ntiles[v] = (int)tiles[v].size();
@@ -601,22 +681,28 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
     Prob &P = p->probs[i];
     const int v = p->variant[i];
     if (v != kVarTc128 && v != kVarTc64) continue;
-    P.pa = (__nv_bfloat16 *)(p->dev + o_planes + plane_off[i]);
+    P.pa = (uint16_t *)(p->dev + o_planes + plane_off[i]);
     P.pb = P.pa + (size_t)kPlanes * P.M * P.Kp;
     P.flags_a = (unsigned long long *)(p->dev + o_flags + flag_off[i]);
     P.flags_b = P.flags_a + (P.M + kBM - 1) / kBM;
+    if (p->f16) {
+      P.max_a = (unsigned *)(p->dev + o_flags + flag_off[i] +
+                             align_up(((P.M + kBM - 1) / kBM + (P.N + 63) / 64) * 8, 256));
+      P.max_b = P.max_a + P.M;
+    }
     const uint32_t bn = v == kVarTc128 ? 128 : 64;
-    if ((e = make_tmap_3d(&tm[2 * i], P.pa, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, kPlanes, P.M,
-                          P.Kp, P.Kp, kBM, kBK)) ||
-        (e = make_tmap_3d(&tm[2 * i + 1], P.pb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, kPlanes,
-                          P.N, P.Kp, P.Kp, bn, kBK))) {
+    const auto dt = p->f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    if ((e = make_tmap_3d(&tm[2 * i], P.pa, dt, 2, kPlanes, P.M, P.Kp, P.Kp, kBM, kBK)) ||
+        (e = make_tmap_3d(&tm[2 * i + 1], P.pb, dt, 2, kPlanes, P.N, P.Kp, P.Kp, bn, kBK))) {
       numc_cuda_gemm_plan_free(p);
       fail(e, "plan tensor maps");
       return nullptr;
     }
   }
   // Kernel attributes are set here, not per run, so runs can be captured.
-  if ((e = prepare_tc<128, 3, 8>()) || (e = prepare_tc<64, 4, 8>()) || !status_word()) {
+  if ((e = prepare_tc<128, 3, kFlushBf16, false>()) || (e = prepare_tc<64, 4, kFlushBf16, false>()) ||
+      (e = prepare_tc<128, 3, kFlushF16, true>()) || (e = prepare_tc<64, 4, kFlushF16, true>()) ||
+      !status_word()) {
     numc_cuda_gemm_plan_free(p);
     fail(e ? e : cudaErrorMemoryAllocation, "plan kernel setup");
     return nullptr;
@@ -626,7 +712,9 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   if ((e = cudaMemcpy(p->d_tmaps, tm.data(), tm.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(p->d_probs, p->probs.data(), count * sizeof(Prob), cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(p->d_split_probs, sp.data(), sp.size() * sizeof(Prob), cudaMemcpyHostToDevice)) ||
-      (e = cudaMemcpy(p->d_prefix, prefix.data(), prefix.size() * sizeof(long long), cudaMemcpyHostToDevice))) {
+      (e = cudaMemcpy(p->d_prefix, prefix.data(), prefix.size() * sizeof(long long), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(p->d_prefix_max, prefix_max.data(), prefix_max.size() * sizeof(long long),
+                      cudaMemcpyHostToDevice))) {
     numc_cuda_gemm_plan_free(p);
     fail(e, "plan upload");
     return nullptr;

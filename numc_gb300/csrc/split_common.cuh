@@ -59,13 +59,15 @@ constexpr int kMaxRows1 = 8, kMaxK1 = 1024, kMaxRows2 = 1024, kMaxK2 = 64, kMaxR
 
 __device__ __forceinline__ unsigned absbits(float x) { return __float_as_uint(x) & 0x7fffffffu; }
 
-static __global__ void __launch_bounds__(256)
-absmax_rows_f32(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_t R,
-                int64_t K, int mode, unsigned *__restrict__ maxbits) {
+// Block (bk, br) of the grid below, executed by a 256-thread block.
+__device__ __forceinline__ void absmax_block(const float *__restrict__ src, int64_t rs_row,
+                                             int64_t rs_k, int64_t R, int64_t K, int mode,
+                                             unsigned *__restrict__ maxbits, int64_t bk,
+                                             int64_t br) {
   const int tid = threadIdx.x;
   if (mode == 1) {
-    const int64_t r = (int64_t)blockIdx.y * kMaxRows1 + (tid >> 5);
-    const int64_t k0 = (int64_t)blockIdx.x * kMaxK1;
+    const int64_t r = br * kMaxRows1 + (tid >> 5);
+    const int64_t k0 = bk * kMaxK1;
     const int lane = tid & 31;
     unsigned m = 0;
     if (r < R) {
@@ -85,8 +87,8 @@ absmax_rows_f32(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int
     m = __reduce_max_sync(0xffffffffu, m);
     if (lane == 0 && r < R && m) atomicMax(&maxbits[r], m);
   } else if (mode == 2) {
-    const int64_t r = (int64_t)blockIdx.y * kMaxRows2 + 4 * tid;
-    const int64_t k0 = (int64_t)blockIdx.x * kMaxK2;
+    const int64_t r = br * kMaxRows2 + 4 * tid;
+    const int64_t k0 = bk * kMaxK2;
     unsigned m[4] = {0, 0, 0, 0};
     if (r < R) {
       const int64_t k1 = k0 + kMaxK2 < K ? k0 + kMaxK2 : K;
@@ -107,8 +109,8 @@ absmax_rows_f32(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int
     for (int t = 0; t < 4; t++)
       if (r + t < R && m[t]) atomicMax(&maxbits[r + t], m[t]);
   } else {
-    const int64_t r = (int64_t)blockIdx.y * kMaxRows0 + tid;
-    const int64_t k0 = (int64_t)blockIdx.x * kMaxK0;
+    const int64_t r = br * kMaxRows0 + tid;
+    const int64_t k0 = bk * kMaxK0;
     unsigned m = 0;
     if (r < R) {
       const int64_t k1 = k0 + kMaxK0 < K ? k0 + kMaxK0 : K;
@@ -118,8 +120,14 @@ absmax_rows_f32(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int
   }
 }
 
+static __global__ void __launch_bounds__(256)
+absmax_rows_f32(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_t R,
+                int64_t K, int mode, unsigned *__restrict__ maxbits) {
+  absmax_block(src, rs_row, rs_k, R, K, mode, maxbits, blockIdx.x, blockIdx.y);
+}
+
 // Grid of absmax_rows_f32 for R rows, K columns, read mode `mode`.
-inline dim3 absmax_grid(int64_t R, int64_t K, int mode) {
+__host__ __device__ inline dim3 absmax_grid(int64_t R, int64_t K, int mode) {
   const int64_t kk = mode == 1 ? kMaxK1 : mode == 2 ? kMaxK2 : kMaxK0;
   const int64_t rr = mode == 1 ? kMaxRows1 : mode == 2 ? kMaxRows2 : kMaxRows0;
   return dim3((unsigned)((K + kk - 1) / kk), (unsigned)((R + rr - 1) / rr));

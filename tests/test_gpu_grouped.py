@@ -2,9 +2,10 @@
 
 Every problem of a plan must match the oracle: the CUDA-core variant is
 numc's FMA chain (same bound as the single-problem SIMT kernel), the
-split-BF16 variants meet the 3-pass bound of test_gpu_split.py.  Plans run
-directly, replayed as CUDA graphs with changed inputs, and captured by the
-caller (an MLP chain, two dependent plans in one graph).
+split-BF16 variants meet the 3-pass bound of test_gpu_split.py and the
+scaled float16 variants (the default) the bound of test_gpu_split16.py.
+Plans run directly, replayed as CUDA graphs with changed inputs, and
+captured by the caller (an MLP chain, two dependent plans in one graph).
 """
 import numpy as np
 import pytest
@@ -21,6 +22,13 @@ torch = pytest.importorskip("torch")
 
 def split_bound(K):
     return 3 * 2.0 ** -16 + 2 * (3 * K + 2) * 2.0 ** -24
+
+
+def f16_bound(K):
+    return 4 * 2.0 ** -22 + 2 * (3 * K + 2) * 2.0 ** -24
+
+
+BOUND = {nc.ALGO_SPLIT_BF16: split_bound, nc.ALGO_SPLIT_FP16: f16_bound}
 
 
 def simt_bound(K):
@@ -48,12 +56,13 @@ def check_all(probs, bound):
 
 
 @pytest.mark.parametrize("param", [0, 128, 64])
-def test_split_plan_matches_oracle(param):
+@pytest.mark.parametrize("algo", [nc.ALGO_SPLIT_FP16, nc.ALGO_SPLIT_BF16])
+def test_split_plan_matches_oracle(param, algo):
     probs = random_problems(40, seed=1)
-    plan = nc.GemmPlan([(p[0], p[1], p[2]) for p in probs], nc.ALGO_SPLIT_BF16, param)
+    plan = nc.GemmPlan([(p[0], p[1], p[2]) for p in probs], algo, param)
     plan.run()
     nc.check_status()
-    check_all(probs, lambda K: max(split_bound(K), simt_bound(K)))
+    check_all(probs, lambda K: max(BOUND[algo](K), simt_bound(K)))
     info = plan.info()
     assert sum(info[k] for k in ("tc128", "tc64", "simt")) == 40
     if param == 128:
@@ -74,9 +83,10 @@ def test_simt_plan_is_numc_arithmetic():
     check_all(probs, simt_bound)
 
 
-def test_graph_replay_sees_new_inputs():
+@pytest.mark.parametrize("algo", [nc.ALGO_SPLIT_FP16, nc.ALGO_SPLIT_BF16])
+def test_graph_replay_sees_new_inputs(algo):
     probs = random_problems(12, seed=3)
-    plan = nc.GemmPlan([(p[0], p[1], p[2]) for p in probs], nc.ALGO_SPLIT_BF16)
+    plan = nc.GemmPlan([(p[0], p[1], p[2]) for p in probs], algo)
     plan.run(graph=True)
     for ta, tb, out, a, b in probs:     # new values, same buffers
         ta.mul_(-2.0)
@@ -86,7 +96,7 @@ def test_graph_replay_sees_new_inputs():
         got = out.cpu().numpy()
         a2 = a * np.float32(-2.0)
         assert rel_err_vs_scale(got, oracle.matmul(a2, b), a2, b) <= \
-            max(split_bound(a.shape[1]), simt_bound(a.shape[1]))
+            max(BOUND[algo](a.shape[1]), simt_bound(a.shape[1]))
 
 
 def test_mlp_chains_in_one_captured_graph():
@@ -117,14 +127,45 @@ def test_mlp_chains_in_one_captured_graph():
     nc.check_status()
     for x, w1, w2, t, h, y in chains:
         ref_h = oracle.matmul(x, w1)
-        assert rel_err_vs_scale(h.cpu().numpy(), ref_h, x, w1) <= split_bound(784)
+        assert rel_err_vs_scale(h.cpu().numpy(), ref_h, x, w1) <= f16_bound(784)
         ref_y = oracle.matmul(ref_h, w2)
         err = np.abs(y.cpu().numpy().astype(np.float64) - ref_y)
         assert err.max() <= 1e-4 * (np.abs(ref_h) @ np.abs(w2)).max()
 
 
-def test_numc_matmul_grouped_host_arrays():
+@pytest.mark.parametrize("f32_algo", [nc.ALGO_AUTO, nc.ALGO_SPLIT_BF16])
+def test_numc_matmul_grouped_host_arrays(f32_algo):
     rng = np.random.default_rng(4)
+    orig = nc.get_algo("float32")
+    nc.set_algo("float32", f32_algo)
+    bound = f16_bound if f32_algo == nc.ALGO_AUTO else split_bound
+    try:
+        _grouped_host_arrays(rng, bound)
+    finally:
+        nc.set_algo("float32", *orig)
+
+
+def test_grouped_f16_not_less_accurate_than_fp32_fma():
+    # Over a plan of mixed shapes, the scaled float16 split must not lose
+    # to numc's FP32 FMA chain against a float64 reference (max and mean
+    # error relative to |A| @ |B|).
+    probs = random_problems(30, lo=64, hi=1024, seed=9)
+    plan = nc.GemmPlan([(p[0], p[1], p[2]) for p in probs], nc.ALGO_SPLIT_FP16, 128)
+    plan.run()
+    nc.check_status()
+    e16, efma = [], []
+    for ta, tb, out, a, b in probs:
+        exact = a.astype(np.float64) @ b.astype(np.float64)
+        scale = np.abs(a.astype(np.float64)) @ np.abs(b.astype(np.float64))
+        e16.append(np.abs(out.cpu().numpy() - exact) / scale)
+        efma.append(np.abs(oracle.matmul(a, b) - exact) / scale)
+    e16 = np.concatenate([x.ravel() for x in e16])
+    efma = np.concatenate([x.ravel() for x in efma])
+    assert e16.max() <= efma.max(), (e16.max(), efma.max())
+    assert e16.mean() <= efma.mean(), (e16.mean(), efma.mean())
+
+
+def _grouped_host_arrays(rng, bound):
     with nc.Ctx() as ctx:
         As, Bs, Cs, refs = [], [], [], []
         for i in range(10):
@@ -139,7 +180,7 @@ def test_numc_matmul_grouped_host_arrays():
         for C, (a, b) in zip(Cs, refs):
             K = a.shape[1]
             assert rel_err_vs_scale(C.numpy(), oracle.matmul(a, b), a, b) <= \
-                max(split_bound(K), simt_bound(K))
+                max(bound(K), simt_bound(K))
         # integer dtypes loop numc_matmul, bit-exact
         a, b = synth.operands("uniform", 50, 600, 40, dtype="int8")
         A, B, C = ctx.from_numpy(a), ctx.from_numpy(b), ctx.zeros((50, 40), "int8")
