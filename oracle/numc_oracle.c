@@ -127,7 +127,7 @@ static void scatter(void *dstv, const void *src, int64_t rows, int64_t cols,
             for (int j = 0; j < NR; j++) {                                    \
               const int64_t col = jc + js * NR + j;                           \
               bp[(js * kc + k) * NR + j] =                                    \
-                  col < N ? b[(pc + k) * N + col] : (T)0;                     \
+                  col < jc + nc ? b[(pc + k) * N + col] : (T)0;               \
             }                                                                 \
         /* (row block, column strip) tiles shared out in contiguous runs,  \
          * so a few row blocks still keep every thread busy. */              \
@@ -140,7 +140,8 @@ static void scatter(void *dstv, const void *src, int64_t rows, int64_t cols,
           T ta[MR * FKC], tc[MR * NR];                                        \
           {                                                                   \
             const int64_t j0 = jc + js * NR;                                  \
-            const int nr = (int)MIN(NR, N - j0);                              \
+            /* the last strip of a panel stops at the panel's end */          \
+            const int nr = (int)MIN(NR, jc + nc - j0);                        \
             const T *bs = bp + js * kc * NR;                                  \
             if (mr == MR && nr == NR) {                                       \
               MICRO(a + i0 * K + pc, K, bs, c + i0 * N + j0, N, kc);          \

@@ -48,6 +48,10 @@ RANDOM_CASES = [
     ("float32", "illscaled", (96, 200, 80)),
     ("float64", "expspread", (96, 200, 80)),
     ("float32", "uniform", (512, 512, 512)),
+    # several column panels of the oracle and of numc (NC = 4080), ragged
+    ("float32", "uniform", (150, 300, 833)),
+    ("float64", "uniform", (120, 260, 700)),
+    ("float32", "normal", (100, 520, 4100)),
     ("int8", "uniform", (1024, 1024, 1024)),
     ("uint8", "uniform", (1024, 1024, 1024)),
     ("int32", "uniform", (1024, 1024, 1024)),
