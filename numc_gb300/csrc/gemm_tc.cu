@@ -270,11 +270,15 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
           const uint32_t st = tc::smem_u32(smem + s * Cfg::STAGE_BYTES);
           const uint32_t bbase = st + PLANES * Cfg::A_BYTES;
           const uint32_t acc_tmem = tmem + buf * BN;
+          // Product by product over the slab, smallest first: the tensor
+          // core truncates the accumulator at every MMA, so the large
+          // x0 y0 terms enter last and are truncated only kBK / 16 times
+          // at full magnitude per chunk start.
 #pragma unroll
-          for (int kk = 0; kk < kBK / 16; kk++) {
-            const uint32_t koff = kk * 32;   // 16 elements = 32 bytes inside the swizzle atom
+          for (int p = 0; p < P::n; p++) {
 #pragma unroll
-            for (int p = 0; p < P::n; p++) {
+            for (int kk = 0; kk < kBK / 16; kk++) {
+              const uint32_t koff = kk * 32;   // 16 elements = 32 bytes inside the swizzle atom
               const uint32_t acc = (!chunk_start || kk > 0 || p > 0) ? 1u : 0u;
               const uint64_t ad = tc::sdesc_k128(st + P::a(p) * Cfg::A_BYTES + koff);
               const uint64_t bd = tc::sdesc_k128(bbase + P::b(p) * Cfg::B_BYTES + koff);
