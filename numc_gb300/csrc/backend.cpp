@@ -9,6 +9,7 @@
 // a usable GPU the call fails with NUMC_ERR_INTERNAL.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cstdlib>
 #include <cstring>
@@ -285,6 +286,122 @@ int check_matmul(const NumcArray *a, const NumcArray *b, const NumcArray *out) {
   return 0;
 }
 
+// A lazily created non-blocking stream kept in the context.
+int ctx_aux_stream(NumcCtx *ctx, void **slot, cudaStream_t *s) {
+  if (!*slot) {
+    cudaStream_t st;
+    CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    *slot = st;
+  }
+  *s = (cudaStream_t)*slot;
+  return 0;
+}
+
+bool rows_contiguous(const NumcArray *x) {
+  return x->strides[1] == x->elem_size && x->strides[0] == x->shape[1] * x->elem_size;
+}
+
+// Whether a split GEMM with host operands runs as a row-panel pipeline.
+bool use_pipeline(const Plan &plan, const NumcArray *a, const NumcArray *b, const NumcArray *out,
+                  size_t M, size_t K, size_t N) {
+  if (plan.algo != NUMC_CUDA_ALGO_SPLIT_FP16 && plan.algo != NUMC_CUDA_ALGO_SPLIT_BF16) return false;
+  if (is_resident(a) || is_resident(b) || is_resident(out)) return false;
+  if (!rows_contiguous(a) || !rows_contiguous(out)) return false;
+  return M >= 1024 && K >= 64 && (double)M * K * N >= 4294967296.0;
+}
+
+// Host operands of a large split GEMM: the host copies overlap the work.
+// The copy-in stream sends B, then A panel by panel; the compute stream
+// splits B once it has arrived and each panel of A once that has, and
+// multiplies the panel; the copy-out stream returns each panel of C as soon
+// as its GEMM is done.  At 8192^3 on GB300 the serial order spends 2.4 ms
+// copying A and B in, 2.3 ms computing and 1.3 ms copying C out.
+int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, const Plan &plan,
+                     cudaStream_t s) {
+  NumcCtx *ctx = out->ctx;
+  const size_t M = a->shape[0], K = a->shape[1], N = b->shape[1], es = 4;
+  const size_t want = M >= 4096 ? 4 : 2;
+  const size_t rows = align_up((M + want - 1) / want, 256);
+  const numc_k::SplitPipe pp = numc_k::split_pipe_layout(plan.algo, plan.param, M, K, N, rows);
+  const size_t sa = array_span_bytes(a), sb = array_span_bytes(b), so = array_span_bytes(out);
+  const size_t off_b = align_up(sa, 256), off_c = off_b + align_up(sb, 256);
+  const size_t off_w = off_c + align_up(so, 256);
+  char *scratch = nullptr;
+  int err;
+  if ((err = ctx_scratch(ctx, off_w + pp.total + 256, s, &scratch))) return err;
+  cudaStream_t cin, cout;
+  if ((err = ctx_aux_stream(ctx, &ctx->copy_in, &cin))) return err;
+  if ((err = ctx_aux_stream(ctx, &ctx->copy_out, &cout))) return err;
+  char *dA = scratch, *dB = scratch + off_b, *dC = scratch + off_c, *ws = scratch + off_w;
+
+  std::vector<cudaEvent_t> ev;
+  auto cleanup = [&] {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  };
+  auto fail_cu = [&](cudaError_t e, const char *what) {
+    cudaStreamSynchronize(cin);
+    cudaStreamSynchronize(s);
+    cudaStreamSynchronize(cout);
+    cleanup();
+    return cuda_fail(e, what);
+  };
+  // ev[0]: B copied; ev[1]: scratch free; ev[2 + p]: panel p of A copied;
+  // ev[2 + np + p]: panel p of C computed.
+  const int np = pp.npanels;
+  for (int i = 0; i < 2 + 2 * np; i++) {
+    cudaEvent_t e;
+    cudaError_t ce = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (ce != cudaSuccess) return fail_cu(ce, "cudaEventCreate");
+    ev.push_back(e);
+  }
+  cudaEvent_t ev_b = ev[0];
+  cudaError_t e;
+  // The previous user of the scratch (the compute stream) must be done
+  // before the copy-in stream overwrites it.
+  if ((e = cudaEventRecord(ev[1], s)) || (e = cudaStreamWaitEvent(cin, ev[1], 0)))
+    return fail_cu(e, "stream order");
+  if ((e = cudaMemcpyAsync(dB, b->data, sb, cudaMemcpyHostToDevice, cin)) ||
+      (e = cudaEventRecord(ev_b, cin)))
+    return fail_cu(e, "copy b to device");
+  for (int p = 0; p < np; p++) {
+    const size_t r0 = (size_t)p * rows, r = std::min(rows, M - r0);
+    if ((e = cudaMemcpyAsync(dA + r0 * K * es, (const char *)a->data + r0 * K * es, r * K * es,
+                             cudaMemcpyHostToDevice, cin)) ||
+        (e = cudaEventRecord(ev[2 + p], cin)))
+      return fail_cu(e, "copy a panel to device");
+  }
+  numc_k::Gemm g;
+  g.a = dA; g.b = dB; g.c = dC;
+  g.M = M; g.K = K; g.N = N;
+  g.rsa = K; g.csa = 1;
+  g.rsb = b->strides[0] / es; g.csb = b->strides[1] / es;
+  g.rso = N; g.cso = 1;
+  const unsigned long long gen = numc_k::split_pipe_gen();
+  if ((e = cudaStreamWaitEvent(s, ev_b, 0)) || (e = numc_k::split_pipe_b(pp, g, ws, gen, s)))
+    return fail_cu(e, "split of b");
+  for (int p = 0; p < np; p++) {
+    const size_t r0 = (size_t)p * rows, r = std::min(rows, M - r0);
+    numc_k::Gemm gp = g;
+    gp.a = dA + r0 * K * es;
+    gp.c = dC + r0 * N * es;
+    gp.M = r;
+    cudaEvent_t done = ev[2 + np + p];
+    if ((e = cudaStreamWaitEvent(s, ev[2 + p], 0)) ||
+        (e = numc_k::split_pipe_panel(pp, p, gp, ws, gen, s)) || (e = cudaEventRecord(done, s)) ||
+        (e = cudaStreamWaitEvent(cout, done, 0)) ||
+        (e = cudaMemcpyAsync((char *)out->data + r0 * N * es, gp.c, r * N * es,
+                             cudaMemcpyDeviceToHost, cout)))
+      return fail_cu(e, "panel");
+  }
+  if ((e = cudaStreamSynchronize(cout)) || (e = cudaStreamSynchronize(s)))
+    return fail_cu(e, "cudaStreamSynchronize");
+  cleanup();
+  unsigned st = 0;
+  CU(numc_k::read_and_clear_status(&st, s), "status read");
+  if (st) return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "matmul kernel abandoned a bounded wait (code %u)", st);
+  return 0;
+}
+
 int matmul_impl(const NumcArray *a, const NumcArray *b, NumcArray *out, int algo, int param) {
   int err = check_matmul(a, b, out);
   if (err) return err;
@@ -296,6 +413,7 @@ int matmul_impl(const NumcArray *a, const NumcArray *b, NumcArray *out, int algo
   NumcCtx *ctx = out->ctx;
   cudaStream_t s;
   if ((err = ctx_stream(ctx, &s))) return err;
+  if (use_pipeline(plan, a, b, out, M, K, N)) return matmul_pipelined(a, b, out, plan, s);
 
   const size_t es = a->elem_size;
   const bool ra = is_resident(a), rb = is_resident(b), ro = is_resident(out);
@@ -381,6 +499,13 @@ void ctx_release_device(NumcCtx *ctx, const ArenaPos *keep_upto) {
     ctx->scratch_bytes = 0;
     if (ctx->stream) cudaStreamDestroy((cudaStream_t)ctx->stream);
     ctx->stream = nullptr;
+    for (void **cs : {&ctx->copy_in, &ctx->copy_out}) {
+      if (*cs) {
+        cudaStreamSynchronize((cudaStream_t)*cs);
+        cudaStreamDestroy((cudaStream_t)*cs);
+      }
+      *cs = nullptr;
+    }
   }
 }
 

@@ -130,6 +130,8 @@ extern "C" NumcCtx *numc_ctx_create(void) {
   ctx->next_seq = 1;
   ctx->pin_host = cuda_present();
   ctx->stream = nullptr;
+  ctx->copy_in = nullptr;
+  ctx->copy_out = nullptr;
   ctx->device = -1;
   ctx->scratch = nullptr;
   ctx->scratch_bytes = 0;

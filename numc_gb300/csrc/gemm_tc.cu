@@ -468,6 +468,24 @@ SplitLayout split_layout(int64_t M, int64_t K, int64_t N, int planes, bool f16 =
   return L;
 }
 
+// Device addresses of one GEMM's split operands.
+struct SplitBufs {
+  uint16_t *pa, *pb;                      // planes
+  unsigned long long *flags_a, *flags_b;  // per 128 rows of A, per 64 columns of B
+  unsigned *max_a, *max_b;                // float16 planes: row / column maxima
+};
+
+SplitBufs bufs_of(const SplitLayout &L, char *ws) {
+  SplitBufs b;
+  b.pa = (uint16_t *)(ws + L.a);
+  b.pb = (uint16_t *)(ws + L.b);
+  b.flags_a = (unsigned long long *)(ws + L.flags_a);
+  b.flags_b = (unsigned long long *)(ws + L.flags_b);
+  b.max_a = L.f16 ? (unsigned *)(ws + L.max_a) : nullptr;
+  b.max_b = L.f16 ? (unsigned *)(ws + L.max_b) : nullptr;
+  return b;
+}
+
 // Streaming multiprocessors of the current device (persistent grid size).
 int sm_count() {
   static int cached[64] = {0};
@@ -484,43 +502,55 @@ int sm_count() {
 // Generation numbers of split calls (never 0; flags hold the last writer's).
 std::atomic<unsigned long long> g_split_gen{0x5eed000000000000ull};
 
-// Launch the split pass of both operands.
-cudaError_t launch_split_pass(const SplitLayout &L, char *ws, const Gemm &g,
-                              unsigned long long gen, cudaStream_t s) {
-  dim3 ga((unsigned)((L.Kp + kSplitK - 1) / kSplitK), (unsigned)((g.M + kSplitRows - 1) / kSplitRows));
-  dim3 gb((unsigned)((L.Kp + kSplitK - 1) / kSplitK), (unsigned)((g.N + kSplitRows - 1) / kSplitRows));
-  if (ga.y > 65535 || gb.y > 65535) return cudaErrorInvalidConfiguration;
-  auto *pa = (uint16_t *)(ws + L.a), *pb = (uint16_t *)(ws + L.b);
-  auto *fa = (unsigned long long *)(ws + L.flags_a), *fb = (unsigned long long *)(ws + L.flags_b);
-  const float *A = (const float *)g.a, *B = (const float *)g.b;
-  const int ma = split_mode(A, g.rsa, g.csa), mb = split_mode(B, g.csb, g.rsb);
+// Split one operand (R rows of src[r * rs_row + k * rs_k], k < K) into
+// planes; for float16 planes first its row maxima.
+cudaError_t split_operand(const SplitLayout &L, const float *src, int64_t rs_row, int64_t rs_k,
+                          int64_t R, int64_t K, uint16_t *planes, unsigned long long *flags,
+                          int flag_rows, unsigned *maxbits, unsigned long long gen,
+                          cudaStream_t s) {
+  const dim3 grid((unsigned)((L.Kp + kSplitK - 1) / kSplitK),
+                  (unsigned)((R + kSplitRows - 1) / kSplitRows));
+  if (grid.y > 65535) return cudaErrorInvalidConfiguration;
+  const int mode = split_mode(src, rs_row, rs_k);
   if (L.f16) {
-    auto *xa = (unsigned *)(ws + L.max_a), *xb = (unsigned *)(ws + L.max_b);
-    const dim3 ra = absmax_grid(g.M, g.K, ma), rb = absmax_grid(g.N, g.K, mb);
-    if (ra.y > 65535 || rb.y > 65535) return cudaErrorInvalidConfiguration;
-    cudaError_t e = cudaMemsetAsync(xa, 0, L.total - L.max_a, s);
+    const dim3 rg = absmax_grid(R, K, mode);
+    if (rg.y > 65535) return cudaErrorInvalidConfiguration;
+    cudaError_t e = cudaMemsetAsync(maxbits, 0, (size_t)R * 4, s);
     if (e != cudaSuccess) return e;
-    absmax_rows_f32<<<ra, 256, 0, s>>>(A, g.rsa, g.csa, g.M, g.K, ma, xa);
-    absmax_rows_f32<<<rb, 256, 0, s>>>(B, g.csb, g.rsb, g.N, g.K, mb, xb);
-    split_planes<2, true><<<ga, 256, 0, s>>>(A, g.rsa, g.csa, g.M, g.K, L.Kp, pa, fa, kBM, gen,
-                                               ma, xa);
-    split_planes<2, true><<<gb, 256, 0, s>>>(B, g.csb, g.rsb, g.N, g.K, L.Kp, pb, fb, 64, gen,
-                                               mb, xb);
-    count_launch(4);
+    absmax_rows_f32<<<rg, 256, 0, s>>>(src, rs_row, rs_k, R, K, mode, maxbits);
+    split_planes<2, true><<<grid, 256, 0, s>>>(src, rs_row, rs_k, R, K, L.Kp, planes, flags,
+                                               flag_rows, gen, mode, maxbits);
+    count_launch(2);
   } else if (L.planes == 3) {
-    split_planes<3, false><<<ga, 256, 0, s>>>(A, g.rsa, g.csa, g.M, g.K, L.Kp, pa, fa, kBM,
-                                                gen, ma, nullptr);
-    split_planes<3, false><<<gb, 256, 0, s>>>(B, g.csb, g.rsb, g.N, g.K, L.Kp, pb, fb, 64, gen,
-                                                mb, nullptr);
-    count_launch(2);
+    split_planes<3, false><<<grid, 256, 0, s>>>(src, rs_row, rs_k, R, K, L.Kp, planes, flags,
+                                                flag_rows, gen, mode, nullptr);
+    count_launch(1);
   } else {
-    split_planes<2, false><<<ga, 256, 0, s>>>(A, g.rsa, g.csa, g.M, g.K, L.Kp, pa, fa, kBM,
-                                                gen, ma, nullptr);
-    split_planes<2, false><<<gb, 256, 0, s>>>(B, g.csb, g.rsb, g.N, g.K, L.Kp, pb, fb, 64, gen,
-                                                mb, nullptr);
-    count_launch(2);
+    split_planes<2, false><<<grid, 256, 0, s>>>(src, rs_row, rs_k, R, K, L.Kp, planes, flags,
+                                                flag_rows, gen, mode, nullptr);
+    count_launch(1);
   }
   return cudaGetLastError();
+}
+
+cudaError_t split_a(const SplitLayout &L, const SplitBufs &b, const Gemm &g,
+                    unsigned long long gen, cudaStream_t s) {
+  return split_operand(L, (const float *)g.a, g.rsa, g.csa, g.M, g.K, b.pa, b.flags_a, kBM,
+                       b.max_a, gen, s);
+}
+
+// B is split as B^T: its rows are B's columns.
+cudaError_t split_b(const SplitLayout &L, const SplitBufs &b, const Gemm &g,
+                    unsigned long long gen, cudaStream_t s) {
+  return split_operand(L, (const float *)g.b, g.csb, g.rsb, g.N, g.K, b.pb, b.flags_b, 64,
+                       b.max_b, gen, s);
+}
+
+// Launch the split pass of both operands.
+cudaError_t launch_split_pass(const SplitLayout &L, const SplitBufs &b, const Gemm &g,
+                              unsigned long long gen, cudaStream_t s) {
+  cudaError_t e = split_a(L, b, g, gen, s);
+  return e != cudaSuccess ? e : split_b(L, b, g, gen, s);
 }
 
 // Co-resident clusters of `kern` launched with `cfg` (0 if the query fails).
@@ -534,14 +564,14 @@ int max_active_clusters(const void *kern, const cudaLaunchConfig_t &cfg) {
 }
 
 template <int BN, int STAGES, int PLANES, int FLUSH, bool F16, int CTAS>
-cudaError_t launch_gemm_status(const SplitLayout &L, char *ws, const Gemm &g,
+cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, const Gemm &g,
                                unsigned long long gen, unsigned *status, cudaStream_t s) {
   using Cfg = SplitCfg<BN, STAGES, PLANES, FLUSH, CTAS>;
   CUtensorMap ta, tb;
   cudaError_t e;
   const auto dtype = F16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-  if ((e = make_tmap_3d(&ta, ws + L.a, dtype, 2, PLANES, g.M, L.Kp, L.Kp, kBM, kBK))) return e;
-  if ((e = make_tmap_3d(&tb, ws + L.b, dtype, 2, PLANES, g.N, L.Kp, L.Kp, Cfg::BN_CTA, kBK)))
+  if ((e = make_tmap_3d(&ta, bufs.pa, dtype, 2, PLANES, g.M, L.Kp, L.Kp, kBM, kBK))) return e;
+  if ((e = make_tmap_3d(&tb, bufs.pb, dtype, 2, PLANES, g.N, L.Kp, L.Kp, Cfg::BN_CTA, kBK)))
     return e;
   auto kern = split_gemm<BN, STAGES, PLANES, FLUSH, F16, CTAS>;
   if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM)))
@@ -553,11 +583,11 @@ cudaError_t launch_gemm_status(const SplitLayout &L, char *ws, const Gemm &g,
   fb.A = (const float *)g.a;
   fb.B = (const float *)g.b;
   fb.rsa = g.rsa; fb.csa = g.csa; fb.rsb = g.rsb; fb.csb = g.csb; fb.K = g.K;
-  fb.flags_a = (const unsigned long long *)(ws + L.flags_a);
-  fb.flags_b = (const unsigned long long *)(ws + L.flags_b);
+  fb.flags_a = bufs.flags_a;
+  fb.flags_b = bufs.flags_b;
   fb.gen = gen;
-  fb.max_a = F16 ? (const unsigned *)(ws + L.max_a) : nullptr;
-  fb.max_b = F16 ? (const unsigned *)(ws + L.max_b) : nullptr;
+  fb.max_a = bufs.max_a;
+  fb.max_b = bufs.max_b;
   const int num_kb = (int)(L.Kp / kBK);
   if (CTAS == 1) {
     const int grid = std::min(tiles_m * tiles_n, sm_count());
@@ -610,7 +640,7 @@ cudaError_t launch_gemm_status(const SplitLayout &L, char *ws, const Gemm &g,
 // (128 x 256, 2 stages of 96 KiB).  Three planes need 128-column tiles to
 // fit a ring of at least two stages.
 template <int CTAS>
-cudaError_t launch_gemm_ctas(const SplitLayout &L, char *ws, const Gemm &g,
+cudaError_t launch_gemm_ctas(const SplitLayout &L, const SplitBufs &ws, const Gemm &g,
                              unsigned long long gen, unsigned *status, cudaStream_t s) {
   constexpr int S2 = CTAS == 2 ? 3 : 2;   // stages of the 2-plane ring
   if (L.f16) {
@@ -638,7 +668,7 @@ int split_ctas() {
   return v;
 }
 
-cudaError_t launch_gemm(const SplitLayout &L, char *ws, const Gemm &g, unsigned long long gen,
+cudaError_t launch_gemm(const SplitLayout &L, const SplitBufs &ws, const Gemm &g, unsigned long long gen,
                         unsigned *status, cudaStream_t s) {
   if (split_ctas() == 2) return launch_gemm_ctas<2>(L, ws, g, gen, status, s);
   return launch_gemm_ctas<1>(L, ws, g, gen, status, s);
@@ -686,6 +716,74 @@ cudaError_t launch_split_f16(const Gemm &g, int flush, void *ws_v, size_t ws_byt
   return run_split(g, split_layout(g.M, g.K, g.N, 2, true, flush), ws_v, ws_bytes, s);
 }
 
+// ---- row-panel pipeline ---------------------------------------------------------
+
+SplitPipe split_pipe_layout(int algo, int param, int64_t M, int64_t K, int64_t N,
+                            int64_t panel_rows) {
+  SplitPipe p;
+  p.f16 = algo == NUMC_CUDA_ALGO_SPLIT_FP16;
+  p.planes = p.f16 ? 2 : planes_for(param);
+  p.flush = p.f16 ? (param ? param : kF16DefaultFlush) : 0;
+  p.M = M; p.K = K; p.N = N;
+  p.Kp = round_up(K > 0 ? K : 1, kBK);
+  p.panel_rows = panel_rows;
+  p.npanels = (int)((M + panel_rows - 1) / panel_rows);
+  // B region: planes, flags, maxima
+  size_t off = (size_t)round_up(p.planes * N * p.Kp * 2, 256);
+  off += (size_t)round_up(((N + 63) / 64) * 8, 256);
+  if (p.f16) off += (size_t)round_up(N * 4, 256);
+  p.panel_off = off;
+  p.panel_bytes = (size_t)round_up(p.planes * panel_rows * p.Kp * 2, 256) +
+                  (size_t)round_up(((panel_rows + kBM - 1) / kBM) * 8, 256) +
+                  (p.f16 ? (size_t)round_up(panel_rows * 4, 256) : 0);
+  p.total = p.panel_off + p.npanels * p.panel_bytes;
+  return p;
+}
+
+unsigned long long split_pipe_gen() { return ++g_split_gen; }
+
+namespace {
+SplitLayout pipe_params(const SplitPipe &p) {
+  SplitLayout L = split_layout(1, p.K, 1, p.planes, p.f16, p.flush);   // offsets unused
+  return L;
+}
+
+SplitBufs pipe_bufs(const SplitPipe &p, int panel, char *ws) {
+  SplitBufs b;
+  char *q = ws;
+  b.pb = (uint16_t *)q;
+  q += round_up(p.planes * p.N * p.Kp * 2, 256);
+  b.flags_b = (unsigned long long *)q;
+  q += round_up(((p.N + 63) / 64) * 8, 256);
+  b.max_b = p.f16 ? (unsigned *)q : nullptr;
+  q = ws + p.panel_off + (size_t)(panel < 0 ? 0 : panel) * p.panel_bytes;
+  b.pa = (uint16_t *)q;
+  q += round_up(p.planes * p.panel_rows * p.Kp * 2, 256);
+  b.flags_a = (unsigned long long *)q;
+  q += round_up(((p.panel_rows + kBM - 1) / kBM) * 8, 256);
+  b.max_a = p.f16 ? (unsigned *)q : nullptr;
+  return b;
+}
+}  // namespace
+
+cudaError_t split_pipe_b(const SplitPipe &p, const Gemm &g, void *ws, unsigned long long gen,
+                         cudaStream_t s) {
+  return split_b(pipe_params(p), pipe_bufs(p, -1, (char *)ws), g, gen, s);
+}
+
+cudaError_t split_pipe_panel(const SplitPipe &p, int panel, const Gemm &g, void *ws,
+                             unsigned long long gen, cudaStream_t s) {
+  if (panel < 0 || panel >= p.npanels || g.M > p.panel_rows || g.M <= 0 || g.N <= 0 ||
+      g.K <= 0)
+    return cudaErrorInvalidValue;
+  unsigned *status = status_word();
+  if (!status) return cudaErrorMemoryAllocation;
+  const SplitLayout L = pipe_params(p);
+  const SplitBufs b = pipe_bufs(p, panel, (char *)ws);
+  cudaError_t e = split_a(L, b, g, gen, s);
+  return e != cudaSuccess ? e : launch_gemm(L, b, g, gen, status, s);
+}
+
 namespace {
 cudaError_t run_split(const Gemm &g, const SplitLayout &L, void *ws_v, size_t ws_bytes,
                       cudaStream_t s) {
@@ -694,15 +792,15 @@ cudaError_t run_split(const Gemm &g, const SplitLayout &L, void *ws_v, size_t ws
   if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31))
     return cudaErrorInvalidValue;
   if (ws_bytes < L.total || ((uintptr_t)ws_v & 255)) return cudaErrorInvalidValue;
-  char *ws = (char *)ws_v;
+  const SplitBufs bufs = bufs_of(L, (char *)ws_v);
   unsigned *status = status_word();
   if (!status) return cudaErrorMemoryAllocation;
   PhaseMark mark(s);
   const unsigned long long gen = ++g_split_gen;
-  cudaError_t e = launch_split_pass(L, ws, g, gen, s);
+  cudaError_t e = launch_split_pass(L, bufs, g, gen, s);
   if (e) return e;
   mark.split_done();
-  e = launch_gemm(L, ws, g, gen, status, s);
+  e = launch_gemm(L, bufs, g, gen, status, s);
   mark.gemm_done();
   return e;
 }
@@ -796,10 +894,10 @@ extern "C" int numc_cuda_sgemm_split_static(const float *a, const float *b, floa
   if (K == 0) {
     e = launch_simt(NUMC_DTYPE_FLOAT32, g, 0, s);   // out = 0, no scratch
   } else {
-    char *ws = (char *)base;
+    const SplitBufs bufs = bufs_of(L, (char *)base);
     const unsigned long long gen = ++g_split_gen;
-    e = launch_split_pass(L, ws, g, gen, s);
-    if (e == cudaSuccess) e = launch_gemm(L, ws, g, gen, status, s);
+    e = launch_split_pass(L, bufs, g, gen, s);
+    if (e == cudaSuccess) e = launch_gemm(L, bufs, g, gen, status, s);
   }
   if (e != cudaSuccess)
     return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "sgemm_split_static: launch failed: %s",

@@ -35,6 +35,28 @@ cudaError_t launch_dmma(const Gemm &g, cudaStream_t s);
 // (three planes): workspace bytes and launcher.
 size_t split_bf16_workspace(int64_t M, int64_t K, int64_t N, int passes);
 size_t split_f16_workspace(int64_t M, int64_t K, int64_t N);
+
+// Row-panel pipeline of the split GEMMs (numc_matmul with host operands
+// overlaps the panels with its host copies): B is split once, then each
+// panel of `panel_rows` rows of A is split and multiplied into the same
+// rows of C.  Workspace: B's planes, flags and maxima, then one region per
+// panel.
+struct SplitPipe {
+  bool f16;
+  int planes, flush;
+  int64_t M, K, N, Kp, panel_rows;
+  int npanels;
+  size_t panel_off, panel_bytes, total;
+};
+// algo / param as resolved for numc_cuda_gemm (SPLIT_BF16 or SPLIT_FP16).
+SplitPipe split_pipe_layout(int algo, int param, int64_t M, int64_t K, int64_t N,
+                            int64_t panel_rows);
+unsigned long long split_pipe_gen();
+cudaError_t split_pipe_b(const SplitPipe &p, const Gemm &g, void *ws, unsigned long long gen,
+                         cudaStream_t s);
+// g: the panel's rows of A and C (g.M = its row count), all of B.
+cudaError_t split_pipe_panel(const SplitPipe &p, int panel, const Gemm &g, void *ws,
+                             unsigned long long gen, cudaStream_t s);
 // float32 from scaled float16 planes (3 products); `flush` = K slabs per
 // TMEM accumulation chain (1, 2, 4, 8; 0 = default).
 cudaError_t launch_split_f16(const Gemm &g, int flush, void *ws, size_t ws_bytes,
