@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip the side workloads")
-    ap.add_argument("--only", choices=["f64", "int", "grouped", "plain"],
+    ap.add_argument("--only", choices=["f64", "int", "grouped", "plain", "splitvar"],
                     help="run one side workload alone (for profiling) and print it")
     return ap.parse_args()
 
@@ -274,6 +274,18 @@ def main():
             part = int_workload(nc, torch, synth, dev)
         elif args.only == "grouped":
             part = grouped_workload(nc, torch, oracle, dev)
+        elif args.only == "splitvar":
+            # the bfloat16-plane variants, two calls each (3 then 6 passes)
+            a = torch.from_numpy(synth.normal(SEED, 3, (M, K), np.float32)).to(dev)
+            b = torch.from_numpy(synth.normal(SEED, 4, (K, N), np.float32)).to(dev)
+            c = torch.empty((M, N), device=dev)
+            part = {}
+            for passes in (3, 6):
+                ws = torch.empty(nc.workspace_size("float32", nc.ALGO_SPLIT_BF16, passes, M, K, N),
+                                 dtype=torch.uint8, device=dev)
+                ms = time_gemm(nc, torch, a, b, c, nc.ALGO_SPLIT_BF16, passes, steps=1, warmup=1,
+                               ws=ws)
+                part[f"bf16_x{passes}"] = {"ms": ms, "tflops": FLOPS / ms / 1e9}
         else:
             a = torch.from_numpy(synth.normal(SEED, 3, (M, K), np.float32)).to(dev)
             b = torch.from_numpy(synth.normal(SEED, 4, (K, N), np.float32)).to(dev)
