@@ -117,3 +117,16 @@ def operands(kind, M, K, N, seed=42, dtype="float32"):
         eb = integers(seed, 12, (K, N), -20, 20, np.int64)
         return ((np.ldexp(a, ea)).astype(dt), (np.ldexp(b, eb)).astype(dt))
     raise ValueError(f"unknown workload kind {kind!r}")
+
+
+def array(kind, shape, seed=42, stream=1, dtype="float32"):
+    """One seeded array of any shape: `uniform` (as in operands) or `normal`
+    (float dtypes), from stream `stream` of `seed`."""
+    dt = np.dtype(dtype)
+    shape = tuple(int(s) for s in shape)
+    if kind == "normal" and dt.kind == "f":
+        return normal(seed, stream, shape, dt)
+    if dt.kind == "f":
+        return uniform(seed, stream, shape, dtype=dt)
+    lo, hi = INT_RANGES[dt.name]
+    return integers(seed, stream, shape, lo, hi, dt)

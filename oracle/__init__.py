@@ -2,11 +2,13 @@
 
 Two checkers live here, both CPU-only:
 
-* ``matmul(a, b, profile)`` — the C restatement in ``numc_oracle.c``
-  (builds on any host; it is what GPU parity tests compare against).
-* ``ref_matmul(a, b)`` — the unmodified numc library compiled from the
-  reference sources (x86-64 hosts with the reference checkout only); used to
-  pin the restatement and to generate the golden fixtures in tests/golden/.
+* ``matmul(a, b, profile)`` and ``dot(a, b)`` — the C restatements in
+  ``numc_oracle.c`` and ``numc_oracle_dot.c`` (build on any host; they are
+  what GPU parity tests compare against).
+* ``ref_matmul(a, b)`` and ``ref_dot(a, b, perms)`` — the unmodified numc
+  library compiled from the reference sources (x86-64 hosts with the
+  reference checkout only); used to pin the restatements and to generate the
+  golden fixtures in tests/golden/.
 
 The product library never imports this package.
 """
@@ -24,7 +26,8 @@ DTYPE_CODE = {name: i for i, name in enumerate(DTYPES)}
 
 PROFILE_X86_AVX2 = 0
 PROFILE_ARM_NEON = 1
-PROFILE_WRAP = 2
+PROFILE_WRAP = 2          # numc_matmul_naive (floats: unfused chains)
+PROFILE_X86_PACKED = 3    # numc's x86 packed kernels called directly (numc_dot)
 
 _lib = None
 _ref = None
@@ -44,6 +47,9 @@ def _load():
         lib.oracle_dot2_f64.argtypes = [vp, vp, i64, i64, vp, vp, i64, vp, vp]
         lib.oracle_dot_f32_ref.argtypes = [vp, vp, i64, i64, vp, vp, i64, vp]
         lib.oracle_num_threads.restype = ctypes.c_int
+        ci = ctypes.c_int
+        lib.oracle_dot.argtypes = [ci, vp, ci, vp, vp, ci, vp, ci, vp, vp, ci, vp, ci, vp, vp]
+        lib.oracle_dot.restype = ci
         _lib = lib
     return _lib
 
@@ -99,6 +105,45 @@ def dot_f32_ref(a, b, rows, cols):
     return out
 
 
+def dot_shape(ashape, bshape):
+    """numc_dot's output shape (numpy.dot's rule)."""
+    if len(ashape) == 0:
+        return tuple(bshape)
+    if len(bshape) == 0:
+        return tuple(ashape)
+    if len(ashape) == 1 and len(bshape) == 1:
+        return (1,)
+    return tuple(ashape[:-1]) + tuple(bshape[:-2]) + ((bshape[-1],) if len(bshape) > 1 else ())
+
+
+def _estrides(x):
+    return [s // x.itemsize for s in x.strides]
+
+
+def dot(a, b, out=None):
+    """numc's result of numc_dot(a, b, out) for numpy arrays (any strides).
+
+    `out` may be given (a writable view with the output shape) to exercise
+    strided outputs; it is returned."""
+    lib = _load()
+    assert a.dtype == b.dtype
+    if out is None:
+        out = np.zeros(dot_shape(a.shape, b.shape), dtype=a.dtype)
+    i64 = ctypes.c_int64
+
+    def arr(vals):
+        return (i64 * max(1, len(vals)))(*vals)
+    ac = int(a.ndim == 1 and a.strides[0] == a.itemsize)
+    bc = int(b.ndim == 1 and b.strides[0] == b.itemsize)
+    rc = lib.oracle_dot(DTYPE_CODE[a.dtype.name],
+                        a.ctypes.data, a.ndim, arr(a.shape), arr(_estrides(a)), ac,
+                        b.ctypes.data, b.ndim, arr(b.shape), arr(_estrides(b)), bc,
+                        out.ctypes.data, out.ndim, arr(out.shape), arr(_estrides(out)))
+    if rc != 0:
+        raise ValueError(f"oracle_dot: unsupported operands (code {rc})")
+    return out
+
+
 # -- the compiled reference ------------------------------------------------
 
 def reference_available():
@@ -125,6 +170,8 @@ def _load_ref():
         lib.numc_matmul.restype = ctypes.c_int
         lib.numc_matmul_naive.argtypes = [vp, vp, vp]
         lib.numc_matmul_naive.restype = ctypes.c_int
+        lib.numc_dot.argtypes = [vp, vp, vp]
+        lib.numc_dot.restype = ctypes.c_int
         _ref = lib
     return _ref
 
@@ -158,5 +205,49 @@ def ref_matmul(a, b, naive=False):
         out = np.empty((M, N), dtype=a.dtype)
         ctypes.memmove(out.ctypes.data, lib.numc_array_data(pc), out.nbytes)
         return out
+    finally:
+        lib.numc_ctx_free(ctx)
+
+
+def ref_dot(a, b, perm_a=None, perm_b=None, perm_out=None):
+    """numc's own numc_dot(a, b, out).  Each operand (and out) is created in
+    numc as a contiguous array holding x.transpose(inverse(perm)) and then
+    viewed with numc_array_transpose(perm), so a perm other than the identity
+    gives numc a strided, non-contiguous view equal to x."""
+    lib = _load_ref()
+    code = DTYPE_CODE[a.dtype.name]
+    oshape = dot_shape(a.shape, b.shape)
+    ctx = lib.numc_ctx_create()
+    try:
+        def make(x_shape, perm, src=None):
+            nd = len(x_shape)
+            perm = list(range(nd)) if perm is None else list(perm)
+            inv = np.argsort(perm)
+            base_shape = [x_shape[i] for i in inv]   # x = base.transpose(perm)
+            sh = (ctypes.c_size_t * max(1, nd))(*base_shape)
+            arr = lib.numc_array_create(ctx, sh, nd, code)
+            if not arr:
+                raise MemoryError("numc_array_create failed")
+            if src is not None:
+                base = np.ascontiguousarray(np.asarray(src).transpose(inv))
+                lib.numc_array_write(arr, base.ctypes.data)
+            else:
+                z = np.zeros(base_shape, dtype=a.dtype)
+                lib.numc_array_write(arr, z.ctypes.data)
+            if perm != list(range(nd)):
+                ax = (ctypes.c_size_t * nd)(*perm)
+                if lib.numc_array_transpose(arr, ax) != 0:
+                    raise RuntimeError("numc_array_transpose failed")
+            return arr, base_shape, inv
+        pa, _, _ = make(a.shape, perm_a, a)
+        pb, _, _ = make(b.shape, perm_b, b)
+        po, obase, oinv = make(oshape, perm_out)
+        rc = lib.numc_dot(pa, pb, po)
+        if rc != 0:
+            raise RuntimeError(f"numc_dot returned {rc}")
+        base = np.empty(obase, dtype=a.dtype)
+        ctypes.memmove(base.ctypes.data, lib.numc_array_data(po), base.nbytes)
+        perm = list(range(len(oshape))) if perm_out is None else list(perm_out)
+        return np.ascontiguousarray(base.transpose(perm)).reshape(oshape)
     finally:
         lib.numc_ctx_free(ctx)

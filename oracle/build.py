@@ -22,7 +22,8 @@ REF_SRC = "/root/reference"
 def build_oracle(force=False):
     src = os.path.join(HERE, "numc_oracle.c")
     micro = os.path.join(HERE, "numc_oracle_micro.c")
-    deps = [src, micro, os.path.join(HERE, "numc_oracle_micro.h")]
+    dot = os.path.join(HERE, "numc_oracle_dot.c")
+    deps = [src, micro, dot, os.path.join(HERE, "numc_oracle_micro.h")]
     if (not force and os.path.exists(ORACLE_SO)
             and os.path.getmtime(ORACLE_SO) >= max(os.path.getmtime(d) for d in deps)):
         return ORACLE_SO
@@ -37,7 +38,7 @@ def build_oracle(force=False):
                            "-o", micro_o])
     tmp = ORACLE_SO + ".tmp"
     subprocess.check_call(["gcc", *flags, "-fopenmp", "-shared",
-                           "-ffp-contract=off", src, micro_o, "-o", tmp, "-lm"])
+                           "-ffp-contract=off", src, dot, micro_o, "-o", tmp, "-lm"])
     os.replace(tmp, ORACLE_SO)
     return ORACLE_SO
 

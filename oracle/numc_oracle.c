@@ -45,6 +45,16 @@
  *
  *    ORACLE_I8_WRAP (numc_matmul_naive, src/matmul/kernel.h:35-62): the sum
  *      truncated to 8 bits.
+ *
+ *    ORACLE_X86_PACKED: numc's x86 packed kernels called directly, as
+ *      numc_dot's GEMM branch does (src/reduction/dot.c:392-398 through
+ *      the gemm_*_avx2 wrappers at dot.c:159-231): the x86 rules without the
+ *      192^3 unpacked threshold, for every dtype.
+ *
+ *  - Naive float32/float64 (profile ORACLE_I8_WRAP, numc_matmul_naive,
+ *    src/matmul/kernel.h:18-33, and numc_dot's strided kernels,
+ *    src/reduction/dot.c:42-72): per output `acc += a * b` in k order from 0
+ *    in ISO C without contraction — each product rounded, then each sum.
  */
 #include <math.h>
 #include <stdint.h>
@@ -60,7 +70,8 @@ enum {
 /* Arithmetic profiles: which numc build's results to reproduce.  They
  * differ for int8/uint8 (store rules) and, in the last bits, for the
  * remainder tiles of float32/float64. */
-enum { ORACLE_I8_X86_AVX2 = 0, ORACLE_I8_ARM_NEON = 1, ORACLE_I8_WRAP = 2 };
+enum { ORACLE_I8_X86_AVX2 = 0, ORACLE_I8_ARM_NEON = 1, ORACLE_I8_WRAP = 2,
+       ORACLE_X86_PACKED = 3 };
 
 static const size_t k_elem[] = {1, 2, 4, 8, 1, 2, 4, 8, 4, 8};
 
@@ -194,8 +205,8 @@ DEFINE_FLOAT_KERNEL(kern_f64, double, oracle_micro_f64, ORACLE_MR, ORACLE_NR_F64
     return d;                                                                 \
   }                                                                           \
   static void NAME(const T *a, const T *b, T *c, int64_t M, int64_t K,       \
-                   int64_t N) {                                               \
-    int packed = (uint64_t)M * (uint64_t)K * (uint64_t)N > (THR);             \
+                   int64_t N, int force_packed) {                             \
+    int packed = force_packed || (uint64_t)M * (uint64_t)K * (uint64_t)N > (THR); \
     if (packed) {                                                             \
       /* Rows of a remainder row tile: every column is a remainder output;   \
        * computed a whole row at a time (same arithmetic per output, B read  \
@@ -251,6 +262,26 @@ DEFINE_FLOAT_KERNEL(kern_f64, double, oracle_micro_f64, ORACLE_MR, ORACLE_NR_F64
 
 DEFINE_FLOAT_EDGES(edges_f32, float, fmaf, 96ULL * 96 * 96, 16, 8, 144)
 DEFINE_FLOAT_EDGES(edges_f64, double, fma, 48ULL * 48 * 48, 8, 4, 72)
+
+/* Naive float kernels: per output `acc = acc + a * b` from 0 in k order,
+ * product and sum each rounded (this file is built without contraction). */
+#define DEFINE_NAIVE_FLOAT(NAME, T)                                           \
+  static void NAME(const T *a, const T *b, T *c, int64_t M, int64_t K,       \
+                   int64_t N) {                                               \
+    _Pragma("omp parallel for schedule(static)")                              \
+    for (int64_t i = 0; i < M; i++)                                           \
+      for (int64_t j = 0; j < N; j++) {                                       \
+        T acc = (T)0;                                                         \
+        for (int64_t k = 0; k < K; k++) {                                     \
+          const T p = a[i * K + k] * b[k * N + j];                            \
+          acc = acc + p;                                                      \
+        }                                                                     \
+        c[i * N + j] = acc;                                                   \
+      }                                                                       \
+  }
+
+DEFINE_NAIVE_FLOAT(naive_f32, float)
+DEFINE_NAIVE_FLOAT(naive_f64, double)
 
 /* Wrapping integer kernels: T is the storage type, U the unsigned type of
  * the same width in which every product and sum wraps. */
@@ -330,8 +361,10 @@ static void kern_8bit(const void *av, const void *bv, void *cv, int64_t M,
                       int64_t K, int64_t N, int is_signed, int profile) {
   const int8_t *as = (const int8_t *)av, *bs = (const int8_t *)bv;
   const uint8_t *au = (const uint8_t *)av, *bu = (const uint8_t *)bv;
-  int x86_packed = profile == ORACLE_I8_X86_AVX2 &&
-                   (uint64_t)M * (uint64_t)K * (uint64_t)N > 192ULL * 192 * 192;
+  int x86_packed = profile == ORACLE_X86_PACKED ||
+                   (profile == ORACLE_I8_X86_AVX2 &&
+                    (uint64_t)M * (uint64_t)K * (uint64_t)N > 192ULL * 192 * 192);
+  if (profile == ORACLE_X86_PACKED) profile = ORACLE_I8_X86_AVX2;
   /* x86 packed blocks K by 512; everything else sums all K in one block. */
   int64_t kblk = x86_packed ? 512 : (K > 0 ? K : 1);
 #pragma omp parallel for schedule(dynamic, 1)
@@ -423,14 +456,23 @@ int oracle_matmul(int dtype, const void *a, const void *b, void *out,
     free(ad); free(bd); free(cd);
     return -1;
   }
+  const int x86 = profile == ORACLE_I8_X86_AVX2 || profile == ORACLE_X86_PACKED;
   switch (dtype) {
   case DT_F32:
+    if (profile == ORACLE_I8_WRAP) {
+      naive_f32(ad, bd, cd, M, K, N);
+      break;
+    }
     kern_f32(ad, bd, cd, M, K, N);
-    if (profile == ORACLE_I8_X86_AVX2) edges_f32(ad, bd, cd, M, K, N);
+    if (x86) edges_f32(ad, bd, cd, M, K, N, profile == ORACLE_X86_PACKED);
     break;
   case DT_F64:
+    if (profile == ORACLE_I8_WRAP) {
+      naive_f64(ad, bd, cd, M, K, N);
+      break;
+    }
     kern_f64(ad, bd, cd, M, K, N);
-    if (profile == ORACLE_I8_X86_AVX2) edges_f64(ad, bd, cd, M, K, N);
+    if (x86) edges_f64(ad, bd, cd, M, K, N, profile == ORACLE_X86_PACKED);
     break;
   case DT_I16: kern_i16(ad, bd, cd, M, K, N); break;
   case DT_U16: kern_u16(ad, bd, cd, M, K, N); break;

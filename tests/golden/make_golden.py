@@ -1,4 +1,5 @@
-"""Generate golden fixtures from numc's own numc_matmul.
+"""Generate golden fixtures from numc's own numc_matmul, numc_matmul_naive
+and numc_dot.
 
 Runs the unmodified numc library (compiled from the reference sources by
 oracle/Makefile.ref, x86-64 AVX2 build) on seeded inputs from
@@ -61,6 +62,54 @@ RANDOM_CASES = [
 ]
 
 
+# numc_matmul_naive on floats (the unfused k-order chains; integers wrap and
+# are covered by the int8 wrap profile tests).
+NAIVE_CASES = [(dt, kind, shape) for dt in ("float32", "float64")
+               for kind, shape in (("uniform", (5, 3, 4)), ("normal", (33, 70, 17)),
+                                   ("normal", (97, 300, 103)))]
+
+# numc_dot cases (a shape, b shape, a/b/out axis permutations: a permutation
+# other than the identity hands numc a transposed, non-contiguous view).
+DOT_SHAPES = [
+    ("0d_x_2d", (), (7, 5), None, None, None),
+    ("2d_x_0d", (6, 9), (), None, None, None),
+    ("1d_x_1d_short", (37,), (37,), None, None, None),
+    ("1d_x_1d_blocks", (1000,), (1000,), None, None, None),
+    ("1d_x_1d_two_chunks", (150000,), (150000,), None, None, None),
+    ("2d_x_1d", (70, 130), (130,), None, None, None),
+    ("1d_x_2d", (130,), (130, 45), None, None, None),
+    ("2d_x_2d_small", (5, 7, ), (7, 3), None, None, None),
+    ("2d_x_2d", (97, 300, ), (300, 103), None, None, None),
+    ("2d_x_2d_bT", (64, 200), (200, 50), None, (1, 0), None),
+    ("2d_x_2d_aT", (64, 200), (200, 50), (1, 0), None, None),
+    ("2d_x_2d_outT", (40, 120), (120, 33), None, None, (1, 0)),
+    ("2d_x_3d_batched", (20, 30), (4, 30, 17), None, None, None),
+    ("2d_x_3d_batched_bT", (20, 30), (3, 30, 17), None, (0, 2, 1), None),
+]
+DOT_DTYPES = ["int8", "uint8", "int16", "int32", "uint32", "int64", "float32", "float64"]
+
+
+def record_op(cases, arrays, name, out, extra):
+    entry = {"name": name, **extra,
+             "sha256": hashlib.sha256(np.ascontiguousarray(out).tobytes()).hexdigest()}
+    if out.nbytes <= FULL_LIMIT:
+        arrays[name] = out
+        entry["stored"] = "full"
+    else:
+        rng = np.random.default_rng(7)
+        idx = np.sort(rng.choice(out.size, SAMPLE, replace=False))
+        arrays[name + "__idx"] = idx.astype(np.int64)
+        arrays[name] = out.reshape(-1)[idx]
+        entry["stored"] = "sample"
+    cases.append(entry)
+
+
+def dot_operands(dt, ashape, bshape, seed):
+    kind = "normal" if np.dtype(dt).kind == "f" else "uniform"
+    return (synth.array(kind, ashape, seed=seed, stream=21, dtype=dt),
+            synth.array(kind, bshape, seed=seed, stream=22, dtype=dt))
+
+
 def record(cases, arrays, name, dt, kind, shape, seed=42):
     M, K, N = shape
     a, b = synth.operands(kind, M, K, N, seed=seed, dtype=dt)
@@ -92,9 +141,27 @@ def main():
         name = f"{kind}_{dt}_{'x'.join(map(str, shape))}"
         record(cases, arrays, name, dt, kind, shape)
         print(name, flush=True)
+    naive_cases = []
+    for dt, kind, shape in NAIVE_CASES:
+        M, K, N = shape
+        name = f"naive_{kind}_{dt}_{M}x{K}x{N}"
+        a, b = synth.operands(kind, M, K, N, seed=42, dtype=dt)
+        record_op(naive_cases, arrays, name, oracle.ref_matmul(a, b, naive=True),
+                  {"dtype": dt, "kind": kind, "shape": [M, K, N], "seed": 42})
+    dot_cases = []
+    for dt in DOT_DTYPES:
+        for tag, ashape, bshape, pa, pb, po in DOT_SHAPES:
+            name = f"dot_{tag}_{dt}"
+            a, b = dot_operands(dt, ashape, bshape, 42)
+            out = oracle.ref_dot(a, b, perm_a=pa, perm_b=pb, perm_out=po)
+            record_op(dot_cases, arrays, name, out,
+                      {"dtype": dt, "a_shape": list(ashape), "b_shape": list(bshape),
+                       "perm_a": pa, "perm_b": pb, "perm_out": po, "seed": 42})
     with open(os.path.join(HERE, "golden.json"), "w") as f:
-        json.dump({"generator": "numc_matmul, x86-64 AVX2 build",
-                   "cases": cases}, f, indent=1)
+        json.dump({"generator": "numc_matmul, numc_matmul_naive and numc_dot, "
+                                "x86-64 AVX2 build",
+                   "cases": cases, "naive_cases": naive_cases, "dot_cases": dot_cases},
+                  f, indent=1)
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
 
 

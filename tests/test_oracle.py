@@ -86,3 +86,38 @@ def test_oracle_matches_compiled_reference(dt):
                         ((300, 90, 260), "smallint")]:
         a, b = synth.operands(kind, *shape, seed=11, dtype=dt)
         np.testing.assert_array_equal(oracle.matmul(a, b), oracle.ref_matmul(a, b))
+
+
+# ---- numc_matmul_naive (floats) and numc_dot -------------------------------
+
+def view_with_perm(x, perm):
+    """x as a view of a contiguous array holding x.transpose(inverse(perm)):
+    the same values with the strides numc's transposed operand has."""
+    if perm is None:
+        return np.array(x, order="C")      # keeps 0-D arrays 0-D
+    inv = np.argsort(perm)
+    return np.ascontiguousarray(x.transpose(inv)).transpose(perm)
+
+
+def dot_case_arrays(case):
+    """(a, b, out) numpy views of a golden numc_dot case (out zero-filled)."""
+    from golden.make_golden import dot_operands
+    a, b = dot_operands(case["dtype"], case["a_shape"], case["b_shape"], case["seed"])
+    a, b = view_with_perm(a, case["perm_a"]), view_with_perm(b, case["perm_b"])
+    out = view_with_perm(np.zeros(oracle.dot_shape(a.shape, b.shape), dtype=a.dtype),
+                         case["perm_out"])
+    return a, b, out
+
+
+@pytest.mark.parametrize("case", GOLDEN["naive_cases"], ids=lambda c: c["name"])
+def test_oracle_naive_float_matches_numc(case):
+    M, K, N = case["shape"]
+    a, b = synth.operands(case["kind"], M, K, N, seed=case["seed"], dtype=case["dtype"])
+    _check(case, oracle.matmul(a, b, oracle.PROFILE_WRAP))
+
+
+@pytest.mark.parametrize("case", GOLDEN["dot_cases"], ids=lambda c: c["name"])
+def test_oracle_dot_matches_numc(case):
+    a, b, out = dot_case_arrays(case)
+    got = oracle.dot(a, b, out)
+    _check(case, np.ascontiguousarray(got).reshape(oracle.dot_shape(a.shape, b.shape)))
