@@ -1,4 +1,4 @@
-/* Matrix multiplication — numc's matmul entry points
+/* Matrix multiplication — numc's matmul and dot entry points
  * (include/numc/math.h:573-604 of numc), served by the CUDA backend. */
 #ifndef NUMC_MATH_H
 #define NUMC_MATH_H
@@ -21,11 +21,26 @@ extern "C" {
 NUMC_API int numc_matmul(const NumcArray *a, const NumcArray *b,
                          NumcArray *out);
 
-/* Wrapping reference product (numc's numc_matmul_naive, matmul.c:333-343):
- * every dtype accumulates in its storage width, so int8/uint8 results are
- * the sum truncated to 8 bits. */
+/* Reference product (numc's numc_matmul_naive, matmul.c:333-343): integer
+ * dtypes accumulate in their storage width (int8/uint8 results are the sum
+ * truncated to 8 bits), floats as `acc += a * b` with every product and sum
+ * rounded (no fused multiply-add), in k order. */
 NUMC_API int numc_matmul_naive(const NumcArray *a, const NumcArray *b,
                                NumcArray *out);
+
+/* numc_dot (numc's math.h:593, src/reduction/dot.c:442-447), numpy.dot's
+ * shape rules: a or b 0-D multiplies by the scalar; both 1-D give the inner
+ * product (out 0-D or one element); otherwise a's last axis contracts with
+ * b's second-to-last (its only axis if 1-D) and out has shape
+ * a.shape[:-1] + b.shape[:-2] + b.shape[-1:].  Same validation and error
+ * codes as numc, same arithmetic per branch: the GEMM branch (b unbatched,
+ * unit column strides of b and out) is numc_matmul's without the small-size
+ * int8/uint8 threshold; strided and batched operands use numc's naive sums
+ * (floats unfused); 1-D floats follow numc's SIMD lane order.  Deviations:
+ * for a of 3+ dims numc's row stride reads past the array, here rows step
+ * through a's (and out's) flattenable leading axes (NUMC_ERR_SHAPE if they
+ * do not flatten); a and b both above 2-D return NUMC_ERR_SHAPE. */
+NUMC_API int numc_dot(const NumcArray *a, const NumcArray *b, NumcArray *out);
 
 #ifdef __cplusplus
 }

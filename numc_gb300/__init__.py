@@ -84,6 +84,7 @@ SIGNATURES = [
     ("numc_array_data", _VP, [_VP]),
     ("numc_matmul", _I, [_VP, _VP, _VP]),
     ("numc_matmul_naive", _I, [_VP, _VP, _VP]),
+    ("numc_dot", _I, [_VP, _VP, _VP]),
     ("numc_set_error", _I, [_I, ctypes.c_char_p]),
     ("numc_get_error", _Err, []),
     ("numc_log_error", None, [_VP]),
@@ -212,7 +213,7 @@ class Ctx:
         return self._make(lib().numc_array_fill, shape, dtype, v.ctypes.data)
 
     def from_numpy(self, x):
-        x = np.ascontiguousarray(x)
+        x = np.array(x, order="C")      # a C-contiguous copy; 0-D stays 0-D
         arr = self.create(x.shape, x.dtype)
         arr.write(x)
         return arr
@@ -314,6 +315,12 @@ def matmul(a, b, out):
 
 def matmul_naive(a, b, out):
     return check(lib().numc_matmul_naive(a.ptr, b.ptr, out.ptr))
+
+
+def dot(a, b, out):
+    """numc_dot(a, b, out); raises NumcError on a nonzero return."""
+    return check(lib().numc_dot(a.ptr if a else None, b.ptr if b else None,
+                                out.ptr if out else None))
 
 
 def workspace_size(dtype, algo, param, M, K, N):

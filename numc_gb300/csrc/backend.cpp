@@ -138,7 +138,10 @@ struct Plan {
   int param;    // rule8 for int8/uint8, slices for Ozaki
 };
 
-int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Plan *p) {
+// `packed_only`: numc's packed kernels are called directly (numc_dot), so
+// the x86 int8/uint8 rule has no small-size unpacked branch.
+int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Plan *p,
+            bool packed_only = false) {
   ensure_algos();
   if (algo == NUMC_CUDA_ALGO_DEFAULT) {
     algo = g_algo[dt].algo.load();
@@ -200,8 +203,9 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
     else if (profile == NUMC_INT8_X86_AVX2)
       // numc's x86 build sends M*K*N <= 192^3 to its unpacked kernels, which
       // truncate (src/matmul/matmul.c:241-256, gemmsup_avx2.h:744-756).
-      p->param = ((uint64_t)M * K * N <= 192ull * 192 * 192) ? numc_k::kRuleWrap
-                                                             : numc_k::kRuleX86Packed;
+      p->param = (!packed_only && (uint64_t)M * K * N <= 192ull * 192 * 192)
+                     ? numc_k::kRuleWrap
+                     : numc_k::kRuleX86Packed;
     else return NUMC_SET_ERROR(NUMC_ERR_VALUE, "unknown int8 profile %d", profile);
   }
   return 0;
@@ -518,10 +522,195 @@ extern "C" int numc_matmul(const NumcArray *a, const NumcArray *b, NumcArray *ou
 }
 
 extern "C" int numc_matmul_naive(const NumcArray *a, const NumcArray *b, NumcArray *out) {
-  // numc's naive kernels accumulate in the storage type (kernel.h:18-62).
-  int param = (a && (a->dtype == NUMC_DTYPE_INT8 || a->dtype == NUMC_DTYPE_UINT8))
-                  ? NUMC_INT8_WRAP : 0;
+  // numc's naive kernels (kernel.h:18-62): integers accumulate in the
+  // storage type (8-bit through 32 bits, truncated), floats `acc += a * b`
+  // without contraction.
+  int param = 0;
+  if (a && (a->dtype == NUMC_DTYPE_INT8 || a->dtype == NUMC_DTYPE_UINT8)) param = NUMC_INT8_WRAP;
+  if (a && (a->dtype == NUMC_DTYPE_FLOAT32 || a->dtype == NUMC_DTYPE_FLOAT64))
+    param = numc_k::kFloatNaive;
   return matmul_impl(a, b, out, NUMC_CUDA_ALGO_SIMT, param);
+}
+
+namespace {
+
+// ---- numc_dot (src/reduction/dot.c of numc) -----------------------------------
+
+// numc's validation (src/reduction/dispatch.h:199-281): same checks, codes
+// and messages.
+int check_dot(const NumcArray *a, const NumcArray *b, const NumcArray *out) {
+  if (!a || !b || !out)
+    return NUMC_SET_ERROR(NUMC_ERR_NULL, "dot: NULL pointer (a=%p b=%p out=%p)",
+                          (const void *)a, (const void *)b, (const void *)out);
+  if (a->dtype != b->dtype || a->dtype != out->dtype)
+    return NUMC_SET_ERROR(NUMC_ERR_TYPE, "dot: dtype mismatch (a=%d b=%d out=%d)", a->dtype,
+                          b->dtype, out->dtype);
+  if (a->dim == 0 || b->dim == 0) {
+    const NumcArray *other = a->dim == 0 ? b : a;
+    if (out->dim != other->dim)
+      return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "dot: output ndim mismatch (out.dim=%zu other.dim=%zu)",
+                            out->dim, other->dim);
+    for (size_t i = 0; i < out->dim; i++)
+      if (out->shape[i] != other->shape[i])
+        return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "dot: shape mismatch at axis %zu", i);
+    return 0;
+  }
+  const size_t a_last = a->dim - 1, b_red = b->dim == 1 ? 0 : b->dim - 2;
+  if (a->shape[a_last] != b->shape[b_red])
+    return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "dot: axis mismatch (a.shape[%zu]=%zu b.shape[%zu]=%zu)",
+                          a_last, a->shape[a_last], b_red, b->shape[b_red]);
+  const size_t expected = (a->dim - 1) + (b->dim > 1 ? b->dim - 1 : 0);
+  const bool scalar_out =
+      (expected == 0 && out->dim == 1 && out->size == 1) || (expected == 0 && out->dim == 0);
+  if (!scalar_out && out->dim != expected)
+    return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "dot: output ndim mismatch (out.dim=%zu expected=%zu)",
+                          out->dim, expected);
+  if (!scalar_out) {
+    size_t o = 0;
+    bool ok = true;
+    for (size_t i = 0; i + 1 < a->dim; i++) ok &= out->shape[o++] == a->shape[i];
+    if (b->dim > 1) {
+      for (size_t i = 0; i + 2 < b->dim; i++) ok &= out->shape[o++] == b->shape[i];
+      ok &= out->shape[o++] == b->shape[b->dim - 1];
+    }
+    if (!ok) return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "dot: output shape mismatch");
+  }
+  return 0;
+}
+
+// Axes [0, upto) of x collapse into one row axis (unit axes ignored).
+bool flattenable(const NumcArray *x, size_t upto) {
+  for (size_t d = 0; d + 1 < upto; d++)
+    if (x->shape[d + 1] != 1 && x->strides[d] != x->strides[d + 1] * x->shape[d + 1]) return false;
+  return true;
+}
+
+int dot_impl(const NumcArray *a, const NumcArray *b, NumcArray *out) {
+  int err = check_dot(a, b, out);
+  if (err) return err;
+  if (out->size == 0) return 0;
+  const NumcDType dt = a->dtype;
+  const int64_t es = (int64_t)a->elem_size;
+  enum { kScalar, kVector, kMatrix } kind =
+      (a->dim == 0 || b->dim == 0) ? kScalar : (a->dim == 1 && b->dim == 1) ? kVector : kMatrix;
+
+  // numc's N-D case (dot.c:367-420), element strides.
+  int64_t M = 0, K = 0, N = 0, P = 1, rsa = 0, csa = 0, rsb = 0, csb = 0, rso = 0, cso = 0;
+  bool gemm_branch = false;
+  Plan plan{NUMC_CUDA_ALGO_SIMT, 0};
+  size_t ws_bytes = 0;
+  if (kind == kMatrix) {
+    if (a->dim >= 3 && b->dim >= 3)
+      return NUMC_SET_ERROR(NUMC_ERR_SHAPE,
+                            "dot: a (%zu-D) and b (%zu-D) both above 2-D are not supported",
+                            a->dim, b->dim);
+    if (a->dim >= 3 && (!flattenable(a, a->dim - 1) || !flattenable(out, a->dim - 1)))
+      return NUMC_SET_ERROR(NUMC_ERR_SHAPE,
+                            "dot: the leading axes of a (and of out) must collapse into rows");
+    K = (int64_t)a->shape[a->dim - 1];
+    N = b->dim == 1 ? 1 : (int64_t)b->shape[b->dim - 1];
+    M = 1;
+    for (size_t d = 0; d + 1 < a->dim; d++) M *= (int64_t)a->shape[d];
+    for (size_t d = 0; d + 2 < b->dim; d++) P *= (int64_t)b->shape[d];
+    // numc's row stride is strides[0]; for a of 3+ dims that walks past
+    // the array, so rows step by the second-to-last axis there.
+    rsa = (int64_t)a->strides[a->dim >= 3 ? a->dim - 2 : 0] / es;
+    csa = (int64_t)a->strides[a->dim - 1] / es;
+    rsb = (int64_t)(b->dim > 1 ? b->strides[b->dim - 2] : b->strides[0]) / es;
+    csb = (int64_t)b->strides[b->dim - 1] / es;
+    rso = (int64_t)out->strides[a->dim >= 3 ? a->dim - 2 : 0] / es;
+    cso = (int64_t)out->strides[out->dim - 1] / es;
+    gemm_branch = P == 1 && csb == 1 && cso == 1;
+    if (gemm_branch) {
+      if ((err = resolve(dt, NUMC_CUDA_ALGO_DEFAULT, -1, M, K, N, &plan, true))) return err;
+      ws_bytes = plan_workspace(plan, M, K, N);
+    }
+  } else if (kind == kVector) {
+    ws_bytes = numc_k::dot1d_scratch_bytes();
+  }
+
+  NumcCtx *ctx = out->ctx;
+  cudaStream_t s;
+  if ((err = ctx_stream(ctx, &s))) return err;
+  const bool ra = is_resident(a), rb = is_resident(b), ro = is_resident(out);
+  const size_t sa = array_span_bytes(a), sb = array_span_bytes(b), so = array_span_bytes(out);
+  const size_t off_b = align_up(ra ? 0 : sa, 256);
+  const size_t off_o = off_b + align_up(rb ? 0 : sb, 256);
+  const size_t off_w = off_o + align_up(ro ? 0 : so, 256);
+  char *scratch = nullptr;
+  if ((err = ctx_scratch(ctx, off_w + ws_bytes + 256, s, &scratch))) return err;
+  const char *da = ra ? a->dev_base : scratch;
+  const char *db = rb ? b->dev_base : scratch + off_b;
+  char *dout = ro ? out->dev_base : scratch + off_o;
+  char *ws = scratch + off_w;
+  if (!ra && sa) CU(cudaMemcpyAsync((void *)da, a->data, sa, cudaMemcpyHostToDevice, s), "copy a to device");
+  if (!rb && sb) CU(cudaMemcpyAsync((void *)db, b->data, sb, cudaMemcpyHostToDevice, s), "copy b to device");
+  if (!ro && so > out->capacity)
+    CU(cudaMemcpyAsync(dout, out->data, so, cudaMemcpyHostToDevice, s), "copy out to device");
+
+  cudaError_t e = cudaSuccess;
+  if (kind == kScalar) {
+    const NumcArray *other = a->dim == 0 ? b : a;
+    const char *dx = a->dim == 0 ? db : da, *dsc = a->dim == 0 ? da : db;
+    if (other->dim > (size_t)numc_k::kDotMaxDims)
+      return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "dot: %zu dimensions (at most %d)", other->dim,
+                            numc_k::kDotMaxDims);
+    numc_k::DotNd ix;
+    ix.dim = (int)other->dim;
+    for (size_t d = 0; d < other->dim; d++) {
+      ix.shape[d] = (int64_t)other->shape[d];
+      ix.xs[d] = (int64_t)other->strides[d] / es;
+      ix.os[d] = (int64_t)out->strides[d] / es;
+    }
+    e = numc_k::launch_dot_scalar(dt, dx, dsc, dout, ix, s);
+  } else if (kind == kVector) {
+    e = numc_k::launch_dot_1d(dt, da, (int64_t)a->strides[0] / es, db,
+                              (int64_t)b->strides[0] / es, (int64_t)a->shape[0],
+                              a->is_contiguous && b->is_contiguous, dout, ws, s);
+  } else {
+    numc_k::Gemm g;
+    g.a = da; g.b = db; g.c = dout;
+    g.M = M; g.K = K; g.N = N;
+    g.rsa = rsa; g.csa = csa; g.rsb = rsb; g.csb = csb; g.rso = rso; g.cso = cso;
+    // numc's naive kernels (dot.c:42-72): integers truncated (int8/uint8
+    // sums wrap), floats unfused.
+    const int naive = (dt == NUMC_DTYPE_INT8 || dt == NUMC_DTYPE_UINT8) ? numc_k::kRuleWrap
+                      : (dt == NUMC_DTYPE_FLOAT32 || dt == NUMC_DTYPE_FLOAT64) ? numc_k::kFloatNaive
+                                                                                : 0;
+    if (gemm_branch) {
+      if ((err = run_plan(dt, plan, g, ws, ws_bytes, s))) return err;
+    } else if (P == 1) {
+      e = numc_k::launch_simt(dt, g, naive, s);
+    } else {
+      for (int64_t p = 0; p < P && e == cudaSuccess; p++) {
+        numc_k::Gemm gp = g;
+        gp.b = db + (b->dim == 3 ? p * (int64_t)b->strides[0] : p * K * N * es);
+        gp.c = dout + (out->dim == 3 ? p * (int64_t)out->strides[1] : p * N * es);
+        e = numc_k::launch_simt(dt, gp, naive, s);
+      }
+    }
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "dot kernel launch");
+
+  if (ro) {
+    out->residency = kDeviceOnly;
+    if (!ra || !rb) CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  } else {
+    CU(cudaMemcpyAsync(out->data, dout, so, cudaMemcpyDeviceToHost, s), "copy out to host");
+    CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  }
+  if (gemm_branch && plan.algo != NUMC_CUDA_ALGO_SIMT && plan.algo != NUMC_CUDA_ALGO_DMMA) {
+    unsigned st = 0;
+    CU(numc_k::read_and_clear_status(&st, s), "status read");
+    if (st) return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "dot kernel abandoned a bounded wait (code %u)", st);
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int numc_dot(const NumcArray *a, const NumcArray *b, NumcArray *out) {
+  return dot_impl(a, b, out);
 }
 
 extern "C" int numc_matmul_grouped(const NumcArray *const *a, const NumcArray *const *b,

@@ -32,8 +32,12 @@ cudaError_t launch_tile(const Gemm &g, int rule8, cudaStream_t s) {
 
 cudaError_t launch_simt(NumcDType dt, const Gemm &g, int rule8, cudaStream_t s) {
   switch (dt) {
-  case NUMC_DTYPE_FLOAT32: return launch_tile<float, 128, 128, 8, 8, simt::kFloat>(g, 0, s);
-  case NUMC_DTYPE_FLOAT64: return launch_tile<double, 64, 64, 4, 4, simt::kFloat>(g, 0, s);
+  case NUMC_DTYPE_FLOAT32:
+    if (rule8 == kFloatNaive) return launch_tile<float, 128, 128, 8, 8, simt::kFloatUnfused>(g, 0, s);
+    return launch_tile<float, 128, 128, 8, 8, simt::kFloat>(g, 0, s);
+  case NUMC_DTYPE_FLOAT64:
+    if (rule8 == kFloatNaive) return launch_tile<double, 64, 64, 4, 4, simt::kFloatUnfused>(g, 0, s);
+    return launch_tile<double, 64, 64, 4, 4, simt::kFloat>(g, 0, s);
   case NUMC_DTYPE_INT16: return launch_tile<int16_t, 128, 128, 8, 8, simt::kWrapInt>(g, 0, s);
   case NUMC_DTYPE_UINT16: return launch_tile<uint16_t, 128, 128, 8, 8, simt::kWrapInt>(g, 0, s);
   case NUMC_DTYPE_INT32: return launch_tile<int32_t, 128, 128, 8, 8, simt::kWrapInt>(g, 0, s);

@@ -26,8 +26,32 @@ enum Rule8 : int {
   kRuleNeon = 2,      // numc aarch64 NEON path (one block over all K)
 };
 
-// CUDA-core kernels for every dtype.  `rule8` only matters for int8/uint8.
+// float32/float64 SIMT variant: kFloatFma = numc's register tiles (one FMA
+// chain per output), kFloatNaive = numc's naive kernels (product and sum
+// each rounded).
+enum FloatSimt : int { kFloatFma = 0, kFloatNaive = 1 };
+
+// CUDA-core kernels for every dtype.  `rule8` is the Rule8 for int8/uint8,
+// the FloatSimt variant for float32/float64, unused otherwise.
 cudaError_t launch_simt(NumcDType dt, const Gemm &g, int rule8, cudaStream_t s);
+
+// numc_dot's non-GEMM cases (dot_kernels.cu), all on device pointers:
+// out[i] = x[i] * scalar over an N-D strided array (scalar read from
+// device memory, converted through double as numc does)...
+constexpr int kDotMaxDims = 16;
+struct DotNd {
+  int dim;
+  int64_t shape[kDotMaxDims], xs[kDotMaxDims], os[kDotMaxDims];   // element strides
+};
+cudaError_t launch_dot_scalar(NumcDType dt, const void *x, const void *scalar, void *out,
+                              const DotNd &ix, cudaStream_t s);
+// ...and the 1-D inner product a . b -> out[0].  `contiguous` selects numc's
+// SIMD arithmetic (else its strided reduction); `scratch` holds at least
+// dot1d_scratch_bytes() bytes.
+size_t dot1d_scratch_bytes();
+cudaError_t launch_dot_1d(NumcDType dt, const void *a, int64_t sa, const void *b, int64_t sb,
+                          int64_t n, bool contiguous, void *out, void *scratch,
+                          cudaStream_t s);
 // float64 on the mma.sync f64 tensor path.
 cudaError_t launch_dmma(const Gemm &g, cudaStream_t s);
 

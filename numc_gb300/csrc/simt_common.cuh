@@ -31,7 +31,10 @@ namespace simt {
 
 constexpr int kThreads = 256;
 
-enum Kind : int { kFloat = 0, kWrapInt = 1, kByte = 2 };
+// kFloat: one fused multiply-add chain per output (numc's register tiles);
+// kFloatUnfused: `acc = acc + a * b`, product and sum each rounded (numc's
+// naive kernels, compiled without contraction).
+enum Kind : int { kFloat = 0, kWrapInt = 1, kByte = 2, kFloatUnfused = 3 };
 
 // ---- numc's int8/uint8 store rules ---------------------------------------
 
@@ -100,6 +103,13 @@ template <> __device__ __forceinline__ float madd(float a, float b, float c) {
 }
 template <> __device__ __forceinline__ double madd(double a, double b, double c) {
   return __fma_rn(a, b, c);
+}
+// The _rn intrinsics are never contracted into a fused multiply-add.
+__device__ __forceinline__ float madd_unfused(float a, float b, float c) {
+  return __fadd_rn(c, __fmul_rn(a, b));
+}
+__device__ __forceinline__ double madd_unfused(double a, double b, double c) {
+  return __dadd_rn(c, __dmul_rn(a, b));
 }
 
 // Widen one element to the accumulation type: sign-extend signed integers,
@@ -209,7 +219,10 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
 #pragma unroll
       for (int i = 0; i < TM; i++)
 #pragma unroll
-        for (int j = 0; j < TN; j++) acc[i][j] = madd<Acc>(av[i], bv[j], acc[i][j]);
+        for (int j = 0; j < TN; j++) {
+          if constexpr (KIND == kFloatUnfused) acc[i][j] = madd_unfused(av[i], bv[j], acc[i][j]);
+          else acc[i][j] = madd<Acc>(av[i], bv[j], acc[i][j]);
+        }
     }
     if constexpr (KIND == kByte) {
       const int64_t kend = (t + 1) * BK;

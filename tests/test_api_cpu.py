@@ -101,6 +101,30 @@ def test_matmul_validation_codes():
         assert nc.last_error()[1]
 
 
+def _dot_rc(a, b, out):
+    return nc.lib().numc_dot(a.ptr if a else None, b.ptr if b else None,
+                             out.ptr if out else None)
+
+
+def test_dot_validation_codes():
+    # numc's _check_dot (src/reduction/dispatch.h:199-281), before any GPU work
+    with nc.Ctx() as ctx:
+        f = np.float32
+        a, b = ctx.zeros((2, 3), f), ctx.zeros((3, 4), f)
+        assert _dot_rc(None, b, ctx.zeros((2, 4), f)) == nc.ERR_NULL
+        assert _dot_rc(a, ctx.zeros((3, 4), np.int32), ctx.zeros((2, 4), f)) == nc.ERR_TYPE
+        assert _dot_rc(a, ctx.zeros((4, 4), f), ctx.zeros((2, 4), f)) == nc.ERR_SHAPE   # axis
+        assert _dot_rc(a, b, ctx.zeros((2, 4, 1), f)) == nc.ERR_SHAPE                 # ndim
+        assert _dot_rc(a, b, ctx.zeros((4, 2), f)) == nc.ERR_SHAPE                    # shape
+        s = ctx.from_numpy(np.array(2.0, dtype=f))
+        assert s.shape == ()
+        assert _dot_rc(s, b, ctx.zeros((3,), f)) == nc.ERR_SHAPE                      # 0-D
+        assert _dot_rc(s, b, ctx.zeros((3, 5), f)) == nc.ERR_SHAPE
+        v = ctx.zeros((3,), f)
+        assert _dot_rc(v, ctx.zeros((4,), f), ctx.zeros((1,), f)) == nc.ERR_SHAPE
+        assert "dot: axis mismatch" in nc.last_error()[1]
+
+
 @pytest.mark.skipif(nc.device_count() > 0, reason="checks the no-GPU behaviour")
 def test_no_cpu_fallback():
     with nc.Ctx() as ctx:
