@@ -194,6 +194,9 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
   default:
     return NUMC_SET_ERROR(NUMC_ERR_VALUE, "unknown algorithm %d", algo);
   }
+  if (algo == NUMC_CUDA_ALGO_SIMT && packed_only &&
+      (dt == NUMC_DTYPE_FLOAT32 || dt == NUMC_DTYPE_FLOAT64) && param == numc_k::kFloatNumc)
+    param = numc_k::kFloatNumcPacked;
   p->algo = algo;
   p->param = param;
   if (dt == NUMC_DTYPE_INT8 || dt == NUMC_DTYPE_UINT8) {

@@ -340,6 +340,11 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
 
 constexpr int kSimtBM = 128, kSimtBN = 128;
 
+// numc_matmul's gemmsup threshold for float32 (src/matmul/matmul.c:241-256).
+__host__ __device__ inline bool numc_packed(const Prob &P) {
+  return (double)P.M * P.K * P.N > 96.0 * 96 * 96;
+}
+
 __global__ void __launch_bounds__(simt::kThreads)
 grouped_simt(const Prob *__restrict__ probs, const Tile *__restrict__ tiles) {
   const Tile tl = tiles[blockIdx.x];
@@ -348,7 +353,27 @@ grouped_simt(const Prob *__restrict__ probs, const Tile *__restrict__ tiles) {
   g.a = P.A; g.b = P.B; g.c = P.C;
   g.M = P.M; g.K = P.K; g.N = P.N;
   g.rsa = P.rsa; g.csa = P.csa; g.rsb = P.rsb; g.csb = P.csb; g.rso = P.rso; g.cso = P.cso;
-  simt::simt_tile<float, kSimtBM, kSimtBN, 8, 8, 8, simt::kFloat>(g, 0, tl.m0, tl.n0);
+  // numc_matmul's arithmetic per problem: packed path above its gemmsup
+  // threshold (remainder tiles redone by grouped_float_edges), unpacked
+  // below — as the single-problem SIMT launcher.
+  if (numc_packed(P))
+    simt::simt_tile<float, kSimtBM, kSimtBN, 8, 8, 8, simt::kFloat>(g, 0, tl.m0, tl.n0);
+  else
+    simt::simt_tile<float, kSimtBM, kSimtBN, 8, 8, 8, simt::kFloatSmall>(g, 0, tl.m0, tl.n0);
+}
+
+// numc's packed-path remainder tiles of the CUDA-core problems listed in
+// `probs_idx`, one block per problem.
+__global__ void __launch_bounds__(256)
+grouped_float_edges(const Prob *__restrict__ probs, const int *__restrict__ probs_idx) {
+  const Prob &P = probs[probs_idx[blockIdx.x]];
+  Gemm g;
+  g.a = P.A; g.b = P.B; g.c = P.C;
+  g.M = P.M; g.K = P.K; g.N = P.N;
+  g.rsa = P.rsa; g.csa = P.csa; g.rsb = P.rsb; g.csb = P.csb; g.rso = P.rso; g.cso = P.cso;
+  const int64_t r0 = simt::edge_row<float>(g.M), c0 = simt::edge_col<float>(g.N);
+  const int64_t n = simt::float_edge_count<float>(g.M, g.N);
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) simt::float_edge_output<float>(g, e, r0, c0);
 }
 
 }  // namespace grouped
@@ -380,6 +405,8 @@ struct NumcCudaGemmPlan {
   Prob *d_split_probs;
   Tile *d_tiles[kNumVar];
   int ntiles[kNumVar];
+  int *d_edge_probs;              // CUDA-core problems with packed-path remainders
+  int n_edge_probs;
   unsigned long long *flags;      // all flag words and maxima (memset per run)
   size_t flags_bytes;
   unsigned long long gen;
@@ -526,6 +553,11 @@ int plan_enqueue(NumcCudaGemmPlan *p, cudaStream_t s, unsigned *kernels) {
     if ((e = cudaGetLastError())) return fail(e, "grouped SIMT");
     ++*kernels;
   }
+  if (p->n_edge_probs) {
+    grouped_float_edges<<<p->n_edge_probs, 256, 0, s>>>(p->d_probs, p->d_edge_probs);
+    if ((e = cudaGetLastError())) return fail(e, "grouped SIMT remainder tiles");
+    ++*kernels;
+  }
   return 0;
 }
 
@@ -620,9 +652,13 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
                    [&](size_t x, size_t y) { return p->probs[x].K > p->probs[y].K; });
   std::vector<Tile> tiles[kNumVar];
   std::vector<size_t> split_idx;
+  std::vector<int> edge_idx;
   for (size_t i : order) {
     const int v = p->variant[i];
     if (v < 0) continue;
+    if (v == kVarSimt && p->probs[i].K > 0 && numc_packed(p->probs[i]) &&
+        simt::float_edge_count<float>(p->probs[i].M, p->probs[i].N) > 0)
+      edge_idx.push_back((int)i);
     const int bn = v == kVarTc128 ? 128 : v == kVarTc64 ? 64 : kSimtBN;
     const int bm = v == kVarSimt ? kSimtBM : kBM;
     for (int m0 = 0; m0 < p->probs[i].M; m0 += bm)
@@ -658,6 +694,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   const size_t o_sprobs = off; off = align_up(off + split_idx.size() * sizeof(Prob), 256);
   const size_t o_prefix = off; off = align_up(off + prefix.size() * sizeof(long long), 256);
   const size_t o_prefix_max = off; off = align_up(off + prefix_max.size() * sizeof(long long), 256);
+  const size_t o_edges = off; off = align_up(off + edge_idx.size() * sizeof(int), 256);
   size_t o_tiles[kNumVar];
   for (int v = 0; v < kNumVar; v++) {
     o_tiles[v] = off;
@@ -677,6 +714,8 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   p->d_split_probs = (Prob *)(p->dev + o_sprobs);
   p->d_prefix = (long long *)(p->dev + o_prefix);
   p->d_prefix_max = (long long *)(p->dev + o_prefix_max);
+  p->d_edge_probs = (int *)(p->dev + o_edges);
+  p->n_edge_probs = (int)edge_idx.size();
   for (int v = 0; v < kNumVar; v++) {
     p->d_tiles[v] = (Tile *)(p->dev + o_tiles[v]);
     p->ntiles[v] = (int)tiles[v].size();
@@ -723,7 +762,10 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
       (e = cudaMemcpy(p->d_split_probs, sp.data(), sp.size() * sizeof(Prob), cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(p->d_prefix, prefix.data(), prefix.size() * sizeof(long long), cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(p->d_prefix_max, prefix_max.data(), prefix_max.size() * sizeof(long long),
-                      cudaMemcpyHostToDevice))) {
+                      cudaMemcpyHostToDevice)) ||
+      (!edge_idx.empty() &&
+       (e = cudaMemcpy(p->d_edge_probs, edge_idx.data(), edge_idx.size() * sizeof(int),
+                       cudaMemcpyHostToDevice)))) {
     numc_cuda_gemm_plan_free(p);
     fail(e, "plan upload");
     return nullptr;

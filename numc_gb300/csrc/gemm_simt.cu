@@ -1,6 +1,7 @@
 // CUDA-core GEMM for all ten numc dtypes: the single-problem launcher of
 // the tile in simt_common.cuh (arithmetic per dtype documented there).
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdint>
 
 #include "kernels.h"
@@ -17,6 +18,25 @@ __global__ void __launch_bounds__(kThreads) simt_gemm(Gemm g, int rule8) {
                                                (int64_t)blockIdx.x * BN);
 }
 
+template <typename T>
+__global__ void __launch_bounds__(256) float_edges(Gemm g, int64_t r0, int64_t c0, int64_t n) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    simt::float_edge_output<T>(g, e, r0, c0);
+}
+
+// numc's packed-path remainder tiles of g, after the GEMM kernel.
+template <typename T>
+cudaError_t launch_float_edges(const Gemm &g, cudaStream_t s) {
+  const int64_t n = simt::float_edge_count<T>(g.M, g.N);
+  if (n == 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, 4096);
+  float_edges<T><<<(unsigned)blocks, 256, 0, s>>>(g, simt::edge_row<T>(g.M),
+                                                 simt::edge_col<T>(g.N), n);
+  count_launch();
+  return cudaGetLastError();
+}
+
 template <typename T, int BM, int BN, int TM, int TN, int KIND>
 cudaError_t launch_tile(const Gemm &g, int rule8, cudaStream_t s) {
   constexpr int BK = 8;
@@ -30,14 +50,33 @@ cudaError_t launch_tile(const Gemm &g, int rule8, cudaStream_t s) {
 
 }  // namespace
 
+int float_rule(NumcDType dt, const Gemm &g, int rule) {
+  if (rule != kFloatNumc) return rule;
+  // numc_matmul's gemmsup threshold (src/matmul/matmul.c:241-256)
+  const double thr = dt == NUMC_DTYPE_FLOAT32 ? 96.0 * 96 * 96 : 48.0 * 48 * 48;
+  return (double)g.M * g.K * g.N > thr ? kFloatNumcPacked : kFloatNumcSmall;
+}
+
 cudaError_t launch_simt(NumcDType dt, const Gemm &g, int rule8, cudaStream_t s) {
   switch (dt) {
   case NUMC_DTYPE_FLOAT32:
-    if (rule8 == kFloatNaive) return launch_tile<float, 128, 128, 8, 8, simt::kFloatUnfused>(g, 0, s);
-    return launch_tile<float, 128, 128, 8, 8, simt::kFloat>(g, 0, s);
+    switch (float_rule(dt, g, rule8)) {
+    case kFloatNaive: return launch_tile<float, 128, 128, 8, 8, simt::kFloatUnfused>(g, 0, s);
+    case kFloatNumcSmall: return launch_tile<float, 128, 128, 8, 8, simt::kFloatSmall>(g, 0, s);
+    default: {
+      cudaError_t e = launch_tile<float, 128, 128, 8, 8, simt::kFloat>(g, 0, s);
+      return e != cudaSuccess || g.K == 0 ? e : launch_float_edges<float>(g, s);
+    }
+    }
   case NUMC_DTYPE_FLOAT64:
-    if (rule8 == kFloatNaive) return launch_tile<double, 64, 64, 4, 4, simt::kFloatUnfused>(g, 0, s);
-    return launch_tile<double, 64, 64, 4, 4, simt::kFloat>(g, 0, s);
+    switch (float_rule(dt, g, rule8)) {
+    case kFloatNaive: return launch_tile<double, 64, 64, 4, 4, simt::kFloatUnfused>(g, 0, s);
+    case kFloatNumcSmall: return launch_tile<double, 64, 64, 4, 4, simt::kFloatSmall>(g, 0, s);
+    default: {
+      cudaError_t e = launch_tile<double, 64, 64, 4, 4, simt::kFloat>(g, 0, s);
+      return e != cudaSuccess || g.K == 0 ? e : launch_float_edges<double>(g, s);
+    }
+    }
   case NUMC_DTYPE_INT16: return launch_tile<int16_t, 128, 128, 8, 8, simt::kWrapInt>(g, 0, s);
   case NUMC_DTYPE_UINT16: return launch_tile<uint16_t, 128, 128, 8, 8, simt::kWrapInt>(g, 0, s);
   case NUMC_DTYPE_INT32: return launch_tile<int32_t, 128, 128, 8, 8, simt::kWrapInt>(g, 0, s);

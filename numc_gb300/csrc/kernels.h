@@ -26,14 +26,24 @@ enum Rule8 : int {
   kRuleNeon = 2,      // numc aarch64 NEON path (one block over all K)
 };
 
-// float32/float64 SIMT variant: kFloatFma = numc's register tiles (one FMA
-// chain per output), kFloatNaive = numc's naive kernels (product and sum
-// each rounded).
-enum FloatSimt : int { kFloatFma = 0, kFloatNaive = 1 };
+// float32/float64 SIMT variant (numc's x86 AVX2 arithmetic, bit-exact):
+//   kFloatNumc       numc_matmul: the packed path above numc's gemmsup
+//                    threshold (M K N > 96^3 float32, 48^3 float64), else
+//                    the unpacked one;
+//   kFloatNaive      numc's naive kernels (product and sum each rounded);
+//   kFloatNumcPacked the packed path at every size (numc_dot's GEMM branch);
+//   kFloatNumcSmall  the unpacked (gemmsup) path at every size.
+// Full register tiles are one FMA chain per output in k order on both
+// paths; remainder tiles differ (see simt_common.cuh).
+enum FloatSimt : int {
+  kFloatNumc = 0, kFloatNaive = 1, kFloatNumcPacked = 2, kFloatNumcSmall = 3
+};
 
 // CUDA-core kernels for every dtype.  `rule8` is the Rule8 for int8/uint8,
 // the FloatSimt variant for float32/float64, unused otherwise.
 cudaError_t launch_simt(NumcDType dt, const Gemm &g, int rule8, cudaStream_t s);
+// The float variant kFloatNumc resolves to for problem g.
+int float_rule(NumcDType dt, const Gemm &g, int rule);
 
 // numc_dot's non-GEMM cases (dot_kernels.cu), all on device pointers:
 // out[i] = x[i] * scalar over an N-D strided array (scalar read from

@@ -31,10 +31,37 @@ namespace simt {
 
 constexpr int kThreads = 256;
 
-// kFloat: one fused multiply-add chain per output (numc's register tiles);
+// kFloat: one fused multiply-add chain per output (numc's full register
+// tiles; numc_float_edges then redoes the packed path's remainder tiles);
+// kFloatSmall: numc's unpacked (gemmsup) float path;
 // kFloatUnfused: `acc = acc + a * b`, product and sum each rounded (numc's
 // naive kernels, compiled without contraction).
-enum Kind : int { kFloat = 0, kWrapInt = 1, kByte = 2, kFloatUnfused = 3 };
+enum Kind : int { kFloat = 0, kWrapInt = 1, kByte = 2, kFloatUnfused = 3, kFloatSmall = 4 };
+
+// ---- numc's float register tiles (x86 AVX2 build) --------------------------
+//
+// Packed path (gemm_avx2.h:852-950 float32, 1377-1475 float64): M in blocks
+// of MC rows (144 / 72) cut into 6-row register tiles, N in panels of 4080
+// columns cut into NR-column tiles (16 / 8), K in blocks of 256.  An output
+// of a full 6 x NR tile is one FMA chain over all K (the micro-kernel
+// reloads C between K blocks); an output of a remainder tile sums each K
+// block as an FMA chain from zero and adds it to the stored value.
+// Unpacked path (gemmsup_avx2.h:97-147, 221-270; M K N at most 96^3 /
+// 48^3): 6 x NR tiles from the origin; in a tile narrower than NR the first
+// (width / VW) x VW columns are vector FMA chains and the rest scalar
+// `c += a * b`, unfused (numc is ISO C without contraction).
+template <typename T> struct NumcTiles;
+template <> struct NumcTiles<float> { static constexpr int MC = 144, NR = 16, VW = 8; };
+template <> struct NumcTiles<double> { static constexpr int MC = 72, NR = 8, VW = 4; };
+constexpr int kNumcMR = 6, kNumcNC = 4080, kNumcKC = 256;
+
+// Unpacked path: column j is one of a narrow tile's scalar (unfused) columns.
+template <typename T>
+__device__ __forceinline__ bool small_col_unfused(int64_t j, int64_t N) {
+  constexpr int NR = NumcTiles<T>::NR, VW = NumcTiles<T>::VW;
+  const int64_t j0 = (j / NR) * NR, nr = min((int64_t)NR, N - j0);
+  return nr < NR && (j - j0) >= (nr / VW) * VW;
+}
 
 // ---- numc's int8/uint8 store rules ---------------------------------------
 
@@ -103,6 +130,11 @@ template <> __device__ __forceinline__ float madd(float a, float b, float c) {
 }
 template <> __device__ __forceinline__ double madd(double a, double b, double c) {
   return __fma_rn(a, b, c);
+}
+template <typename T>
+__device__ __forceinline__ T add_rn(T a, T b) {
+  if constexpr (std::is_same<T, float>::value) return __fadd_rn(a, b);
+  else return __dadd_rn(a, b);
 }
 // The _rn intrinsics are never contracted into a fused multiply-add.
 __device__ __forceinline__ float madd_unfused(float a, float b, float c) {
@@ -203,6 +235,13 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
   const int64_t kblock = (KIND == kByte && rule8 == kRuleX86Packed) ? 512 : (int64_t)1 << 62;
   int64_t block_idx = 0;
 
+  uint32_t unf_mask = 0;   // kFloatSmall: bit j: column j is an unfused one
+  if constexpr (KIND == kFloatSmall) {
+#pragma unroll
+    for (int j = 0; j < TN; j++)
+      if (small_col_unfused<T>(n0 + col_of(j), g.N)) unf_mask |= 1u << j;
+  }
+
   load_tiles(0);
   store_tiles(0);
   __syncthreads();
@@ -220,8 +259,14 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
       for (int i = 0; i < TM; i++)
 #pragma unroll
         for (int j = 0; j < TN; j++) {
-          if constexpr (KIND == kFloatUnfused) acc[i][j] = madd_unfused(av[i], bv[j], acc[i][j]);
-          else acc[i][j] = madd<Acc>(av[i], bv[j], acc[i][j]);
+          if constexpr (KIND == kFloatUnfused) {
+            acc[i][j] = madd_unfused(av[i], bv[j], acc[i][j]);
+          } else if constexpr (KIND == kFloatSmall) {
+            acc[i][j] = ((unf_mask >> j) & 1u) ? madd_unfused(av[i], bv[j], acc[i][j])
+                                               : madd<Acc>(av[i], bv[j], acc[i][j]);
+          } else {
+            acc[i][j] = madd<Acc>(av[i], bv[j], acc[i][j]);
+          }
         }
     }
     if constexpr (KIND == kByte) {
@@ -265,6 +310,57 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
       C[gi * g.rso + gj * g.cso] = v;
     }
   }
+}
+
+// ---- numc's packed-path remainder tiles (floats) --------------------------
+//
+// Only the last, partial MC block of rows and the last, partial NR tile of
+// the last 4080-column panel hold remainder tiles (MC and 4080 are
+// multiples of the tile sizes): rows from edge_row(M), columns from
+// edge_col(N).  Their outputs are recomputed after the GEMM kernel: each
+// 256-deep K block as an FMA chain from zero, added to the running value.
+template <typename T> __host__ __device__ inline int64_t edge_row(int64_t M) {
+  if (M == 0) return 0;
+  const int64_t ic = ((M - 1) / NumcTiles<T>::MC) * NumcTiles<T>::MC;
+  return ic + ((M - ic) / kNumcMR) * kNumcMR;
+}
+template <typename T> __host__ __device__ inline int64_t edge_col(int64_t N) {
+  if (N == 0) return 0;
+  const int64_t jc = ((N - 1) / kNumcNC) * kNumcNC;
+  return jc + ((N - jc) / NumcTiles<T>::NR) * NumcTiles<T>::NR;
+}
+
+// Output e of the remainder set (rows >= r0: all columns; then rows < r0:
+// columns >= c0), computed by one thread.
+template <typename T>
+__device__ __forceinline__ void float_edge_output(const Gemm &g, int64_t e, int64_t r0,
+                                                  int64_t c0) {
+  int64_t i, j;
+  const int64_t nbottom = (g.M - r0) * g.N;
+  if (e < nbottom) {
+    i = r0 + e / g.N;
+    j = e % g.N;
+  } else {
+    const int64_t w = g.N - c0;
+    i = (e - nbottom) / w;
+    j = c0 + (e - nbottom) % w;
+  }
+  const T *A = (const T *)g.a, *B = (const T *)g.b;
+  T d = T(0);
+  for (int64_t pc = 0; pc < g.K; pc += kNumcKC) {
+    const int64_t pe = min(pc + (int64_t)kNumcKC, g.K);
+    T t = T(0);
+    for (int64_t k = pc; k < pe; k++)
+      t = madd<T>(A[i * g.rsa + k * g.csa], B[k * g.rsb + j * g.csb], t);
+    d = pc == 0 ? t : add_rn<T>(d, t);
+  }
+  ((T *)g.c)[i * g.rso + j * g.cso] = d;
+}
+
+template <typename T>
+__host__ __device__ inline int64_t float_edge_count(int64_t M, int64_t N) {
+  const int64_t r0 = edge_row<T>(M), c0 = edge_col<T>(N);
+  return (M - r0) * N + r0 * (N - c0);
 }
 
 }  // namespace simt

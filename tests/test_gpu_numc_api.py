@@ -111,13 +111,9 @@ def test_true_transposed_views(ctx, dt):
     Bt = ctx.from_numpy(np.ascontiguousarray(b.T)).transpose((1, 0))
     C = ctx.zeros((Nn, M), dt).transpose((1, 0))
     nc.matmul(At, Bt, C)
+    # numc's arithmetic on the same values (floats included: bit-exact)
     ref = oracle.matmul(a, b, oracle.PROFILE_WRAP if dt in ("int8", "uint8") else 0)
-    got = C.numpy()
-    if dt.startswith("float"):
-        np.testing.assert_allclose(got, ref, rtol=1e-5 if dt == "float32" else 1e-13,
-                                   atol=1e-5 if dt == "float32" else 1e-13)
-    else:
-        np.testing.assert_array_equal(got, ref)
+    np.testing.assert_array_equal(C.numpy(), ref)
 
 
 def test_strided_slice_output_keeps_gaps(ctx):
