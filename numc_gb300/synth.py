@@ -11,8 +11,60 @@ Value maps (x is a 64-bit draw):
   float64 uniform [lo, hi):  u = (x >> 11) * 2^-53
   integers uniform [lo, hi]: lo + ((x >> 32) * (hi - lo + 1)) >> 32
   normal:                    Box-Muller on two float64 uniforms
+
+Bit-for-bit on every host: the logarithm, cosine and exponential needed by
+Box-Muller and the ill-scaled factors are evaluated here from IEEE
+additions, multiplications, divisions and square roots in a fixed order
+(series after exact range reduction), never through the platform's libm,
+whose last bits differ between x86-64 and aarch64 builds.
 """
+import math
+
 import numpy as np
+
+_CHUNK = 1 << 20
+_LN2 = 0.6931471805599453        # float64 nearest ln 2
+_LN10 = 2.302585092994046        # float64 nearest ln 10
+_TWO_PI = 6.283185307179586      # float64 nearest 2 pi
+# log(m) = 2 z sum z^2n / (2n + 1), z = (m - 1) / (m + 1), |z| <= 1/3
+_LOG_C = [1.0 / (2 * n + 1) for n in range(19)]
+# cos x = sum (-1)^n x^2n / (2n)!, 0 <= x <= pi / 2
+_COS_C = [(-1.0) ** n / math.factorial(2 * n) for n in range(14)]
+# exp r = sum r^n / n!, |r| <= ln 2 / 2
+_EXP_C = [1.0 / math.factorial(n) for n in range(20)]
+
+
+def _horner(coeffs, x):
+    s = np.full_like(x, coeffs[-1])
+    for c in reversed(coeffs[:-1]):
+        s *= x
+        s += c
+    return s
+
+
+def _log01(u):
+    """ln u for float64 u in (0, 1]."""
+    m, e = np.frexp(u)                       # u = m 2^e exactly, m in [0.5, 1)
+    z = (m - 1.0) / (m + 1.0)
+    return e * _LN2 + 2.0 * z * _horner(_LOG_C, z * z)
+
+
+def _cos2pi(v):
+    """cos(2 pi v) for float64 v in [0, 1)."""
+    w = np.where(v >= 0.5, v - 1.0, v)       # exact, in [-0.5, 0.5)
+    r = np.abs(w)
+    flip = r > 0.25
+    r = np.where(flip, 0.5 - r, r)           # exact, in [0, 0.25]
+    x = _TWO_PI * r
+    c = _horner(_COS_C, x * x)
+    return np.where(flip, -c, c)
+
+
+def _exp(y):
+    """e^y for float64 y of moderate size (|y| < 700)."""
+    k = np.rint(y / _LN2)
+    r = y - k * _LN2
+    return np.ldexp(_horner(_EXP_C, r), k.astype(np.int64))
 
 GOLDEN = np.uint64(0x9E3779B97F4A7C15)
 _M1 = np.uint64(0xBF58476D1CE4E5B9)
@@ -57,10 +109,14 @@ def integers(seed, stream, shape, lo, hi, dtype):
 def normal(seed, stream, shape, dtype=np.float32):
     n = int(np.prod(shape))
     x = draws(seed, stream, 2 * n)
-    u1 = ((x[0::2] >> np.uint64(11)).astype(np.float64) + 1.0) * 2.0 ** -53
-    u2 = (x[1::2] >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
-    z = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
-    return z.astype(dtype).reshape(shape)
+    out = np.empty(n, dtype=dtype)
+    for s in range(0, n, _CHUNK):             # chunks stay in cache
+        xs = x[2 * s: 2 * min(n, s + _CHUNK)]
+        u1 = ((xs[0::2] >> np.uint64(11)).astype(np.float64) + 1.0) * 2.0 ** -53
+        u2 = (xs[1::2] >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+        z = np.sqrt(-2.0 * _log01(u1)) * _cos2pi(u2)
+        out[s: s + len(z)] = z.astype(dtype)
+    return out.reshape(shape)
 
 
 def ill_scales(seed, M, N):
@@ -68,7 +124,7 @@ def ill_scales(seed, M, N):
     for the ill-scaled workload (applied to the `normal` operands)."""
     u = uniform(seed, 7, (M,), -4.0, 4.0, np.float64)
     v = uniform(seed, 8, (N,), -4.0, 4.0, np.float64)
-    return 10.0 ** u, 10.0 ** v
+    return _exp(u * _LN10), _exp(v * _LN10)
 
 
 # Value ranges of the integer-exactness workload (1024^3).
