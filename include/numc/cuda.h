@@ -122,6 +122,10 @@ NUMC_API int numc_cuda_check_status(void *stream);
 
 /* Number of kernels this library has launched since load (diagnostics). */
 NUMC_API uint64_t numc_cuda_launch_count(void);
+/* Bytes of array data this library has copied between host and device
+ * (operand staging, results, numc_cuda_array_to_device/_to_host); lets a
+ * caller check that a chain of device-resident calls makes no round trip. */
+NUMC_API uint64_t numc_cuda_transfer_bytes(void);
 
 /* Per-phase timing of the tensor-core GEMMs (split-BF16, Ozaki): when
  * enabled, each call records CUDA events on its stream around the operand

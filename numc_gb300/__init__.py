@@ -85,6 +85,7 @@ SIGNATURES = [
     ("numc_matmul", _I, [_VP, _VP, _VP]),
     ("numc_matmul_naive", _I, [_VP, _VP, _VP]),
     ("numc_dot", _I, [_VP, _VP, _VP]),
+    ("numc_cuda_transfer_bytes", ctypes.c_uint64, []),
     ("numc_set_error", _I, [_I, ctypes.c_char_p]),
     ("numc_get_error", _Err, []),
     ("numc_log_error", None, [_VP]),
@@ -161,6 +162,11 @@ def get_algo(dtype):
 
 def launch_count():
     return lib().numc_cuda_launch_count()
+
+
+def transfer_bytes():
+    """Bytes of array data copied between host and device so far."""
+    return lib().numc_cuda_transfer_bytes()
 
 
 class Ctx:
@@ -288,6 +294,12 @@ class Array:
         if not p:
             raise NumcError(*last_error())
         return Array(p, self.ctx)
+
+    def contiguous(self):
+        """numc_array_contiguous: re-lay this array out row-major in place."""
+        if lib().numc_array_contiguous(self.ptr) != 0:
+            raise NumcError(*last_error())
+        return self
 
     def is_contiguous(self):
         return lib().numc_array_is_contiguous(self.ptr)

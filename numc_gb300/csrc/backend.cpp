@@ -89,6 +89,17 @@ int device_count() {
   return g_device_count;
 }
 
+// Bytes of array data copied between host and device by this library
+// (numc_cuda_transfer_bytes): staging of host operands and results,
+// numc_cuda_array_to_device / _to_host.
+std::atomic<uint64_t> g_transfer_bytes{0};
+
+cudaError_t xfer_async(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind,
+                       cudaStream_t s) {
+  g_transfer_bytes += bytes;
+  return cudaMemcpyAsync(dst, src, bytes, kind, s);
+}
+
 int cuda_fail(cudaError_t e, const char *what) {
   int code = (e == cudaErrorMemoryAllocation) ? NUMC_ERR_MALLOC : NUMC_ERR_INTERNAL;
   cudaGetLastError();
@@ -367,12 +378,12 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
   // before the copy-in stream overwrites it.
   if ((e = cudaEventRecord(ev[1], s)) || (e = cudaStreamWaitEvent(cin, ev[1], 0)))
     return fail_cu(e, "stream order");
-  if ((e = cudaMemcpyAsync(dB, b->data, sb, cudaMemcpyHostToDevice, cin)) ||
+  if ((e = xfer_async(dB, b->data, sb, cudaMemcpyHostToDevice, cin)) ||
       (e = cudaEventRecord(ev_b, cin)))
     return fail_cu(e, "copy b to device");
   for (int p = 0; p < np; p++) {
     const size_t r0 = (size_t)p * rows, r = std::min(rows, M - r0);
-    if ((e = cudaMemcpyAsync(dA + r0 * K * es, (const char *)a->data + r0 * K * es, r * K * es,
+    if ((e = xfer_async(dA + r0 * K * es, (const char *)a->data + r0 * K * es, r * K * es,
                              cudaMemcpyHostToDevice, cin)) ||
         (e = cudaEventRecord(ev[2 + p], cin)))
       return fail_cu(e, "copy a panel to device");
@@ -396,7 +407,7 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
     if ((e = cudaStreamWaitEvent(s, ev[2 + p], 0)) ||
         (e = numc_k::split_pipe_panel(pp, p, gp, ws, gen, s)) || (e = cudaEventRecord(done, s)) ||
         (e = cudaStreamWaitEvent(cout, done, 0)) ||
-        (e = cudaMemcpyAsync((char *)out->data + r0 * N * es, gp.c, r * N * es,
+        (e = xfer_async((char *)out->data + r0 * N * es, gp.c, r * N * es,
                              cudaMemcpyDeviceToHost, cout)))
       return fail_cu(e, "panel");
   }
@@ -435,11 +446,11 @@ int matmul_impl(const NumcArray *a, const NumcArray *b, NumcArray *out, int algo
   const char *da = ra ? a->dev_base : scratch + off_a;
   const char *db = rb ? b->dev_base : scratch + off_b;
   char *dout = ro ? out->dev_base : scratch + off_o;
-  if (!ra) CU(cudaMemcpyAsync((void *)da, a->data, sa, cudaMemcpyHostToDevice, s), "copy a to device");
-  if (!rb) CU(cudaMemcpyAsync((void *)db, b->data, sb, cudaMemcpyHostToDevice, s), "copy b to device");
+  if (!ra) CU(xfer_async((void *)da, a->data, sa, cudaMemcpyHostToDevice, s), "copy a to device");
+  if (!rb) CU(xfer_async((void *)db, b->data, sb, cudaMemcpyHostToDevice, s), "copy b to device");
   // A strided `out` with gaps between rows keeps the gap bytes: stage them.
   if (!ro && so > out->capacity)
-    CU(cudaMemcpyAsync(dout, out->data, so, cudaMemcpyHostToDevice, s), "copy out to device");
+    CU(xfer_async(dout, out->data, so, cudaMemcpyHostToDevice, s), "copy out to device");
 
   numc_k::Gemm g;
   g.a = da; g.b = db; g.c = dout;
@@ -455,7 +466,7 @@ int matmul_impl(const NumcArray *a, const NumcArray *b, NumcArray *out, int algo
     // the caller may modify the host buffers.
     if (!ra || !rb) CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   } else {
-    CU(cudaMemcpyAsync(out->data, dout, so, cudaMemcpyDeviceToHost, s), "copy out to host");
+    CU(xfer_async(out->data, dout, so, cudaMemcpyDeviceToHost, s), "copy out to host");
     CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   }
   if (plan.algo == NUMC_CUDA_ALGO_SPLIT_BF16 || plan.algo == NUMC_CUDA_ALGO_SPLIT_FP16 ||
@@ -485,6 +496,35 @@ void *host_alloc_pinned(size_t bytes) {
 }
 
 void host_free_pinned(void *p) { cudaFreeHost(p); }
+
+int device_copy_contiguous(const NumcArray *src, NumcArray *dst) {
+  if (src->dim > (size_t)numc_k::kDotMaxDims)
+    return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "device copy: %zu dimensions (at most %d)", src->dim,
+                          numc_k::kDotMaxDims);
+  cudaStream_t s;
+  int err = ctx_stream(dst->ctx, &s);
+  if (err) return err;
+  if (!dst->dev_base) {
+    const size_t bytes = dst->capacity;
+    void *p = nullptr;
+    CU(cudaMalloc(&p, align_up(bytes ? bytes : 1, 256)), "cudaMalloc(array)");
+    dst->ctx->dev_allocs->push_back(DeviceAlloc{p, bytes, dst->pos});
+    dst->dev_base = (char *)p;
+  }
+  numc_k::DotNd ix;
+  ix.dim = (int)src->dim;
+  for (size_t d = 0; d < src->dim; d++) {
+    ix.shape[d] = (int64_t)src->shape[d];
+    ix.xs[d] = (int64_t)(src->strides[d] / src->elem_size);
+    ix.os[d] = 0;
+  }
+  cudaError_t e = numc_k::launch_gather(src->dev_base, dst->dev_base, src->elem_size, ix, s);
+  if (e != cudaSuccess) return cuda_fail(e, "device gather");
+  // The source may be released by the caller right after: finish here.
+  CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  dst->residency = kDeviceOnly;
+  return 0;
+}
 
 void ctx_release_device(NumcCtx *ctx, const ArenaPos *keep_upto) {
   if (!ctx->dev_allocs) return;
@@ -646,10 +686,10 @@ int dot_impl(const NumcArray *a, const NumcArray *b, NumcArray *out) {
   const char *db = rb ? b->dev_base : scratch + off_b;
   char *dout = ro ? out->dev_base : scratch + off_o;
   char *ws = scratch + off_w;
-  if (!ra && sa) CU(cudaMemcpyAsync((void *)da, a->data, sa, cudaMemcpyHostToDevice, s), "copy a to device");
-  if (!rb && sb) CU(cudaMemcpyAsync((void *)db, b->data, sb, cudaMemcpyHostToDevice, s), "copy b to device");
+  if (!ra && sa) CU(xfer_async((void *)da, a->data, sa, cudaMemcpyHostToDevice, s), "copy a to device");
+  if (!rb && sb) CU(xfer_async((void *)db, b->data, sb, cudaMemcpyHostToDevice, s), "copy b to device");
   if (!ro && so > out->capacity)
-    CU(cudaMemcpyAsync(dout, out->data, so, cudaMemcpyHostToDevice, s), "copy out to device");
+    CU(xfer_async(dout, out->data, so, cudaMemcpyHostToDevice, s), "copy out to device");
 
   cudaError_t e = cudaSuccess;
   if (kind == kScalar) {
@@ -699,7 +739,7 @@ int dot_impl(const NumcArray *a, const NumcArray *b, NumcArray *out) {
     out->residency = kDeviceOnly;
     if (!ra || !rb) CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   } else {
-    CU(cudaMemcpyAsync(out->data, dout, so, cudaMemcpyDeviceToHost, s), "copy out to host");
+    CU(xfer_async(out->data, dout, so, cudaMemcpyDeviceToHost, s), "copy out to host");
     CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   }
   if (gemm_branch && plan.algo != NUMC_CUDA_ALGO_SIMT && plan.algo != NUMC_CUDA_ALGO_DMMA) {
@@ -772,7 +812,7 @@ extern "C" int numc_matmul_grouped(const NumcArray *const *a, const NumcArray *c
         dev[t] = scratch + off[3 * i + t];
         const size_t span = array_span_bytes(arrs[t]);
         if (span && (t < 2 || span > arrs[t]->capacity))
-          CU(cudaMemcpyAsync(dev[t], arrs[t]->data, span, cudaMemcpyHostToDevice, s), "stage operand");
+          CU(xfer_async(dev[t], arrs[t]->data, span, cudaMemcpyHostToDevice, s), "stage operand");
       }
     }
     NumcCudaGemmDesc &d = descs[i];
@@ -792,7 +832,7 @@ extern "C" int numc_matmul_grouped(const NumcArray *const *a, const NumcArray *c
     }
     const size_t span = array_span_bytes(out[i]);
     if (span) {
-      cudaError_t e = cudaMemcpyAsync(out[i]->data, descs[i].out, span, cudaMemcpyDeviceToHost, s);
+      cudaError_t e = xfer_async(out[i]->data, descs[i].out, span, cudaMemcpyDeviceToHost, s);
       if (e) err = cuda_fail(e, "copy out to host");
     }
   }
@@ -844,7 +884,7 @@ extern "C" int numc_cuda_array_to_device(NumcArray *arr) {
     arr->ctx->dev_allocs->push_back(DeviceAlloc{p, span, arr->pos});
     arr->dev_base = (char *)p;
   }
-  if (span) CU(cudaMemcpyAsync(arr->dev_base, arr->data, span, cudaMemcpyHostToDevice, s), "copy to device");
+  if (span) CU(xfer_async(arr->dev_base, arr->data, span, cudaMemcpyHostToDevice, s), "copy to device");
   CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   arr->residency = kBoth;
   return 0;
@@ -857,11 +897,13 @@ extern "C" int numc_cuda_array_to_host(NumcArray *arr) {
   int err = ctx_stream(arr->ctx, &s);
   if (err) return err;
   size_t span = array_span_bytes(arr);
-  if (span) CU(cudaMemcpyAsync(arr->data, arr->dev_base, span, cudaMemcpyDeviceToHost, s), "copy to host");
+  if (span) CU(xfer_async(arr->data, arr->dev_base, span, cudaMemcpyDeviceToHost, s), "copy to host");
   CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   arr->residency = kBoth;
   return 0;
 }
+
+extern "C" uint64_t numc_cuda_transfer_bytes(void) { return g_transfer_bytes.load(); }
 
 extern "C" void *numc_cuda_array_device_data(const NumcArray *arr) {
   return (arr && is_resident(arr)) ? arr->dev_base : nullptr;

@@ -320,11 +320,16 @@ extern "C" NumcArray *numc_array_copy(const NumcArray *arr) {
     NUMC_SET_ERROR(NUMC_ERR_NULL, "array_copy: arr is NULL");
     return nullptr;
   }
-  if (arr->residency == kDeviceOnly &&
-      numc_cuda_array_to_host(const_cast<NumcArray *>(arr)) != 0)
-    return nullptr;
+  const bool resident = arr->residency != kHostOnly && arr->dev_base;
   NumcArray *copy = numc_array_create(arr->ctx, arr->shape, arr->dim, arr->dtype);
   if (!copy) return nullptr;
+  if (resident) {
+    // Copy on the GPU: the copy is resident and contiguous there; the host
+    // buffer is copied too only when it is current.
+    if (device_copy_contiguous(arr, copy) != 0) return nullptr;
+    if (arr->residency == kDeviceOnly) return copy;
+    copy->residency = kBoth;
+  }
   if (arr->is_contiguous) {
     memcpy(copy->data, arr->data, arr->capacity);
   } else {
@@ -351,22 +356,33 @@ extern "C" int numc_array_contiguous(NumcArray *arr) {
     return -1;
   }
   if (numc_array_is_contiguous(arr)) return 0;
-  if (arr->residency == kDeviceOnly && numc_cuda_array_to_host(arr) != 0)
-    return -1;
+  const int was = arr->residency;
+  const bool resident = was != kHostOnly && arr->dev_base;
   char *fresh = (char *)arena_alloc(arr->ctx, arr->capacity, kDataAlign, nullptr);
   if (!fresh) {
     NUMC_SET_ERROR(NUMC_ERR_MALLOC, "array_contiguous: failed to allocate %zu bytes",
                    arr->capacity);
     return -1;
   }
-  for_each_elem(arr, [&](size_t n, size_t off) {
-    memcpy(fresh + n * arr->elem_size, (const char *)arr->data + off, arr->elem_size);
-  });
+  char *fresh_dev = nullptr;
+  if (resident) {
+    // Re-layout on the GPU into a new device buffer owned by this array.
+    NumcArray tmp = *arr;
+    tmp.data = fresh;
+    tmp.dev_base = nullptr;
+    if (device_copy_contiguous(arr, &tmp) != 0) return -1;
+    fresh_dev = tmp.dev_base;
+  }
+  if (!resident || was == kBoth) {
+    for_each_elem(arr, [&](size_t n, size_t off) {
+      memcpy(fresh + n * arr->elem_size, (const char *)arr->data + off, arr->elem_size);
+    });
+  }
   arr->data = fresh;
   contiguous_strides(arr->strides, arr->shape, arr->dim, arr->elem_size);
   arr->is_contiguous = true;
-  arr->residency = kHostOnly;   // the device mirror described the old layout
-  arr->dev_base = nullptr;
+  arr->residency = resident ? (was == kBoth ? kBoth : kDeviceOnly) : kHostOnly;
+  arr->dev_base = fresh_dev;
   return 0;
 }
 

@@ -59,6 +59,10 @@ cudaError_t launch_dot_scalar(NumcDType dt, const void *x, const void *scalar, v
 // SIMD arithmetic (else its strided reduction); `scratch` holds at least
 // dot1d_scratch_bytes() bytes.
 size_t dot1d_scratch_bytes();
+// dst[e] = src at the e-th multi-index of ix (row-major order) for
+// elements of elem_size bytes (1, 2, 4 or 8): strided -> contiguous.
+cudaError_t launch_gather(const void *src, void *dst, size_t elem_size, const DotNd &ix,
+                          cudaStream_t s);
 cudaError_t launch_dot_1d(NumcDType dt, const void *a, int64_t sa, const void *b, int64_t sb,
                           int64_t n, bool contiguous, void *out, void *scratch,
                           cudaStream_t s);

@@ -92,5 +92,9 @@ bool cuda_present();
 void *host_alloc_pinned(size_t bytes);
 void host_free_pinned(void *p);
 void ctx_release_device(NumcCtx *ctx, const ArenaPos *keep_upto);
+// Device-resident arrays: copy `src` (any strides) into the contiguous
+// device buffer of `dst` (allocated here if it has none), on the GPU; dst
+// becomes device-resident (kDeviceOnly).  0 or a NumcErrorCode.
+int device_copy_contiguous(const NumcArray *src, NumcArray *dst);
 
 }  // namespace numc_rt
