@@ -42,6 +42,21 @@ NUMC_API int numc_matmul_naive(const NumcArray *a, const NumcArray *b,
  * do not flatten); a and b both above 2-D return NUMC_ERR_SHAPE. */
 NUMC_API int numc_dot(const NumcArray *a, const NumcArray *b, NumcArray *out);
 
+/* Fused linear layer out = x @ w + bias (numc's ROADMAP.md "Linear
+ * algebra"; not in numc's current API): x (M, K), w (K, N), bias (N,) or
+ * NULL, out (M, N).  Results equal numc_matmul(x, w, out) followed by
+ * adding bias to every row with numc's elementwise add (floats rounded
+ * once, integers modulo 2^bits); the CUDA-core and split kernels add the
+ * bias in their store, other algorithms in one extra pass. */
+NUMC_API int numc_linear(const NumcArray *x, const NumcArray *w, const NumcArray *bias,
+                         NumcArray *out);
+
+/* Batched matrix multiply (numc's ROADMAP.md; not in numc's current API):
+ * a (..., M, K), b (..., K, N), out (..., M, N) with the same leading batch
+ * axes; every batch is numc_matmul(a[i], b[i], out[i]) with numc_matmul's
+ * arithmetic and algorithm choice.  Any strides. */
+NUMC_API int numc_bmm(const NumcArray *a, const NumcArray *b, NumcArray *out);
+
 #ifdef __cplusplus
 }
 #endif

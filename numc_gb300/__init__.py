@@ -85,6 +85,8 @@ SIGNATURES = [
     ("numc_matmul", _I, [_VP, _VP, _VP]),
     ("numc_matmul_naive", _I, [_VP, _VP, _VP]),
     ("numc_dot", _I, [_VP, _VP, _VP]),
+    ("numc_linear", _I, [_VP, _VP, _VP, _VP]),
+    ("numc_bmm", _I, [_VP, _VP, _VP]),
     ("numc_cuda_transfer_bytes", ctypes.c_uint64, []),
     ("numc_set_error", _I, [_I, ctypes.c_char_p]),
     ("numc_get_error", _Err, []),
@@ -327,6 +329,18 @@ def matmul(a, b, out):
 
 def matmul_naive(a, b, out):
     return check(lib().numc_matmul_naive(a.ptr, b.ptr, out.ptr))
+
+
+def linear(x, w, bias, out):
+    """numc_linear(x, w, bias, out): out = x @ w + bias (bias may be None)."""
+    return check(lib().numc_linear(x.ptr if x else None, w.ptr if w else None,
+                                   bias.ptr if bias else None, out.ptr if out else None))
+
+
+def bmm(a, b, out):
+    """numc_bmm(a, b, out): batched numc_matmul over the leading axes."""
+    return check(lib().numc_bmm(a.ptr if a else None, b.ptr if b else None,
+                                out.ptr if out else None))
 
 
 def dot(a, b, out):

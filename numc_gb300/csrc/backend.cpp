@@ -420,7 +420,10 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
   return 0;
 }
 
-int matmul_impl(const NumcArray *a, const NumcArray *b, NumcArray *out, int algo, int param) {
+// `bias` (numc_linear): a 1-D array of N elements added to every row of the
+// product, or null.
+int matmul_impl(const NumcArray *a, const NumcArray *b, NumcArray *out, int algo, int param,
+                const NumcArray *bias = nullptr) {
   int err = check_matmul(a, b, out);
   if (err) return err;
   const size_t M = a->shape[0], K = a->shape[1], N = b->shape[1];
@@ -431,14 +434,17 @@ int matmul_impl(const NumcArray *a, const NumcArray *b, NumcArray *out, int algo
   NumcCtx *ctx = out->ctx;
   cudaStream_t s;
   if ((err = ctx_stream(ctx, &s))) return err;
-  if (use_pipeline(plan, a, b, out, M, K, N)) return matmul_pipelined(a, b, out, plan, s);
+  if (!bias && use_pipeline(plan, a, b, out, M, K, N)) return matmul_pipelined(a, b, out, plan, s);
 
   const size_t es = a->elem_size;
   const bool ra = is_resident(a), rb = is_resident(b), ro = is_resident(out);
+  const bool rbias = bias && is_resident(bias);
   const size_t sa = array_span_bytes(a), sb = array_span_bytes(b), so = array_span_bytes(out);
+  const size_t sbias = bias ? array_span_bytes(bias) : 0;
   size_t off_a = 0, off_b = align_up(ra ? 0 : sa, 256);
   size_t off_o = off_b + align_up(rb ? 0 : sb, 256);
-  size_t off_w = off_o + align_up(ro ? 0 : so, 256);
+  size_t off_bias = off_o + align_up(ro ? 0 : so, 256);
+  size_t off_w = off_bias + align_up(rbias ? 0 : sbias, 256);
   size_t ws_bytes = plan_workspace(plan, M, K, N);
   char *scratch = nullptr;
   if ((err = ctx_scratch(ctx, off_w + ws_bytes + 256, s, &scratch))) return err;
@@ -458,7 +464,21 @@ int matmul_impl(const NumcArray *a, const NumcArray *b, NumcArray *out, int algo
   g.rsa = a->strides[0] / es; g.csa = a->strides[1] / es;
   g.rsb = b->strides[0] / es; g.csb = b->strides[1] / es;
   g.rso = out->strides[0] / es; g.cso = out->strides[1] / es;
-  if ((err = run_plan(dt, plan, g, scratch + off_w, ws_bytes, s))) return err;
+  if (bias) {
+    const char *dbias = rbias ? bias->dev_base : scratch + off_bias;
+    if (!rbias && sbias)
+      CU(xfer_async((void *)dbias, bias->data, sbias, cudaMemcpyHostToDevice, s), "copy bias to device");
+    g.bias = dbias;
+    g.bias_stride = (int64_t)(bias->strides[0] / es);
+  }
+  // The fused epilogues add the bias themselves; the others get one pass.
+  numc_k::Gemm gk = g;
+  if (!numc_k::fuses_bias(plan.algo)) gk.bias = nullptr;
+  if ((err = run_plan(dt, plan, gk, scratch + off_w, ws_bytes, s))) return err;
+  if (g.bias && !gk.bias) {
+    cudaError_t be = numc_k::launch_bias_add(dt, g, s);
+    if (be != cudaSuccess) return cuda_fail(be, "bias add");
+  }
 
   if (ro) {
     out->residency = kDeviceOnly;
@@ -573,6 +593,118 @@ extern "C" int numc_matmul_naive(const NumcArray *a, const NumcArray *b, NumcArr
   if (a && (a->dtype == NUMC_DTYPE_FLOAT32 || a->dtype == NUMC_DTYPE_FLOAT64))
     param = numc_k::kFloatNaive;
   return matmul_impl(a, b, out, NUMC_CUDA_ALGO_SIMT, param);
+}
+
+// ---- numc_linear / numc_bmm (numc's ROADMAP.md, "Linear algebra") -------------
+
+extern "C" int numc_linear(const NumcArray *x, const NumcArray *w, const NumcArray *bias,
+                           NumcArray *out) {
+  if (bias) {
+    if (!x || !w || !out)
+      return NUMC_SET_ERROR(NUMC_ERR_NULL, "linear: NULL pointer (x=%p w=%p out=%p)",
+                            (const void *)x, (const void *)w, (const void *)out);
+    if (bias->dtype != x->dtype)
+      return NUMC_SET_ERROR(NUMC_ERR_TYPE, "linear: bias dtype %d differs from x dtype %d",
+                            bias->dtype, x->dtype);
+    if (bias->dim != 1 || w->dim != 2 || bias->shape[0] != w->shape[1])
+      return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "linear: bias must be 1-D of length N = %zu",
+                            w->dim == 2 ? w->shape[1] : (size_t)0);
+  }
+  return matmul_impl(x, w, out, NUMC_CUDA_ALGO_DEFAULT, -1, bias);
+}
+
+namespace {
+
+int check_bmm(const NumcArray *a, const NumcArray *b, const NumcArray *out) {
+  if (!a || !b || !out)
+    return NUMC_SET_ERROR(NUMC_ERR_NULL, "bmm: NULL pointer (a=%p b=%p out=%p)",
+                          (const void *)a, (const void *)b, (const void *)out);
+  if (a->dtype != b->dtype || a->dtype != out->dtype)
+    return NUMC_SET_ERROR(NUMC_ERR_TYPE, "bmm: dtype mismatch (a=%d b=%d out=%d)", a->dtype,
+                          b->dtype, out->dtype);
+  if (a->dim < 2 || a->dim != b->dim || a->dim != out->dim)
+    return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "bmm: ndim mismatch (a.dim=%zu b.dim=%zu out.dim=%zu)",
+                          a->dim, b->dim, out->dim);
+  const size_t d = a->dim;
+  for (size_t i = 0; i + 2 < d; i++)
+    if (a->shape[i] != b->shape[i] || a->shape[i] != out->shape[i])
+      return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "bmm: batch axis %zu differs", i);
+  if (a->shape[d - 1] != b->shape[d - 2])
+    return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "bmm: shape mismatch (a.shape[-1]=%zu b.shape[-2]=%zu)",
+                          a->shape[d - 1], b->shape[d - 2]);
+  if (out->shape[d - 2] != a->shape[d - 2] || out->shape[d - 1] != b->shape[d - 1])
+    return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "bmm: out shape (%zu, %zu) != (%zu, %zu)",
+                          out->shape[d - 2], out->shape[d - 1], a->shape[d - 2], b->shape[d - 1]);
+  return 0;
+}
+
+// numc_bmm: numc_matmul of every batch (the leading axes), one plan reused.
+int bmm_impl(const NumcArray *a, const NumcArray *b, NumcArray *out) {
+  int err = check_bmm(a, b, out);
+  if (err) return err;
+  const size_t d = a->dim;
+  const size_t M = a->shape[d - 2], K = a->shape[d - 1], N = b->shape[d - 1];
+  size_t P = 1;
+  for (size_t i = 0; i + 2 < d; i++) P *= a->shape[i];
+  if (P == 0 || M == 0 || N == 0) return 0;
+  const NumcDType dt = a->dtype;
+  Plan plan;
+  if ((err = resolve(dt, NUMC_CUDA_ALGO_DEFAULT, -1, M, K, N, &plan))) return err;
+  NumcCtx *ctx = out->ctx;
+  cudaStream_t s;
+  if ((err = ctx_stream(ctx, &s))) return err;
+  const size_t es = a->elem_size;
+  const bool ra = is_resident(a), rb = is_resident(b), ro = is_resident(out);
+  const size_t sa = array_span_bytes(a), sb = array_span_bytes(b), so = array_span_bytes(out);
+  const size_t off_b = align_up(ra ? 0 : sa, 256);
+  const size_t off_o = off_b + align_up(rb ? 0 : sb, 256);
+  const size_t off_w = off_o + align_up(ro ? 0 : so, 256);
+  const size_t ws_bytes = plan_workspace(plan, M, K, N);
+  char *scratch = nullptr;
+  if ((err = ctx_scratch(ctx, off_w + ws_bytes + 256, s, &scratch))) return err;
+  const char *da = ra ? a->dev_base : scratch;
+  const char *db = rb ? b->dev_base : scratch + off_b;
+  char *dout = ro ? out->dev_base : scratch + off_o;
+  if (!ra && sa) CU(xfer_async((void *)da, a->data, sa, cudaMemcpyHostToDevice, s), "copy a to device");
+  if (!rb && sb) CU(xfer_async((void *)db, b->data, sb, cudaMemcpyHostToDevice, s), "copy b to device");
+  if (!ro && so > out->capacity)
+    CU(xfer_async(dout, out->data, so, cudaMemcpyHostToDevice, s), "copy out to device");
+  for (size_t p = 0; p < P; p++) {
+    size_t rem = p, oa = 0, ob = 0, oo = 0;   // byte offsets of batch p
+    for (size_t i = d - 2; i-- > 0;) {
+      const size_t q = rem % a->shape[i];
+      rem /= a->shape[i];
+      oa += q * a->strides[i];
+      ob += q * b->strides[i];
+      oo += q * out->strides[i];
+    }
+    numc_k::Gemm g;
+    g.a = da + oa; g.b = db + ob; g.c = dout + oo;
+    g.M = M; g.K = K; g.N = N;
+    g.rsa = a->strides[d - 2] / es; g.csa = a->strides[d - 1] / es;
+    g.rsb = b->strides[d - 2] / es; g.csb = b->strides[d - 1] / es;
+    g.rso = out->strides[d - 2] / es; g.cso = out->strides[d - 1] / es;
+    if ((err = run_plan(dt, plan, g, scratch + off_w, ws_bytes, s))) return err;
+  }
+  if (ro) {
+    out->residency = kDeviceOnly;
+    if (!ra || !rb) CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  } else {
+    CU(xfer_async(out->data, dout, so, cudaMemcpyDeviceToHost, s), "copy out to host");
+    CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  }
+  if (plan.algo != NUMC_CUDA_ALGO_SIMT && plan.algo != NUMC_CUDA_ALGO_DMMA) {
+    unsigned st = 0;
+    CU(numc_k::read_and_clear_status(&st, s), "status read");
+    if (st) return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "bmm kernel abandoned a bounded wait (code %u)", st);
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int numc_bmm(const NumcArray *a, const NumcArray *b, NumcArray *out) {
+  return bmm_impl(a, b, out);
 }
 
 namespace {

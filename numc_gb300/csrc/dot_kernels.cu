@@ -247,50 +247,3 @@ cudaError_t launch_dot_1d(NumcDType dt, const void *a, int64_t sa, const void *b
 
 }  // namespace numc_k
 
-// ---- device gather (resident numc_array_copy / numc_array_contiguous) --------
-
-namespace numc_k {
-namespace {
-
-template <typename W>
-__global__ void gather_kernel(const W *__restrict__ src, W *__restrict__ dst, DotNd ix,
-                              int64_t total) {
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    int64_t rem = e, so = 0;
-    for (int d = ix.dim - 1; d >= 0; d--) {
-      const int64_t q = rem % ix.shape[d];
-      rem /= ix.shape[d];
-      so += q * ix.xs[d];
-    }
-    dst[e] = src[so];
-  }
-}
-
-template <typename W>
-cudaError_t gather_t(const void *src, void *dst, const DotNd &ix, int64_t total,
-                     cudaStream_t s) {
-  const int64_t blocks = (total + 255) / 256;
-  gather_kernel<W><<<(unsigned)(blocks < 8192 ? blocks : 8192), 256, 0, s>>>(
-      (const W *)src, (W *)dst, ix, total);
-  count_launch();
-  return cudaGetLastError();
-}
-
-}  // namespace
-
-cudaError_t launch_gather(const void *src, void *dst, size_t elem_size, const DotNd &ix,
-                          cudaStream_t s) {
-  int64_t total = 1;
-  for (int d = 0; d < ix.dim; d++) total *= ix.shape[d];
-  if (total == 0) return cudaSuccess;
-  switch (elem_size) {
-  case 1: return gather_t<uint8_t>(src, dst, ix, total, s);
-  case 2: return gather_t<uint16_t>(src, dst, ix, total, s);
-  case 4: return gather_t<uint32_t>(src, dst, ix, total, s);
-  case 8: return gather_t<uint64_t>(src, dst, ix, total, s);
-  }
-  return cudaErrorInvalidValue;
-}
-
-}  // namespace numc_k

@@ -81,6 +81,8 @@ struct Fallback {
   const unsigned long long *flags_a, *flags_b;   // per 128 rows of A, per 64 columns of B
   unsigned long long gen;
   const unsigned *max_a, *max_b;   // scaled float16 planes: row / column maxima
+  const float *bias;                // numc_linear: added to each column, or null
+  int64_t bias_stride;
 };
 
 template <int BN, int STAGES, int PLANES, int FLUSH, int CTAS>
@@ -376,7 +378,9 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
           }
 #pragma unroll
           for (int j = 0; j < 32; j++)
-            if (n0 + c0 + j < N) C[(int64_t)row * rso + (int64_t)(n0 + c0 + j) * cso] = f[j];
+            if (n0 + c0 + j < N)
+              C[(int64_t)row * rso + (int64_t)(n0 + c0 + j) * cso] =
+                  fb.bias ? __fadd_rn(f[j], fb.bias[(int64_t)(n0 + c0 + j) * fb.bias_stride]) : f[j];
         }
       } else if (row < M) {
         if (F16) {
@@ -406,6 +410,13 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
               const int e = -(sa + (col < N ? f16_scale_exp(fb.max_b[col]) : 0));
               acc[j] = ldexpf(acc[j], e);
             }
+          }
+        }
+        if (fb.bias) {
+#pragma unroll
+          for (int j = 0; j < CW; j++) {
+            const int col = n0 + cbase + j;
+            if (col < N) acc[j] = __fadd_rn(acc[j], fb.bias[(int64_t)col * fb.bias_stride]);
           }
         }
         float *crow = C + (int64_t)row * rso;
@@ -588,6 +599,8 @@ cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, cons
   fb.gen = gen;
   fb.max_a = bufs.max_a;
   fb.max_b = bufs.max_b;
+  fb.bias = (const float *)g.bias;
+  fb.bias_stride = g.bias_stride;
   const int num_kb = (int)(L.Kp / kBK);
   if (CTAS == 1) {
     const int grid = std::min(tiles_m * tiles_n, sm_count());

@@ -17,7 +17,18 @@ struct Gemm {
   void *c;
   int64_t M, K, N;
   int64_t rsa, csa, rsb, csb, rso, cso;
+  // numc_linear: bias[j * bias_stride] added to column j of the product as
+  // numc's elementwise add would (floats: one rounding; integers: modulo
+  // 2^bits), folded into the store of the kernels that support it.
+  const void *bias = nullptr;
+  int64_t bias_stride = 1;
 };
+
+// Whether `algo` adds Gemm::bias in its own epilogue (else the caller runs
+// launch_bias_add after the GEMM).
+bool fuses_bias(int algo);
+// out[i, j] += bias[j] for an M x N output (the unfused form).
+cudaError_t launch_bias_add(NumcDType dt, const Gemm &g, cudaStream_t s);
 
 // int8/uint8 store rule applied by the SIMT integer kernel.
 enum Rule8 : int {

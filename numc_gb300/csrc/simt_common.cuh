@@ -136,6 +136,13 @@ __device__ __forceinline__ T add_rn(T a, T b) {
   if constexpr (std::is_same<T, float>::value) return __fadd_rn(a, b);
   else return __dadd_rn(a, b);
 }
+// numc's elementwise a + b in the dtype: rounded once for floats, modulo
+// 2^bits for integers.
+template <typename T>
+__device__ __forceinline__ T add_elem(T a, T b) {
+  if constexpr (std::is_floating_point<T>::value) return add_rn<T>(a, b);
+  else return (T)((uint64_t)(int64_t)a + (uint64_t)(int64_t)b);
+}
 // The _rn intrinsics are never contracted into a fused multiply-add.
 __device__ __forceinline__ float madd_unfused(float a, float b, float c) {
   return __fadd_rn(c, __fmul_rn(a, b));
@@ -307,6 +314,7 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
       T v;
       if constexpr (KIND == kByte) v = (T)dst[i][j];
       else v = (T)acc[i][j];
+      if (g.bias) v = add_elem<T>(v, ((const T *)g.bias)[gj * g.bias_stride]);
       C[gi * g.rso + gj * g.cso] = v;
     }
   }
@@ -354,6 +362,7 @@ __device__ __forceinline__ void float_edge_output(const Gemm &g, int64_t e, int6
       t = madd<T>(A[i * g.rsa + k * g.csa], B[k * g.rsb + j * g.csb], t);
     d = pc == 0 ? t : add_rn<T>(d, t);
   }
+  if (g.bias) d = add_elem<T>(d, ((const T *)g.bias)[j * g.bias_stride]);
   ((T *)g.c)[i * g.rso + j * g.cso] = d;
 }
 
