@@ -363,17 +363,22 @@ grouped_simt(const Prob *__restrict__ probs, const Tile *__restrict__ tiles) {
 }
 
 // numc's packed-path remainder tiles of the CUDA-core problems listed in
-// `probs_idx`, one block per problem.
+// `probs_idx`: 32 outputs per block (simt::kEdgeLanes lanes each), block b
+// belonging to the problem q with prefix[q] <= b < prefix[q + 1].
 __global__ void __launch_bounds__(256)
-grouped_float_edges(const Prob *__restrict__ probs, const int *__restrict__ probs_idx) {
-  const Prob &P = probs[probs_idx[blockIdx.x]];
+grouped_float_edges(const Prob *__restrict__ probs, const int *__restrict__ probs_idx,
+                    const long long *__restrict__ prefix, int nedge) {
+  const long long b = blockIdx.x;
+  const int q = find_problem(prefix, nedge, b);
+  const Prob &P = probs[probs_idx[q]];
   Gemm g;
   g.a = P.A; g.b = P.B; g.c = P.C;
   g.M = P.M; g.K = P.K; g.N = P.N;
   g.rsa = P.rsa; g.csa = P.csa; g.rsb = P.rsb; g.csb = P.csb; g.rso = P.rso; g.cso = P.cso;
   const int64_t r0 = simt::edge_row<float>(g.M), c0 = simt::edge_col<float>(g.N);
   const int64_t n = simt::float_edge_count<float>(g.M, g.N);
-  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) simt::float_edge_output<float>(g, e, r0, c0);
+  const int64_t e = (b - prefix[q]) * (256 / simt::kEdgeLanes) + threadIdx.x / simt::kEdgeLanes;
+  simt::float_edge_output<float>(g, e, e < n, r0, c0);
 }
 
 }  // namespace grouped
@@ -406,7 +411,9 @@ struct NumcCudaGemmPlan {
   Tile *d_tiles[kNumVar];
   int ntiles[kNumVar];
   int *d_edge_probs;              // CUDA-core problems with packed-path remainders
+  long long *d_edge_prefix;       // their block prefix (32 outputs a block)
   int n_edge_probs;
+  long long edge_jobs;
   unsigned long long *flags;      // all flag words and maxima (memset per run)
   size_t flags_bytes;
   unsigned long long gen;
@@ -554,7 +561,8 @@ int plan_enqueue(NumcCudaGemmPlan *p, cudaStream_t s, unsigned *kernels) {
     ++*kernels;
   }
   if (p->n_edge_probs) {
-    grouped_float_edges<<<p->n_edge_probs, 256, 0, s>>>(p->d_probs, p->d_edge_probs);
+    grouped_float_edges<<<(unsigned)p->edge_jobs, 256, 0, s>>>(p->d_probs, p->d_edge_probs,
+                                                               p->d_edge_prefix, p->n_edge_probs);
     if ((e = cudaGetLastError())) return fail(e, "grouped SIMT remainder tiles");
     ++*kernels;
   }
@@ -656,7 +664,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   for (size_t i : order) {
     const int v = p->variant[i];
     if (v < 0) continue;
-    if (v == kVarSimt && p->probs[i].K > 0 && numc_packed(p->probs[i]) &&
+    if (v == kVarSimt && simt::float_edges_needed<float>(p->probs[i].K) && numc_packed(p->probs[i]) &&
         simt::float_edge_count<float>(p->probs[i].M, p->probs[i].N) > 0)
       edge_idx.push_back((int)i);
     const int bn = v == kVarTc128 ? 128 : v == kVarTc64 ? 64 : kSimtBN;
@@ -681,7 +689,13 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
     prefix_max[q + 1] = prefix_max[q] + (long long)ga.x * ga.y + (long long)gb.x * gb.y;
   }
   p->max_jobs = p->f16 ? prefix_max.back() : 0;
-  if (p->split_jobs > 0x7FFFFFFFll || p->max_jobs > 0x7FFFFFFFll) {
+  std::vector<long long> edge_prefix(edge_idx.size() + 1, 0);
+  for (size_t q = 0; q < edge_idx.size(); q++) {
+    const Prob &P = p->probs[edge_idx[q]];
+    edge_prefix[q + 1] = edge_prefix[q] + (simt::float_edge_count<float>(P.M, P.N) + 31) / 32;
+  }
+  p->edge_jobs = edge_prefix.back();
+  if (p->split_jobs > 0x7FFFFFFFll || p->max_jobs > 0x7FFFFFFFll || p->edge_jobs > 0x7FFFFFFFll) {
     delete p;
     NUMC_SET_ERROR(NUMC_ERR_VALUE, "plan_create: too many split blocks");
     return nullptr;
@@ -695,6 +709,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   const size_t o_prefix = off; off = align_up(off + prefix.size() * sizeof(long long), 256);
   const size_t o_prefix_max = off; off = align_up(off + prefix_max.size() * sizeof(long long), 256);
   const size_t o_edges = off; off = align_up(off + edge_idx.size() * sizeof(int), 256);
+  const size_t o_edge_prefix = off; off = align_up(off + edge_prefix.size() * sizeof(long long), 256);
   size_t o_tiles[kNumVar];
   for (int v = 0; v < kNumVar; v++) {
     o_tiles[v] = off;
@@ -715,6 +730,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   p->d_prefix = (long long *)(p->dev + o_prefix);
   p->d_prefix_max = (long long *)(p->dev + o_prefix_max);
   p->d_edge_probs = (int *)(p->dev + o_edges);
+  p->d_edge_prefix = (long long *)(p->dev + o_edge_prefix);
   p->n_edge_probs = (int)edge_idx.size();
   for (int v = 0; v < kNumVar; v++) {
     p->d_tiles[v] = (Tile *)(p->dev + o_tiles[v]);
@@ -764,8 +780,10 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
       (e = cudaMemcpy(p->d_prefix_max, prefix_max.data(), prefix_max.size() * sizeof(long long),
                       cudaMemcpyHostToDevice)) ||
       (!edge_idx.empty() &&
-       (e = cudaMemcpy(p->d_edge_probs, edge_idx.data(), edge_idx.size() * sizeof(int),
-                       cudaMemcpyHostToDevice)))) {
+       ((e = cudaMemcpy(p->d_edge_probs, edge_idx.data(), edge_idx.size() * sizeof(int),
+                        cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(p->d_edge_prefix, edge_prefix.data(), edge_prefix.size() * sizeof(long long),
+                        cudaMemcpyHostToDevice))))) {
     numc_cuda_gemm_plan_free(p);
     fail(e, "plan upload");
     return nullptr;

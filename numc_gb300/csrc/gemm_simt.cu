@@ -18,19 +18,24 @@ __global__ void __launch_bounds__(kThreads) simt_gemm(Gemm g, int rule8) {
                                                (int64_t)blockIdx.x * BN);
 }
 
+// kEdgeLanes lanes per remainder output, 32 outputs per 256-thread block;
+// the loop bound is uniform over the block, so every warp reaches the
+// fold's shuffles together.
 template <typename T>
 __global__ void __launch_bounds__(256) float_edges(Gemm g, int64_t r0, int64_t c0, int64_t n) {
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * blockDim.x)
-    simt::float_edge_output<T>(g, e, r0, c0);
+  constexpr int64_t per_block = 256 / simt::kEdgeLanes;
+  for (int64_t e0 = (int64_t)blockIdx.x * per_block; e0 < n; e0 += (int64_t)gridDim.x * per_block) {
+    const int64_t e = e0 + threadIdx.x / simt::kEdgeLanes;
+    simt::float_edge_output<T>(g, e, e < n, r0, c0);
+  }
 }
 
 // numc's packed-path remainder tiles of g, after the GEMM kernel.
 template <typename T>
 cudaError_t launch_float_edges(const Gemm &g, cudaStream_t s) {
   const int64_t n = simt::float_edge_count<T>(g.M, g.N);
-  if (n == 0) return cudaSuccess;
-  const int64_t blocks = std::min<int64_t>((n + 255) / 256, 4096);
+  if (n == 0 || !simt::float_edges_needed<T>(g.K)) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((n + 31) / 32, 152 * 16);
   float_edges<T><<<(unsigned)blocks, 256, 0, s>>>(g, simt::edge_row<T>(g.M),
                                                  simt::edge_col<T>(g.N), n);
   count_launch();

@@ -338,33 +338,60 @@ template <typename T> __host__ __device__ inline int64_t edge_col(int64_t N) {
   return jc + ((N - jc) / NumcTiles<T>::NR) * NumcTiles<T>::NR;
 }
 
+// Lanes per remainder output: lane l of a group sums K blocks l, l + 8, ...
+constexpr int kEdgeLanes = 8;
+
 // Output e of the remainder set (rows >= r0: all columns; then rows < r0:
-// columns >= c0), computed by one thread.
+// columns >= c0), computed by a group of kEdgeLanes lanes of one warp: each
+// lane runs its K blocks as FMA chains from zero and the group folds the
+// block sums in K order (d = t0, then d = d + t1, ...) — numc's per-block
+// accumulation with the blocks computed in parallel.  Every lane of the
+// warp calls this with the same K (the fold shuffles across the warp);
+// `valid` is false for lanes past the last output.
 template <typename T>
-__device__ __forceinline__ void float_edge_output(const Gemm &g, int64_t e, int64_t r0,
+__device__ __forceinline__ void float_edge_output(const Gemm &g, int64_t e, bool valid, int64_t r0,
                                                   int64_t c0) {
-  int64_t i, j;
-  const int64_t nbottom = (g.M - r0) * g.N;
-  if (e < nbottom) {
-    i = r0 + e / g.N;
-    j = e % g.N;
-  } else {
-    const int64_t w = g.N - c0;
-    i = (e - nbottom) / w;
-    j = c0 + (e - nbottom) % w;
+  const int lane = threadIdx.x & 31, sub = lane & (kEdgeLanes - 1), base = lane & ~(kEdgeLanes - 1);
+  int64_t i = 0, j = 0;
+  if (valid) {
+    const int64_t nbottom = (g.M - r0) * g.N;
+    if (e < nbottom) {
+      i = r0 + e / g.N;
+      j = e % g.N;
+    } else {
+      const int64_t w = g.N - c0;
+      i = (e - nbottom) / w;
+      j = c0 + (e - nbottom) % w;
+    }
   }
-  const T *A = (const T *)g.a, *B = (const T *)g.b;
+  const T *A = (const T *)g.a + i * g.rsa, *B = (const T *)g.b + j * g.csb;
+  const int64_t nkb = (g.K + kNumcKC - 1) / kNumcKC;
   T d = T(0);
-  for (int64_t pc = 0; pc < g.K; pc += kNumcKC) {
-    const int64_t pe = min(pc + (int64_t)kNumcKC, g.K);
+  for (int64_t r = 0; r < nkb; r += kEdgeLanes) {
+    const int64_t kb = r + sub;
     T t = T(0);
-    for (int64_t k = pc; k < pe; k++)
-      t = madd<T>(A[i * g.rsa + k * g.csa], B[k * g.rsb + j * g.csb], t);
-    d = pc == 0 ? t : add_rn<T>(d, t);
+    if (valid && kb < nkb) {
+      const int64_t pc = kb * kNumcKC, pe = min(pc + (int64_t)kNumcKC, g.K);
+#pragma unroll 8
+      for (int64_t k = pc; k < pe; k++) t = madd<T>(A[k * g.csa], B[k * g.rsb], t);
+    }
+#pragma unroll
+    for (int q = 0; q < kEdgeLanes; q++) {
+      const T v = __shfl_sync(0xffffffffu, t, base + q);
+      if (r + q < nkb) d = r + q == 0 ? v : add_rn<T>(d, v);
+    }
   }
-  if (g.bias) d = add_elem<T>(d, ((const T *)g.bias)[j * g.bias_stride]);
-  ((T *)g.c)[i * g.rso + j * g.cso] = d;
+  if (valid && sub == 0) {
+    if (g.bias) d = add_elem<T>(d, ((const T *)g.bias)[j * g.bias_stride]);
+    ((T *)g.c)[i * g.rso + j * g.cso] = d;
+  }
 }
+
+// Remainder outputs exist only where the packed path ran more than one K
+// block: with K <= 256 every remainder output is a single FMA chain from
+// zero, which the tile kernel already produced.
+template <typename T>
+__host__ __device__ inline bool float_edges_needed(int64_t K) { return K > kNumcKC; }
 
 template <typename T>
 __host__ __device__ inline int64_t float_edge_count(int64_t M, int64_t N) {
