@@ -50,6 +50,11 @@ def _load():
         ci = ctypes.c_int
         lib.oracle_dot.argtypes = [ci, vp, ci, vp, vp, ci, vp, ci, vp, vp, ci, vp, ci, vp, vp]
         lib.oracle_dot.restype = ci
+        lib.oracle_rand_seed.argtypes = [ctypes.c_uint64, vp]
+        lib.oracle_rand_fill.argtypes = [ci, vp, i64, ci, vp]
+        lib.oracle_rand_fill.restype = ci
+        lib.oracle_rand_threads.argtypes = [ci, i64, ci]
+        lib.oracle_rand_threads.restype = ci
         _lib = lib
     return _lib
 
@@ -144,6 +149,38 @@ def dot(a, b, out=None):
     return out
 
 
+# numc's default seed for a thread that never called numc_manual_seed
+# (src/random/kernel.h:123-126)
+RAND_DEFAULT_SEED = 0xdeadbeefcafe1234
+
+
+def rand_seed(seed=RAND_DEFAULT_SEED):
+    """numc's four-lane xoshiro256** state after numc_manual_seed(seed), as
+    16 uint64 words in numc's layout (word * 4 + lane)."""
+    st = np.zeros(16, dtype=np.uint64)
+    _load().oracle_rand_seed(int(seed) & (2**64 - 1), st.ctypes.data)
+    return st
+
+
+def rand_threads(dtype, n, max_threads):
+    """numc's fill thread count (0: the single-threaded small path)."""
+    return _load().oracle_rand_threads(DTYPE_CODE[np.dtype(dtype).name], int(n), int(max_threads))
+
+
+def rand(dtype, shape, state, max_threads):
+    """numc_array_rand(shape, dtype) from `state` (updated in place, as
+    numc's thread-local state is) with numc's OpenMP maximum of
+    `max_threads` threads.  Returns the array."""
+    dt = np.dtype(dtype)
+    assert state.dtype == np.uint64 and state.size == 16 and state.flags.c_contiguous
+    out = np.empty(shape, dtype=dt)
+    rc = _load().oracle_rand_fill(DTYPE_CODE[dt.name], out.ctypes.data, out.size,
+                                  int(max_threads), state.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("oracle_rand_fill failed")
+    return out
+
+
 # -- the compiled reference ------------------------------------------------
 
 def reference_available():
@@ -172,6 +209,9 @@ def _load_ref():
         lib.numc_matmul_naive.restype = ctypes.c_int
         lib.numc_dot.argtypes = [vp, vp, vp]
         lib.numc_dot.restype = ctypes.c_int
+        lib.numc_manual_seed.argtypes = [ctypes.c_uint64]
+        lib.numc_array_rand.restype = vp
+        lib.numc_array_rand.argtypes = [vp, vp, ctypes.c_size_t, ctypes.c_int]
         _ref = lib
     return _ref
 
@@ -251,3 +291,40 @@ def ref_dot(a, b, perm_a=None, perm_b=None, perm_out=None):
         return np.ascontiguousarray(base.transpose(perm)).reshape(oshape)
     finally:
         lib.numc_ctx_free(ctx)
+
+
+def ref_rand_sequence(seed, calls, omp_threads):
+    """numc's own numc_array_rand over `calls` [(dtype, shape), ...] in one
+    thread after numc_manual_seed(seed) (no seeding if seed is None), with
+    numc's OpenMP maximum set to `omp_threads`.  Returns the arrays."""
+    import threading
+    lib = _load_ref()
+    gomp = ctypes.CDLL("libgomp.so.1")
+    result = {}
+
+    def body():
+        gomp.omp_set_num_threads(int(omp_threads))
+        if seed is not None:
+            lib.numc_manual_seed(int(seed) & (2**64 - 1))
+        ctx = lib.numc_ctx_create()
+        try:
+            outs = []
+            for dtype, shape in calls:
+                dt = np.dtype(dtype)
+                sh = (ctypes.c_size_t * len(shape))(*shape)
+                arr = lib.numc_array_rand(ctx, sh, len(shape), DTYPE_CODE[dt.name])
+                if not arr:
+                    raise RuntimeError("numc_array_rand failed")
+                out = np.empty(shape, dtype=dt)
+                ctypes.memmove(out.ctypes.data, lib.numc_array_data(arr), out.nbytes)
+                outs.append(out)
+            result["outs"] = outs
+        finally:
+            lib.numc_ctx_free(ctx)
+
+    # a fresh thread: numc's PRNG state is thread-local, so an unseeded
+    # sequence starts from numc's default seed
+    th = threading.Thread(target=body)
+    th.start()
+    th.join()
+    return result["outs"]

@@ -23,7 +23,8 @@ def build_oracle(force=False):
     src = os.path.join(HERE, "numc_oracle.c")
     micro = os.path.join(HERE, "numc_oracle_micro.c")
     dot = os.path.join(HERE, "numc_oracle_dot.c")
-    deps = [src, micro, dot, os.path.join(HERE, "numc_oracle_micro.h")]
+    rand = os.path.join(HERE, "numc_oracle_rand.c")
+    deps = [src, micro, dot, rand, os.path.join(HERE, "numc_oracle_micro.h")]
     if (not force and os.path.exists(ORACLE_SO)
             and os.path.getmtime(ORACLE_SO) >= max(os.path.getmtime(d) for d in deps)):
         return ORACLE_SO
@@ -38,7 +39,7 @@ def build_oracle(force=False):
                            "-o", micro_o])
     tmp = ORACLE_SO + ".tmp"
     subprocess.check_call(["gcc", *flags, "-fopenmp", "-shared",
-                           "-ffp-contract=off", src, dot, micro_o, "-o", tmp, "-lm"])
+                           "-ffp-contract=off", src, dot, rand, micro_o, "-o", tmp, "-lm"])
     os.replace(tmp, ORACLE_SO)
     return ORACLE_SO
 
