@@ -94,6 +94,26 @@ NUMC_API int numc_cuda_array_is_resident(const NumcArray *arr);
 NUMC_API void *numc_cuda_ctx_stream(NumcCtx *ctx);
 NUMC_API int numc_cuda_ctx_synchronize(NumcCtx *ctx);
 
+/* --- random inputs generated in HBM (no numc counterpart) --------------- */
+
+/* numc_array_rand into a device-resident array: the same values and state
+ * advance as numc_array_rand, but the data stays in HBM (the host buffer is
+ * not written; numc_cuda_array_to_host copies it).  Asynchronous on the
+ * context's stream. */
+NUMC_API NumcArray *numc_cuda_array_rand(NumcCtx *ctx, const size_t *shape,
+                                         size_t dim, NumcDType dtype);
+/* numc_array_rand's fill of n elements of `dtype` at device pointer `out`,
+ * enqueued on `stream` (a cudaStream_t); advances the calling thread's
+ * state.  The first fill on a device uploads the generator's 1 MiB jump
+ * tables there (cudaMalloc, kept until exit). */
+NUMC_API int numc_cuda_rand_fill(NumcDType dtype, void *out, size_t n,
+                                 void *stream);
+/* numc's OpenMP maximum thread count that the large-array layout follows
+ * (numc's omp_get_max_threads()); 0 restores the default: OMP_NUM_THREADS,
+ * else the number of online CPUs. */
+NUMC_API int numc_cuda_rand_set_threads(int threads);
+NUMC_API int numc_cuda_rand_threads(void);
+
 /* --- C-ABI GEMM on device pointers -------------------------------------- */
 
 /* Scratch bytes numc_cuda_gemm needs for this problem (0 for SIMT/DMMA). */

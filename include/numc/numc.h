@@ -8,6 +8,7 @@
 #include "numc/error.h"
 #include "numc/array.h"
 #include "numc/math.h"
+#include "numc/random.h"
 #include "numc/cuda.h"
 
 #endif /* NUMC_NUMC_H */

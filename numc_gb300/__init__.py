@@ -114,6 +114,12 @@ SIGNATURES = [
     ("numc_matmul_grouped", _I, [_VP, _VP, _VP, _SZ]),
     ("numc_cuda_sgemm_split_static", _I, [_VP, _VP, _VP, _SZ, _SZ, _SZ, _IP, _IP, _IP, _IP,
                                           _IP, _IP, _VP, _VP]),
+    ("numc_manual_seed", None, [ctypes.c_uint64]),
+    ("numc_array_rand", _VP, [_VP, _VP, _SZ, _I]),
+    ("numc_cuda_array_rand", _VP, [_VP, _VP, _SZ, _I]),
+    ("numc_cuda_rand_fill", _I, [_I, _VP, _SZ, _VP]),
+    ("numc_cuda_rand_set_threads", _I, [_I]),
+    ("numc_cuda_rand_threads", _I, []),
     ("numc_cuda_phase_timing", _I, [_I]),
     ("numc_cuda_phase_times", _I, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                    ctypes.POINTER(ctypes.c_uint64)]),
@@ -219,6 +225,15 @@ class Ctx:
     def fill(self, shape, dtype, value):
         v = np.array(value, dtype=dtype)
         return self._make(lib().numc_array_fill, shape, dtype, v.ctypes.data)
+
+    def rand(self, shape, dtype):
+        """numc_array_rand: numc's uniform values, generated on the GPU and
+        copied into the host buffer."""
+        return self._make(lib().numc_array_rand, shape, dtype)
+
+    def rand_device(self, shape, dtype):
+        """numc_cuda_array_rand: the same values, left resident in HBM."""
+        return self._make(lib().numc_cuda_array_rand, shape, dtype)
 
     def from_numpy(self, x):
         x = np.array(x, order="C")      # a C-contiguous copy; 0-D stays 0-D
@@ -370,6 +385,31 @@ def gemm(a, b, out, algo=ALGO_DEFAULT, param=-1, workspace=None, stream=None):
                               out.stride(0), out.stride(1), ws_ptr, ws_bytes,
                               stream.cuda_stream)
     return check(rc)
+
+
+def manual_seed(seed):
+    """numc_manual_seed for the calling thread."""
+    lib().numc_manual_seed(int(seed) & (2**64 - 1))
+
+
+def rand_set_threads(threads):
+    """numc's OpenMP maximum that the large-array rand layout follows (0: default)."""
+    check(lib().numc_cuda_rand_set_threads(int(threads)))
+
+
+def rand_threads():
+    return lib().numc_cuda_rand_threads()
+
+
+def rand_fill(t, stream=None):
+    """numc_cuda_rand_fill over a contiguous torch CUDA tensor (numc's dtype
+    of the same name; float32/float64 or an integer type)."""
+    import torch
+    assert t.is_contiguous()
+    dt = CODE[str(t.dtype).replace("torch.", "")]
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return check(lib().numc_cuda_rand_fill(dt, t.data_ptr(), t.numel(), stream.cuda_stream))
 
 
 def check_status(stream=None):

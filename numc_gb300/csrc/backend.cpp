@@ -1037,6 +1037,90 @@ extern "C" int numc_cuda_array_to_host(NumcArray *arr) {
 
 extern "C" uint64_t numc_cuda_transfer_bytes(void) { return g_transfer_bytes.load(); }
 
+// ---- numc_manual_seed / numc_array_rand (numc's src/random/random.c) --------
+
+extern "C" void numc_manual_seed(uint64_t seed) { numc_k::rand_seed(seed); }
+
+namespace {
+
+// A new array filled on the GPU, in its own device buffer, as numc's
+// numc_array_rand fills it (_rand_impl, random.c:279-296); `to_host` copies
+// it into the host buffer as well.
+NumcArray *rand_array(NumcCtx *ctx, const size_t *shape, size_t dim, NumcDType dtype,
+                      bool to_host) {
+  if (!ctx || !shape || dim == 0) {
+    NUMC_SET_ERROR(NUMC_ERR_NULL, "rand: NULL or invalid args (ctx=%p shape=%p dim=%zu)",
+                   (void *)ctx, (const void *)shape, dim);
+    return nullptr;
+  }
+  NumcArray *arr = numc_array_create(ctx, shape, dim, dtype);
+  if (!arr) return nullptr;
+  cudaStream_t s;
+  if (ctx_stream(ctx, &s)) return nullptr;
+  const size_t bytes = arr->capacity;
+  if (!arr->dev_base) {
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, align_up(bytes ? bytes : 1, 256));
+    if (e != cudaSuccess) {
+      cuda_fail(e, "cudaMalloc(array)");
+      return nullptr;
+    }
+    ctx->dev_allocs->push_back(DeviceAlloc{p, bytes, arr->pos});
+    arr->dev_base = (char *)p;
+  }
+  cudaError_t e = numc_k::rand_fill(dtype, arr->dev_base, arr->size, s);
+  if (e != cudaSuccess) {
+    cuda_fail(e, "rand fill");
+    return nullptr;
+  }
+  if (to_host) {
+    if (bytes && (e = xfer_async(arr->data, arr->dev_base, bytes, cudaMemcpyDeviceToHost, s)) !=
+                     cudaSuccess) {
+      cuda_fail(e, "copy to host");
+      return nullptr;
+    }
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) {
+      cuda_fail(e, "cudaStreamSynchronize");
+      return nullptr;
+    }
+    arr->residency = kBoth;
+  } else {
+    arr->residency = kDeviceOnly;
+  }
+  return arr;
+}
+
+}  // namespace
+
+extern "C" NumcArray *numc_array_rand(NumcCtx *ctx, const size_t *shape, size_t dim,
+                                      NumcDType dtype) {
+  return rand_array(ctx, shape, dim, dtype, true);
+}
+
+extern "C" NumcArray *numc_cuda_array_rand(NumcCtx *ctx, const size_t *shape, size_t dim,
+                                           NumcDType dtype) {
+  return rand_array(ctx, shape, dim, dtype, false);
+}
+
+extern "C" int numc_cuda_rand_fill(NumcDType dtype, void *out, size_t n, void *stream) {
+  if ((int)dtype < 0 || (int)dtype >= NUMC_DTYPE_COUNT)
+    return NUMC_SET_ERROR(NUMC_ERR_TYPE, "rand_fill: unknown dtype %d", (int)dtype);
+  if (!out && n) return NUMC_SET_ERROR(NUMC_ERR_NULL, "rand_fill: out is NULL");
+  if (device_count() <= 0)
+    return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "no CUDA device available (the GB300 backend has no CPU fallback)");
+  CU(numc_k::rand_fill(dtype, out, n, (cudaStream_t)stream), "rand fill");
+  return 0;
+}
+
+extern "C" int numc_cuda_rand_set_threads(int threads) {
+  if (threads < 0) return NUMC_SET_ERROR(NUMC_ERR_VALUE, "rand_set_threads: %d < 0", threads);
+  numc_k::rand_set_threads(threads);
+  return 0;
+}
+
+extern "C" int numc_cuda_rand_threads(void) { return numc_k::rand_threads(); }
+
+
 extern "C" void *numc_cuda_array_device_data(const NumcArray *arr) {
   return (arr && is_resident(arr)) ? arr->dev_base : nullptr;
 }

@@ -123,6 +123,16 @@ size_t ozaki_workspace(int64_t M, int64_t K, int64_t N, int slices);
 cudaError_t launch_ozaki(const Gemm &g, int slices, void *ws, size_t ws_bytes,
                          cudaStream_t s);
 
+// numc_array_rand's generator (rand.cu): numc's four-lane xoshiro256**
+// state of the calling host thread, and numc's OpenMP maximum thread count
+// (its large-array fill splits the stream by thread count).
+void rand_seed(uint64_t seed);
+int rand_threads();
+void rand_set_threads(int threads);
+// Fill n elements of dtype at device pointer `out` as numc_array_rand
+// would, and advance the calling thread's state as numc does.
+cudaError_t rand_fill(NumcDType dt, void *out, size_t n, cudaStream_t s);
+
 // Device-side status word set by kernels that give up on a bounded wait.
 cudaError_t read_and_clear_status(unsigned *status, cudaStream_t s);
 

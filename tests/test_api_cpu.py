@@ -135,6 +135,36 @@ def test_no_cpu_fallback():
         assert "no CUDA device" in nc.last_error()[1]
 
 
+def test_rand_validation():
+    # numc's _rand_impl (src/random/random.c:279-296; tests/random/test_rand.c:181-201)
+    L = nc.lib()
+    sh = (ctypes.c_size_t * 1)(4)
+    assert not L.numc_array_rand(None, sh, 1, 8)
+    assert nc.last_error()[0] == nc.ERR_NULL
+    with nc.Ctx() as ctx:
+        assert not L.numc_array_rand(ctx.ptr, None, 1, 8)
+        assert nc.last_error()[0] == nc.ERR_NULL
+        assert not L.numc_array_rand(ctx.ptr, sh, 0, 8)
+        assert nc.last_error()[0] == nc.ERR_NULL
+        assert not L.numc_cuda_array_rand(ctx.ptr, sh, 0, 8)
+        assert nc.last_error()[0] == nc.ERR_NULL
+    assert L.numc_cuda_rand_fill(99, None, 0, None) == nc.ERR_TYPE
+    assert nc.rand_threads() > 0
+    nc.rand_set_threads(7)
+    assert nc.rand_threads() == 7
+    nc.rand_set_threads(0)
+    assert nc.rand_threads() > 0
+    assert L.numc_cuda_rand_set_threads(-1) == nc.ERR_VALUE
+
+
+@pytest.mark.skipif(nc.device_count() > 0, reason="checks the no-GPU behaviour")
+def test_rand_no_cpu_fallback():
+    with nc.Ctx() as ctx:
+        sh = (ctypes.c_size_t * 1)(16)
+        assert not nc.lib().numc_array_rand(ctx.ptr, sh, 1, 8)
+        assert nc.last_error()[0] == nc.ERR_INTERNAL
+
+
 def test_algo_settings():
     orig = nc.get_algo("float64")
     try:
