@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip the side workloads")
-    ap.add_argument("--only", choices=["f64", "int", "grouped", "plain", "splitvar"],
+    ap.add_argument("--only", choices=["f64", "int", "grouped", "plain", "splitvar", "rand"],
                     help="run one side workload alone (for profiling) and print it")
     return ap.parse_args()
 
@@ -274,6 +274,8 @@ def main():
             part = int_workload(nc, torch, synth, dev)
         elif args.only == "grouped":
             part = grouped_workload(nc, torch, oracle, dev)
+        elif args.only == "rand":
+            part = rand_workload(nc, torch, oracle, dev)
         elif args.only == "splitvar":
             # the bfloat16-plane variants, two calls each (3 then 6 passes)
             a = torch.from_numpy(synth.normal(SEED, 3, (M, K), np.float32)).to(dev)
@@ -492,7 +494,59 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
     out["f64_4096"] = f64_workload(nc, torch, oracle, synth, dev)
     out["int_1024"] = int_workload(nc, torch, synth, dev)
     out["grouped"] = grouped_workload(nc, torch, oracle, dev)
+    out["rand"] = rand_workload(nc, torch, oracle, dev)
     return out
+
+
+def rand_workload(nc, torch, oracle, dev):
+    """numc_array_rand's fill in HBM: 64 Mi float32 (256 MiB) with numc's
+    per-thread layout for this host's thread count, bytes written per second
+    against the measured HBM copy bandwidth; bit-exact check against the
+    oracle on 4 Mi + 3 elements; the oracle's sequential fill (numc's own
+    cost structure: n steps generated, every lane skipped n steps) timed on
+    the host as the CPU baseline."""
+    threads = nc.rand_threads()
+    n = 64 << 20
+    t = torch.empty(n, dtype=torch.float32, device=dev)
+    nc.manual_seed(SEED)
+    for _ in range(3):
+        nc.rand_fill(t)
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    e0.record(s)
+    for _ in range(reps):
+        nc.rand_fill(t)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    del t
+    gbs = n * 4 / ms / 1e6
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    # bit-exact check against the oracle (same seed, same thread count)
+    m = (4 << 20) + 3
+    chk = torch.empty(m, dtype=torch.float32, device=dev)
+    nc.manual_seed(7)
+    nc.rand_fill(chk)
+    torch.cuda.synchronize()
+    st = oracle.rand_seed(7)
+    t0 = time.perf_counter()
+    want = oracle.rand("float32", (m,), st, threads)
+    cpu_s = time.perf_counter() - t0
+    exact = chk.cpu().numpy().tobytes() == want.tobytes()
+    return {"workload": f"float32 {n} elements (256 MiB), numc layout for {threads} threads",
+            "us": ms * 1e3, "gb_per_s": gbs,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": gbs / hbm, "algorithmic_bytes": n * 4,
+                         "kernel": "rand_fill_kernel<uint32_t,1,1,8>"},
+            "bitexact_vs_oracle": exact,
+            "cpu_baseline": {"value": m * 4 / cpu_s / 1e9, "unit": "GB/s", "cores": 1,
+                             "kind": "port", "sample": f"{m} float32 elements ({cpu_s:.2f} s)"}}
 
 
 def f64_workload(nc, torch, oracle, synth, dev):

@@ -328,21 +328,39 @@ bool use_pipeline(const Plan &plan, const NumcArray *a, const NumcArray *b, cons
   return M >= 1024 && K >= 64 && (double)M * K * N >= 4294967296.0;
 }
 
+cudaError_t xfer2d_async(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width,
+                         size_t height, cudaMemcpyKind kind, cudaStream_t s) {
+  g_transfer_bytes += width * height;
+  return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, kind, s);
+}
+
 // Host operands of a large split GEMM: the host copies overlap the work.
-// The copy-in stream sends B, then A panel by panel; the compute stream
-// splits B once it has arrived and each panel of A once that has, and
-// multiplies the panel; the copy-out stream returns each panel of C as soon
-// as its GEMM is done.  At 8192^3 on GB300 the serial order spends 2.4 ms
-// copying A and B in, 2.3 ms computing and 1.3 ms copying C out.
+// A moves in row panels and B in column panels, interleaved on the copy-in
+// stream (A0, B0, A1, B1, ...); the compute stream splits each panel once it
+// has arrived and multiplies every (row panel, column panel) pair as soon as
+// both are split; the copy-out stream returns each block of C as soon as its
+// GEMM is done.  The GEMMs thus start after two panels instead of after all
+// of B.  Every output's arithmetic is that of one device-resident call (the
+// float16 planes' scales are per row of A and per column of B), so the
+// results are identical.  B whose rows and columns are both strided moves
+// whole, as one column panel.
 int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, const Plan &plan,
                      cudaStream_t s) {
   NumcCtx *ctx = out->ctx;
   const size_t M = a->shape[0], K = a->shape[1], N = b->shape[1], es = 4;
   const size_t want = M >= 4096 ? 4 : 2;
   const size_t rows = align_up((M + want - 1) / want, 256);
-  const numc_k::SplitPipe pp = numc_k::split_pipe_layout(plan.algo, plan.param, M, K, N, rows);
-  const size_t sa = array_span_bytes(a), sb = array_span_bytes(b), so = array_span_bytes(out);
-  const size_t off_b = align_up(sa, 256), off_c = off_b + align_up(sb, 256);
+  const size_t sb0 = b->strides[0], sb1 = b->strides[1];
+  // 1: B's rows contiguous, 2: its columns contiguous, 0: neither
+  const int bmode = (sb1 == es && sb0 % es == 0 && sb0 >= N * es) ? 1
+                    : (sb0 == es && sb1 % es == 0 && sb1 >= K * es) ? 2 : 0;
+  const size_t bcols = (bmode && N >= 1024) ? align_up((N + want - 1) / want, 256) : N;
+  const numc_k::SplitPipe pp =
+      numc_k::split_pipe_layout(plan.algo, plan.param, M, K, N, rows, bcols);
+  const int na = pp.npanels, nb = pp.nbpanels;
+  const size_t sa = array_span_bytes(a), so = array_span_bytes(out);
+  const size_t sbytes = bmode ? K * N * es : array_span_bytes(b);
+  const size_t off_b = align_up(sa, 256), off_c = off_b + align_up(sbytes, 256);
   const size_t off_w = off_c + align_up(so, 256);
   char *scratch = nullptr;
   int err;
@@ -363,53 +381,102 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
     cleanup();
     return cuda_fail(e, what);
   };
-  // ev[0]: B copied; ev[1]: scratch free; ev[2 + p]: panel p of A copied;
-  // ev[2 + np + p]: panel p of C computed.
-  const int np = pp.npanels;
-  for (int i = 0; i < 2 + 2 * np; i++) {
+  // ev[0]: scratch free; ev[1 + p]: A panel p copied; ev[1 + na + q]: B
+  // panel q copied; ev[1 + na + nb + p nb + q]: block (p, q) of C computed.
+  for (int i = 0; i < 1 + na + nb + na * nb; i++) {
     cudaEvent_t e;
     cudaError_t ce = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     if (ce != cudaSuccess) return fail_cu(ce, "cudaEventCreate");
     ev.push_back(e);
   }
-  cudaEvent_t ev_b = ev[0];
+  auto ev_a = [&](int p) { return ev[1 + p]; };
+  auto ev_b = [&](int q) { return ev[1 + na + q]; };
+  auto ev_c = [&](int p, int q) { return ev[1 + na + nb + p * nb + q]; };
+  auto arows = [&](int p) { return std::min(rows, M - (size_t)p * rows); };
+  auto bcount = [&](int q) { return std::min(bcols, N - (size_t)q * bcols); };
+  // B column panel q on the device: compact K x nq (bmode 1 row-major,
+  // bmode 2 column-major), or all of B with its own strides (bmode 0).
+  auto b_panel = [&](int q, numc_k::Gemm *g) {
+    const size_t n0 = (size_t)q * bcols, nq = bcount(q);
+    if (bmode == 1) {
+      g->b = dB + K * n0 * es; g->rsb = (int64_t)nq; g->csb = 1;
+    } else if (bmode == 2) {
+      g->b = dB + K * n0 * es; g->rsb = 1; g->csb = (int64_t)K;
+    } else {
+      g->b = dB; g->rsb = (int64_t)(sb0 / es); g->csb = (int64_t)(sb1 / es);
+    }
+    g->N = (int64_t)nq;
+  };
   cudaError_t e;
   // The previous user of the scratch (the compute stream) must be done
   // before the copy-in stream overwrites it.
-  if ((e = cudaEventRecord(ev[1], s)) || (e = cudaStreamWaitEvent(cin, ev[1], 0)))
+  if ((e = cudaEventRecord(ev[0], s)) || (e = cudaStreamWaitEvent(cin, ev[0], 0)))
     return fail_cu(e, "stream order");
-  if ((e = xfer_async(dB, b->data, sb, cudaMemcpyHostToDevice, cin)) ||
-      (e = cudaEventRecord(ev_b, cin)))
-    return fail_cu(e, "copy b to device");
-  for (int p = 0; p < np; p++) {
-    const size_t r0 = (size_t)p * rows, r = std::min(rows, M - r0);
-    if ((e = xfer_async(dA + r0 * K * es, (const char *)a->data + r0 * K * es, r * K * es,
-                             cudaMemcpyHostToDevice, cin)) ||
-        (e = cudaEventRecord(ev[2 + p], cin)))
-      return fail_cu(e, "copy a panel to device");
+  for (int i = 0; i < std::max(na, nb); i++) {
+    if (i < na) {
+      const size_t r0 = (size_t)i * rows;
+      if ((e = xfer_async(dA + r0 * K * es, (const char *)a->data + r0 * K * es,
+                          arows(i) * K * es, cudaMemcpyHostToDevice, cin)) ||
+          (e = cudaEventRecord(ev_a(i), cin)))
+        return fail_cu(e, "copy an A panel to device");
+    }
+    if (i < nb) {
+      const size_t n0 = (size_t)i * bcols, nq = bcount(i);
+      if (bmode == 1)
+        e = xfer2d_async(dB + K * n0 * es, nq * es, (const char *)b->data + n0 * sb1, sb0,
+                         nq * es, K, cudaMemcpyHostToDevice, cin);
+      else if (bmode == 2)
+        e = xfer2d_async(dB + K * n0 * es, K * es, (const char *)b->data + n0 * sb1, sb1,
+                         K * es, nq, cudaMemcpyHostToDevice, cin);
+      else
+        e = xfer_async(dB, b->data, sbytes, cudaMemcpyHostToDevice, cin);
+      if (e || (e = cudaEventRecord(ev_b(i), cin))) return fail_cu(e, "copy a B panel to device");
+    }
   }
   numc_k::Gemm g;
   g.a = dA; g.b = dB; g.c = dC;
   g.M = M; g.K = K; g.N = N;
   g.rsa = K; g.csa = 1;
-  g.rsb = b->strides[0] / es; g.csb = b->strides[1] / es;
+  g.rsb = 0; g.csb = 0;
   g.rso = N; g.cso = 1;
   const unsigned long long gen = numc_k::split_pipe_gen();
-  if ((e = cudaStreamWaitEvent(s, ev_b, 0)) || (e = numc_k::split_pipe_b(pp, g, ws, gen, s)))
-    return fail_cu(e, "split of b");
-  for (int p = 0; p < np; p++) {
-    const size_t r0 = (size_t)p * rows, r = std::min(rows, M - r0);
+  auto gemm_block = [&](int p, int q) -> cudaError_t {
+    const size_t r0 = (size_t)p * rows, n0 = (size_t)q * bcols;
     numc_k::Gemm gp = g;
     gp.a = dA + r0 * K * es;
-    gp.c = dC + r0 * N * es;
-    gp.M = r;
-    cudaEvent_t done = ev[2 + np + p];
-    if ((e = cudaStreamWaitEvent(s, ev[2 + p], 0)) ||
-        (e = numc_k::split_pipe_panel(pp, p, gp, ws, gen, s)) || (e = cudaEventRecord(done, s)) ||
-        (e = cudaStreamWaitEvent(cout, done, 0)) ||
-        (e = xfer_async((char *)out->data + r0 * N * es, gp.c, r * N * es,
-                             cudaMemcpyDeviceToHost, cout)))
-      return fail_cu(e, "panel");
+    gp.M = (int64_t)arows(p);
+    b_panel(q, &gp);
+    gp.c = dC + (r0 * N + n0) * es;
+    cudaError_t ce;
+    if ((ce = numc_k::split_pipe_gemm(pp, p, q, gp, ws, gen, s)) ||
+        (ce = cudaEventRecord(ev_c(p, q), s)) || (ce = cudaStreamWaitEvent(cout, ev_c(p, q), 0)))
+      return ce;
+    char *hc = (char *)out->data + (r0 * N + n0) * es;
+    if (nb == 1)
+      return xfer_async(hc, gp.c, arows(p) * N * es, cudaMemcpyDeviceToHost, cout);
+    return xfer2d_async(hc, N * es, gp.c, N * es, bcount(q) * es, arows(p),
+                        cudaMemcpyDeviceToHost, cout);
+  };
+  for (int i = 0; i < std::max(na, nb); i++) {
+    if (i < na) {       // A panel i: split, then its blocks with the B panels before it
+      numc_k::Gemm gp = g;
+      gp.a = dA + (size_t)i * rows * K * es;
+      gp.M = (int64_t)arows(i);
+      if ((e = cudaStreamWaitEvent(s, ev_a(i), 0)) ||
+          (e = numc_k::split_pipe_a(pp, i, gp, ws, gen, s)))
+        return fail_cu(e, "split of an A panel");
+      for (int q = 0; q < std::min(i, nb); q++)
+        if ((e = gemm_block(i, q))) return fail_cu(e, "panel GEMM");
+    }
+    if (i < nb) {       // B panel i: split, then its blocks with the A panels so far
+      numc_k::Gemm gp = g;
+      b_panel(i, &gp);
+      if ((e = cudaStreamWaitEvent(s, ev_b(i), 0)) ||
+          (e = numc_k::split_pipe_b(pp, i, gp, ws, gen, s)))
+        return fail_cu(e, "split of a B panel");
+      for (int p = 0; p < std::min(i + 1, na); p++)
+        if ((e = gemm_block(p, i))) return fail_cu(e, "panel GEMM");
+    }
   }
   if ((e = cudaStreamSynchronize(cout)) || (e = cudaStreamSynchronize(s)))
     return fail_cu(e, "cudaStreamSynchronize");

@@ -12,7 +12,7 @@
 //      one grouped scale pass: row maxima of every A, column maxima of
 //      every B,
 //   3. one grouped split pass over every tensor-core problem (x -> two
-//      16-bit planes; a block binary-searches its problem in a prefix sum),
+//      16-bit planes; a block reads its problem from a job table),
 //   4. one persistent split tcgen05 kernel per tile width (128 or 64
 //      columns): each CTA walks a static share of the variant's tile list;
 //      the TMA ring, the MMA chunk stream and the TMEM buffers run on
@@ -67,54 +67,41 @@ struct Tile {
   int prob, m0, n0, pad;
 };
 
-// Problem owning job b: prefix[p] <= b < prefix[p + 1].
-__device__ __forceinline__ int find_problem(const long long *__restrict__ prefix, int nprob,
-                                            long long b) {
-  int lo = 0, hi = nprob - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (prefix[mid] <= b) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
-}
-
 // ---- grouped scale pass (float16 planes) -----------------------------------------
 
-// Block b handles scale job b of problem p = find_problem(b): the blocks of
+// Block b handles scale job jobs[b] = (problem p, job j of p): the blocks of
 // absmax_grid(M, K) over A's rows, then those of absmax_grid(N, K) over B's
 // columns.
 __global__ void __launch_bounds__(256)
-grouped_absmax(const Prob *__restrict__ probs, const long long *__restrict__ prefix,
-               int nprob) {
-  const long long b = blockIdx.x;
-  const int p = find_problem(prefix, nprob, b);
-  const Prob &P = probs[p];
-  long long j = b - prefix[p];
-  const dim3 ga = absmax_grid(P.M, P.K, P.split_mode_a);
+grouped_absmax(const Prob *__restrict__ probs, const int2 *__restrict__ jobs) {
+  const int2 job = jobs[blockIdx.x];
+  const Prob &P = probs[job.x];
+  long long j = job.y;
+  const int ma = absmax_mode(P.split_mode_a, P.csa);
+  const dim3 ga = absmax_grid(P.M, P.K, ma);
   const long long a_jobs = (long long)ga.x * ga.y;
   if (j < a_jobs) {
-    absmax_block(P.A, P.rsa, P.csa, P.M, P.K, P.split_mode_a, P.max_a, j % ga.x, j / ga.x);
+    absmax_block(P.A, P.rsa, P.csa, P.M, P.K, ma, P.max_a, j % ga.x, j / ga.x);
   } else {
     j -= a_jobs;
-    const dim3 gb = absmax_grid(P.N, P.K, P.split_mode_b);
-    absmax_block(P.B, P.csb, P.rsb, P.N, P.K, P.split_mode_b, P.max_b, j % gb.x, j / gb.x);
+    const int mb = absmax_mode(P.split_mode_b, P.rsb);
+    const dim3 gb = absmax_grid(P.N, P.K, mb);
+    absmax_block(P.B, P.csb, P.rsb, P.N, P.K, mb, P.max_b, j % gb.x, j / gb.x);
   }
 }
 
 // ---- grouped split pass --------------------------------------------------------
 
-// Block b handles split job b of problem p = find_problem(b): A tiles
+// Block b handles split job jobs[b] = (problem p, job j of p): A tiles
 // (ceil(M/32) x ceil(Kp/128)) come first, then B tiles.
 template <bool F16>
 __global__ void __launch_bounds__(256)
-grouped_split(const Prob *__restrict__ probs, const long long *__restrict__ prefix, int nprob,
+grouped_split(const Prob *__restrict__ probs, const int2 *__restrict__ jobs,
               unsigned long long gen) {
   __shared__ __align__(16) float tile[kSplitRows][kSplitK + 4];
-  const long long b = blockIdx.x;
-  const int p = find_problem(prefix, nprob, b);
-  const Prob &P = probs[p];
-  long long j = b - prefix[p];
+  const int2 job = jobs[blockIdx.x];
+  const Prob &P = probs[job.x];
+  long long j = job.y;
   const long long kt = (P.Kp + kSplitK - 1) / kSplitK;
   const long long a_jobs = (long long)((P.M + kSplitRows - 1) / kSplitRows) * kt;
   if (j < a_jobs) {
@@ -364,20 +351,19 @@ grouped_simt(const Prob *__restrict__ probs, const Tile *__restrict__ tiles) {
 
 // numc's packed-path remainder tiles of the CUDA-core problems listed in
 // `probs_idx`: 32 outputs per block (simt::kEdgeLanes lanes each), block b
-// belonging to the problem q with prefix[q] <= b < prefix[q + 1].
+// being block jobs[b].y of problem probs_idx[jobs[b].x].
 __global__ void __launch_bounds__(256)
 grouped_float_edges(const Prob *__restrict__ probs, const int *__restrict__ probs_idx,
-                    const long long *__restrict__ prefix, int nedge) {
-  const long long b = blockIdx.x;
-  const int q = find_problem(prefix, nedge, b);
-  const Prob &P = probs[probs_idx[q]];
+                    const int2 *__restrict__ jobs) {
+  const int2 job = jobs[blockIdx.x];
+  const Prob &P = probs[probs_idx[job.x]];
   Gemm g;
   g.a = P.A; g.b = P.B; g.c = P.C;
   g.M = P.M; g.K = P.K; g.N = P.N;
   g.rsa = P.rsa; g.csa = P.csa; g.rsb = P.rsb; g.csb = P.csb; g.rso = P.rso; g.cso = P.cso;
   const int64_t r0 = simt::edge_row<float>(g.M), c0 = simt::edge_col<float>(g.N);
   const int64_t n = simt::float_edge_count<float>(g.M, g.N);
-  const int64_t e = (b - prefix[q]) * (256 / simt::kEdgeLanes) + threadIdx.x / simt::kEdgeLanes;
+  const int64_t e = (int64_t)job.y * (256 / simt::kEdgeLanes) + threadIdx.x / simt::kEdgeLanes;
   simt::float_edge_output<float>(g, e, e < n, r0, c0);
 }
 
@@ -401,17 +387,17 @@ struct NumcCudaGemmPlan {
   size_t dev_bytes;
   CUtensorMap *d_tmaps;
   Prob *d_probs;
-  long long *d_prefix;
+  int2 *d_split_jobs;             // (problem, job) of each split block
   long long split_jobs;
   bool f16;                       // scaled float16 planes (else bfloat16)
-  long long *d_prefix_max;        // scale-pass job prefix (float16 planes)
+  int2 *d_max_jobs;               // (problem, job) of each scale block (float16 planes)
   long long max_jobs;
   int n_split_probs;
   Prob *d_split_probs;
   Tile *d_tiles[kNumVar];
   int ntiles[kNumVar];
   int *d_edge_probs;              // CUDA-core problems with packed-path remainders
-  long long *d_edge_prefix;       // their block prefix (32 outputs a block)
+  int2 *d_edge_jobs;              // (edge problem, block) of each remainder block
   int n_edge_probs;
   long long edge_jobs;
   unsigned long long *flags;      // all flag words and maxima (memset per run)
@@ -528,18 +514,17 @@ int plan_enqueue(NumcCudaGemmPlan *p, cudaStream_t s, unsigned *kernels) {
   if (p->flags_bytes && (e = cudaMemsetAsync(p->flags, 0, p->flags_bytes, s)))
     return fail(e, "plan flags");
   if (p->f16 && p->max_jobs > 0) {
-    grouped_absmax<<<(unsigned)p->max_jobs, 256, 0, s>>>(p->d_split_probs, p->d_prefix_max,
-                                                         p->n_split_probs);
+    grouped_absmax<<<(unsigned)p->max_jobs, 256, 0, s>>>(p->d_split_probs, p->d_max_jobs);
     if ((e = cudaGetLastError())) return fail(e, "grouped scale pass");
     ++*kernels;
   }
   if (p->split_jobs > 0) {
     if (p->f16)
-      grouped_split<true><<<(unsigned)p->split_jobs, 256, 0, s>>>(p->d_split_probs, p->d_prefix,
-                                                                  p->n_split_probs, p->gen);
+      grouped_split<true><<<(unsigned)p->split_jobs, 256, 0, s>>>(p->d_split_probs,
+                                                                  p->d_split_jobs, p->gen);
     else
-      grouped_split<false><<<(unsigned)p->split_jobs, 256, 0, s>>>(p->d_split_probs, p->d_prefix,
-                                                                   p->n_split_probs, p->gen);
+      grouped_split<false><<<(unsigned)p->split_jobs, 256, 0, s>>>(p->d_split_probs,
+                                                                   p->d_split_jobs, p->gen);
     if ((e = cudaGetLastError())) return fail(e, "grouped split");
     ++*kernels;
   }
@@ -562,7 +547,7 @@ int plan_enqueue(NumcCudaGemmPlan *p, cudaStream_t s, unsigned *kernels) {
   }
   if (p->n_edge_probs) {
     grouped_float_edges<<<(unsigned)p->edge_jobs, 256, 0, s>>>(p->d_probs, p->d_edge_probs,
-                                                               p->d_edge_prefix, p->n_edge_probs);
+                                                               p->d_edge_jobs);
     if ((e = cudaGetLastError())) return fail(e, "grouped SIMT remainder tiles");
     ++*kernels;
   }
@@ -673,43 +658,46 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
       for (int n0 = 0; n0 < p->probs[i].N; n0 += bn) tiles[v].push_back(Tile{(int)i, m0, n0, 0});
     if (v != kVarSimt) split_idx.push_back(i);
   }
-  std::vector<long long> prefix(split_idx.size() + 1, 0);
+  // Job tables: (problem, job within it) for every block of the scale,
+  // split and remainder passes, so a block finds its problem in one load.
+  std::vector<int2> split_jobs, max_jobs, edge_jobs;
   for (size_t q = 0; q < split_idx.size(); q++) {
     const Prob &P = p->probs[split_idx[q]];
     const long long kt = (P.Kp + kSplitK - 1) / kSplitK;
-    prefix[q + 1] = prefix[q] + ((P.M + kSplitRows - 1) / kSplitRows) * kt +
-                    ((P.N + kSplitRows - 1) / kSplitRows) * kt;
+    const long long n = ((P.M + kSplitRows - 1) / kSplitRows) * kt +
+                        ((P.N + kSplitRows - 1) / kSplitRows) * kt;
+    for (long long j = 0; j < n; j++) split_jobs.push_back(make_int2((int)q, (int)j));
+    if (p->f16) {
+      const dim3 ga = absmax_grid(P.M, P.K, absmax_mode(P.split_mode_a, P.csa));
+      const dim3 gb = absmax_grid(P.N, P.K, absmax_mode(P.split_mode_b, P.rsb));
+      const long long nm = (long long)ga.x * ga.y + (long long)gb.x * gb.y;
+      for (long long j = 0; j < nm; j++) max_jobs.push_back(make_int2((int)q, (int)j));
+    }
   }
-  p->split_jobs = prefix.back();
-  p->n_split_probs = (int)split_idx.size();
-  std::vector<long long> prefix_max(split_idx.size() + 1, 0);
-  for (size_t q = 0; q < split_idx.size() && p->f16; q++) {
-    const Prob &P = p->probs[split_idx[q]];
-    const dim3 ga = absmax_grid(P.M, P.K, P.split_mode_a), gb = absmax_grid(P.N, P.K, P.split_mode_b);
-    prefix_max[q + 1] = prefix_max[q] + (long long)ga.x * ga.y + (long long)gb.x * gb.y;
-  }
-  p->max_jobs = p->f16 ? prefix_max.back() : 0;
-  std::vector<long long> edge_prefix(edge_idx.size() + 1, 0);
   for (size_t q = 0; q < edge_idx.size(); q++) {
     const Prob &P = p->probs[edge_idx[q]];
-    edge_prefix[q + 1] = edge_prefix[q] + (simt::float_edge_count<float>(P.M, P.N) + 31) / 32;
+    const long long n = (simt::float_edge_count<float>(P.M, P.N) + 31) / 32;
+    for (long long j = 0; j < n; j++) edge_jobs.push_back(make_int2((int)q, (int)j));
   }
-  p->edge_jobs = edge_prefix.back();
+  p->split_jobs = (long long)split_jobs.size();
+  p->n_split_probs = (int)split_idx.size();
+  p->max_jobs = (long long)max_jobs.size();
+  p->edge_jobs = (long long)edge_jobs.size();
   if (p->split_jobs > 0x7FFFFFFFll || p->max_jobs > 0x7FFFFFFFll || p->edge_jobs > 0x7FFFFFFFll) {
     delete p;
     NUMC_SET_ERROR(NUMC_ERR_VALUE, "plan_create: too many split blocks");
     return nullptr;
   }
 
-  // One device block: tmaps | probs | split probs | prefix | tiles | flags | planes.
+  // One device block: tmaps | probs | split probs | job tables | tiles | flags | planes.
   size_t off = 0;
   const size_t o_tmaps = off; off = align_up(off + count * 2 * sizeof(CUtensorMap), 256);
   const size_t o_probs = off; off = align_up(off + count * sizeof(Prob), 256);
   const size_t o_sprobs = off; off = align_up(off + split_idx.size() * sizeof(Prob), 256);
-  const size_t o_prefix = off; off = align_up(off + prefix.size() * sizeof(long long), 256);
-  const size_t o_prefix_max = off; off = align_up(off + prefix_max.size() * sizeof(long long), 256);
+  const size_t o_split_jobs = off; off = align_up(off + split_jobs.size() * sizeof(int2), 256);
+  const size_t o_max_jobs = off; off = align_up(off + max_jobs.size() * sizeof(int2), 256);
   const size_t o_edges = off; off = align_up(off + edge_idx.size() * sizeof(int), 256);
-  const size_t o_edge_prefix = off; off = align_up(off + edge_prefix.size() * sizeof(long long), 256);
+  const size_t o_edge_jobs = off; off = align_up(off + edge_jobs.size() * sizeof(int2), 256);
   size_t o_tiles[kNumVar];
   for (int v = 0; v < kNumVar; v++) {
     o_tiles[v] = off;
@@ -727,10 +715,10 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   p->d_tmaps = (CUtensorMap *)(p->dev + o_tmaps);
   p->d_probs = (Prob *)(p->dev + o_probs);
   p->d_split_probs = (Prob *)(p->dev + o_sprobs);
-  p->d_prefix = (long long *)(p->dev + o_prefix);
-  p->d_prefix_max = (long long *)(p->dev + o_prefix_max);
+  p->d_split_jobs = (int2 *)(p->dev + o_split_jobs);
+  p->d_max_jobs = (int2 *)(p->dev + o_max_jobs);
   p->d_edge_probs = (int *)(p->dev + o_edges);
-  p->d_edge_prefix = (long long *)(p->dev + o_edge_prefix);
+  p->d_edge_jobs = (int2 *)(p->dev + o_edge_jobs);
   p->n_edge_probs = (int)edge_idx.size();
   for (int v = 0; v < kNumVar; v++) {
     p->d_tiles[v] = (Tile *)(p->dev + o_tiles[v]);
@@ -776,13 +764,16 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   if ((e = cudaMemcpy(p->d_tmaps, tm.data(), tm.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(p->d_probs, p->probs.data(), count * sizeof(Prob), cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(p->d_split_probs, sp.data(), sp.size() * sizeof(Prob), cudaMemcpyHostToDevice)) ||
-      (e = cudaMemcpy(p->d_prefix, prefix.data(), prefix.size() * sizeof(long long), cudaMemcpyHostToDevice)) ||
-      (e = cudaMemcpy(p->d_prefix_max, prefix_max.data(), prefix_max.size() * sizeof(long long),
-                      cudaMemcpyHostToDevice)) ||
+      (!split_jobs.empty() &&
+       (e = cudaMemcpy(p->d_split_jobs, split_jobs.data(), split_jobs.size() * sizeof(int2),
+                       cudaMemcpyHostToDevice))) ||
+      (!max_jobs.empty() &&
+       (e = cudaMemcpy(p->d_max_jobs, max_jobs.data(), max_jobs.size() * sizeof(int2),
+                       cudaMemcpyHostToDevice))) ||
       (!edge_idx.empty() &&
        ((e = cudaMemcpy(p->d_edge_probs, edge_idx.data(), edge_idx.size() * sizeof(int),
                         cudaMemcpyHostToDevice)) ||
-        (e = cudaMemcpy(p->d_edge_prefix, edge_prefix.data(), edge_prefix.size() * sizeof(long long),
+        (e = cudaMemcpy(p->d_edge_jobs, edge_jobs.data(), edge_jobs.size() * sizeof(int2),
                         cudaMemcpyHostToDevice))))) {
     numc_cuda_gemm_plan_free(p);
     fail(e, "plan upload");

@@ -524,11 +524,12 @@ cudaError_t split_operand(const SplitLayout &L, const float *src, int64_t rs_row
   if (grid.y > 65535) return cudaErrorInvalidConfiguration;
   const int mode = split_mode(src, rs_row, rs_k);
   if (L.f16) {
-    const dim3 rg = absmax_grid(R, K, mode);
+    const int amode = absmax_mode(mode, rs_k);
+    const dim3 rg = absmax_grid(R, K, amode);
     if (rg.y > 65535) return cudaErrorInvalidConfiguration;
     cudaError_t e = cudaMemsetAsync(maxbits, 0, (size_t)R * 4, s);
     if (e != cudaSuccess) return e;
-    absmax_rows_f32<<<rg, 256, 0, s>>>(src, rs_row, rs_k, R, K, mode, maxbits);
+    absmax_rows_f32<<<rg, 256, 0, s>>>(src, rs_row, rs_k, R, K, amode, maxbits);
     split_planes<2, true><<<grid, 256, 0, s>>>(src, rs_row, rs_k, R, K, L.Kp, planes, flags,
                                                flag_rows, gen, mode, maxbits);
     count_launch(2);
@@ -732,7 +733,7 @@ cudaError_t launch_split_f16(const Gemm &g, int flush, void *ws_v, size_t ws_byt
 // ---- row-panel pipeline ---------------------------------------------------------
 
 SplitPipe split_pipe_layout(int algo, int param, int64_t M, int64_t K, int64_t N,
-                            int64_t panel_rows) {
+                            int64_t panel_rows, int64_t bpanel_cols) {
   SplitPipe p;
   p.f16 = algo == NUMC_CUDA_ALGO_SPLIT_FP16;
   p.planes = p.f16 ? 2 : planes_for(param);
@@ -741,11 +742,13 @@ SplitPipe split_pipe_layout(int algo, int param, int64_t M, int64_t K, int64_t N
   p.Kp = round_up(K > 0 ? K : 1, kBK);
   p.panel_rows = panel_rows;
   p.npanels = (int)((M + panel_rows - 1) / panel_rows);
-  // B region: planes, flags, maxima
-  size_t off = (size_t)round_up(p.planes * N * p.Kp * 2, 256);
-  off += (size_t)round_up(((N + 63) / 64) * 8, 256);
-  if (p.f16) off += (size_t)round_up(N * 4, 256);
-  p.panel_off = off;
+  p.bpanel_cols = bpanel_cols;
+  p.nbpanels = (int)((N + bpanel_cols - 1) / bpanel_cols);
+  // one region per column panel of B: planes, flags, maxima
+  p.bregion_bytes = (size_t)round_up(p.planes * bpanel_cols * p.Kp * 2, 256) +
+                    (size_t)round_up(((bpanel_cols + 63) / 64) * 8, 256) +
+                    (p.f16 ? (size_t)round_up(bpanel_cols * 4, 256) : 0);
+  p.panel_off = p.nbpanels * p.bregion_bytes;
   p.panel_bytes = (size_t)round_up(p.planes * panel_rows * p.Kp * 2, 256) +
                   (size_t)round_up(((panel_rows + kBM - 1) / kBM) * 8, 256) +
                   (p.f16 ? (size_t)round_up(panel_rows * 4, 256) : 0);
@@ -761,13 +764,13 @@ SplitLayout pipe_params(const SplitPipe &p) {
   return L;
 }
 
-SplitBufs pipe_bufs(const SplitPipe &p, int panel, char *ws) {
+SplitBufs pipe_bufs(const SplitPipe &p, int panel, int bpanel, char *ws) {
   SplitBufs b;
-  char *q = ws;
+  char *q = ws + (size_t)(bpanel < 0 ? 0 : bpanel) * p.bregion_bytes;
   b.pb = (uint16_t *)q;
-  q += round_up(p.planes * p.N * p.Kp * 2, 256);
+  q += round_up(p.planes * p.bpanel_cols * p.Kp * 2, 256);
   b.flags_b = (unsigned long long *)q;
-  q += round_up(((p.N + 63) / 64) * 8, 256);
+  q += round_up(((p.bpanel_cols + 63) / 64) * 8, 256);
   b.max_b = p.f16 ? (unsigned *)q : nullptr;
   q = ws + p.panel_off + (size_t)(panel < 0 ? 0 : panel) * p.panel_bytes;
   b.pa = (uint16_t *)q;
@@ -779,22 +782,28 @@ SplitBufs pipe_bufs(const SplitPipe &p, int panel, char *ws) {
 }
 }  // namespace
 
-cudaError_t split_pipe_b(const SplitPipe &p, const Gemm &g, void *ws, unsigned long long gen,
-                         cudaStream_t s) {
-  return split_b(pipe_params(p), pipe_bufs(p, -1, (char *)ws), g, gen, s);
+cudaError_t split_pipe_b(const SplitPipe &p, int bpanel, const Gemm &g, void *ws,
+                         unsigned long long gen, cudaStream_t s) {
+  if (bpanel < 0 || bpanel >= p.nbpanels || g.N > p.bpanel_cols || g.N <= 0 || g.K <= 0)
+    return cudaErrorInvalidValue;
+  return split_b(pipe_params(p), pipe_bufs(p, -1, bpanel, (char *)ws), g, gen, s);
 }
 
-cudaError_t split_pipe_panel(const SplitPipe &p, int panel, const Gemm &g, void *ws,
-                             unsigned long long gen, cudaStream_t s) {
-  if (panel < 0 || panel >= p.npanels || g.M > p.panel_rows || g.M <= 0 || g.N <= 0 ||
-      g.K <= 0)
+cudaError_t split_pipe_a(const SplitPipe &p, int panel, const Gemm &g, void *ws,
+                         unsigned long long gen, cudaStream_t s) {
+  if (panel < 0 || panel >= p.npanels || g.M > p.panel_rows || g.M <= 0 || g.K <= 0)
+    return cudaErrorInvalidValue;
+  return split_a(pipe_params(p), pipe_bufs(p, panel, -1, (char *)ws), g, gen, s);
+}
+
+cudaError_t split_pipe_gemm(const SplitPipe &p, int panel, int bpanel, const Gemm &g, void *ws,
+                            unsigned long long gen, cudaStream_t s) {
+  if (panel < 0 || panel >= p.npanels || g.M > p.panel_rows || g.M <= 0 || bpanel < 0 ||
+      bpanel >= p.nbpanels || g.N > p.bpanel_cols || g.N <= 0 || g.K <= 0)
     return cudaErrorInvalidValue;
   unsigned *status = status_word();
   if (!status) return cudaErrorMemoryAllocation;
-  const SplitLayout L = pipe_params(p);
-  const SplitBufs b = pipe_bufs(p, panel, (char *)ws);
-  cudaError_t e = split_a(L, b, g, gen, s);
-  return e != cudaSuccess ? e : launch_gemm(L, b, g, gen, status, s);
+  return launch_gemm(pipe_params(p), pipe_bufs(p, panel, bpanel, (char *)ws), g, gen, status, s);
 }
 
 namespace {

@@ -93,19 +93,27 @@ size_t split_f16_workspace(int64_t M, int64_t K, int64_t N);
 struct SplitPipe {
   bool f16;
   int planes, flush;
-  int64_t M, K, N, Kp, panel_rows;
-  int npanels;
-  size_t panel_off, panel_bytes, total;
+  int64_t M, K, N, Kp, panel_rows, bpanel_cols;
+  int npanels, nbpanels;
+  size_t bregion_bytes, panel_off, panel_bytes, total;
 };
-// algo / param as resolved for numc_cuda_gemm (SPLIT_BF16 or SPLIT_FP16).
+// algo / param as resolved for numc_cuda_gemm (SPLIT_BF16 or SPLIT_FP16);
+// A in row panels of panel_rows, B in column panels of bpanel_cols (a
+// multiple of 256, or N for one panel).
 SplitPipe split_pipe_layout(int algo, int param, int64_t M, int64_t K, int64_t N,
-                            int64_t panel_rows);
+                            int64_t panel_rows, int64_t bpanel_cols);
 unsigned long long split_pipe_gen();
-cudaError_t split_pipe_b(const SplitPipe &p, const Gemm &g, void *ws, unsigned long long gen,
-                         cudaStream_t s);
-// g: the panel's rows of A and C (g.M = its row count), all of B.
-cudaError_t split_pipe_panel(const SplitPipe &p, int panel, const Gemm &g, void *ws,
-                             unsigned long long gen, cudaStream_t s);
+// g: B's column panel `bpanel` as its own K x g.N matrix (g.b, g.rsb, g.csb).
+cudaError_t split_pipe_b(const SplitPipe &p, int bpanel, const Gemm &g, void *ws,
+                         unsigned long long gen, cudaStream_t s);
+// g: A's row panel `panel` (g.a, g.M rows).
+cudaError_t split_pipe_a(const SplitPipe &p, int panel, const Gemm &g, void *ws,
+                         unsigned long long gen, cudaStream_t s);
+// The product of A's row panel `panel` and B's column panel `bpanel`, both
+// split: g.a / g.M the panel's rows, g.b / g.N the column panel as given to
+// split_pipe_b, g.c its block of C.
+cudaError_t split_pipe_gemm(const SplitPipe &p, int panel, int bpanel, const Gemm &g, void *ws,
+                            unsigned long long gen, cudaStream_t s);
 // float32 from scaled float16 planes (3 products); `flush` = K slabs per
 // TMEM accumulation chain (1, 2, 4, 8; 0 = default).
 cudaError_t launch_split_f16(const Gemm &g, int flush, void *ws, size_t ws_bytes,

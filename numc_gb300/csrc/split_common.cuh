@@ -52,6 +52,7 @@ __device__ __forceinline__ float scale_pow2(float x, int s) {
 // k < K, as float32 bits, merged into maxbits[r] with atomicMax (maxbits
 // starts at zero).  A 256-thread block covers
 //   mode 1 (k contiguous):    8 rows x 1024 k, one warp per row;
+//   mode 3 (k contiguous, rows not 16-byte aligned): the same, scalar loads;
 //   mode 2 (rows contiguous): 1024 rows x 64 k, 4 rows per thread;
 //   mode 0 (general):         256 rows x 64 k, one row per thread.
 constexpr int kMaxRows1 = 8, kMaxK1 = 1024, kMaxRows2 = 1024, kMaxK2 = 64, kMaxRows0 = 256,
@@ -65,7 +66,20 @@ __device__ __forceinline__ void absmax_block(const float *__restrict__ src, int6
                                              unsigned *__restrict__ maxbits, int64_t bk,
                                              int64_t br) {
   const int tid = threadIdx.x;
-  if (mode == 1) {
+  if (mode == 3) {
+    const int64_t r = br * kMaxRows1 + (tid >> 5);
+    const int64_t k0 = bk * kMaxK1;
+    const int lane = tid & 31;
+    unsigned m = 0;
+    if (r < R) {
+      const float *row = src + r * rs_row;
+      const int64_t k1 = k0 + kMaxK1 < K ? k0 + kMaxK1 : K;
+#pragma unroll 4
+      for (int64_t k = k0 + lane; k < k1; k += 32) m = max(m, absbits(row[k]));
+    }
+    m = __reduce_max_sync(0xffffffffu, m);
+    if (lane == 0 && r < R && m) atomicMax(&maxbits[r], m);
+  } else if (mode == 1) {
     const int64_t r = br * kMaxRows1 + (tid >> 5);
     const int64_t k0 = bk * kMaxK1;
     const int lane = tid & 31;
@@ -128,8 +142,9 @@ absmax_rows_f32(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int
 
 // Grid of absmax_rows_f32 for R rows, K columns, read mode `mode`.
 __host__ __device__ inline dim3 absmax_grid(int64_t R, int64_t K, int mode) {
-  const int64_t kk = mode == 1 ? kMaxK1 : mode == 2 ? kMaxK2 : kMaxK0;
-  const int64_t rr = mode == 1 ? kMaxRows1 : mode == 2 ? kMaxRows2 : kMaxRows0;
+  const bool rowwise = mode == 1 || mode == 3;
+  const int64_t kk = rowwise ? kMaxK1 : mode == 2 ? kMaxK2 : kMaxK0;
+  const int64_t rr = rowwise ? kMaxRows1 : mode == 2 ? kMaxRows2 : kMaxRows0;
   return dim3((unsigned)((K + kk - 1) / kk), (unsigned)((R + rr - 1) / rr));
 }
 
@@ -266,6 +281,13 @@ __device__ __forceinline__ void split_tile(const float *__restrict__ src, int64_
       *reinterpret_cast<uint2 *>(planes + p * plane_elems + off) = w;
     }
   }
+}
+
+// Read mode of the scale pass for a source of split mode `mode`: k-contiguous
+// rows that are not 16-byte aligned are read one warp per row (3), not one
+// thread per row.
+__host__ __device__ inline int absmax_mode(int mode, int64_t rs_k) {
+  return mode == 0 && rs_k == 1 ? 3 : mode;
 }
 
 // Read mode of a split source: 1 = k contiguous (float4 along k), 2 = rows
