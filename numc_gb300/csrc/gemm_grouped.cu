@@ -332,7 +332,10 @@ __host__ __device__ inline bool numc_packed(const Prob &P) {
   return (double)P.M * P.K * P.N > 96.0 * 96 * 96;
 }
 
-__global__ void __launch_bounds__(simt::kThreads)
+// One instantiation per kernel (the packed and the unpacked arithmetic in
+// one kernel needed 255 registers, half the occupancy of either alone).
+template <int KIND>
+__global__ void __launch_bounds__(simt::kThreads, 2)
 grouped_simt(const Prob *__restrict__ probs, const Tile *__restrict__ tiles) {
   const Tile tl = tiles[blockIdx.x];
   const Prob &P = probs[tl.prob];
@@ -340,13 +343,7 @@ grouped_simt(const Prob *__restrict__ probs, const Tile *__restrict__ tiles) {
   g.a = P.A; g.b = P.B; g.c = P.C;
   g.M = P.M; g.K = P.K; g.N = P.N;
   g.rsa = P.rsa; g.csa = P.csa; g.rsb = P.rsb; g.csb = P.csb; g.rso = P.rso; g.cso = P.cso;
-  // numc_matmul's arithmetic per problem: packed path above its gemmsup
-  // threshold (remainder tiles redone by grouped_float_edges), unpacked
-  // below — as the single-problem SIMT launcher.
-  if (numc_packed(P))
-    simt::simt_tile<float, kSimtBM, kSimtBN, 8, 8, 8, simt::kFloat>(g, 0, tl.m0, tl.n0);
-  else
-    simt::simt_tile<float, kSimtBM, kSimtBN, 8, 8, 8, simt::kFloatSmall>(g, 0, tl.m0, tl.n0);
+  simt::simt_tile<float, kSimtBM, kSimtBN, 8, 8, 8, KIND>(g, 0, tl.m0, tl.n0);
 }
 
 // numc's packed-path remainder tiles of the CUDA-core problems listed in
@@ -396,6 +393,7 @@ struct NumcCudaGemmPlan {
   Prob *d_split_probs;
   Tile *d_tiles[kNumVar];
   int ntiles[kNumVar];
+  int nsimt_packed;               // CUDA-core tiles of numc's packed path (listed first)
   int *d_edge_probs;              // CUDA-core problems with packed-path remainders
   int2 *d_edge_jobs;              // (edge problem, block) of each remainder block
   int n_edge_probs;
@@ -540,9 +538,16 @@ int plan_enqueue(NumcCudaGemmPlan *p, cudaStream_t s, unsigned *kernels) {
     if (e) return fail(e, "grouped split GEMM (64)");
     ++*kernels;
   }
-  if (p->ntiles[kVarSimt]) {
-    grouped_simt<<<p->ntiles[kVarSimt], simt::kThreads, 0, s>>>(p->d_probs, p->d_tiles[kVarSimt]);
+  if (p->nsimt_packed) {
+    grouped_simt<simt::kFloat><<<p->nsimt_packed, simt::kThreads, 0, s>>>(
+        p->d_probs, p->d_tiles[kVarSimt]);
     if ((e = cudaGetLastError())) return fail(e, "grouped SIMT");
+    ++*kernels;
+  }
+  if (p->ntiles[kVarSimt] > p->nsimt_packed) {
+    grouped_simt<simt::kFloatSmall><<<p->ntiles[kVarSimt] - p->nsimt_packed, simt::kThreads, 0,
+                                      s>>>(p->d_probs, p->d_tiles[kVarSimt] + p->nsimt_packed);
+    if ((e = cudaGetLastError())) return fail(e, "grouped SIMT (unpacked path)");
     ++*kernels;
   }
   if (p->n_edge_probs) {
@@ -643,7 +648,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   for (size_t i = 0; i < count; i++) order[i] = i;
   std::stable_sort(order.begin(), order.end(),
                    [&](size_t x, size_t y) { return p->probs[x].K > p->probs[y].K; });
-  std::vector<Tile> tiles[kNumVar];
+  std::vector<Tile> tiles[kNumVar], simt_small;
   std::vector<size_t> split_idx;
   std::vector<int> edge_idx;
   for (size_t i : order) {
@@ -654,10 +659,15 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
       edge_idx.push_back((int)i);
     const int bn = v == kVarTc128 ? 128 : v == kVarTc64 ? 64 : kSimtBN;
     const int bm = v == kVarSimt ? kSimtBM : kBM;
+    // CUDA-core problems on numc's unpacked path go to a list of their own
+    std::vector<Tile> &tl = (v == kVarSimt && !numc_packed(p->probs[i])) ? simt_small : tiles[v];
     for (int m0 = 0; m0 < p->probs[i].M; m0 += bm)
-      for (int n0 = 0; n0 < p->probs[i].N; n0 += bn) tiles[v].push_back(Tile{(int)i, m0, n0, 0});
+      for (int n0 = 0; n0 < p->probs[i].N; n0 += bn) tl.push_back(Tile{(int)i, m0, n0, 0});
     if (v != kVarSimt) split_idx.push_back(i);
   }
+  // the CUDA-core list: numc's packed-path problems, then the unpacked ones
+  p->nsimt_packed = (int)tiles[kVarSimt].size();
+  tiles[kVarSimt].insert(tiles[kVarSimt].end(), simt_small.begin(), simt_small.end());
   // Job tables: (problem, job within it) for every block of the scale,
   // split and remainder passes, so a block finds its problem in one load.
   std::vector<int2> split_jobs, max_jobs, edge_jobs;

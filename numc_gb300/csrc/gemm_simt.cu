@@ -12,8 +12,12 @@ namespace {
 
 using simt::kThreads;
 
+// Two CTAs per SM (at most 128 registers) except for the int8/uint8 kernel,
+// whose per-block store rule keeps 64 partial sums and 64 stored bytes per
+// thread.
 template <typename T, int BM, int BN, int BK, int TM, int TN, int KIND>
-__global__ void __launch_bounds__(kThreads) simt_gemm(Gemm g, int rule8) {
+__global__ void __launch_bounds__(kThreads, KIND == simt::kByte ? 1 : 2)
+simt_gemm(Gemm g, int rule8) {
   simt::simt_tile<T, BM, BN, BK, TM, TN, KIND>(g, rule8, (int64_t)blockIdx.y * BM,
                                                (int64_t)blockIdx.x * BN);
 }
