@@ -59,16 +59,33 @@ __host__ __device__ inline int64_t round_up(int64_t x, int64_t a) { return (x + 
 
 // ---- pass 1: split float32 into bf16 planes (split_common.cuh) -------------
 
-template <int PLANES, bool F16>
+template <int PLANES, bool F16, int MODE>
 __global__ void __launch_bounds__(256)
 split_planes(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_t R,
                int64_t K, int64_t Kp, uint16_t *__restrict__ planes,
-               unsigned long long *flags, int flag_rows, unsigned long long gen, int mode,
+               unsigned long long *flags, int flag_rows, unsigned long long gen,
                const unsigned *maxbits) {
   __shared__ __align__(16) float tile[kSplitRows][kSplitK + 4];
-  split_tile<PLANES, F16>(src, rs_row, rs_k, R, K, Kp, planes, flags, flag_rows, gen, mode,
-                          (int64_t)blockIdx.y * kSplitRows, (int64_t)blockIdx.x * kSplitK, tile,
-                          maxbits);
+  split_tile<PLANES, F16, MODE>(src, rs_row, rs_k, R, K, Kp, planes, flags, flag_rows, gen,
+                                MODE, (int64_t)blockIdx.y * kSplitRows,
+                                (int64_t)blockIdx.x * kSplitK, tile, maxbits);
+}
+
+// split_planes with the read mode as a template argument.
+template <int PLANES, bool F16>
+void launch_split_planes(dim3 grid, cudaStream_t s, int mode, const float *src, int64_t rs_row,
+                         int64_t rs_k, int64_t R, int64_t K, int64_t Kp, uint16_t *planes,
+                         unsigned long long *flags, int flag_rows, unsigned long long gen,
+                         const unsigned *maxbits) {
+  if (mode == 1)
+    split_planes<PLANES, F16, 1><<<grid, 256, 0, s>>>(src, rs_row, rs_k, R, K, Kp, planes,
+                                                      flags, flag_rows, gen, maxbits);
+  else if (mode == 2)
+    split_planes<PLANES, F16, 2><<<grid, 256, 0, s>>>(src, rs_row, rs_k, R, K, Kp, planes,
+                                                      flags, flag_rows, gen, maxbits);
+  else
+    split_planes<PLANES, F16, 0><<<grid, 256, 0, s>>>(src, rs_row, rs_k, R, K, Kp, planes,
+                                                      flags, flag_rows, gen, maxbits);
 }
 
 // ---- pass 2: the tcgen05 GEMM ------------------------------------------------
@@ -530,16 +547,16 @@ cudaError_t split_operand(const SplitLayout &L, const float *src, int64_t rs_row
     cudaError_t e = cudaMemsetAsync(maxbits, 0, (size_t)R * 4, s);
     if (e != cudaSuccess) return e;
     absmax_rows_f32<<<rg, 256, 0, s>>>(src, rs_row, rs_k, R, K, amode, maxbits);
-    split_planes<2, true><<<grid, 256, 0, s>>>(src, rs_row, rs_k, R, K, L.Kp, planes, flags,
-                                               flag_rows, gen, mode, maxbits);
+    launch_split_planes<2, true>(grid, s, mode, src, rs_row, rs_k, R, K, L.Kp, planes, flags,
+                                 flag_rows, gen, maxbits);
     count_launch(2);
   } else if (L.planes == 3) {
-    split_planes<3, false><<<grid, 256, 0, s>>>(src, rs_row, rs_k, R, K, L.Kp, planes, flags,
-                                                flag_rows, gen, mode, nullptr);
+    launch_split_planes<3, false>(grid, s, mode, src, rs_row, rs_k, R, K, L.Kp, planes, flags,
+                                  flag_rows, gen, nullptr);
     count_launch(1);
   } else {
-    split_planes<2, false><<<grid, 256, 0, s>>>(src, rs_row, rs_k, R, K, L.Kp, planes, flags,
-                                                flag_rows, gen, mode, nullptr);
+    launch_split_planes<2, false>(grid, s, mode, src, rs_row, rs_k, R, K, L.Kp, planes, flags,
+                                  flag_rows, gen, nullptr);
     count_launch(1);
   }
   return cudaGetLastError();

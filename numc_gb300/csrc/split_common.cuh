@@ -128,7 +128,9 @@ __device__ __forceinline__ void absmax_block(const float *__restrict__ src, int6
     unsigned m = 0;
     if (r < R) {
       const int64_t k1 = k0 + kMaxK0 < K ? k0 + kMaxK0 : K;
-      for (int64_t k = k0; k < k1; k++) m = max(m, absbits(src[r * rs_row + k * rs_k]));
+      const float *p = src + r * rs_row + k0 * rs_k;
+#pragma unroll 8
+      for (int64_t k = k0; k < k1; k++, p += rs_k) m = max(m, absbits(*p));
     }
     if (r < R && m) atomicMax(&maxbits[r], m);
   }
@@ -167,7 +169,9 @@ constexpr int kSplitRows = 32, kSplitK = 128;
 
 // One 32-row x 128-k tile at (r0, k0), executed by a 256-thread block;
 // `tile` is the block's shared staging buffer.
-template <int PLANES, bool F16 = false>
+// MODE >= 0 fixes the read mode at compile time (one read path per kernel,
+// fewer registers); -1 takes `mode` at run time (grouped passes).
+template <int PLANES, bool F16 = false, int MODE = -1>
 __device__ __forceinline__ void split_tile(const float *__restrict__ src, int64_t rs_row,
                                            int64_t rs_k, int64_t R, int64_t K, int64_t Kp,
                                            void *__restrict__ planes_v,
@@ -178,6 +182,7 @@ __device__ __forceinline__ void split_tile(const float *__restrict__ src, int64_
   uint16_t *planes = (uint16_t *)planes_v;
   const int tid = threadIdx.x;
   bool bad = false;
+  if (MODE >= 0) mode = MODE;
   if (mode == 1) {            // k contiguous, 16-byte aligned rows
 #pragma unroll
     for (int q = 0; q < 4; q++) {
@@ -216,6 +221,34 @@ __device__ __forceinline__ void split_tile(const float *__restrict__ src, int64_
       tile[rq + 1][k] = v.y;
       tile[rq + 2][k] = v.z;
       tile[rq + 3][k] = v.w;
+    }
+  } else if (rs_k == 1) {     // k contiguous, rows not 16-byte aligned
+    // thread: column k0 + tid % 128 of rows r0 + tid / 128 + 2q
+    const int k = tid % kSplitK, rr = tid / kSplitK;
+    const int64_t gk = k0 + k;
+    const float *p = src + (r0 + rr) * rs_row + gk;
+    float x[16];
+#pragma unroll
+    for (int q = 0; q < 16; q++)
+      x[q] = (r0 + rr + 2 * q < R && gk < K) ? p[2 * q * rs_row] : 0.0f;
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      bad |= !isfinite(x[q]);
+      tile[rr + 2 * q][k] = x[q];
+    }
+  } else if (rs_row == 1) {   // rows contiguous, k not 16-byte aligned
+    // thread: row r0 + tid % 32 of k0 + tid / 32 + 8q
+    const int r = tid % kSplitRows, kk = tid / kSplitRows;
+    const int64_t gr = r0 + r;
+    const float *p = src + gr + (k0 + kk) * rs_k;
+    float x[16];
+#pragma unroll
+    for (int q = 0; q < 16; q++)
+      x[q] = (gr < R && k0 + kk + 8 * q < K) ? p[8 * q * rs_k] : 0.0f;
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      bad |= !isfinite(x[q]);
+      tile[r][kk + 8 * q] = x[q];
     }
   } else {                    // general strides
     const bool kfast = rs_k == 1 || rs_row != 1;

@@ -79,3 +79,37 @@ def test_non_contiguous_a_takes_the_plain_path():
     finally:
         nc.set_algo("float32", *orig)
     np.testing.assert_array_equal(got, _device_result(a, b, nc.ALGO_SPLIT_FP16, 0))
+
+
+def test_pipeline_strided_b_moves_whole():
+    # B with strided rows and columns (every other column of a wider array):
+    # it moves as one column panel; results still equal the device call
+    M, K, N = 2048, 1024, 2304
+    a, b = synth.operands("normal", M, K, N, dtype="float32", seed=20)
+    wide = np.zeros((K, 2 * N), dtype=np.float32)
+    wide[:, ::2] = b
+    orig = nc.get_algo("float32")
+    nc.set_algo("float32", nc.ALGO_SPLIT_FP16)
+    try:
+        with nc.Ctx() as ctx:
+            A = ctx.from_numpy(a)
+            B = ctx.from_numpy(wide).slice(1, 0, 2 * N, 2)
+            assert B.shape == (K, N) and B.strides == (2 * N * 4, 8)
+            C = ctx.zeros((M, N), "float32")
+            nc.matmul(A, B, C)
+            got = C.numpy()
+    finally:
+        nc.set_algo("float32", *orig)
+    np.testing.assert_array_equal(got, _device_result(a, b, nc.ALGO_SPLIT_FP16, 0))
+
+
+@pytest.mark.parametrize("shape", [(4096, 512, 4096), (4608, 1024, 1100)],
+                         ids=lambda s: "x".join(map(str, s)))
+def test_pipeline_panel_grid(shape):
+    # four row panels of A, four (or two ragged) column panels of B
+    M, K, N = shape
+    a, b = synth.operands("uniform", M, K, N, dtype="float32", seed=21)
+    got = _host_result(a, b, nc.ALGO_SPLIT_FP16, 0)
+    np.testing.assert_array_equal(got, _device_result(a, b, nc.ALGO_SPLIT_FP16, 0))
+    got3 = _host_result(a, b, nc.ALGO_SPLIT_BF16, 3)
+    np.testing.assert_array_equal(got3, _device_result(a, b, nc.ALGO_SPLIT_BF16, 3))
