@@ -340,7 +340,9 @@ cudaError_t xfer2d_async(void *dst, size_t dpitch, const void *src, size_t spitc
 // has arrived and multiplies every (row panel, column panel) pair as soon as
 // both are split; the copy-out stream returns each block of C as soon as its
 // GEMM is done.  The GEMMs thus start after two panels instead of after all
-// of B.  Every output's arithmetic is that of one device-resident call (the
+// of B.  Consecutive block GEMMs alternate between the compute stream and a
+// second one, so a block's kernel starts on the SMs its predecessor leaves
+// idle (a 2048 x 2048 block is 64 tiles for 76 CTA pairs).  Every output's arithmetic is that of one device-resident call (the
 // float16 planes' scales are per row of A and per column of B), so the
 // results are identical.  B whose rows and columns are both strided moves
 // whole, as one column panel.
@@ -365,9 +367,10 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
   char *scratch = nullptr;
   int err;
   if ((err = ctx_scratch(ctx, off_w + pp.total + 256, s, &scratch))) return err;
-  cudaStream_t cin, cout;
+  cudaStream_t cin, cout, s2;
   if ((err = ctx_aux_stream(ctx, &ctx->copy_in, &cin))) return err;
   if ((err = ctx_aux_stream(ctx, &ctx->copy_out, &cout))) return err;
+  if ((err = ctx_aux_stream(ctx, &ctx->gemm2, &s2))) return err;
   char *dA = scratch, *dB = scratch + off_b, *dC = scratch + off_c, *ws = scratch + off_w;
 
   std::vector<cudaEvent_t> ev;
@@ -377,13 +380,15 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
   auto fail_cu = [&](cudaError_t e, const char *what) {
     cudaStreamSynchronize(cin);
     cudaStreamSynchronize(s);
+    cudaStreamSynchronize(s2);
     cudaStreamSynchronize(cout);
     cleanup();
     return cuda_fail(e, what);
   };
   // ev[0]: scratch free; ev[1 + p]: A panel p copied; ev[1 + na + q]: B
-  // panel q copied; ev[1 + na + nb + p nb + q]: block (p, q) of C computed.
-  for (int i = 0; i < 1 + na + nb + na * nb; i++) {
+  // panel q copied; ev[1 + na + nb + p nb + q]: block (p, q) of C computed;
+  // then A panel p split, then B panel q split.
+  for (int i = 0; i < 1 + 2 * (na + nb) + na * nb; i++) {
     cudaEvent_t e;
     cudaError_t ce = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
     if (ce != cudaSuccess) return fail_cu(ce, "cudaEventCreate");
@@ -392,6 +397,9 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
   auto ev_a = [&](int p) { return ev[1 + p]; };
   auto ev_b = [&](int q) { return ev[1 + na + q]; };
   auto ev_c = [&](int p, int q) { return ev[1 + na + nb + p * nb + q]; };
+  auto ev_sa = [&](int p) { return ev[1 + na + nb + na * nb + p]; };
+  auto ev_sb = [&](int q) { return ev[1 + 2 * na + nb + na * nb + q]; };
+  int nblock = 0;   // blocks issued so far: even ones on s, odd ones on s2
   auto arows = [&](int p) { return std::min(rows, M - (size_t)p * rows); };
   auto bcount = [&](int q) { return std::min(bcols, N - (size_t)q * bcols); };
   // B column panel q on the device: compact K x nq (bmode 1 row-major,
@@ -447,9 +455,11 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
     gp.M = (int64_t)arows(p);
     b_panel(q, &gp);
     gp.c = dC + (r0 * N + n0) * es;
+    cudaStream_t gs = (nblock++ % 2) ? s2 : s;
     cudaError_t ce;
-    if ((ce = numc_k::split_pipe_gemm(pp, p, q, gp, ws, gen, s)) ||
-        (ce = cudaEventRecord(ev_c(p, q), s)) || (ce = cudaStreamWaitEvent(cout, ev_c(p, q), 0)))
+    if ((ce = cudaStreamWaitEvent(gs, ev_sa(p), 0)) || (ce = cudaStreamWaitEvent(gs, ev_sb(q), 0)) ||
+        (ce = numc_k::split_pipe_gemm(pp, p, q, gp, ws, gen, gs)) ||
+        (ce = cudaEventRecord(ev_c(p, q), gs)) || (ce = cudaStreamWaitEvent(cout, ev_c(p, q), 0)))
       return ce;
     char *hc = (char *)out->data + (r0 * N + n0) * es;
     if (nb == 1)
@@ -463,7 +473,7 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
       gp.a = dA + (size_t)i * rows * K * es;
       gp.M = (int64_t)arows(i);
       if ((e = cudaStreamWaitEvent(s, ev_a(i), 0)) ||
-          (e = numc_k::split_pipe_a(pp, i, gp, ws, gen, s)))
+          (e = numc_k::split_pipe_a(pp, i, gp, ws, gen, s)) || (e = cudaEventRecord(ev_sa(i), s)))
         return fail_cu(e, "split of an A panel");
       for (int q = 0; q < std::min(i, nb); q++)
         if ((e = gemm_block(i, q))) return fail_cu(e, "panel GEMM");
@@ -472,13 +482,14 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
       numc_k::Gemm gp = g;
       b_panel(i, &gp);
       if ((e = cudaStreamWaitEvent(s, ev_b(i), 0)) ||
-          (e = numc_k::split_pipe_b(pp, i, gp, ws, gen, s)))
+          (e = numc_k::split_pipe_b(pp, i, gp, ws, gen, s)) || (e = cudaEventRecord(ev_sb(i), s)))
         return fail_cu(e, "split of a B panel");
       for (int p = 0; p < std::min(i + 1, na); p++)
         if ((e = gemm_block(p, i))) return fail_cu(e, "panel GEMM");
     }
   }
-  if ((e = cudaStreamSynchronize(cout)) || (e = cudaStreamSynchronize(s)))
+  if ((e = cudaStreamSynchronize(cout)) || (e = cudaStreamSynchronize(s)) ||
+      (e = cudaStreamSynchronize(s2)))
     return fail_cu(e, "cudaStreamSynchronize");
   cleanup();
   unsigned st = 0;
@@ -633,7 +644,7 @@ void ctx_release_device(NumcCtx *ctx, const ArenaPos *keep_upto) {
     ctx->scratch_bytes = 0;
     if (ctx->stream) cudaStreamDestroy((cudaStream_t)ctx->stream);
     ctx->stream = nullptr;
-    for (void **cs : {&ctx->copy_in, &ctx->copy_out}) {
+    for (void **cs : {&ctx->copy_in, &ctx->copy_out, &ctx->gemm2}) {
       if (*cs) {
         cudaStreamSynchronize((cudaStream_t)*cs);
         cudaStreamDestroy((cudaStream_t)*cs);

@@ -132,6 +132,7 @@ extern "C" NumcCtx *numc_ctx_create(void) {
   ctx->stream = nullptr;
   ctx->copy_in = nullptr;
   ctx->copy_out = nullptr;
+  ctx->gemm2 = nullptr;
   ctx->device = -1;
   ctx->scratch = nullptr;
   ctx->scratch_bytes = 0;
