@@ -340,9 +340,10 @@ cudaError_t xfer2d_async(void *dst, size_t dpitch, const void *src, size_t spitc
 // has arrived and multiplies every (row panel, column panel) pair as soon as
 // both are split; the copy-out stream returns each block of C as soon as its
 // GEMM is done.  The GEMMs thus start after two panels instead of after all
-// of B.  Consecutive block GEMMs alternate between the compute stream and a
-// second one, so a block's kernel starts on the SMs its predecessor leaves
-// idle (a 2048 x 2048 block is 64 tiles for 76 CTA pairs).  Every output's arithmetic is that of one device-resident call (the
+// of B.  The splits run on the compute stream and the block GEMMs alternate
+// between two more streams, so a split never queues behind a GEMM and a
+// block's kernel starts on the SMs its predecessor leaves idle (a 2048 x
+// 2048 block is 64 tiles for 76 CTA pairs).  Every output's arithmetic is that of one device-resident call (the
 // float16 planes' scales are per row of A and per column of B), so the
 // results are identical.  B whose rows and columns are both strided moves
 // whole, as one column panel.
@@ -367,10 +368,11 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
   char *scratch = nullptr;
   int err;
   if ((err = ctx_scratch(ctx, off_w + pp.total + 256, s, &scratch))) return err;
-  cudaStream_t cin, cout, s2;
+  cudaStream_t cin, cout, s2, s3;
   if ((err = ctx_aux_stream(ctx, &ctx->copy_in, &cin))) return err;
   if ((err = ctx_aux_stream(ctx, &ctx->copy_out, &cout))) return err;
   if ((err = ctx_aux_stream(ctx, &ctx->gemm2, &s2))) return err;
+  if ((err = ctx_aux_stream(ctx, &ctx->gemm3, &s3))) return err;
   char *dA = scratch, *dB = scratch + off_b, *dC = scratch + off_c, *ws = scratch + off_w;
 
   std::vector<cudaEvent_t> ev;
@@ -381,6 +383,7 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
     cudaStreamSynchronize(cin);
     cudaStreamSynchronize(s);
     cudaStreamSynchronize(s2);
+    cudaStreamSynchronize(s3);
     cudaStreamSynchronize(cout);
     cleanup();
     return cuda_fail(e, what);
@@ -399,7 +402,7 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
   auto ev_c = [&](int p, int q) { return ev[1 + na + nb + p * nb + q]; };
   auto ev_sa = [&](int p) { return ev[1 + na + nb + na * nb + p]; };
   auto ev_sb = [&](int q) { return ev[1 + 2 * na + nb + na * nb + q]; };
-  int nblock = 0;   // blocks issued so far: even ones on s, odd ones on s2
+  int nblock = 0;   // blocks issued so far: even ones on s2, odd ones on s3
   auto arows = [&](int p) { return std::min(rows, M - (size_t)p * rows); };
   auto bcount = [&](int q) { return std::min(bcols, N - (size_t)q * bcols); };
   // B column panel q on the device: compact K x nq (bmode 1 row-major,
@@ -455,7 +458,7 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
     gp.M = (int64_t)arows(p);
     b_panel(q, &gp);
     gp.c = dC + (r0 * N + n0) * es;
-    cudaStream_t gs = (nblock++ % 2) ? s2 : s;
+    cudaStream_t gs = (nblock++ % 2) ? s3 : s2;
     cudaError_t ce;
     if ((ce = cudaStreamWaitEvent(gs, ev_sa(p), 0)) || (ce = cudaStreamWaitEvent(gs, ev_sb(q), 0)) ||
         (ce = numc_k::split_pipe_gemm(pp, p, q, gp, ws, gen, gs)) ||
@@ -489,7 +492,7 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
     }
   }
   if ((e = cudaStreamSynchronize(cout)) || (e = cudaStreamSynchronize(s)) ||
-      (e = cudaStreamSynchronize(s2)))
+      (e = cudaStreamSynchronize(s2)) || (e = cudaStreamSynchronize(s3)))
     return fail_cu(e, "cudaStreamSynchronize");
   cleanup();
   unsigned st = 0;
@@ -644,7 +647,7 @@ void ctx_release_device(NumcCtx *ctx, const ArenaPos *keep_upto) {
     ctx->scratch_bytes = 0;
     if (ctx->stream) cudaStreamDestroy((cudaStream_t)ctx->stream);
     ctx->stream = nullptr;
-    for (void **cs : {&ctx->copy_in, &ctx->copy_out, &ctx->gemm2}) {
+    for (void **cs : {&ctx->copy_in, &ctx->copy_out, &ctx->gemm2, &ctx->gemm3}) {
       if (*cs) {
         cudaStreamSynchronize((cudaStream_t)*cs);
         cudaStreamDestroy((cudaStream_t)*cs);

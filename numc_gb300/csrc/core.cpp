@@ -133,6 +133,7 @@ extern "C" NumcCtx *numc_ctx_create(void) {
   ctx->copy_in = nullptr;
   ctx->copy_out = nullptr;
   ctx->gemm2 = nullptr;
+  ctx->gemm3 = nullptr;
   ctx->device = -1;
   ctx->scratch = nullptr;
   ctx->scratch_bytes = 0;

@@ -57,7 +57,7 @@ struct NumcCtx {
   bool pin_host;                      // page-lock arena blocks (GPU present)
   void *stream;                       // cudaStream_t, created lazily
   void *copy_in, *copy_out;           // copy streams of pipelined matmuls (lazy)
-  void *gemm2;                        // second GEMM stream of pipelined matmuls (lazy)
+  void *gemm2, *gemm3;                // GEMM streams of pipelined matmuls (lazy)
   int device;                         // device the stream belongs to
   void *scratch;                      // device scratch (staging, splits)
   size_t scratch_bytes;
