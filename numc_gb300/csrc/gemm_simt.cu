@@ -57,6 +57,33 @@ cudaError_t launch_tile(const Gemm &g, int rule8, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// SMs of the current device (cached per device).
+int sms() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  if (!cache[dev]) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 152;
+    cache[dev] = n;
+  }
+  return cache[dev];
+}
+
+// Square tile for a problem: the largest of `big`, big/2, ... 32 whose grid
+// still gives every SM a CTA (a 512 x 512 output is 16 tiles of 128 but 256
+// of 32).  Each output's arithmetic does not depend on the tile.
+template <typename T, int KIND, int BIG>
+cudaError_t launch_sized(const Gemm &g, int rule8, cudaStream_t s) {
+  int t = BIG;
+  while (t > 32 && ((g.M + t - 1) / t) * ((g.N + t - 1) / t) < sms()) t /= 2;
+  if constexpr (BIG >= 128)
+    if (t == 128) return launch_tile<T, 128, 128, 8, 8, KIND>(g, rule8, s);
+  if (t >= 64) return launch_tile<T, 64, 64, 4, 4, KIND>(g, rule8, s);
+  return launch_tile<T, 32, 32, 2, 2, KIND>(g, rule8, s);
+}
+
 }  // namespace
 
 int float_rule(NumcDType dt, const Gemm &g, int rule) {
@@ -70,28 +97,28 @@ cudaError_t launch_simt(NumcDType dt, const Gemm &g, int rule8, cudaStream_t s) 
   switch (dt) {
   case NUMC_DTYPE_FLOAT32:
     switch (float_rule(dt, g, rule8)) {
-    case kFloatNaive: return launch_tile<float, 128, 128, 8, 8, simt::kFloatUnfused>(g, 0, s);
-    case kFloatNumcSmall: return launch_tile<float, 128, 128, 8, 8, simt::kFloatSmall>(g, 0, s);
+    case kFloatNaive: return launch_sized<float, simt::kFloatUnfused, 128>(g, 0, s);
+    case kFloatNumcSmall: return launch_sized<float, simt::kFloatSmall, 128>(g, 0, s);
     default: {
-      cudaError_t e = launch_tile<float, 128, 128, 8, 8, simt::kFloat>(g, 0, s);
+      cudaError_t e = launch_sized<float, simt::kFloat, 128>(g, 0, s);
       return e != cudaSuccess || g.K == 0 ? e : launch_float_edges<float>(g, s);
     }
     }
   case NUMC_DTYPE_FLOAT64:
     switch (float_rule(dt, g, rule8)) {
-    case kFloatNaive: return launch_tile<double, 64, 64, 4, 4, simt::kFloatUnfused>(g, 0, s);
-    case kFloatNumcSmall: return launch_tile<double, 64, 64, 4, 4, simt::kFloatSmall>(g, 0, s);
+    case kFloatNaive: return launch_sized<double, simt::kFloatUnfused, 64>(g, 0, s);
+    case kFloatNumcSmall: return launch_sized<double, simt::kFloatSmall, 64>(g, 0, s);
     default: {
-      cudaError_t e = launch_tile<double, 64, 64, 4, 4, simt::kFloat>(g, 0, s);
+      cudaError_t e = launch_sized<double, simt::kFloat, 64>(g, 0, s);
       return e != cudaSuccess || g.K == 0 ? e : launch_float_edges<double>(g, s);
     }
     }
-  case NUMC_DTYPE_INT16: return launch_tile<int16_t, 128, 128, 8, 8, simt::kWrapInt>(g, 0, s);
-  case NUMC_DTYPE_UINT16: return launch_tile<uint16_t, 128, 128, 8, 8, simt::kWrapInt>(g, 0, s);
-  case NUMC_DTYPE_INT32: return launch_tile<int32_t, 128, 128, 8, 8, simt::kWrapInt>(g, 0, s);
-  case NUMC_DTYPE_UINT32: return launch_tile<uint32_t, 128, 128, 8, 8, simt::kWrapInt>(g, 0, s);
-  case NUMC_DTYPE_INT64: return launch_tile<int64_t, 64, 64, 4, 4, simt::kWrapInt>(g, 0, s);
-  case NUMC_DTYPE_UINT64: return launch_tile<uint64_t, 64, 64, 4, 4, simt::kWrapInt>(g, 0, s);
+  case NUMC_DTYPE_INT16: return launch_sized<int16_t, simt::kWrapInt, 128>(g, 0, s);
+  case NUMC_DTYPE_UINT16: return launch_sized<uint16_t, simt::kWrapInt, 128>(g, 0, s);
+  case NUMC_DTYPE_INT32: return launch_sized<int32_t, simt::kWrapInt, 128>(g, 0, s);
+  case NUMC_DTYPE_UINT32: return launch_sized<uint32_t, simt::kWrapInt, 128>(g, 0, s);
+  case NUMC_DTYPE_INT64: return launch_sized<int64_t, simt::kWrapInt, 64>(g, 0, s);
+  case NUMC_DTYPE_UINT64: return launch_sized<uint64_t, simt::kWrapInt, 64>(g, 0, s);
   case NUMC_DTYPE_INT8: return launch_tile<int8_t, 128, 128, 8, 8, simt::kByte>(g, rule8, s);
   case NUMC_DTYPE_UINT8: return launch_tile<uint8_t, 128, 128, 8, 8, simt::kByte>(g, rule8, s);
   }
