@@ -46,9 +46,8 @@ cudaError_t launch_float_edges(const Gemm &g, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-template <typename T, int BM, int BN, int TM, int TN, int KIND>
+template <typename T, int BM, int BN, int TM, int TN, int KIND, int BK = 8>
 cudaError_t launch_tile(const Gemm &g, int rule8, cudaStream_t s) {
-  constexpr int BK = 8;
   if (g.M == 0 || g.N == 0) return cudaSuccess;
   int64_t gx = (g.N + BN - 1) / BN, gy = (g.M + BM - 1) / BM;
   if (gy > 65535 || gx > 0x7FFFFFFF) return cudaErrorInvalidConfiguration;
