@@ -33,10 +33,13 @@
 //
 // Kernels: row/column absolute maxima (atomicMax on the bit patterns),
 // slicing into s K-major bf16 planes per operand (B transposed), and the
-// GEMM: one 128 x 64 output tile per CTA; warp 0 streams one (A_p, B_q)
+// GEMM: one 128 x 128 output tile per CTA; warp 0 streams one (A_p, B_q)
 // 64-deep slab pair per ring stage with TMA; warp 1 issues 4 tcgen05.mma
-// per stage into one of four TMEM buffers (one buffer per chunk); warps
-// 2-9 fold finished chunks into the int64 accumulators and store.
+// (M = N = 128) per stage into one of four TMEM buffers (one buffer per
+// chunk); warps 2-17 (four per TMEM lane quarter, 32 columns each) fold
+// finished chunks into the int64 accumulators and store.  (A 128 x 64 tile
+// fetched each slab pair for half the MMA work: 16 % tensor-active, bound by
+// the L2 -> shared-memory operand traffic.)
 // Non-finite inputs are flagged and their tiles recomputed with FP64 FMA
 // chains (numc's arithmetic).
 #include <cuda.h>
@@ -54,12 +57,12 @@
 namespace numc_k {
 namespace {
 
-constexpr int kBM = 128, kBN = 64, kBK = 64;
-constexpr int kStages = 8;
+constexpr int kBM = 128, kBN = 128, kBK = 64;
+constexpr int kStages = 6;             // 32 KiB a stage
 constexpr int kChunkSlabs = 4;         // 4 * 64 * 255^2 < 2^24
-constexpr int kAccWarps = 8;
+constexpr int kAccWarps = 16;          // 4 per TMEM lane quarter, 32 columns each
 constexpr int kThreads = 64 + 32 * kAccWarps;
-constexpr int kNumBuf = 4;             // 4 x 64 TMEM columns
+constexpr int kNumBuf = 4;             // 4 x 128 TMEM columns
 constexpr int kMaxSlices = 8;
 
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
@@ -299,10 +302,10 @@ ozaki_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
     }
     __syncwarp();
   } else {
-    constexpr int CW = kBN / 2;
-    const int quad = warp & 3, half = (warp - 2) >> 2;
+    constexpr int CW = kBN / 4;   // 32 columns per thread (the bit-drop group)
+    const int quad = warp & 3, quarter = (warp - 2) >> 2;
     const int row = m0 + quad * 32 + lane;
-    const int cbase = half * CW;
+    const int cbase = quarter * CW;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     long long acc[CW];
 #pragma unroll
@@ -337,12 +340,12 @@ ozaki_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
         if (!ok) break;
         tc::tc_fence_after();
 #pragma unroll
-        for (int c0 = 0; c0 < CW; c0 += 32) {
-          uint32_t r[32];
-          tc::tmem_ld_32x32b_x32(tmem + lane_off + buf * kBN + cbase + c0, r);
+        for (int c0 = 0; c0 < CW; c0 += 16) {   // 16 columns a load: fewer live registers
+          uint32_t r[16];
+          tc::tmem_ld_32x32b_x16(tmem + lane_off + buf * kBN + cbase + c0, r);
           tc::tmem_ld_wait();
 #pragma unroll
-          for (int j = 0; j < 32; j++) {
+          for (int j = 0; j < 16; j++) {
             const long long v = (long long)__float2int_rn(__uint_as_float(r[j]));  // exact
             acc[c0 + j] += sh == 0 ? v : (sh >= 63 ? 0 : ((v + (1ll << (sh - 1))) >> sh));
           }
