@@ -116,6 +116,119 @@ grouped_split(const Prob *__restrict__ probs, const int2 *__restrict__ jobs,
   }
 }
 
+// ---- fused scale and split (float16 planes, K up to kFusedMaxKp) -------------------
+
+// One block: kFusedRows rows of one operand (A's rows, or B's columns as the
+// rows of B^T) over the whole of K, staged in shared memory; the block
+// takes each row's largest magnitude (the scale pass's result, stored for
+// the GEMM's final rescale), then splits the rows into the two float16
+// planes — one read of the operand instead of two.  jobs[b] = (problem,
+// block), A's blocks first.  Problems with Kp above kFusedMaxKp use the
+// separate passes.
+constexpr int kFusedRows = 16, kFusedMaxKp = 1024;
+
+__global__ void __launch_bounds__(256)
+grouped_scale_split(const Prob *__restrict__ probs, const int2 *__restrict__ jobs,
+                    unsigned long long gen) {
+  extern __shared__ __align__(16) float rowbuf[];   // [kFusedRows][Kp]
+  const int2 job = jobs[blockIdx.x];
+  const Prob &P = probs[job.x];
+  const int a_blocks = (P.M + kFusedRows - 1) / kFusedRows;
+  const bool is_a = job.y < a_blocks;
+  const float *src = is_a ? P.A : P.B;
+  const int64_t rs_row = is_a ? P.rsa : P.csb, rs_k = is_a ? P.csa : P.rsb;
+  const int R = is_a ? P.M : P.N, K = P.K, Kp = P.Kp;
+  const int r0 = (is_a ? job.y : job.y - a_blocks) * kFusedRows;
+  uint16_t *planes = is_a ? P.pa : P.pb;
+  unsigned long long *flags = is_a ? P.flags_a : P.flags_b;
+  const int flag_rows = is_a ? kBM : 64;
+  unsigned *maxbits = is_a ? P.max_a : P.max_b;
+  const int tid = threadIdx.x;
+
+  // Load the rows (zero past K and past R), 16 threads a row.
+  bool bad = false;
+  if (rs_k == 1) {           // along k: 16 consecutive k a row per step
+    const int r = tid / 16, sub = tid % 16;
+    const float *p = src + (int64_t)(r0 + r) * rs_row;
+    const bool live = r0 + r < R;
+    for (int k = sub; k < Kp; k += 16 * 8) {
+      float x[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int kk = k + 16 * u;
+        x[u] = (live && kk < K) ? p[kk] : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int kk = k + 16 * u;
+        if (kk < Kp) {
+          bad |= !isfinite(x[u]);
+          rowbuf[r * Kp + kk] = x[u];
+        }
+      }
+    }
+  } else {                   // across rows: 16 consecutive rows per k
+    const int r = tid % 16, sub = tid / 16;
+    const float *p = src + (int64_t)(r0 + r) * rs_row;
+    const bool live = r0 + r < R;
+    for (int k = sub; k < Kp; k += 16 * 8) {
+      float x[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int kk = k + 16 * u;
+        x[u] = (live && kk < K) ? p[(int64_t)kk * rs_k] : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int kk = k + 16 * u;
+        if (kk < Kp) {
+          bad |= !isfinite(x[u]);
+          rowbuf[r * Kp + kk] = x[u];
+        }
+      }
+    }
+  }
+  if (__syncthreads_or(bad) && tid == 0) flags[r0 / flag_rows] = gen;
+
+  // Row maxima: the 16 threads of a row (one half-warp) reduce its k range.
+  const int r = tid / 16, sub = tid % 16;
+  unsigned m = 0;
+  for (int k = sub; k < Kp; k += 16) m = max(m, absbits(rowbuf[r * Kp + k]));
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  const bool live = r0 + r < R;
+  if (live && sub == 0) maxbits[r0 + r] = m;
+
+  // Split: thread (r, sub) converts k = 4 sub + 64 i .. +3 of row r.
+  if (live) {
+    const int sexp = f16_scale_exp(m);
+    const int64_t plane_elems = (int64_t)R * Kp;
+    for (int k = 4 * sub; k < Kp; k += 64) {
+      const float4 v = *reinterpret_cast<const float4 *>(&rowbuf[r * Kp + k]);
+      const float rem[4] = {v.x, v.y, v.z, v.w};
+      uint16_t out[kPlanes][4];
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        float x = isfinite(rem[t]) ? scale_pow2(rem[t], sexp) : 0.0f;
+#pragma unroll
+        for (int pl = 0; pl < kPlanes; pl++) {
+          const __half h = __float2half_rn(x);
+          out[pl][t] = __half_as_ushort(h);
+          x -= __half2float(h);
+        }
+      }
+      const int64_t off = (int64_t)(r0 + r) * Kp + k;
+#pragma unroll
+      for (int pl = 0; pl < kPlanes; pl++) {
+        uint2 w;
+        w.x = (uint32_t)out[pl][0] | ((uint32_t)out[pl][1] << 16);
+        w.y = (uint32_t)out[pl][2] | ((uint32_t)out[pl][3] << 16);
+        *reinterpret_cast<uint2 *>(planes + pl * plane_elems + off) = w;
+      }
+    }
+  }
+}
+
 // ---- persistent grouped split GEMM ----------------------------------------------
 
 template <int BN, int STAGES, int FLUSH>
@@ -388,6 +501,9 @@ struct NumcCudaGemmPlan {
   long long split_jobs;
   bool f16;                       // scaled float16 planes (else bfloat16)
   int2 *d_max_jobs;               // (problem, job) of each scale block (float16 planes)
+  int2 *d_fused_jobs;             // (problem, block) of the fused scale + split pass
+  long long fused_jobs;
+  int fused_smem;                 // its shared memory (kFusedRows x the largest Kp)
   long long max_jobs;
   int n_split_probs;
   Prob *d_split_probs;
@@ -514,6 +630,12 @@ int plan_enqueue(NumcCudaGemmPlan *p, cudaStream_t s, unsigned *kernels) {
   if (p->f16 && p->max_jobs > 0) {
     grouped_absmax<<<(unsigned)p->max_jobs, 256, 0, s>>>(p->d_split_probs, p->d_max_jobs);
     if ((e = cudaGetLastError())) return fail(e, "grouped scale pass");
+    ++*kernels;
+  }
+  if (p->fused_jobs > 0) {
+    grouped_scale_split<<<(unsigned)p->fused_jobs, 256, p->fused_smem, s>>>(
+        p->d_split_probs, p->d_fused_jobs, p->gen);
+    if ((e = cudaGetLastError())) return fail(e, "grouped scale and split");
     ++*kernels;
   }
   if (p->split_jobs > 0) {
@@ -670,9 +792,16 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   tiles[kVarSimt].insert(tiles[kVarSimt].end(), simt_small.begin(), simt_small.end());
   // Job tables: (problem, job within it) for every block of the scale,
   // split and remainder passes, so a block finds its problem in one load.
-  std::vector<int2> split_jobs, max_jobs, edge_jobs;
+  std::vector<int2> split_jobs, max_jobs, edge_jobs, fused_jobs;
+  int fused_kp = 0;
   for (size_t q = 0; q < split_idx.size(); q++) {
     const Prob &P = p->probs[split_idx[q]];
+    if (p->f16 && P.Kp <= kFusedMaxKp) {   // one fused scale + split pass
+      const long long n = (P.M + kFusedRows - 1) / kFusedRows + (P.N + kFusedRows - 1) / kFusedRows;
+      for (long long j = 0; j < n; j++) fused_jobs.push_back(make_int2((int)q, (int)j));
+      fused_kp = std::max(fused_kp, P.Kp);
+      continue;
+    }
     const long long kt = (P.Kp + kSplitK - 1) / kSplitK;
     const long long n = ((P.M + kSplitRows - 1) / kSplitRows) * kt +
                         ((P.N + kSplitRows - 1) / kSplitRows) * kt;
@@ -693,7 +822,10 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   p->n_split_probs = (int)split_idx.size();
   p->max_jobs = (long long)max_jobs.size();
   p->edge_jobs = (long long)edge_jobs.size();
-  if (p->split_jobs > 0x7FFFFFFFll || p->max_jobs > 0x7FFFFFFFll || p->edge_jobs > 0x7FFFFFFFll) {
+  p->fused_jobs = (long long)fused_jobs.size();
+  p->fused_smem = kFusedRows * fused_kp * 4;
+  if (p->split_jobs > 0x7FFFFFFFll || p->max_jobs > 0x7FFFFFFFll || p->edge_jobs > 0x7FFFFFFFll ||
+      p->fused_jobs > 0x7FFFFFFFll) {
     delete p;
     NUMC_SET_ERROR(NUMC_ERR_VALUE, "plan_create: too many split blocks");
     return nullptr;
@@ -706,6 +838,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   const size_t o_sprobs = off; off = align_up(off + split_idx.size() * sizeof(Prob), 256);
   const size_t o_split_jobs = off; off = align_up(off + split_jobs.size() * sizeof(int2), 256);
   const size_t o_max_jobs = off; off = align_up(off + max_jobs.size() * sizeof(int2), 256);
+  const size_t o_fused_jobs = off; off = align_up(off + fused_jobs.size() * sizeof(int2), 256);
   const size_t o_edges = off; off = align_up(off + edge_idx.size() * sizeof(int), 256);
   const size_t o_edge_jobs = off; off = align_up(off + edge_jobs.size() * sizeof(int2), 256);
   size_t o_tiles[kNumVar];
@@ -727,6 +860,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   p->d_split_probs = (Prob *)(p->dev + o_sprobs);
   p->d_split_jobs = (int2 *)(p->dev + o_split_jobs);
   p->d_max_jobs = (int2 *)(p->dev + o_max_jobs);
+  p->d_fused_jobs = (int2 *)(p->dev + o_fused_jobs);
   p->d_edge_probs = (int *)(p->dev + o_edges);
   p->d_edge_jobs = (int2 *)(p->dev + o_edge_jobs);
   p->n_edge_probs = (int)edge_idx.size();
@@ -762,7 +896,9 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
     }
   }
   // Kernel attributes are set here, not per run, so runs can be captured.
-  if ((e = prepare_tc<128, 3, kFlushBf16, false>()) || (e = prepare_tc<64, 4, kFlushBf16, false>()) ||
+  if ((e = cudaFuncSetAttribute(grouped_scale_split, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                kFusedRows * kFusedMaxKp * 4)) ||
+      (e = prepare_tc<128, 3, kFlushBf16, false>()) || (e = prepare_tc<64, 4, kFlushBf16, false>()) ||
       (e = prepare_tc<128, 3, kFlushF16, true>()) || (e = prepare_tc<64, 4, kFlushF16, true>()) ||
       !status_word()) {
     numc_cuda_gemm_plan_free(p);
@@ -779,6 +915,9 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
                        cudaMemcpyHostToDevice))) ||
       (!max_jobs.empty() &&
        (e = cudaMemcpy(p->d_max_jobs, max_jobs.data(), max_jobs.size() * sizeof(int2),
+                       cudaMemcpyHostToDevice))) ||
+      (!fused_jobs.empty() &&
+       (e = cudaMemcpy(p->d_fused_jobs, fused_jobs.data(), fused_jobs.size() * sizeof(int2),
                        cudaMemcpyHostToDevice))) ||
       (!edge_idx.empty() &&
        ((e = cudaMemcpy(p->d_edge_probs, edge_idx.data(), edge_idx.size() * sizeof(int),
