@@ -487,8 +487,27 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
     f1 = 2.0 * 512 ** 3
     ms_p = time_gemm(nc, torch, ta1, tb1, tc1, nc.ALGO_SIMT, 0, steps=200, warmup=10)
     ms_s = time_gemm(nc, torch, ta1, tb1, tc1, HEAD_ALGO, 0, steps=200, warmup=10)
+    # the same call through numc_matmul on host arrays (numc's own default:
+    # the CUDA-core kernel, numc's arithmetic), copies and sync included,
+    # beside numc's arithmetic on the host cores
+    with nc.Ctx() as ctx:
+        A1, B1, C1 = ctx.from_numpy(a1), ctx.from_numpy(b1), ctx.zeros((512, 512), "float32")
+        for _ in range(5):
+            nc.matmul(A1, B1, C1)
+        t0 = time.perf_counter()
+        for _ in range(50):
+            nc.matmul(A1, B1, C1)
+        e2e_us = (time.perf_counter() - t0) / 50 * 1e6
+        exact = C1.numpy().tobytes() == oracle.matmul(a1, b1).tobytes()
+    oracle.matmul(a1, b1)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        oracle.matmul(a1, b1)
+    cpu_us = (time.perf_counter() - t0) / 5 * 1e6
     out["f32_512"] = {"plain_tflops": f1 / ms_p / 1e9, "split_tflops": f1 / ms_s / 1e9,
                       "plain_us": ms_p * 1e3, "split_us": ms_s * 1e3,
+                      "e2e_numc_matmul_us": e2e_us, "e2e_bitexact_vs_numc": exact,
+                      "cpu_port_us": cpu_us, "cpu_cores": oracle.num_threads(),
                       "note": "L2-resident, latency-bound"}
 
     out["f64_4096"] = f64_workload(nc, torch, oracle, synth, dev)

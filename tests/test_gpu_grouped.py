@@ -199,3 +199,35 @@ def test_empty_and_degenerate_problems():
     plan.run()
     torch.cuda.synchronize()
     assert bool((o == 0).all())
+
+
+def test_f16_plan_across_the_fused_pass_limit():
+    # float16 plans scale and split problems with K <= 1024 in one fused
+    # pass, larger K in two; both kinds in one plan, tensor-core variant
+    # forced, one fused problem with an infinity (its tiles fall back to
+    # numc's FMA chains)
+    shapes = [(300, 1000, 200), (257, 1024, 130), (300, 1025, 200), (129, 1100, 64),
+              (64, 2000, 128), (100, 3, 70)]
+    probs = []
+    for i, (M, K, N) in enumerate(shapes):
+        a, b = synth.operands("normal", M, K, N, dtype="float32", seed=2000 + i)
+        if i == 1:
+            a[5, 17] = np.inf
+        probs.append((torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(),
+                      torch.full((M, N), float("nan"), device="cuda"), a, b))
+    plan = nc.GemmPlan([(p[0], p[1], p[2]) for p in probs], nc.ALGO_SPLIT_FP16, 128)
+    plan.run()
+    nc.check_status()
+    for i, (ta, tb, out, a, b) in enumerate(probs):
+        got = out.cpu().numpy()
+        ref = oracle.matmul(a, b)
+        fin = np.isfinite(ref)
+        np.testing.assert_array_equal(np.isfinite(got), fin)
+        np.testing.assert_array_equal(got[~fin], ref[~fin])   # same infinities / NaN pattern
+        if i == 1:
+            assert not fin[5].all()
+        rows = np.where(fin.all(axis=1))[0]
+        K = a.shape[1]
+        assert rel_err_vs_scale(got[rows], ref[rows], a[rows], b) <= \
+            max(f16_bound(K), simt_bound(K))
+    plan.free()
