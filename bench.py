@@ -44,7 +44,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip the side workloads")
-    ap.add_argument("--only", choices=["f64", "int", "grouped", "plain", "splitvar", "rand"],
+    ap.add_argument("--only", choices=["f64", "int", "grouped", "plain", "splitvar", "rand",
+                                       "misc"],
                     help="run one side workload alone (for profiling) and print it")
     return ap.parse_args()
 
@@ -276,6 +277,8 @@ def main():
             part = grouped_workload(nc, torch, oracle, dev)
         elif args.only == "rand":
             part = rand_workload(nc, torch, oracle, dev)
+        elif args.only == "misc":
+            part = misc_workload(nc, synth, oracle)
         elif args.only == "splitvar":
             # the bfloat16-plane variants, two calls each (3 then 6 passes)
             a = torch.from_numpy(synth.normal(SEED, 3, (M, K), np.float32)).to(dev)
@@ -514,6 +517,67 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
     out["int_1024"] = int_workload(nc, torch, synth, dev)
     out["grouped"] = grouped_workload(nc, torch, oracle, dev)
     out["rand"] = rand_workload(nc, torch, oracle, dev)
+    return out
+
+
+def misc_workload(nc, synth, oracle):
+    """The path's other entry points on device-resident numc arrays (calls
+    on resident arrays are asynchronous on the context's stream), timed per
+    call by wall clock from a synchronised start to a synchronised end:
+    numc_linear with its bias in the split and CUDA-core epilogues or in a
+    separate pass, the float32 CUDA-core kernel with numc's remainder-tile
+    fix-up, and numc_dot's 1-D float32 SIMD-order reduction."""
+    out = {}
+    with nc.Ctx() as ctx:
+        def per_call(fn, reps):
+            fn()
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                fn()
+            ctx.synchronize()
+            return (time.perf_counter() - t0) / reps * 1e3
+
+        def resident(x):
+            arr = ctx.from_numpy(x)
+            arr.to_device()
+            return arr
+        for dt, algo, n, reps in (("float32", nc.ALGO_SPLIT_FP16, 4096, 20),
+                                  ("float32", nc.ALGO_SIMT, 2048, 5),
+                                  ("int8", nc.ALGO_TC_INT8, 4096, 20)):
+            x, w = synth.operands("uniform", n, n, n, dtype=dt, seed=3)
+            bias = synth.array("uniform", (n,), seed=3, stream=5, dtype=dt)
+            X, W, Bi = resident(x), resident(w), resident(bias)
+            O = ctx.zeros((n, n), dt)
+            O.to_device()
+            orig = nc.get_algo(dt)
+            nc.set_algo(dt, algo, 0)
+            try:
+                t_mm = per_call(lambda: nc.matmul(X, W, O), reps)
+                t_lin = per_call(lambda: nc.linear(X, W, Bi, O), reps)
+            finally:
+                nc.set_algo(dt, *orig)
+            out[f"linear_{dt}_{n}_algo{algo}"] = {"matmul_ms": t_mm, "linear_ms": t_lin,
+                                                  "bias_ms": t_lin - t_mm}
+        # CUDA-core float32 with numc's remainder tiles (1000 = 6 x 166 + 4 rows)
+        a, b = synth.operands("normal", 1000, 1000, 1000, dtype="float32", seed=4)
+        A, B = resident(a), resident(b)
+        C = ctx.zeros((1000, 1000), "float32")
+        C.to_device()
+        t = per_call(lambda: nc.matmul(A, B, C), 20)
+        C.to_host()
+        out["simt_f32_1000_with_edges"] = {"ms": t, "tflops": 2e9 / t / 1e9,
+                                           "bitexact_vs_numc":
+                                               C.numpy().tobytes() == oracle.matmul(a, b).tobytes()}
+        # numc_dot 1-D float32: numc's lane order, 4 OpenMP chunks
+        n = 16 << 20
+        u = synth.array("normal", (n,), seed=5, stream=1, dtype="float32")
+        v = synth.array("normal", (n,), seed=5, stream=2, dtype="float32")
+        U, V = resident(u), resident(v)
+        R = ctx.zeros((1,), "float32")
+        R.to_device()
+        t = per_call(lambda: nc.dot(U, V, R), 5)
+        out["dot_1d_f32_16Mi"] = {"ms": t, "gb_per_s": 2 * n * 4 / t / 1e6}
     return out
 
 

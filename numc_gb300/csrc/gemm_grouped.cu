@@ -460,7 +460,7 @@ grouped_simt(const Prob *__restrict__ probs, const Tile *__restrict__ tiles) {
 }
 
 // numc's packed-path remainder tiles of the CUDA-core problems listed in
-// `probs_idx`: 32 outputs per block (simt::kEdgeLanes lanes each), block b
+// `probs_idx`: 16 remainder groups per block (one a half-warp), block b
 // being block jobs[b].y of problem probs_idx[jobs[b].x].
 __global__ void __launch_bounds__(256)
 grouped_float_edges(const Prob *__restrict__ probs, const int *__restrict__ probs_idx,
@@ -472,9 +472,9 @@ grouped_float_edges(const Prob *__restrict__ probs, const int *__restrict__ prob
   g.M = P.M; g.K = P.K; g.N = P.N;
   g.rsa = P.rsa; g.csa = P.csa; g.rsb = P.rsb; g.csb = P.csb; g.rso = P.rso; g.cso = P.cso;
   const int64_t r0 = simt::edge_row<float>(g.M), c0 = simt::edge_col<float>(g.N);
-  const int64_t n = simt::float_edge_count<float>(g.M, g.N);
-  const int64_t e = (int64_t)job.y * (256 / simt::kEdgeLanes) + threadIdx.x / simt::kEdgeLanes;
-  simt::float_edge_output<float>(g, e, e < n, r0, c0);
+  const int64_t n = simt::float_edge_groups<float>(g.M, g.N);
+  const int64_t gi = (int64_t)job.y * 16 + threadIdx.x / 16;
+  if (gi < n) simt::float_edge_output<float>(g, gi, threadIdx.x % 16, r0, c0);
 }
 
 }  // namespace grouped
@@ -815,7 +815,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   }
   for (size_t q = 0; q < edge_idx.size(); q++) {
     const Prob &P = p->probs[edge_idx[q]];
-    const long long n = (simt::float_edge_count<float>(P.M, P.N) + 31) / 32;
+    const long long n = (simt::float_edge_groups<float>(P.M, P.N) + 15) / 16;
     for (long long j = 0; j < n; j++) edge_jobs.push_back(make_int2((int)q, (int)j));
   }
   p->split_jobs = (long long)split_jobs.size();

@@ -338,18 +338,60 @@ template <typename T> __host__ __device__ inline int64_t edge_col(int64_t N) {
   return jc + ((N - jc) / NumcTiles<T>::NR) * NumcTiles<T>::NR;
 }
 
+// Short K or many problems: remainder outputs in groups of 16 consecutive
+// columns of one row: first
+// the rows >= r0 (all columns, ceil(N / 16) groups a row), then the rows
+// < r0 (columns c0..N-1, at most 15: one group a row).  A half-warp takes a
+// group, one output a lane, so its loads of B are consecutive and its loads
+// of A one address.
+template <typename T>
+__host__ __device__ inline int64_t float_edge_groups(int64_t M, int64_t N) {
+  const int64_t r0 = edge_row<T>(M), c0 = edge_col<T>(N);
+  return (M - r0) * ((N + 15) / 16) + (c0 < N ? r0 : 0);
+}
+
+// Output `sub` (0..15) of remainder group `gi`: each 256-deep K block as an
+// FMA chain from zero, the block sums added in K order (numc's remainder
+// tiles).  Lanes past the last column return.
+template <typename T>
+__device__ __forceinline__ void float_edge_output(const Gemm &g, int64_t gi, int sub, int64_t r0,
+                                                  int64_t c0) {
+  const int64_t nb = (g.N + 15) / 16, nbottom = (g.M - r0) * nb;
+  int64_t i, j;
+  if (gi < nbottom) {
+    i = r0 + gi / nb;
+    j = (gi % nb) * 16 + sub;
+  } else {
+    i = gi - nbottom;
+    j = c0 + sub;
+  }
+  if (j >= g.N) return;
+  const T *A = (const T *)g.a + i * g.rsa, *B = (const T *)g.b + j * g.csb;
+  T d = T(0);
+  for (int64_t pc = 0; pc < g.K; pc += kNumcKC) {
+    const int64_t pe = min(pc + (int64_t)kNumcKC, g.K);
+    T t = T(0);
+#pragma unroll 8
+    for (int64_t k = pc; k < pe; k++) t = madd<T>(A[k * g.csa], B[k * g.rsb], t);
+    d = pc == 0 ? t : add_rn<T>(d, t);
+  }
+  if (g.bias) d = add_elem<T>(d, ((const T *)g.bias)[j * g.bias_stride]);
+  ((T *)g.c)[i * g.rso + j * g.cso] = d;
+}
+
 // Lanes per remainder output: lane l of a group sums K blocks l, l + 8, ...
 constexpr int kEdgeLanes = 8;
 
-// Output e of the remainder set (rows >= r0: all columns; then rows < r0:
-// columns >= c0), computed by a group of kEdgeLanes lanes of one warp: each
+// Long K (several blocks an output, few outputs): output e of the
+// remainder set (rows >= r0: all columns; then rows < r0: columns >= c0),
+// computed by a group of kEdgeLanes lanes of one warp: each
 // lane runs its K blocks as FMA chains from zero and the group folds the
 // block sums in K order (d = t0, then d = d + t1, ...) — numc's per-block
 // accumulation with the blocks computed in parallel.  Every lane of the
 // warp calls this with the same K (the fold shuffles across the warp);
 // `valid` is false for lanes past the last output.
 template <typename T>
-__device__ __forceinline__ void float_edge_output(const Gemm &g, int64_t e, bool valid, int64_t r0,
+__device__ __forceinline__ void float_edge_output_lanes(const Gemm &g, int64_t e, bool valid, int64_t r0,
                                                   int64_t c0) {
   const int lane = threadIdx.x & 31, sub = lane & (kEdgeLanes - 1), base = lane & ~(kEdgeLanes - 1);
   int64_t i = 0, j = 0;
