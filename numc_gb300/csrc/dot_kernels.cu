@@ -109,44 +109,100 @@ __global__ void dot1d_int_final(const uint64_t *__restrict__ part, int nparts, T
 
 // ---- 1-D: floats ------------------------------------------------------------
 
-// One OpenMP chunk of numc's SIMD dot per block of 8W threads.
+// numc's SIMD dot as 8W independent FMA chains per OpenMP chunk: chain t
+// of chunk c runs over elements s_c + t, s_c + t + 8W, ... of the chunk's
+// full 8W-element blocks.  Each chain is sequential, so the parallelism is
+// the chains: a block takes 32 bytes' worth of consecutive chains of one
+// chunk (8 float32 / 4 float64 — whole DRAM sectors), and while its first
+// warp runs the chains over one stage of kDotRows blocks held in shared
+// memory, the other seven warps load the stage after next.  16 Mi float32
+// (4 chunks, 64 chains of 65536 FMAs each): 0.64 ms, against 6.8 ms with one
+// 64-thread block a chunk reading its operands directly.
+constexpr int kDotRows = 256, kDotStages = 3;   // 3 x 2 operands: 48 KiB of shared memory
+
 template <typename T, int W>
-__global__ void dot1d_simd_chunks(const T *__restrict__ a, const T *__restrict__ b, int64_t n,
-                                  int nt, T *__restrict__ part) {
-  __shared__ T lanes[8 * W];
-  const int c = blockIdx.x, t = threadIdx.x;
+__global__ void __launch_bounds__(256)
+dot1d_simd_chains(const T *__restrict__ a, const T *__restrict__ b, int64_t n, int nt,
+                  T *__restrict__ lanes_out) {
+  constexpr int CG = 32 / (int)sizeof(T);        // chains a block
+  constexpr int GROUPS = 8 * W / CG;             // blocks a chunk (8)
+  __shared__ T sa[kDotStages][kDotRows][CG], sb[kDotStages][kDotRows][CG];
+  const int c = blockIdx.x / GROUPS, grp = blockIdx.x % GROUPS;
+  const int64_t per = n / nt;
+  const int64_t s = (int64_t)c * per, e = (c == nt - 1) ? n : s + per;
+  const int64_t rows = (e - s) / (8 * W);        // full 8W-element blocks
+  const int64_t stages = (rows + kDotRows - 1) / kDotRows;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t col0 = s + grp * CG;             // element of chain grp*CG, row 0
+
+  // loaders (warps 1-7): rows r0 .. r0 + kDotRows of this block's chains
+  auto load = [&](int buf, int64_t r0) {
+    const int lt = tid - 32;                     // 0 .. 223
+    const int ch = lt % CG;
+    for (int r = lt / CG; r < kDotRows; r += 224 / CG) {
+      const int64_t row = r0 + r;
+      T x = T(0), y = T(0);
+      if (row < rows) {
+        const int64_t idx = col0 + row * 8 * W + ch;
+        x = a[idx];
+        y = b[idx];
+      }
+      sa[buf][r][ch] = x;
+      sb[buf][r][ch] = y;
+    }
+  };
+  if (warp > 0) {
+    load(0, 0);
+    if (stages > 1) load(1, kDotRows);
+  }
+  __syncthreads();
+  T acc = T(0);
+  for (int64_t st = 0; st < stages; st++) {
+    const int buf = (int)(st % kDotStages);
+    if (warp > 0) {
+      if (st + 2 < stages) load((int)((st + 2) % kDotStages), (st + 2) * kDotRows);
+    } else if (lane < CG) {
+      const int nr = (int)min((int64_t)kDotRows, rows - st * kDotRows);
+#pragma unroll 8
+      for (int r = 0; r < nr; r++) acc = fma_rn<T>(sa[buf][r][lane], sb[buf][r][lane], acc);
+    }
+    __syncthreads();
+  }
+  if (warp == 0 && lane < CG) lanes_out[(int64_t)c * 8 * W + grp * CG + lane] = acc;
+}
+
+// Chunk c's result from its 8W chain values: numc's pairwise accumulator
+// sums, horizontal lane sum and unfused tail.
+template <typename T, int W>
+__global__ void dot1d_simd_combine(const T *__restrict__ a, const T *__restrict__ b, int64_t n,
+                                   int nt, const T *__restrict__ lanes, T *__restrict__ part) {
+  const int c = blockIdx.x;
   const int64_t per = n / nt;
   const int64_t s = (int64_t)c * per, e = (c == nt - 1) ? n : s + per;
   const int64_t full_end = s + ((e - s) / (8 * W)) * (8 * W);
-  T acc = T(0);
-  for (int64_t i = s; i < full_end; i += 8 * W) acc = fma_rn<T>(a[i + t], b[i + t], acc);
-  lanes[t] = acc;
-  __syncthreads();
-  if (t == 0) {
-    T v[8][W];
-    for (int j = 0; j < 8; j++)
-      for (int l = 0; l < W; l++) v[j][l] = lanes[W * j + l];
-    for (int l = 0; l < W; l++) {
-      v[0][l] = add_rn<T>(v[0][l], v[1][l]);
-      v[2][l] = add_rn<T>(v[2][l], v[3][l]);
-      v[4][l] = add_rn<T>(v[4][l], v[5][l]);
-      v[6][l] = add_rn<T>(v[6][l], v[7][l]);
-      v[0][l] = add_rn<T>(v[0][l], v[2][l]);
-      v[4][l] = add_rn<T>(v[4][l], v[6][l]);
-      v[0][l] = add_rn<T>(v[0][l], v[4][l]);
-    }
-    T result;
-    if constexpr (W == 8) {   // _hsum_ps_avx2
-      const T s0 = add_rn<T>(v[0][0], v[0][4]), s1 = add_rn<T>(v[0][1], v[0][5]);
-      const T s2 = add_rn<T>(v[0][2], v[0][6]), s3 = add_rn<T>(v[0][3], v[0][7]);
-      result = add_rn<T>(add_rn<T>(s0, s2), add_rn<T>(s1, s3));
-    } else {                  // _hsum_pd_avx2
-      result = add_rn<T>(add_rn<T>(v[0][0], v[0][2]), add_rn<T>(v[0][1], v[0][3]));
-    }
-    T tail = T(0);
-    for (int64_t i = full_end; i < e; i++) tail = add_rn<T>(tail, mul_rn<T>(a[i], b[i]));
-    part[c] = add_rn<T>(result, tail);
+  T v[8][W];
+  for (int j = 0; j < 8; j++)
+    for (int l = 0; l < W; l++) v[j][l] = lanes[(int64_t)c * 8 * W + W * j + l];
+  for (int l = 0; l < W; l++) {
+    v[0][l] = add_rn<T>(v[0][l], v[1][l]);
+    v[2][l] = add_rn<T>(v[2][l], v[3][l]);
+    v[4][l] = add_rn<T>(v[4][l], v[5][l]);
+    v[6][l] = add_rn<T>(v[6][l], v[7][l]);
+    v[0][l] = add_rn<T>(v[0][l], v[2][l]);
+    v[4][l] = add_rn<T>(v[4][l], v[6][l]);
+    v[0][l] = add_rn<T>(v[0][l], v[4][l]);
   }
+  T result;
+  if constexpr (W == 8) {   // _hsum_ps_avx2
+    const T s0 = add_rn<T>(v[0][0], v[0][4]), s1 = add_rn<T>(v[0][1], v[0][5]);
+    const T s2 = add_rn<T>(v[0][2], v[0][6]), s3 = add_rn<T>(v[0][3], v[0][7]);
+    result = add_rn<T>(add_rn<T>(s0, s2), add_rn<T>(s1, s3));
+  } else {                  // _hsum_pd_avx2
+    result = add_rn<T>(add_rn<T>(v[0][0], v[0][2]), add_rn<T>(v[0][1], v[0][3]));
+  }
+  T tail = T(0);
+  for (int64_t i = full_end; i < e; i++) tail = add_rn<T>(tail, mul_rn<T>(a[i], b[i]));
+  part[c] = add_rn<T>(result, tail);
 }
 
 template <typename T>
@@ -191,10 +247,12 @@ cudaError_t dot1d_t(const void *a, int64_t sa, const void *b, int64_t sb, int64_
     int nt = (int)(bytes / (1u << 19));
     if (nt > 4) nt = 4;
     if (!(bytes > (1u << 20) && nt >= 2)) nt = 1;
-    T *part = (T *)scratch;
-    dot1d_simd_chunks<T, W><<<nt, 8 * W, 0, s>>>((const T *)a, (const T *)b, n, nt, part);
+    T *lanes = (T *)scratch, *part = lanes + 4 * 8 * W;   // nt <= 4 chunks
+    constexpr int GROUPS = 8 * W / (32 / (int)sizeof(T));
+    dot1d_simd_chains<T, W><<<nt * GROUPS, 256, 0, s>>>((const T *)a, (const T *)b, n, nt, lanes);
+    dot1d_simd_combine<T, W><<<nt, 1, 0, s>>>((const T *)a, (const T *)b, n, nt, lanes, part);
     dot1d_float_final<T><<<1, 1, 0, s>>>(part, nt, (T *)out);
-    count_launch(2);
+    count_launch(3);
     return cudaGetLastError();
   } else {
     uint64_t *part = (uint64_t *)scratch;
@@ -208,7 +266,11 @@ cudaError_t dot1d_t(const void *a, int64_t sa, const void *b, int64_t sb, int64_
 
 }  // namespace
 
-size_t dot1d_scratch_bytes() { return (size_t)kIntBlocks * 8; }
+// integer partial sums, or float chain values (4 chunks x 64) and chunk sums
+size_t dot1d_scratch_bytes() {
+  const size_t f = (4 * 64 + 4) * 8;
+  return (size_t)kIntBlocks * 8 > f ? (size_t)kIntBlocks * 8 : f;
+}
 
 cudaError_t launch_dot_scalar(NumcDType dt, const void *x, const void *scalar, void *out,
                               const DotNd &ix, cudaStream_t s) {
