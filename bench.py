@@ -679,6 +679,16 @@ def int_workload(nc, torch, synth, dev):
             h = hashlib.sha256(tc_.cpu().numpy().tobytes()).hexdigest()
             ints.setdefault(dt, {})[name] = {"tops": 2.0 * 1024 ** 3 / ms_ / 1e9, "ms": ms_,
                                              "bitexact_vs_numc": h == want}
+    # int8 4096^3 on the tensor path (128 x 128 tiles), checked against the
+    # CUDA-core path, which follows numc's arithmetic independently
+    ai_, bi_ = synth.operands("uniform", 4096, 4096, 4096, dtype="int8")
+    ta_, tb_ = torch.from_numpy(ai_).to(dev), torch.from_numpy(bi_).to(dev)
+    tc_ = torch.empty((4096, 4096), dtype=torch.int8, device=dev)
+    ms_s = time_gemm(nc, torch, ta_, tb_, tc_, nc.ALGO_SIMT, nc.INT8_X86_AVX2, steps=3, warmup=1)
+    ref_ = tc_.clone()
+    ms_ = time_gemm(nc, torch, ta_, tb_, tc_, nc.ALGO_TC_INT8, nc.INT8_X86_AVX2, steps=20, warmup=2)
+    ints["int8_4096"] = {"tensor_tops": 2.0 * 4096 ** 3 / ms_ / 1e9, "tensor_ms": ms_,
+                         "simt_ms": ms_s, "tensor_equals_simt": bool(torch.equal(tc_, ref_))}
     return ints
 
 

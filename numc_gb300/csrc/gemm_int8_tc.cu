@@ -30,9 +30,17 @@
 namespace numc_k {
 namespace {
 
-constexpr int kBM = 128, kBN = 64, kBK = 64, kStages = 8, kNumBuf = 8;
+constexpr int kBM = 128, kBK = 64;
 constexpr int kBlockK = 512;                 // numc's int8 K block (KC)
-constexpr int kAccWarps = 8, kThreads = 64 + 32 * kAccWarps;
+
+// Output tile 128 x BN: BN = 64 (8 accumulator warps, 8 TMEM buffers, 8
+// ring stages of 24 KiB) for problems with few tiles, BN = 128 (16 warps,
+// 4 buffers, 6 stages of 32 KiB: half the operand traffic per MMA) when
+// the 128-column tiles still give every SM one.
+template <int BN> struct I8Cfg {
+  static constexpr int kNumBuf = 512 / BN, kStages = BN == 64 ? 8 : 6;
+  static constexpr int kAccWarps = BN / 8, kThreads = 64 + 32 * kAccWarps;
+};
 
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
@@ -74,11 +82,13 @@ int8_to_bf16(const uint8_t *__restrict__ src, int64_t rs_row, int64_t rs_k, int6
   }
 }
 
-template <bool SIGNED>
-__global__ void __launch_bounds__(kThreads, 1)
+template <bool SIGNED, int kBN>
+__global__ void __launch_bounds__(I8Cfg<kBN>::kThreads, 1)
 int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB,
              uint8_t *__restrict__ C, int64_t rso, int64_t cso, int M, int N, int num_kb,
              int tiles_m, int tiles_n, int rule, unsigned *status) {
+  constexpr int kNumBuf = I8Cfg<kBN>::kNumBuf, kStages = I8Cfg<kBN>::kStages;
+  constexpr int kAccWarps = I8Cfg<kBN>::kAccWarps;
   // slabs per TMEM chunk: a whole 512-deep block for int8, half for uint8
   constexpr int CHUNK = SIGNED ? kBlockK / kBK : kBlockK / kBK / 2;
   constexpr int CHUNKS_PER_BLOCK = kBlockK / kBK / CHUNK;
@@ -161,14 +171,19 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
     }
     __syncwarp();
   } else {
-    constexpr int CW = kBN / 2;
-    const int quad = warp & 3, half = (warp - 2) >> 2;
+    constexpr int CW = 32;   // columns per accumulator thread
+    const int quad = warp & 3, group = (warp - 2) >> 2;
     const int row = m0 + quad * 32 + lane;
-    const int cbase = half * CW;
+    const int cbase = group * CW;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     int32_t d[CW], part[CW];
+    uint32_t fullmask = 0;   // x86 rule: columns inside numc's full 6x16 tiles
 #pragma unroll
-    for (int j = 0; j < CW; j++) d[j] = 0;
+    for (int j = 0; j < CW; j++) {
+      d[j] = 0;
+      if (rule == kRuleX86Packed && simt::x86_full(row, n0 + cbase + j, M, N))
+        fullmask |= 1u << j;
+    }
     const int nchunks = num_kb / CHUNK;   // num_kb is a multiple of the block size
     bool ok = true;
     for (int chunk = 0; chunk < nchunks; chunk++) {
@@ -178,18 +193,21 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
       ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
       if (!ok) break;
       tc::tc_fence_after();
-      uint32_t r[32];
-      tc::tmem_ld_32x32b_x32(tmem + lane_off + buf * kBN + cbase, r);
-      tc::tmem_ld_wait();
+      const bool block_start = chunk % CHUNKS_PER_BLOCK == 0;
+#pragma unroll
+      for (int c0 = 0; c0 < CW; c0 += 16) {   // 16 columns a load: fewer live registers
+        uint32_t r[16];
+        tc::tmem_ld_32x32b_x16(tmem + lane_off + buf * kBN + cbase + c0, r);
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const int32_t v = __float2int_rn(__uint_as_float(r[j]));   // exact
+          part[c0 + j] = block_start ? v : part[c0 + j] + v;
+        }
+      }
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tempty[buf]));
-      const bool block_start = chunk % CHUNKS_PER_BLOCK == 0;
-#pragma unroll
-      for (int j = 0; j < CW; j++) {
-        const int32_t v = __float2int_rn(__uint_as_float(r[j]));   // exact
-        part[j] = block_start ? v : part[j] + v;
-      }
       if (chunk % CHUNKS_PER_BLOCK == CHUNKS_PER_BLOCK - 1) {
         const int b = chunk / CHUNKS_PER_BLOCK;
         if (rule == kRuleNeon || rule == kRuleWrap) {
@@ -199,18 +217,36 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
         } else {
 #pragma unroll
           for (int j = 0; j < CW; j++)
-            d[j] = simt::fold8(d[j], part[j], b == 0, rule, SIGNED, row, n0 + cbase + j, M, N);
+            d[j] = simt::fold8_x86(d[j], part[j], b == 0, (fullmask >> j) & 1u, SIGNED);
         }
       }
     }
     if (ok && row < M) {
+      if (rule == kRuleNeon || rule == kRuleWrap) {
 #pragma unroll
-      for (int j = 0; j < CW; j++) {
-        const int col = n0 + cbase + j;
-        if (col >= N) continue;
-        int32_t v = d[j];
-        if (rule == kRuleNeon || rule == kRuleWrap) v = simt::fold8(0, v, true, rule, SIGNED, row, col, M, N);
-        C[(int64_t)row * rso + (int64_t)col * cso] = (uint8_t)v;
+        for (int j = 0; j < CW; j++)
+          d[j] = simt::fold8(0, d[j], true, rule, SIGNED, row, n0 + cbase + j, M, N);
+      }
+      const int col0 = n0 + cbase;
+      uint8_t *dst = C + (int64_t)row * rso + (int64_t)col0 * cso;
+      if (cso == 1 && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) && col0 + CW <= N) {
+        // the thread's 32 bytes of its row: two 16-byte stores, one sector
+        // (byte stores would cost a sector write each)
+#pragma unroll
+        for (int h = 0; h < CW / 16; h++) {
+          uint32_t w[4];
+#pragma unroll
+          for (int q = 0; q < 4; q++)
+            w[q] = (uint32_t)(uint8_t)d[16 * h + 4 * q] |
+                   ((uint32_t)(uint8_t)d[16 * h + 4 * q + 1] << 8) |
+                   ((uint32_t)(uint8_t)d[16 * h + 4 * q + 2] << 16) |
+                   ((uint32_t)(uint8_t)d[16 * h + 4 * q + 3] << 24);
+          *reinterpret_cast<uint4 *>(dst + 16 * h) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < CW; j++)
+          if (col0 + j < N) dst[(int64_t)j * cso] = (uint8_t)d[j];
       }
     }
   }
@@ -236,6 +272,31 @@ I8Layout i8_layout(int64_t M, int64_t K, int64_t N) {
   return L;
 }
 
+template <bool SIGNED, int kBN>
+cudaError_t launch_i8_gemm(const Gemm &g, int rule, const I8Layout &L, __nv_bfloat16 *pa,
+                           __nv_bfloat16 *pb, unsigned *status, cudaStream_t s) {
+  using Cfg = I8Cfg<kBN>;
+  CUtensorMap ta, tb;
+  cudaError_t e;
+  if ((e = make_tmap_2d(&ta, pa, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, g.M, L.Kp, L.Kp, kBM, kBK)))
+    return e;
+  if ((e = make_tmap_2d(&tb, pb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, g.N, L.Kp, L.Kp, kBN, kBK)))
+    return e;
+  constexpr uint32_t kBarBytes = 512;   // 2*(kStages + kNumBuf) mbarriers + TMEM slot
+  static_assert((2 * Cfg::kStages + 2 * Cfg::kNumBuf) * 8 + 4 <= kBarBytes, "barrier space");
+  constexpr uint32_t SMEM = Cfg::kStages * (kBM + kBN) * kBK * 2 + 1024 + kBarBytes;
+  static_assert(SMEM <= 232448, "shared memory");
+  if ((e = cudaFuncSetAttribute(int8_tc_gemm<SIGNED, kBN>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM)))
+    return e;
+  const int tiles_m = (int)((g.M + kBM - 1) / kBM), tiles_n = (int)((g.N + kBN - 1) / kBN);
+  int8_tc_gemm<SIGNED, kBN><<<tiles_m * tiles_n, Cfg::kThreads, SMEM, s>>>(
+      ta, tb, (uint8_t *)g.c, g.rso, g.cso, (int)g.M, (int)g.N, (int)(L.Kp / kBK), tiles_m,
+      tiles_n, rule, status);
+  count_launch();
+  return cudaGetLastError();
+}
+
 template <bool SIGNED>
 cudaError_t launch_i8(const Gemm &g, int rule, char *ws, const I8Layout &L, cudaStream_t s) {
   unsigned *status = status_word();
@@ -251,24 +312,9 @@ cudaError_t launch_i8(const Gemm &g, int rule, char *ws, const I8Layout &L, cuda
   cudaError_t e = cudaGetLastError();
   if (e) return e;
   mark.split_done();
-  CUtensorMap ta, tb;
-  if ((e = make_tmap_2d(&ta, pa, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, g.M, L.Kp, L.Kp, kBM, kBK)))
-    return e;
-  if ((e = make_tmap_2d(&tb, pb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, g.N, L.Kp, L.Kp, kBN, kBK)))
-    return e;
-  constexpr uint32_t kBarBytes = 512;   // 2*(kStages + kNumBuf) mbarriers + TMEM slot
-  static_assert((2 * kStages + 2 * kNumBuf) * 8 + 4 <= kBarBytes, "barrier space");
-  constexpr uint32_t SMEM = kStages * (kBM + kBN) * kBK * 2 + 1024 + kBarBytes;
-  static_assert(SMEM <= 232448, "shared memory");
-  if ((e = cudaFuncSetAttribute(int8_tc_gemm<SIGNED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                SMEM)))
-    return e;
-  const int tiles_m = (int)((g.M + kBM - 1) / kBM), tiles_n = (int)((g.N + kBN - 1) / kBN);
-  int8_tc_gemm<SIGNED><<<tiles_m * tiles_n, kThreads, SMEM, s>>>(
-      ta, tb, (uint8_t *)g.c, g.rso, g.cso, (int)g.M, (int)g.N, (int)(L.Kp / kBK), tiles_m,
-      tiles_n, rule, status);
-  count_launch();
-  e = cudaGetLastError();
+  const int64_t tiles128 = ((g.M + kBM - 1) / kBM) * ((g.N + 127) / 128);
+  e = tiles128 >= 152 ? launch_i8_gemm<SIGNED, 128>(g, rule, L, pa, pb, status, s)
+                      : launch_i8_gemm<SIGNED, 64>(g, rule, L, pa, pb, status, s);
   mark.gemm_done();
   return e;
 }

@@ -98,17 +98,22 @@ __device__ __forceinline__ bool neon_full(int64_t i, int64_t j, int64_t M,
 
 // One K-block end for element (i, j): fold the block's partial sum P into
 // the stored value d according to the rule.  `first` marks block 0.
+// x86 packed rule with the element's tile class known (`full`: inside a
+// full 6x16 register tile).
+__device__ __forceinline__ int32_t fold8_x86(int32_t d, int32_t P, bool first,
+                                             bool full, bool is_signed) {
+  if (full) {
+    int32_t v = d + P;
+    return is_signed ? sat_s8(v) : sat_u8_x86(v);
+  }
+  int32_t t = is_signed ? sat_s8(P) : sat_u8_x86(P);
+  return first ? t : wrap8(d + t, is_signed);
+}
 __device__ __forceinline__ int32_t fold8(int32_t d, int32_t P, bool first,
                                          int rule, bool is_signed, int64_t i,
                                          int64_t j, int64_t M, int64_t N) {
-  if (rule == kRuleX86Packed) {
-    if (x86_full(i, j, M, N)) {
-      int32_t v = d + P;
-      return is_signed ? sat_s8(v) : sat_u8_x86(v);
-    }
-    int32_t t = is_signed ? sat_s8(P) : sat_u8_x86(P);
-    return first ? t : wrap8(d + t, is_signed);
-  }
+  if (rule == kRuleX86Packed)
+    return fold8_x86(d, P, first, x86_full(i, j, M, N), is_signed);
   if (rule == kRuleNeon) {
     if (neon_full(i, j, M, N))
       return is_signed ? sat_s8(P) : ((uint32_t)P > 255u ? 255 : P);

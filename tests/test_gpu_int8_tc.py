@@ -2,7 +2,9 @@
 
 Every stored byte must equal numc's own (golden SHA-256 at 1024^3 and
 300x4100x4200) and the oracle's for each store-rule profile, including
-shapes with remainder tiles and K not a multiple of numc's 512 block.
+shapes with remainder tiles and K not a multiple of numc's 512 block, on
+both tile widths (128 x 64 tiles, and 128 x 128 once those give every SM
+one).
 """
 import numpy as np
 import pytest
@@ -30,7 +32,9 @@ def _tc(a, b, profile):
 @pytest.mark.parametrize("dt", ["int8", "uint8"])
 @pytest.mark.parametrize("profile", [nc.INT8_X86_AVX2, nc.INT8_ARM_NEON, nc.INT8_WRAP])
 @pytest.mark.parametrize("shape", [(150, 1500, 140), (97, 1100, 203), (5, 3, 4),
-                                   (300, 513, 64), (128, 64, 65), (200, 4096, 300)],
+                                   (300, 513, 64), (128, 64, 65), (200, 4096, 300),
+                                   # enough 128-column tiles for the 128 x 128 tile kernel
+                                   (2000, 700, 1250), (2304, 1536, 1280)],
                          ids=lambda s: "x".join(map(str, s)))
 def test_profiles_vs_oracle(dt, profile, shape):
     a, b = synth.operands("uniform", *shape, dtype=dt, seed=sum(shape))
