@@ -12,7 +12,7 @@
 // the CUDA-core kernel uses (simt::fold8: x86 packed saturation per block
 // and tile class, NEON clamp-once, or truncation).  Results are bit-exact.
 //
-// Passes: a convert kernel writes A as bf16 (M x Kp, K-major) and B^T as
+// Passes: one convert launch writes A as bf16 (M x Kp, K-major) and B^T as
 // bf16 (N x Kp), K padded to 512 with zeros; then one 128 x 64 output tile
 // per CTA with a 24 KiB TMA ring stage (8 stages), 320 threads (TMA warp,
 // MMA warp, 8 accumulator warps of 32 columns).
@@ -44,41 +44,101 @@ template <int BN> struct I8Cfg {
 
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
-// dst(row, k) = bf16(src[row * rs_row + k * rs_k]) for row < R, k < K; zero
-// up to Kp.  32 rows x 128 k per block through shared memory.
+// One operand of the conversion pass: dst(row, k) = bf16(src[row * rs_row +
+// k * rs_k]) for row < R, k < K, zero for K <= k < Kp.
+struct I8Operand {
+  const uint8_t *src;
+  int64_t rs_row, rs_k, R;
+  __nv_bfloat16 *dst;
+};
+
+constexpr int kCvtRows = 64, kCvtK = 128;
+
+// Both operands in one launch (A's tiles first, then B^T's), 64 rows x 128 k
+// a block staged in shared memory: 16-byte loads along whichever source
+// axis is contiguous (k for row-major A, rows for row-major B), 16-byte
+// stores of 8 bfloat16 along k.  Integers of 8 bits are exact in bfloat16:
+// the value's float32 bits with the low 16 (zero) dropped.
 template <bool SIGNED>
 __global__ void __launch_bounds__(256)
-int8_to_bf16(const uint8_t *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_t R,
-             int64_t K, int64_t Kp, __nv_bfloat16 *__restrict__ dst) {
-  __shared__ short tile[32][129];
-  const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 128;
+int8_pair_to_bf16(I8Operand a, I8Operand b, int64_t K, int64_t Kp, int64_t blocks_a) {
+  __shared__ uint8_t tile[kCvtRows][kCvtK + 16];
+  int64_t blk = blockIdx.x;
+  const I8Operand &op = blk < blocks_a ? a : b;
+  if (blk >= blocks_a) blk -= blocks_a;
+  const int64_t kblocks = Kp / kCvtK;
+  const int64_t r0 = (blk / kblocks) * kCvtRows, k0 = (blk % kblocks) * kCvtK;
   const int tid = threadIdx.x;
-  const bool kfast = rs_k == 1 || rs_row != 1;
-#pragma unroll 4
-  for (int q = 0; q < 16; q++) {
-    const int e = tid + 256 * q;
-    const int r = kfast ? e / 128 : e % 32, k = kfast ? e % 128 : e / 32;
-    const int64_t gr = r0 + r, gk = k0 + k;
-    short v = 0;
-    if (gr < R && gk < K) {
-      const uint8_t b = src[gr * rs_row + gk * rs_k];
-      v = SIGNED ? (short)(int8_t)b : (short)b;
+  const uint8_t *src = op.src;
+  if (op.rs_k == 1) {
+#pragma unroll
+    for (int it = 0; it < 2; it++) {   // 8 threads a row, 16 bytes each
+      const int r = (tid >> 3) + 32 * it, kk = (tid & 7) * 16;
+      const int64_t gr = r0 + r, gk = k0 + kk;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (gr < op.R && gk < K) {
+        const uint8_t *p = src + gr * op.rs_row + gk;
+        if (gk + 16 <= K && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+          v = *reinterpret_cast<const uint4 *>(p);
+        } else {
+          alignas(16) uint8_t t[16];
+#pragma unroll
+          for (int i = 0; i < 16; i++) t[i] = gk + i < K ? p[i] : 0;
+          v = *reinterpret_cast<uint4 *>(t);
+        }
+      }
+      *reinterpret_cast<uint4 *>(&tile[r][kk]) = v;
     }
-    tile[r][k] = v;
+  } else if (op.rs_row == 1) {
+#pragma unroll
+    for (int it = 0; it < 2; it++) {   // 4 threads a k, 16 rows each
+      const int kk = (tid >> 2) + 64 * it, r = (tid & 3) * 16;
+      const int64_t gr = r0 + r, gk = k0 + kk;
+      alignas(16) uint8_t t[16];
+      if (gk < K && gr < op.R) {
+        const uint8_t *p = src + gk * op.rs_k + gr;
+        if (gr + 16 <= op.R && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+          *reinterpret_cast<uint4 *>(t) = *reinterpret_cast<const uint4 *>(p);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; i++) t[i] = gr + i < op.R ? p[i] : 0;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 16; i++) t[i] = 0;
+      }
+#pragma unroll
+      for (int i = 0; i < 16; i++) tile[r + i][kk] = t[i];
+    }
+  } else {
+#pragma unroll 4
+    for (int q = 0; q < kCvtRows * kCvtK / 256; q++) {
+      const int e = tid + 256 * q, r = e / kCvtK, kk = e % kCvtK;
+      const int64_t gr = r0 + r, gk = k0 + kk;
+      tile[r][kk] = (gr < op.R && gk < K) ? src[gr * op.rs_row + gk * op.rs_k] : 0;
+    }
   }
   __syncthreads();
-  const int warp = tid >> 5, lane = tid & 31;
 #pragma unroll
-  for (int rr = 0; rr < 4; rr++) {
-    const int r = warp + 8 * rr;
-    const int64_t gr = r0 + r, gk = k0 + 4 * lane;
-    if (gr >= R || gk >= Kp) continue;
-    uint2 w;
-    w.x = (uint32_t)__bfloat16_as_ushort(__int2bfloat16_rn(tile[r][4 * lane])) |
-          ((uint32_t)__bfloat16_as_ushort(__int2bfloat16_rn(tile[r][4 * lane + 1])) << 16);
-    w.y = (uint32_t)__bfloat16_as_ushort(__int2bfloat16_rn(tile[r][4 * lane + 2])) |
-          ((uint32_t)__bfloat16_as_ushort(__int2bfloat16_rn(tile[r][4 * lane + 3])) << 16);
-    *reinterpret_cast<uint2 *>(dst + gr * Kp + gk) = w;
+  for (int it = 0; it < 4; it++) {     // 16 threads a row, 8 k each
+    const int r = (tid >> 4) + 16 * it, kk = (tid & 15) * 8;
+    const int64_t gr = r0 + r;
+    if (gr >= op.R) continue;
+    const uint2 raw = *reinterpret_cast<const uint2 *>(&tile[r][kk]);
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const uint32_t word = q < 2 ? raw.x : raw.y;
+      uint32_t h[2];
+#pragma unroll
+      for (int i = 0; i < 2; i++) {
+        const uint32_t byte = (word >> (8 * (2 * (q & 1) + i))) & 0xFFu;
+        const int v = SIGNED ? (int)(int8_t)byte : (int)byte;
+        h[i] = __float_as_uint((float)v) >> 16;
+      }
+      w[q] = h[0] | (h[1] << 16);
+    }
+    *reinterpret_cast<uint4 *>(op.dst + gr * Kp + k0 + kk) = make_uint4(w[0], w[1], w[2], w[3]);
   }
 }
 
@@ -303,12 +363,15 @@ cudaError_t launch_i8(const Gemm &g, int rule, char *ws, const I8Layout &L, cuda
   if (!status) return cudaErrorMemoryAllocation;
   PhaseMark mark(s);
   auto *pa = (__nv_bfloat16 *)(ws + L.a), *pb = (__nv_bfloat16 *)(ws + L.b);
-  dim3 ga((unsigned)(L.Kp / 128), (unsigned)((g.M + 31) / 32));
-  dim3 gb((unsigned)(L.Kp / 128), (unsigned)((g.N + 31) / 32));
-  if (ga.y > 65535 || gb.y > 65535) return cudaErrorInvalidConfiguration;
-  int8_to_bf16<SIGNED><<<ga, 256, 0, s>>>((const uint8_t *)g.a, g.rsa, g.csa, g.M, g.K, L.Kp, pa);
-  int8_to_bf16<SIGNED><<<gb, 256, 0, s>>>((const uint8_t *)g.b, g.csb, g.rsb, g.N, g.K, L.Kp, pb);
-  count_launch(2);
+  const I8Operand oa{(const uint8_t *)g.a, g.rsa, g.csa, g.M, pa};
+  const I8Operand ob{(const uint8_t *)g.b, g.csb, g.rsb, g.N, pb};   // B^T
+  const int64_t kblocks = L.Kp / kCvtK;
+  const int64_t blocks_a = (g.M + kCvtRows - 1) / kCvtRows * kblocks;
+  const int64_t blocks_b = (g.N + kCvtRows - 1) / kCvtRows * kblocks;
+  if (blocks_a + blocks_b >= (1ll << 31)) return cudaErrorInvalidConfiguration;
+  int8_pair_to_bf16<SIGNED><<<(unsigned)(blocks_a + blocks_b), 256, 0, s>>>(oa, ob, g.K, L.Kp,
+                                                                          blocks_a);
+  count_launch();
   cudaError_t e = cudaGetLastError();
   if (e) return e;
   mark.split_done();

@@ -67,3 +67,25 @@ def test_strided_and_through_numc_matmul():
             np.testing.assert_array_equal(C.numpy(), oracle.matmul(a, b))
     finally:
         nc.set_algo("int8", *orig)
+
+
+@pytest.mark.parametrize("dt", ["int8", "uint8"])
+def test_unaligned_and_general_strides(dt):
+    """Operand rows off the 16-byte grid, a column-sliced B (rows contiguous
+    but unaligned) and a B with no unit stride at all."""
+    a, b = synth.operands("uniform", 130, 700, 90, dtype=dt, seed=5)
+    want = oracle.matmul(a, b)
+    abig = np.zeros((130, 703), a.dtype)
+    abig[:, 1:701] = a
+    ta = torch.from_numpy(abig).cuda()[:, 1:701]              # k contiguous, rows unaligned
+    bsl = np.zeros((700, 93), b.dtype)
+    bsl[:, 3:93] = b
+    tb1 = torch.from_numpy(bsl).cuda()[:, 3:93]               # columns contiguous, unaligned
+    bst = np.zeros((700, 180), b.dtype)
+    bst[:, ::2] = b
+    tb2 = torch.from_numpy(bst).cuda()[:, ::2]                # no unit stride
+    for tb in (tb1, tb2):
+        out = torch.full((130, 90), 77, dtype=ta.dtype, device="cuda")
+        nc.gemm(ta, tb, out, algo=nc.ALGO_TC_INT8, param=nc.INT8_X86_AVX2)
+        nc.check_status()
+        np.testing.assert_array_equal(out.cpu().numpy(), want)
