@@ -55,7 +55,11 @@ template <typename T>
 cudaError_t launch_float_edges(const Gemm &g, cudaStream_t s) {
   if (!simt::float_edges_needed<T>(g.K)) return cudaSuccess;
   const int64_t r0 = simt::edge_row<T>(g.M), c0 = simt::edge_col<T>(g.N);
-  if ((g.K + simt::kNumcKC - 1) / simt::kNumcKC >= 4) {
+  // K blocks on separate lanes when there are enough of them, or when the
+  // outputs are too few to fill the GPU one lane each (the chains are then
+  // the whole latency)
+  const int64_t nkb = (g.K + simt::kNumcKC - 1) / simt::kNumcKC;
+  if (nkb >= 4 || simt::float_edge_count<T>(g.M, g.N) <= 152 * 128) {
     const int64_t n = simt::float_edge_count<T>(g.M, g.N);
     if (n == 0) return cudaSuccess;
     const int64_t blocks = std::min<int64_t>((n + 31) / 32, 152 * 16);
@@ -107,6 +111,25 @@ cudaError_t launch_sized(const Gemm &g, int rule8, cudaStream_t s) {
   return launch_tile<T, 32, 32, 2, 2, KIND>(g, rule8, s);
 }
 
+// numc's packed float path: 64- and 32-wide tiles sum the remainder-tile
+// outputs per K block in the tile kernel (kFloatEdges); 128-wide tiles
+// (8 x 8 outputs a thread, no registers to spare) leave them to the
+// float_edges pass.
+template <typename T, int BIG>
+cudaError_t launch_float_packed(const Gemm &g, cudaStream_t s) {
+  int t = BIG;
+  while (t > 32 && ((g.M + t - 1) / t) * ((g.N + t - 1) / t) < sms()) t /= 2;
+  cudaError_t e;
+  if constexpr (BIG >= 128) {
+    if (t == 128) {
+      e = launch_tile<T, 128, 128, 8, 8, simt::kFloat>(g, 0, s);
+      return e != cudaSuccess || g.K == 0 ? e : launch_float_edges<T>(g, s);
+    }
+  }
+  if (t >= 64) return launch_tile<T, 64, 64, 4, 4, simt::kFloatEdges>(g, 0, s);
+  return launch_tile<T, 32, 32, 2, 2, simt::kFloatEdges>(g, 0, s);
+}
+
 }  // namespace
 
 int float_rule(NumcDType dt, const Gemm &g, int rule) {
@@ -122,19 +145,13 @@ cudaError_t launch_simt(NumcDType dt, const Gemm &g, int rule8, cudaStream_t s) 
     switch (float_rule(dt, g, rule8)) {
     case kFloatNaive: return launch_sized<float, simt::kFloatUnfused, 128>(g, 0, s);
     case kFloatNumcSmall: return launch_sized<float, simt::kFloatSmall, 128>(g, 0, s);
-    default: {
-      cudaError_t e = launch_sized<float, simt::kFloat, 128>(g, 0, s);
-      return e != cudaSuccess || g.K == 0 ? e : launch_float_edges<float>(g, s);
-    }
+    default: return launch_float_packed<float, 128>(g, s);
     }
   case NUMC_DTYPE_FLOAT64:
     switch (float_rule(dt, g, rule8)) {
     case kFloatNaive: return launch_sized<double, simt::kFloatUnfused, 64>(g, 0, s);
     case kFloatNumcSmall: return launch_sized<double, simt::kFloatSmall, 64>(g, 0, s);
-    default: {
-      cudaError_t e = launch_sized<double, simt::kFloat, 64>(g, 0, s);
-      return e != cudaSuccess || g.K == 0 ? e : launch_float_edges<double>(g, s);
-    }
+    default: return launch_float_packed<double, 64>(g, s);
     }
   case NUMC_DTYPE_INT16: return launch_sized<int16_t, simt::kWrapInt, 128>(g, 0, s);
   case NUMC_DTYPE_UINT16: return launch_sized<uint16_t, simt::kWrapInt, 128>(g, 0, s);

@@ -33,10 +33,13 @@ constexpr int kThreads = 256;
 
 // kFloat: one fused multiply-add chain per output (numc's full register
 // tiles; numc_float_edges then redoes the packed path's remainder tiles);
+// kFloatEdges: kFloat with the remainder-tile outputs summed per 256-deep K
+// block inside the tile kernel (chain from zero each block, added in order);
 // kFloatSmall: numc's unpacked (gemmsup) float path;
 // kFloatUnfused: `acc = acc + a * b`, product and sum each rounded (numc's
 // naive kernels, compiled without contraction).
-enum Kind : int { kFloat = 0, kWrapInt = 1, kByte = 2, kFloatUnfused = 3, kFloatSmall = 4 };
+enum Kind : int { kFloat = 0, kWrapInt = 1, kByte = 2, kFloatUnfused = 3, kFloatSmall = 4,
+                  kFloatEdges = 5 };
 
 // ---- numc's float register tiles (x86 AVX2 build) --------------------------
 //
@@ -54,6 +57,20 @@ template <typename T> struct NumcTiles;
 template <> struct NumcTiles<float> { static constexpr int MC = 144, NR = 16, VW = 8; };
 template <> struct NumcTiles<double> { static constexpr int MC = 72, NR = 8, VW = 4; };
 constexpr int kNumcMR = 6, kNumcNC = 4080, kNumcKC = 256;
+
+// First row / column of numc's remainder register tiles: rows from
+// edge_row(M) (the last MC block's partial MR tile), and, above them,
+// columns from edge_col(N) (the last 4080-column panel's partial NR tile).
+template <typename T> __host__ __device__ inline int64_t edge_row(int64_t M) {
+  if (M == 0) return 0;
+  const int64_t ic = ((M - 1) / NumcTiles<T>::MC) * NumcTiles<T>::MC;
+  return ic + ((M - ic) / kNumcMR) * kNumcMR;
+}
+template <typename T> __host__ __device__ inline int64_t edge_col(int64_t N) {
+  if (N == 0) return 0;
+  const int64_t jc = ((N - 1) / kNumcNC) * kNumcNC;
+  return jc + ((N - jc) / NumcTiles<T>::NR) * NumcTiles<T>::NR;
+}
 
 // Unpacked path: column j is one of a narrow tile's scalar (unfused) columns.
 template <typename T>
@@ -247,6 +264,26 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
   const int64_t kblock = (KIND == kByte && rule8 == kRuleX86Packed) ? 512 : (int64_t)1 << 62;
   int64_t block_idx = 0;
 
+  // kFloatEdges: bit i*TN+j: output (i, j) lies in a remainder tile and K
+  // spans several blocks; its block sums accumulate in bsum.
+  static_assert(KIND != kFloatEdges || TM * TN <= 32, "edge mask");
+  constexpr bool kEdges = KIND == kFloatEdges;
+  Acc bsum[kEdges ? TM : 1][kEdges ? TN : 1];
+  uint32_t edge_mask = 0;
+  if constexpr (kEdges) {
+    if (g.K > kNumcKC) {
+      const int64_t er = edge_row<T>(g.M), ec = edge_col<T>(g.N);
+#pragma unroll
+      for (int i = 0; i < TM; i++)
+#pragma unroll
+        for (int j = 0; j < TN; j++) {
+          bsum[i][j] = Acc(0);
+          if (m0 + row_of(i) >= er || n0 + col_of(j) >= ec) edge_mask |= 1u << (i * TN + j);
+        }
+    }
+  }
+  int64_t edge_blk = 0;
+
   uint32_t unf_mask = 0;   // kFloatSmall: bit j: column j is an unfused one
   if constexpr (KIND == kFloatSmall) {
 #pragma unroll
@@ -280,6 +317,20 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
             acc[i][j] = madd<Acc>(av[i], bv[j], acc[i][j]);
           }
         }
+    }
+    if constexpr (kEdges) {
+      const int64_t kend = (t + 1) * BK;
+      if (edge_mask && (kend % kNumcKC == 0 || t + 1 == ntiles)) {
+#pragma unroll
+        for (int i = 0; i < TM; i++)
+#pragma unroll
+          for (int j = 0; j < TN; j++)
+            if ((edge_mask >> (i * TN + j)) & 1u) {
+              bsum[i][j] = edge_blk == 0 ? acc[i][j] : add_rn<Acc>(bsum[i][j], acc[i][j]);
+              acc[i][j] = Acc(0);
+            }
+        edge_blk++;
+      }
     }
     if constexpr (KIND == kByte) {
       const int64_t kend = (t + 1) * BK;
@@ -318,6 +369,7 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
       if (gj >= g.N) continue;
       T v;
       if constexpr (KIND == kByte) v = (T)dst[i][j];
+      else if constexpr (kEdges) v = (T)(((edge_mask >> (i * TN + j)) & 1u) ? bsum[i][j] : acc[i][j]);
       else v = (T)acc[i][j];
       if (g.bias) v = add_elem<T>(v, ((const T *)g.bias)[gj * g.bias_stride]);
       C[gi * g.rso + gj * g.cso] = v;
@@ -332,16 +384,6 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
 // multiples of the tile sizes): rows from edge_row(M), columns from
 // edge_col(N).  Their outputs are recomputed after the GEMM kernel: each
 // 256-deep K block as an FMA chain from zero, added to the running value.
-template <typename T> __host__ __device__ inline int64_t edge_row(int64_t M) {
-  if (M == 0) return 0;
-  const int64_t ic = ((M - 1) / NumcTiles<T>::MC) * NumcTiles<T>::MC;
-  return ic + ((M - ic) / kNumcMR) * kNumcMR;
-}
-template <typename T> __host__ __device__ inline int64_t edge_col(int64_t N) {
-  if (N == 0) return 0;
-  const int64_t jc = ((N - 1) / kNumcNC) * kNumcNC;
-  return jc + ((N - jc) / NumcTiles<T>::NR) * NumcTiles<T>::NR;
-}
 
 // Short K or many problems: remainder outputs in groups of 16 consecutive
 // columns of one row: first
@@ -358,6 +400,30 @@ __host__ __device__ inline int64_t float_edge_groups(int64_t M, int64_t N) {
 // Output `sub` (0..15) of remainder group `gi`: each 256-deep K block as an
 // FMA chain from zero, the block sums added in K order (numc's remainder
 // tiles).  Lanes past the last column return.
+// One numc K block of an output as an FMA chain from zero, k = pc .. pe-1
+// in order.  The operands are fetched 32 steps ahead into registers so the
+// chain waits for memory once per 32 steps, not once per step.
+template <typename T>
+__device__ __forceinline__ T chain_block(const T *A, int64_t csa, const T *B, int64_t rsb,
+                                         int64_t pc, int64_t pe) {
+  constexpr int U = 32;
+  T t = T(0);
+#pragma unroll 1
+  for (int64_t k0 = pc; k0 < pe; k0 += U) {
+    T av[U], bv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const bool in = k0 + u < pe;
+      av[u] = in ? A[(k0 + u) * csa] : T(0);
+      bv[u] = in ? B[(k0 + u) * rsb] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (k0 + u < pe) t = madd<T>(av[u], bv[u], t);
+  }
+  return t;
+}
+
 template <typename T>
 __device__ __forceinline__ void float_edge_output(const Gemm &g, int64_t gi, int sub, int64_t r0,
                                                   int64_t c0) {
@@ -375,9 +441,7 @@ __device__ __forceinline__ void float_edge_output(const Gemm &g, int64_t gi, int
   T d = T(0);
   for (int64_t pc = 0; pc < g.K; pc += kNumcKC) {
     const int64_t pe = min(pc + (int64_t)kNumcKC, g.K);
-    T t = T(0);
-#pragma unroll 8
-    for (int64_t k = pc; k < pe; k++) t = madd<T>(A[k * g.csa], B[k * g.rsb], t);
+    const T t = chain_block<T>(A, g.csa, B, g.rsb, pc, pe);
     d = pc == 0 ? t : add_rn<T>(d, t);
   }
   if (g.bias) d = add_elem<T>(d, ((const T *)g.bias)[j * g.bias_stride]);
@@ -419,8 +483,7 @@ __device__ __forceinline__ void float_edge_output_lanes(const Gemm &g, int64_t e
     T t = T(0);
     if (valid && kb < nkb) {
       const int64_t pc = kb * kNumcKC, pe = min(pc + (int64_t)kNumcKC, g.K);
-#pragma unroll 8
-      for (int64_t k = pc; k < pe; k++) t = madd<T>(A[k * g.csa], B[k * g.rsb], t);
+      t = chain_block<T>(A, g.csa, B, g.rsb, pc, pe);
     }
 #pragma unroll
     for (int q = 0; q < kEdgeLanes; q++) {

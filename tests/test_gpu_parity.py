@@ -62,6 +62,19 @@ def test_simt_is_numc_fma_chain(ctx, dt):
     np.testing.assert_array_equal(got, oracle.matmul(a, b))
 
 
+@pytest.mark.parametrize("dt", ["float32", "float64"])
+@pytest.mark.parametrize("shape", [(511, 600, 509), (512, 512, 512), (300, 257, 700),
+                                   (1000, 700, 1100), (1003, 1024, 997), (70, 300, 4200),
+                                   (2000, 600, 1700)],
+                         ids=lambda s: "x".join(map(str, s)))
+def test_remainder_tiles_every_tile_width(ctx, dt, shape):
+    """numc's remainder-tile outputs (per-256 K-block sums) on each tile
+    width the CUDA-core kernel picks: 32 and 64 sum them inside the tile
+    kernel, 128 in the separate fix-up pass."""
+    a, b = synth.operands("uniform", *shape, dtype=dt, seed=shape[1])
+    np.testing.assert_array_equal(_run_numc(ctx, a, b), oracle.matmul(a, b))
+
+
 @pytest.mark.parametrize("dt", ["int8", "uint8"])
 @pytest.mark.parametrize("profile", [nc.INT8_X86_AVX2, nc.INT8_ARM_NEON, nc.INT8_WRAP])
 def test_int8_profiles(ctx, dt, profile):
