@@ -127,7 +127,7 @@ cudaError_t launch_float_packed(const Gemm &g, cudaStream_t s) {
     }
   }
   if (t >= 64) return launch_tile<T, 64, 64, 4, 4, simt::kFloatEdges>(g, 0, s);
-  return launch_tile<T, 32, 32, 2, 2, simt::kFloatEdges>(g, 0, s);
+  return launch_tile<T, 32, 32, 2, 2, simt::kFloatEdges, 32>(g, 0, s);
 }
 
 }  // namespace

@@ -191,7 +191,10 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
   constexpr int LB = BK * BN / kThreads;   // B elements loaded per thread
   constexpr int TX = BN / TN;              // threads along N
   static_assert(TX * (BM / TM) == kThreads, "thread grid");
-  __shared__ __align__(16) Acc As[2][BK][BM];
+  // A is stored transposed (k-major): rows padded so that the lanes of a
+  // warp, which load along k for row-major A, store to distinct banks
+  constexpr int APAD = BK >= 32 ? 2 : 4;
+  __shared__ __align__(16) Acc As[2][BK][BM + APAD];
   __shared__ __align__(16) Acc Bs[2][BK][BN];
 
   const T *__restrict__ A = (const T *)g.a;
@@ -237,11 +240,14 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
     }
   };
 
-  // Rows/columns of this thread's register tile: two halves BM/2 apart.
+  // Rows/columns of this thread's register tile: two halves BM/2 apart,
+  // or, for 2 x 2 tiles, one adjacent pair (one 8-byte shared load each).
   auto row_of = [&](int i) {
+    if constexpr (TM == 2) return ty * 2 + i;
     return i < TM / 2 ? ty * (TM / 2) + i : BM / 2 + ty * (TM / 2) + (i - TM / 2);
   };
   auto col_of = [&](int j) {
+    if constexpr (TN == 2) return tx * 2 + j;
     return j < TN / 2 ? tx * (TN / 2) + j : BN / 2 + tx * (TN / 2) + (j - TN / 2);
   };
 
