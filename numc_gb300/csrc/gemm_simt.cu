@@ -108,7 +108,7 @@ cudaError_t launch_sized(const Gemm &g, int rule8, cudaStream_t s) {
   if constexpr (BIG >= 128)
     if (t == 128) return launch_tile<T, 128, 128, 8, 8, KIND>(g, rule8, s);
   if (t >= 64) return launch_tile<T, 64, 64, 4, 4, KIND>(g, rule8, s);
-  return launch_tile<T, 32, 32, 2, 2, KIND>(g, rule8, s);
+  return launch_tile<T, 32, 32, 2, 2, KIND, 32>(g, rule8, s);
 }
 
 // numc's packed float path: 64- and 32-wide tiles sum the remainder-tile
