@@ -408,7 +408,8 @@ __host__ __device__ inline int64_t float_edge_groups(int64_t M, int64_t N) {
 // tiles).  Lanes past the last column return.
 // One numc K block of an output as an FMA chain from zero, k = pc .. pe-1
 // in order.  The operands are fetched 32 steps ahead into registers so the
-// chain waits for memory once per 32 steps, not once per step.
+// chain waits for memory once per 32 steps, not once per step (for the
+// few-output, latency-bound fix-up; 232 registers a thread).
 template <typename T>
 __device__ __forceinline__ T chain_block(const T *A, int64_t csa, const T *B, int64_t rsb,
                                          int64_t pc, int64_t pe) {
@@ -447,7 +448,9 @@ __device__ __forceinline__ void float_edge_output(const Gemm &g, int64_t gi, int
   T d = T(0);
   for (int64_t pc = 0; pc < g.K; pc += kNumcKC) {
     const int64_t pe = min(pc + (int64_t)kNumcKC, g.K);
-    const T t = chain_block<T>(A, g.csa, B, g.rsb, pc, pe);
+    T t = T(0);
+#pragma unroll 8
+    for (int64_t k = pc; k < pe; k++) t = madd<T>(A[k * g.csa], B[k * g.rsb], t);
     d = pc == 0 ? t : add_rn<T>(d, t);
   }
   if (g.bias) d = add_elem<T>(d, ((const T *)g.bias)[j * g.bias_stride]);
