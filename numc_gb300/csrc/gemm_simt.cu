@@ -15,11 +15,11 @@ using simt::kThreads;
 // Two CTAs per SM (at most 128 registers) except for the int8/uint8 kernel,
 // whose per-block store rule keeps 64 partial sums and 64 stored bytes per
 // thread.
-template <typename T, int BM, int BN, int BK, int TM, int TN, int KIND, bool ROWMAJOR>
+template <typename T, int BM, int BN, int BK, int TM, int TN, int KIND>
 __global__ void __launch_bounds__(kThreads, KIND == simt::kByte ? 1 : 2)
 simt_gemm(Gemm g, int rule8) {
-  simt::simt_tile<T, BM, BN, BK, TM, TN, KIND, ROWMAJOR>(g, rule8, (int64_t)blockIdx.y * BM,
-                                                         (int64_t)blockIdx.x * BN);
+  simt::simt_tile<T, BM, BN, BK, TM, TN, KIND>(g, rule8, (int64_t)blockIdx.y * BM,
+                                               (int64_t)blockIdx.x * BN);
 }
 
 // 16 remainder groups (one a half-warp) per 256-thread block.
@@ -79,11 +79,7 @@ cudaError_t launch_tile(const Gemm &g, int rule8, cudaStream_t s) {
   if (g.M == 0 || g.N == 0) return cudaSuccess;
   int64_t gx = (g.N + BN - 1) / BN, gy = (g.M + BM - 1) / BM;
   if (gy > 65535 || gx > 0x7FFFFFFF) return cudaErrorInvalidConfiguration;
-  const dim3 grid((unsigned)gx, (unsigned)gy);
-  if (g.csa == 1 && g.csb == 1)
-    simt_gemm<T, BM, BN, BK, TM, TN, KIND, true><<<grid, kThreads, 0, s>>>(g, rule8);
-  else
-    simt_gemm<T, BM, BN, BK, TM, TN, KIND, false><<<grid, kThreads, 0, s>>>(g, rule8);
+  simt_gemm<T, BM, BN, BK, TM, TN, KIND><<<dim3((unsigned)gx, (unsigned)gy), kThreads, 0, s>>>(g, rule8);
   count_launch();
   return cudaGetLastError();
 }

@@ -184,7 +184,7 @@ __device__ __forceinline__ Acc widen(T v) {
 
 // One BM x BN output tile at (m0, n0) of problem g, by a kThreads-thread
 // block.
-template <typename T, int BM, int BN, int BK, int TM, int TN, int KIND, bool ROWMAJOR = false>
+template <typename T, int BM, int BN, int BK, int TM, int TN, int KIND>
 __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, int64_t n0) {
   using Acc = typename AccOf<T>::type;
   constexpr int LA = BM * BK / kThreads;   // A elements loaded per thread
@@ -205,30 +205,23 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
   const bool a_kfast = g.csa == 1, b_nfast = g.csb == 1 || g.rsb != 1;
 
   Acc ra[LA], rb[LB];
-  // ROWMAJOR (A and B with unit column stride, numc's contiguous arrays):
-  // each thread's operand elements sit at fixed offsets from two pointers,
-  // so tiles inside the matrix load without index arithmetic or checks.
-  const T *pa = A, *pb = B;
-  int64_t a_step = 0, b_step = 0;
-  bool inner_mn = false;
-  if constexpr (ROWMAJOR) {
-    static_assert(kThreads % BK == 0 && kThreads % BN == 0, "load mapping");
-    pa = A + (m0 + tid / BK) * g.rsa + tid % BK;          // row tid/BK + q*256/BK
-    pb = B + (int64_t)(tid / BN) * g.rsb + n0 + tid % BN;  // k tid/BN + q*256/BN
-    a_step = (int64_t)(kThreads / BK) * g.rsa;
-    b_step = (int64_t)(kThreads / BN) * g.rsb;
-    inner_mn = m0 + BM <= g.M && n0 + BN <= g.N;
-  }
+  // A and B with unit column stride (numc's contiguous arrays) and a tile
+  // inside the matrix: each thread's operand elements sit at fixed offsets
+  // from two pointers, so they load without index arithmetic or checks.
+  static_assert(kThreads % BK == 0 && kThreads % BN == 0, "load mapping");
+  const bool inner_mn = g.csa == 1 && g.csb == 1 && m0 + BM <= g.M && n0 + BN <= g.N;
+  const T *pa = A + (m0 + tid / BK) * g.rsa + tid % BK;          // row tid/BK + q*256/BK
+  const T *pb = B + (int64_t)(tid / BN) * g.rsb + n0 + tid % BN;  // k tid/BN + q*256/BN
+  const int64_t a_step = (int64_t)(kThreads / BK) * g.rsa;
+  const int64_t b_step = (int64_t)(kThreads / BN) * g.rsb;
   auto load_tiles = [&](int64_t k0) {
-    if constexpr (ROWMAJOR) {
-      if (inner_mn && k0 + BK <= g.K) {
-        const T *a0 = pa + k0, *b0 = pb + k0 * g.rsb;
+    if (inner_mn && k0 + BK <= g.K) {
+      const T *a0 = pa + k0, *b0 = pb + k0 * g.rsb;
 #pragma unroll
-        for (int q = 0; q < LA; q++) ra[q] = widen<T, Acc>(a0[q * a_step]);
+      for (int q = 0; q < LA; q++) ra[q] = widen<T, Acc>(a0[q * a_step]);
 #pragma unroll
-        for (int q = 0; q < LB; q++) rb[q] = widen<T, Acc>(b0[q * b_step]);
-        return;
-      }
+      for (int q = 0; q < LB; q++) rb[q] = widen<T, Acc>(b0[q * b_step]);
+      return;
     }
 #pragma unroll
     for (int q = 0; q < LA; q++) {
