@@ -351,7 +351,13 @@ int matmul_pipelined(const NumcArray *a, const NumcArray *b, NumcArray *out, con
                      cudaStream_t s) {
   NumcCtx *ctx = out->ctx;
   const size_t M = a->shape[0], K = a->shape[1], N = b->shape[1], es = 4;
-  const size_t want = M >= 4096 ? 4 : 2;
+  // panels of A (rows) and of B (columns): NUMC_CUDA_PIPE_PANELS, else 4
+  // from 4096 rows, 2 below
+  size_t want = M >= 4096 ? 4 : 2;
+  if (const char *pe = getenv("NUMC_CUDA_PIPE_PANELS")) {
+    const long v = strtol(pe, nullptr, 10);
+    if (v >= 1 && v <= 64) want = (size_t)v;
+  }
   const size_t rows = align_up((M + want - 1) / want, 256);
   const size_t sb0 = b->strides[0], sb1 = b->strides[1];
   // 1: B's rows contiguous, 2: its columns contiguous, 0: neither
