@@ -113,3 +113,13 @@ def test_pipeline_panel_grid(shape):
     np.testing.assert_array_equal(got, _device_result(a, b, nc.ALGO_SPLIT_FP16, 0))
     got3 = _host_result(a, b, nc.ALGO_SPLIT_BF16, 3)
     np.testing.assert_array_equal(got3, _device_result(a, b, nc.ALGO_SPLIT_BF16, 3))
+
+
+@pytest.mark.parametrize("panels", ["1", "3", "5"])
+def test_panel_count_knob(panels, monkeypatch):
+    """NUMC_CUDA_PIPE_PANELS changes only where the panels split."""
+    M, K, N = 2304, 1024, 2560   # M K N >= 2^32: the pipeline's threshold
+    a, b = synth.operands("normal", M, K, N, dtype="float32", seed=19)
+    monkeypatch.setenv("NUMC_CUDA_PIPE_PANELS", panels)
+    got = _host_result(a, b, nc.ALGO_SPLIT_FP16, 0)
+    np.testing.assert_array_equal(got, _device_result(a, b, nc.ALGO_SPLIT_FP16, 0))
