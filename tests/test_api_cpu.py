@@ -176,3 +176,25 @@ def test_algo_settings():
             nc.set_algo("int32", nc.ALGO_SPLIT_BF16, 0)
     finally:
         nc.set_algo("float64", *orig)
+
+
+def _up(x, a):
+    return (x + a - 1) // a * a
+
+
+@pytest.mark.parametrize("M,K,N", [(1000, 700, 300), (1, 1, 1), (4096, 4096, 4096), (129, 513, 65)])
+def test_workspace_sizes(M, K, N):
+    """numc_cuda_gemm_workspace_size: the layouts the kernels carve their
+    scratch into (each part 256-byte aligned), computed on the host."""
+    kp = _up(K, 512)
+    assert nc.workspace_size("int8", nc.ALGO_TC_INT8, 0, M, K, N) == \
+        _up(M * kp * 2, 256) + _up(N * kp * 2, 256)
+    for s in (4, 8):
+        kp = _up(K, 64)
+        want = (_up(M * 8, 256) + _up(N * 8, 256) + _up(-(-M // 128) * 8, 256) +
+                _up(-(-N // 64) * 8, 256) + _up(s * M * kp * 2, 256) + _up(s * N * kp * 2, 256))
+        assert nc.workspace_size("float64", nc.ALGO_OZAKI, s, M, K, N) == want
+    assert nc.workspace_size("float32", nc.ALGO_SIMT, 0, M, K, N) == 0
+    assert nc.workspace_size("float64", nc.ALGO_DMMA, 0, M, K, N) == 0
+    # split products: at least the two 16-bit planes of both operands
+    assert nc.workspace_size("float32", nc.ALGO_SPLIT_FP16, 0, M, K, N) >= 4 * (M + N) * _up(K, 64)
