@@ -13,9 +13,11 @@
 // and tile class, NEON clamp-once, or truncation).  Results are bit-exact.
 //
 // Passes: one convert launch writes A as bf16 (M x Kp, K-major) and B^T as
-// bf16 (N x Kp), K padded to 512 with zeros; then one 128 x 64 output tile
-// per CTA with a 24 KiB TMA ring stage (8 stages), 320 threads (TMA warp,
-// MMA warp, 8 accumulator warps of 32 columns).
+// bf16 (N x Kp), K padded to 512 with zeros; then one output tile per CTA:
+// 128 x 64 (24 KiB TMA ring stages, 8 of them, 320 threads) or, once the
+// 128 x 128 tiles give every SM one, 128 x 128 (32 KiB stages, 6 of them,
+// 576 threads): a TMA warp, an MMA warp and accumulator warps of 32 columns
+// each, which store their 32 output bytes of a row as two 16-byte stores.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
