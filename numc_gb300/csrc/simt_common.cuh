@@ -2,16 +2,20 @@
 //
 // One templated tile kernel: a BM x BN output tile per 256-thread CTA, a
 // BK-deep K slab staged through double-buffered shared memory (next slab
-// prefetched into registers while the current one is consumed), and a
-// TM x TN register tile per thread split into two halves BM/2 (BN/2) apart
-// so shared-memory reads are conflict-free float4-width rows.
+// prefetched into registers while the current one is consumed; for
+// row-major operands and inner tiles from fixed per-thread offsets, with
+// no index arithmetic), and a TM x TN register tile per thread split into
+// two halves BM/2 (BN/2) apart so shared-memory reads are conflict-free
+// float4-width rows (2 x 2 tiles: one adjacent pair).
 //
 // Arithmetic per dtype reproduces numc (src/intrinsics/gemm_avx2.h):
 //   float32/float64  one fused multiply-add chain per output in k order
 //                    from +0, exactly numc's full-tile micro-kernels
 //                    (gemm_ukernel_f32_6x16_avx2.S keeps one FMA
 //                    accumulator per output and reloads it between K
-//                    blocks); only numc's remainder tiles round differently.
+//                    blocks); numc's remainder tiles sum each 256-deep K
+//                    block separately (kFloatEdges, or the float_edges
+//                    pass after 128-wide tiles).
 //   int16..uint64    products and sums wrap in 32 (16- and 32-bit types)
 //                    or 64 bits, then truncate: the exact sum modulo 2^bits,
 //                    as numc's vpmullw/vpmulld/emulated-64-bit kernels give.
