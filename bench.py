@@ -35,6 +35,9 @@ sys.path.insert(0, ROOT)
 M = N = K = 8192
 SEED = 42
 FLOPS = 2.0 * M * N * K
+# One metric string for both arms (ours and --impl reference), so the two
+# lines compare directly; how each arm computes it goes into `config`.
+METRIC = "numc_matmul float32 8192^3 TFLOP/s"
 
 
 def parse():
@@ -224,11 +227,13 @@ def run_reference(args, world, rank):
     value = 2.0 * rows * K * N / dt / 1e12
     sample = f"first {rows} of {M} rows of A per step (float32 N(0,1), K=N={K})"
     print(json.dumps({
-        "impl": "reference", "metric": "numc_matmul float32 8192^3 TFLOP/s",
+        "impl": "reference", "metric": METRIC,
         "value": value, "unit": "TFLOP/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "f32 8192x8192x8192 N(0,1), seed 42", "sample": sample},
+        "config": {"workload": "f32 8192x8192x8192 N(0,1), seed 42",
+                   "method": f"numc's float32 arithmetic on the host cores ({kind})",
+                   "sample": sample},
         "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": kind,
                          "sample": sample},
         "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
@@ -391,14 +396,14 @@ def main():
                 "algorithmic_flops_per_launch": tensor_flops}
 
     result = {
-        "metric": "numc_matmul float32 8192^3 TFLOP/s (3-pass split on tcgen05 at float32-level "
-                  "error vs plain FP32-SIMT)",
+        "metric": METRIC,
         "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded splitmix64 N(0,1))",
-        "config": {"workload": "f32 8192x8192x8192 N(0,1), seed 42, 3-pass split from "
-                               "row/column-scaled float16 planes (NUMC_CUDA_ALGO_SPLIT_FP16)",
+        "config": {"workload": "f32 8192x8192x8192 N(0,1), seed 42",
+                   "method": "3-pass split on tcgen05 from row/column-scaled float16 planes "
+                             "(NUMC_CUDA_ALGO_SPLIT_FP16), float32-level error vs plain FP32-SIMT",
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs 512 MiB + split planes 512 MiB > 126 MiB L2, no flush"},
         "gpu_launches": int(launches),
@@ -416,10 +421,51 @@ def main():
         result["cpu_baseline"] = {
             "value": tflops, "unit": "TFLOP/s", "cores": cores, "kind": kind,
             "sample": f"first {rows} of {M} rows of A ({t:.1f} s), numc float32 arithmetic"}
+        if not args.quick:
+            # last key: the end of the line is what a truncated log keeps
+            result["accuracy"] = accuracy_summary(result)
         print(json.dumps(result), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def accuracy_summary(r):
+    """The speed-ups and errors against float64-accurate oracles that the
+    side workloads measured, in short keys: max / mean elementwise relative
+    error (float32 and grouped workloads) or max error relative to |A||B|
+    (float64), and integer bit-exactness against numc's outputs."""
+    def mm(e):
+        return [float(f"{e['max_rel']:.3g}"), float(f"{e['mean_rel']:.3g}")]
+    out = {}
+    ev = r.get("errors_vs_fp64_oracle", {})
+    for case in ("well_scaled", "ill_scaled"):
+        if case in ev:
+            out[f"f32_8192_{case}"] = {"split16": mm(ev[case]["split_fp16 (headline)"]),
+                                       "plain": mm(ev[case]["plain_fp32"])}
+    if "split_vs_plain" in r:
+        out["f32_8192_split_vs_plain"] = round(r["split_vs_plain"], 2)
+    f64 = r.get("f64_4096")
+    if f64:
+        out["f64_4096_err_to_absprod"] = {
+            k: float(f"{v['max_rel_to_absprod']:.3g}") for k, v in f64.items()
+            if isinstance(v, dict) and "max_rel_to_absprod" in v}
+        out["f64_4096_ozaki_s8_vs_dmma"] = round(f64["ozaki_s8_vs_dmma"], 2)
+        out["f64_4096_ozaki_s7_vs_dmma"] = round(f64["ozaki_s7"]["tflops"] /
+                                                 f64["dmma"]["tflops"], 2)
+    g = r.get("grouped")
+    if g:
+        out["grouped_err_to_absprod"] = {
+            k: [float(f"{g[k]['max_rel_to_absprod']:.3g}"),
+                float(f"{g[k]['mean_rel_to_absprod']:.3g}")]
+            for k in ("split_fp16", "split_bf16", "plain") if k in g}
+        out["grouped_split_vs_plain"] = round(g["split_vs_plain_grouped"], 2)
+    ints = r.get("int_1024")
+    if ints:
+        out["int_1024_bitexact"] = all(
+            v["bitexact_vs_numc"] for dt in ("int8", "uint8", "int32", "int64")
+            for v in ints.get(dt, {}).values())
+    return out
 
 
 # The headline kernel, and its DRAM bytes (read + write) per launch at
@@ -726,23 +772,8 @@ def grouped_workload(nc, torch, oracle, dev):
     (scaled float16 planes, the default, and bfloat16 planes) vs plain,
     against one launch per problem (also graph-captured, so host overhead is
     excluded)."""
-    rng = np.random.default_rng(SEED)
-    dims = np.exp(rng.uniform(np.log(16), np.log(1024), (2048, 3))).round().astype(int)
-    gen = torch.Generator(device=dev).manual_seed(SEED)
-    probs = []
-    for (Mi, Ni, Ki) in dims:
-        a = torch.rand((Mi, Ki), device=dev, generator=gen) * 2 - 1
-        b = torch.rand((Ki, Ni), device=dev, generator=gen) * 2 - 1
-        probs.append((a, b, torch.empty((Mi, Ni), device=dev)))
-    chains = []
-    for _ in range(256):
-        x = torch.rand((256, 784), device=dev, generator=gen) * 2 - 1
-        w1 = torch.randn((784, 128), device=dev, generator=gen) * 0.05
-        w2 = torch.randn((128, 10), device=dev, generator=gen) * 0.05
-        chains.append((x, w1, w2, torch.empty((256, 128), device=dev),
-                       torch.empty((256, 10), device=dev)))
-    flops = float(sum(2.0 * m * n * k for m, n, k in dims)) + \
-        256 * 2.0 * 256 * (784 * 128 + 128 * 10)
+    from numc_gb300 import synth
+    dims, probs, chains, flops = synth.grouped_case(torch, dev, SEED)
 
     def timed(fn, reps=10):
         fn()

@@ -140,6 +140,18 @@ NUMC_API int numc_cuda_gemm(NumcDType dtype, int algo, int param,
  * wait (NUMC_ERR_INTERNAL); clears the flag. */
 NUMC_API int numc_cuda_check_status(void *stream);
 
+/* Testing aids for the failure paths (no counterpart in numc).
+ * numc_cuda_debug_fail_malloc: the next `count` device allocations this
+ * library makes fail as if the device were out of memory, so the calls
+ * that needed them return NUMC_ERR_MALLOC (0 cancels).
+ * numc_cuda_debug_wait_timeout: the tensor-core kernels launched from now
+ * on give up a bounded wait after `limit_ns` nanoseconds (0 restores the
+ * default, 2 s); with `starve` nonzero their TMA producers also issue no
+ * loads, so every wait runs out, no copy or MMA is in flight when the
+ * kernel leaves, and numc_cuda_check_status() reports NUMC_ERR_INTERNAL. */
+NUMC_API int numc_cuda_debug_fail_malloc(int count);
+NUMC_API int numc_cuda_debug_wait_timeout(unsigned long long limit_ns, int starve);
+
 /* Number of kernels this library has launched since load (diagnostics). */
 NUMC_API uint64_t numc_cuda_launch_count(void);
 /* Bytes of array data this library has copied between host and device
@@ -200,19 +212,25 @@ NUMC_API int numc_matmul_grouped(const NumcArray *const *a,
                                  NumcArray *const *out, size_t n);
 
 /* float32 split-BF16 GEMM that allocates nothing.  No counterpart in the
- * reference (numc has no GPU API); it exists for callers that cannot
- * allocate device memory when they call — work recorded into CUDA graphs
- * or issued from stream callbacks, services that forbid allocation after
- * start-up, hosts whose device memory belongs to another allocator.
+ * reference (numc has no GPU API).  It is for callers that cannot call
+ * cudaMalloc when they run a product: services that forbid device
+ * allocation after start-up (an allocation can synchronise the device and
+ * take milliseconds), and plugins inside a host program whose device memory
+ * belongs to that program's own allocator.
  * Scratch is a 64 MiB array compiled into the library (held by every GPU
  * that loads it until exit), so 4*(M+N)*roundup(K,64) bytes plus a few
  * flag words must fit; larger problems are rejected with NUMC_ERR_VALUE.
- * The caller passes device pointers for a, b, out and, optionally, a
+ * The caller passes device pointers for a, b and out and, optionally, a
  * device word `status` that the call clears and a kernel sets nonzero if
- * it abandoned a bounded wait.  The first call on each device looks up the
- * scratch address (make it before any stream capture).  Calls share the
- * scratch: calls that overlap on the GPU race and must be serialised.
- * Asynchronous on `stream`, like numc_cuda_gemm. */
+ * it abandoned a bounded wait.  With status == NULL the library's own
+ * status word is used instead: it keeps the first failure until
+ * numc_cuda_check_status() reads it.  Either way `out` is valid only if
+ * the status word reads 0 after the call's work has finished.  The first
+ * call on each device looks up the scratch address, which loads the
+ * library's device code there if it is not loaded yet; make that first call
+ * before any stream capture.  Calls share the scratch: calls that overlap
+ * on the GPU race and must be serialised.  Asynchronous on `stream`, like
+ * numc_cuda_gemm. */
 NUMC_API int numc_cuda_sgemm_split_static(const float *a, const float *b,
                                           float *out, size_t M, size_t K,
                                           size_t N, intptr_t rsa, intptr_t csa,

@@ -19,6 +19,7 @@
 
 #include "kernels.h"
 #include "runtime.h"
+#include "status.h"
 
 using namespace numc_rt;
 
@@ -132,7 +133,7 @@ int library_workspace(size_t bytes, cudaStream_t s, void **out) {
       g_ws_bytes[dev] = 0;
     }
     size_t grow = bytes + bytes / 4;
-    CU(cudaMalloc(&g_ws[dev], grow), "cudaMalloc(workspace)");
+    CU(numc_k::dev_malloc(&g_ws[dev], grow), "cudaMalloc(workspace)");
     g_ws_bytes[dev] = grow;
   }
   (void)s;
@@ -274,7 +275,7 @@ int ctx_scratch(NumcCtx *ctx, size_t bytes, cudaStream_t s, char **out) {
       ctx->scratch_bytes = 0;
     }
     size_t grow = align_up(bytes + bytes / 4, 1 << 20);
-    CU(cudaMalloc(&ctx->scratch, grow), "cudaMalloc(scratch)");
+    CU(numc_k::dev_malloc(&ctx->scratch, grow), "cudaMalloc(scratch)");
     ctx->scratch_bytes = grow;
   }
   *out = (char *)ctx->scratch;
@@ -614,7 +615,7 @@ int device_copy_contiguous(const NumcArray *src, NumcArray *dst) {
   if (!dst->dev_base) {
     const size_t bytes = dst->capacity;
     void *p = nullptr;
-    CU(cudaMalloc(&p, align_up(bytes ? bytes : 1, 256)), "cudaMalloc(array)");
+    CU(numc_k::dev_malloc(&p, align_up(bytes ? bytes : 1, 256)), "cudaMalloc(array)");
     dst->ctx->dev_allocs->push_back(DeviceAlloc{p, bytes, dst->pos});
     dst->dev_base = (char *)p;
   }
@@ -1099,7 +1100,7 @@ extern "C" int numc_cuda_array_to_device(NumcArray *arr) {
   size_t span = array_span_bytes(arr);
   if (!arr->dev_base) {
     void *p = nullptr;
-    CU(cudaMalloc(&p, align_up(span ? span : 1, 256)), "cudaMalloc(array)");
+    CU(numc_k::dev_malloc(&p, align_up(span ? span : 1, 256)), "cudaMalloc(array)");
     arr->ctx->dev_allocs->push_back(DeviceAlloc{p, span, arr->pos});
     arr->dev_base = (char *)p;
   }
@@ -1147,7 +1148,7 @@ NumcArray *rand_array(NumcCtx *ctx, const size_t *shape, size_t dim, NumcDType d
   const size_t bytes = arr->capacity;
   if (!arr->dev_base) {
     void *p = nullptr;
-    cudaError_t e = cudaMalloc(&p, align_up(bytes ? bytes : 1, 256));
+    cudaError_t e = numc_k::dev_malloc(&p, align_up(bytes ? bytes : 1, 256));
     if (e != cudaSuccess) {
       cuda_fail(e, "cudaMalloc(array)");
       return nullptr;
@@ -1275,8 +1276,12 @@ extern "C" int numc_cuda_gemm(NumcDType dt, int algo, int param, const void *a,
 }
 
 extern "C" int numc_cuda_check_status(void *stream) {
-  unsigned st = 0;
+  unsigned st = 0, st_static = 0;
   CU(numc_k::read_and_clear_status(&st, (cudaStream_t)stream), "status read");
+  // numc_cuda_sgemm_split_static calls made without a status word of their
+  // own report through the library's static word.
+  CU((cudaError_t)numc_k::static_status_read_and_clear(&st_static, stream), "status read");
+  if (!st) st = st_static;
   if (st) return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "a kernel abandoned a bounded wait (code %u)", st);
   return 0;
 }

@@ -241,14 +241,14 @@ struct Cfg {
   static constexpr int CW = BN / 2;
   static constexpr int THREADS = 64 + 32 * ACC_WARPS;
   static_assert(SMEM <= 232448, "shared memory");
-  static_assert((2 * STAGES + 2 * NBUF) * 8 + 4 <= 256, "barrier space");
+  static_assert((2 * STAGES + 2 * NBUF + 1) * 8 + 4 <= 256, "barrier space");
 };
 
 template <int BN, int STAGES, int FLUSH, bool F16>
 __global__ void __launch_bounds__(Cfg<BN, STAGES, FLUSH>::THREADS, 1)
 grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict__ probs,
                    const Tile *__restrict__ tiles, int ntiles, unsigned *status,
-                   unsigned long long gen) {
+                   unsigned long long gen, WaitCfg wc) {
   using C_ = Cfg<BN, STAGES, FLUSH>;
   constexpr int NBUF = C_::NBUF;
   extern __shared__ uint8_t smem_raw[];
@@ -256,7 +256,8 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
   uint64_t *bars = (uint64_t *)(smem + STAGES * C_::STAGE_BYTES);
   uint64_t *full = bars, *empty = bars + STAGES;
   uint64_t *tfull = bars + 2 * STAGES, *tempty = tfull + NBUF;
-  uint32_t *tmem_slot = (uint32_t *)(tempty + NBUF);
+  uint64_t *drain = tempty + NBUF;   // all issued MMAs complete
+  uint32_t *tmem_slot = (uint32_t *)(drain + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
@@ -268,6 +269,7 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
       tc::mbar_init(tc::smem_u32(&tfull[b]), 1);
       tc::mbar_init(tc::smem_u32(&tempty[b]), C_::ACC_WARPS);
     }
+    tc::mbar_init(tc::smem_u32(drain), 1);
     tc::fence_barrier_init();
   }
   if (warp == 1) tc::tmem_alloc(tc::smem_u32(tmem_slot), 512);
@@ -290,10 +292,11 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
           const int s = g % STAGES;
           if (g >= STAGES &&
               !tc::mbar_wait_bounded(tc::smem_u32(&empty[s]), ((g / STAGES) & 1) ^ 1, status,
-                                     kStatusTimeoutProducer)) {
+                                     kStatusTimeoutProducer, wc.limit_ns)) {
             live = false;
             break;
           }
+          if (wc.starve) continue;   // give-up test: no load, no barrier completes
           const uint32_t fbar = tc::smem_u32(&full[s]);
           const uint32_t st = tc::smem_u32(smem + s * C_::STAGE_BYTES);
           tc::mbar_arrive_expect_tx(fbar, C_::STAGE_BYTES);
@@ -320,12 +323,12 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
           const bool cend = kb % FLUSH == FLUSH - 1 || kb == nkb - 1;
           if (cstart && chunk >= NBUF &&
               !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / NBUF) & 1) ^ 1,
-                                     status, kStatusTimeoutMma)) {
+                                     status, kStatusTimeoutMma, wc.limit_ns)) {
             live = false;
             break;
           }
           if (!tc::mbar_wait_bounded(tc::smem_u32(&full[s]), (g / STAGES) & 1, status,
-                                     kStatusTimeoutMma)) {
+                                     kStatusTimeoutMma, wc.limit_ns)) {
             live = false;
             break;
           }
@@ -353,6 +356,10 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
           }
         }
       }
+      // Every MMA issued above completes before TMEM is released, also when
+      // the loop gave up (a commit with none outstanding arrives at once).
+      tc::mma_commit(tc::smem_u32(drain));
+      tc::mbar_wait_bounded(tc::smem_u32(drain), 0, status, kStatusTimeoutDrain, wc.limit_ns);
     }
     __syncwarp();
   } else {
@@ -373,7 +380,7 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
       for (int c = 0; c < nchunks; c++, chunk++) {
         const int buf = chunk % NBUF;
         ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / NBUF) & 1, status,
-                                   kStatusTimeoutEpilogue);
+                                   kStatusTimeoutEpilogue, wc.limit_ns);
         ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
         if (!ok) break;
         tc::tc_fence_after();
@@ -615,7 +622,7 @@ cudaError_t launch_tc(const NumcCudaGemmPlan *p, int var, unsigned *status, cuda
   auto kern = grouped_split_gemm<BN, STAGES, FLUSH, F16>;
   const int grid = std::min(p->ntiles[var], p->sms);
   kern<<<grid, C_::THREADS, C_::SMEM, s>>>(p->d_tmaps, p->d_probs, p->d_tiles[var],
-                                          p->ntiles[var], status, p->gen);
+                                          p->ntiles[var], status, p->gen, wait_cfg());
   return cudaGetLastError();
 }
 
@@ -849,7 +856,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   const size_t o_flags = off; off = align_up(off + flags_bytes, 256);
   const size_t o_planes = off; off += planes_bytes;
   p->dev_bytes = off;
-  cudaError_t e = cudaMalloc(&p->dev, off ? off : 256);
+  cudaError_t e = dev_malloc((void **)&p->dev, off ? off : 256);
   if (e) {
     delete p;
     fail(e, "plan workspace");

@@ -148,7 +148,7 @@ template <bool SIGNED, int kBN>
 __global__ void __launch_bounds__(I8Cfg<kBN>::kThreads, 1)
 int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB,
              uint8_t *__restrict__ C, int64_t rso, int64_t cso, int M, int N, int num_kb,
-             int tiles_m, int tiles_n, int rule, unsigned *status) {
+             int tiles_m, int tiles_n, int rule, unsigned *status, WaitCfg wc) {
   constexpr int kNumBuf = I8Cfg<kBN>::kNumBuf, kStages = I8Cfg<kBN>::kStages;
   constexpr int kAccWarps = I8Cfg<kBN>::kAccWarps;
   // slabs per TMEM chunk: a whole 512-deep block for int8, half for uint8
@@ -161,7 +161,8 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
   uint64_t *bars = (uint64_t *)(smem + kStages * STAGE_BYTES);
   uint64_t *full = bars, *empty = bars + kStages;
   uint64_t *tfull = bars + 2 * kStages, *tempty = tfull + kNumBuf;
-  uint32_t *tmem_slot = (uint32_t *)(tempty + kNumBuf);
+  uint64_t *drain = tempty + kNumBuf;   // all issued MMAs complete
+  uint32_t *tmem_slot = (uint32_t *)(drain + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   const int tile = blockIdx.x;
@@ -182,6 +183,7 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
       tc::mbar_init(tc::smem_u32(&tfull[b]), 1);
       tc::mbar_init(tc::smem_u32(&tempty[b]), kAccWarps);
     }
+    tc::mbar_init(tc::smem_u32(drain), 1);
     tc::fence_barrier_init();
     tc::tma_prefetch_desc(&tA);
     tc::tma_prefetch_desc(&tB);
@@ -198,8 +200,9 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
         const int s = kb % kStages;
         if (kb >= kStages &&
             !tc::mbar_wait_bounded(tc::smem_u32(&empty[s]), ((kb / kStages) & 1) ^ 1, status,
-                                   kStatusTimeoutProducer))
+                                   kStatusTimeoutProducer, wc.limit_ns))
           break;
+        if (wc.starve) continue;   // give-up test: no load, no barrier completes
         const uint32_t fbar = tc::smem_u32(&full[s]);
         const uint32_t st = tc::smem_u32(smem + s * STAGE_BYTES);
         tc::mbar_arrive_expect_tx(fbar, STAGE_BYTES);
@@ -216,10 +219,10 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
         const bool cstart = kb % CHUNK == 0, cend = kb % CHUNK == CHUNK - 1;
         if (cstart && chunk >= kNumBuf &&
             !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / kNumBuf) & 1) ^ 1,
-                                   status, kStatusTimeoutMma))
+                                   status, kStatusTimeoutMma, wc.limit_ns))
           break;
         if (!tc::mbar_wait_bounded(tc::smem_u32(&full[s]), (kb / kStages) & 1, status,
-                                   kStatusTimeoutMma))
+                                   kStatusTimeoutMma, wc.limit_ns))
           break;
         tc::tc_fence_after();
         const uint32_t sa = tc::smem_u32(smem + s * STAGE_BYTES), sb = sa + A_BYTES;
@@ -230,6 +233,10 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
         tc::mma_commit(tc::smem_u32(&empty[s]));
         if (cend) tc::mma_commit(tc::smem_u32(&tfull[buf]));
       }
+      // Every MMA issued above completes before TMEM is released, also when
+      // the loop gave up (a commit with none outstanding arrives at once).
+      tc::mma_commit(tc::smem_u32(drain));
+      tc::mbar_wait_bounded(tc::smem_u32(drain), 0, status, kStatusTimeoutDrain, wc.limit_ns);
     }
     __syncwarp();
   } else {
@@ -251,7 +258,7 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
     for (int chunk = 0; chunk < nchunks; chunk++) {
       const int buf = chunk % kNumBuf;
       ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / kNumBuf) & 1, status,
-                                 kStatusTimeoutEpilogue);
+                                 kStatusTimeoutEpilogue, wc.limit_ns);
       ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
       if (!ok) break;
       tc::tc_fence_after();
@@ -345,7 +352,7 @@ cudaError_t launch_i8_gemm(const Gemm &g, int rule, const I8Layout &L, __nv_bflo
   if ((e = make_tmap_2d(&tb, pb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, g.N, L.Kp, L.Kp, kBN, kBK)))
     return e;
   constexpr uint32_t kBarBytes = 512;   // 2*(kStages + kNumBuf) mbarriers + TMEM slot
-  static_assert((2 * Cfg::kStages + 2 * Cfg::kNumBuf) * 8 + 4 <= kBarBytes, "barrier space");
+  static_assert((2 * Cfg::kStages + 2 * Cfg::kNumBuf + 1) * 8 + 4 <= kBarBytes, "barrier space");
   constexpr uint32_t SMEM = Cfg::kStages * (kBM + kBN) * kBK * 2 + 1024 + kBarBytes;
   static_assert(SMEM <= 232448, "shared memory");
   if ((e = cudaFuncSetAttribute(int8_tc_gemm<SIGNED, kBN>,
@@ -354,7 +361,7 @@ cudaError_t launch_i8_gemm(const Gemm &g, int rule, const I8Layout &L, __nv_bflo
   const int tiles_m = (int)((g.M + kBM - 1) / kBM), tiles_n = (int)((g.N + kBN - 1) / kBN);
   int8_tc_gemm<SIGNED, kBN><<<tiles_m * tiles_n, Cfg::kThreads, SMEM, s>>>(
       ta, tb, (uint8_t *)g.c, g.rso, g.cso, (int)g.M, (int)g.N, (int)(L.Kp / kBK), tiles_m,
-      tiles_n, rule, status);
+      tiles_n, rule, status, wait_cfg());
   count_launch();
   return cudaGetLastError();
 }

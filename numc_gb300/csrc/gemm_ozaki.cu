@@ -196,7 +196,7 @@ __device__ __forceinline__ int exponent_of(unsigned long long bits) {
 __global__ void __launch_bounds__(kThreads, 1)
 ozaki_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB,
            double *__restrict__ C, int64_t rso, int64_t cso, int M, int N, int num_kb,
-           int tiles_m, int tiles_n, unsigned *status, OzParams op) {
+           int tiles_m, int tiles_n, unsigned *status, OzParams op, WaitCfg wc) {
   constexpr uint32_t A_BYTES = kBM * kBK * 2, B_BYTES = kBN * kBK * 2;
   constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
   extern __shared__ uint8_t smem_raw[];
@@ -204,7 +204,8 @@ ozaki_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
   uint64_t *bars = (uint64_t *)(smem + kStages * STAGE_BYTES);
   uint64_t *full = bars, *empty = bars + kStages;
   uint64_t *tfull = bars + 2 * kStages, *tempty = tfull + kNumBuf;
-  uint32_t *tmem_slot = (uint32_t *)(tempty + kNumBuf);
+  uint64_t *drain = tempty + kNumBuf;   // all issued MMAs complete
+  uint32_t *tmem_slot = (uint32_t *)(drain + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = op.slices;
@@ -227,6 +228,7 @@ ozaki_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
       tc::mbar_init(tc::smem_u32(&tfull[b]), 1);
       tc::mbar_init(tc::smem_u32(&tempty[b]), kAccWarps);
     }
+    tc::mbar_init(tc::smem_u32(drain), 1);
     tc::fence_barrier_init();
     tc::tma_prefetch_desc(&tA);
     tc::tma_prefetch_desc(&tB);
@@ -249,10 +251,11 @@ ozaki_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
             const int st = g % kStages;
             if (g >= kStages &&
                 !tc::mbar_wait_bounded(tc::smem_u32(&empty[st]), ((g / kStages) & 1) ^ 1,
-                                       status, kStatusTimeoutProducer)) {
+                                       status, kStatusTimeoutProducer, wc.limit_ns)) {
               live = false;
               break;
             }
+            if (wc.starve) continue;   // give-up test: no load, no barrier completes
             const uint32_t fbar = tc::smem_u32(&full[st]);
             const uint32_t sa = tc::smem_u32(smem + st * STAGE_BYTES);
             tc::mbar_arrive_expect_tx(fbar, STAGE_BYTES);
@@ -275,12 +278,12 @@ ozaki_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
           const int buf = chunk % kNumBuf;
           if (cstart && chunk >= kNumBuf &&
               !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / kNumBuf) & 1) ^ 1,
-                                     status, kStatusTimeoutMma)) {
+                                     status, kStatusTimeoutMma, wc.limit_ns)) {
             live = false;
             break;
           }
           if (!tc::mbar_wait_bounded(tc::smem_u32(&full[st]), (g / kStages) & 1, status,
-                                     kStatusTimeoutMma)) {
+                                     kStatusTimeoutMma, wc.limit_ns)) {
             live = false;
             break;
           }
@@ -299,6 +302,10 @@ ozaki_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
           }
         }
       }
+      // Every MMA issued above completes before TMEM is released, also when
+      // the loop gave up (a commit with none outstanding arrives at once).
+      tc::mma_commit(tc::smem_u32(drain));
+      tc::mbar_wait_bounded(tc::smem_u32(drain), 0, status, kStatusTimeoutDrain, wc.limit_ns);
     }
     __syncwarp();
   } else {
@@ -335,7 +342,7 @@ ozaki_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
       for (int c = 0; c < nchunks; c++, chunk++) {
         const int buf = chunk % kNumBuf;
         ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / kNumBuf) & 1, status,
-                                   kStatusTimeoutEpilogue);
+                                   kStatusTimeoutEpilogue, wc.limit_ns);
         ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
         if (!ok) break;
         tc::tc_fence_after();
@@ -464,7 +471,7 @@ cudaError_t launch_ozaki(const Gemm &g, int slices, void *ws_v, size_t ws_bytes,
     return e;
   constexpr uint32_t SMEM = kStages * (kBM + kBN) * kBK * 2 + 1024 + 256;
   static_assert(SMEM <= 232448, "shared memory");
-  static_assert((2 * kStages + 2 * kNumBuf) * 8 + 4 <= 256, "barrier space");
+  static_assert((2 * kStages + 2 * kNumBuf + 1) * 8 + 4 <= 256, "barrier space");
   if ((e = cudaFuncSetAttribute(ozaki_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM)))
     return e;
   OzParams op;
@@ -474,7 +481,8 @@ cudaError_t launch_ozaki(const Gemm &g, int slices, void *ws_v, size_t ws_bytes,
   const int tiles_m = (int)((g.M + kBM - 1) / kBM), tiles_n = (int)((g.N + kBN - 1) / kBN);
   ozaki_gemm<<<tiles_m * tiles_n, kThreads, SMEM, s>>>(ta, tb, (double *)g.c, g.rso, g.cso,
                                                        (int)g.M, (int)g.N, (int)(L.Kp / kBK),
-                                                       tiles_m, tiles_n, status, op);
+                                                       tiles_m, tiles_n, status, op,
+                                                       wait_cfg());
   count_launch();
   e = cudaGetLastError();
   mark.gemm_done();

@@ -117,7 +117,7 @@ struct SplitCfg {
   static_assert(BN == 128 || BN == 256, "tile width");
   static_assert(CTAS == 1 || CTAS == 2, "one CTA or a CTA pair");
   static_assert(SMEM <= 232448, "shared memory");
-  static_assert((2 * STAGES + 2 * NBUF) * 8 + 4 <= 256, "barrier space");
+  static_assert((2 * STAGES + 2 * NBUF + 1) * 8 + 4 <= 256, "barrier space");
   static_assert(TMEM_COLS <= 512, "tensor memory");
 };
 
@@ -167,7 +167,7 @@ template <int BN, int STAGES, int PLANES, int FLUSH, bool F16, int CTAS>
 __global__ void __launch_bounds__(SplitCfg<BN, STAGES, PLANES, FLUSH, CTAS>::THREADS, 1)
 split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB,
            float *__restrict__ C, int64_t rso, int64_t cso, int M, int N, int num_kb,
-           int tiles_m, int tiles_n, int vec4, unsigned *status, Fallback fb) {
+           int tiles_m, int tiles_n, int vec4, unsigned *status, Fallback fb, WaitCfg wc) {
   using Cfg = SplitCfg<BN, STAGES, PLANES, FLUSH, CTAS>;
   using P = Products<PLANES>;
   constexpr bool PAIR = CTAS == 2;
@@ -177,7 +177,8 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
   uint64_t *full = bars, *empty = bars + STAGES;
   constexpr int NBUF = Cfg::NBUF;
   uint64_t *tfull = bars + 2 * STAGES, *tempty = bars + 2 * STAGES + NBUF;
-  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * STAGES + 2 * NBUF);
+  uint64_t *drain = bars + 2 * STAGES + 2 * NBUF;   // all issued MMAs complete
+  uint32_t *tmem_slot = (uint32_t *)(bars + 2 * STAGES + 2 * NBUF + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = tiles_m * tiles_n;   // tiles of CTAS * 128 rows
@@ -208,6 +209,7 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
       // one arrive per accumulator warp of every CTA
       tc::mbar_init(tc::smem_u32(&tempty[b]), Cfg::ACC_WARPS * CTAS);
     }
+    tc::mbar_init(tc::smem_u32(drain), 1);
     tc::fence_barrier_init();
     tc::tma_prefetch_desc(&tA);
     tc::tma_prefetch_desc(&tB);
@@ -235,10 +237,11 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
           const int s = g % STAGES;
           if (g >= STAGES &&
               !tc::mbar_wait_bounded(tc::smem_u32(&empty[s]), ((g / STAGES) & 1) ^ 1, status,
-                                     kStatusTimeoutProducer)) {
+                                     kStatusTimeoutProducer, wc.limit_ns)) {
             live = false;
             break;
           }
+          if (wc.starve) continue;   // give-up test: no load, no barrier ever completes
           const uint32_t fbar = tc::smem_u32(&full[s]);
           const uint32_t st = tc::smem_u32(smem + s * Cfg::STAGE_BYTES);
           // The even CTA's full barrier counts the bytes of both CTAs.
@@ -276,12 +279,12 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
           const bool chunk_end = kb % FLUSH == FLUSH - 1 || kb == num_kb - 1;
           if (chunk_start && chunk >= NBUF &&
               !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / NBUF) & 1) ^ 1,
-                                     status, kStatusTimeoutMma)) {
+                                     status, kStatusTimeoutMma, wc.limit_ns)) {
             live = false;
             break;
           }
           if (!tc::mbar_wait_bounded(tc::smem_u32(&full[s]), (g / STAGES) & 1, status,
-                                     kStatusTimeoutMma)) {
+                                     kStatusTimeoutMma, wc.limit_ns)) {
             live = false;
             break;
           }
@@ -315,6 +318,12 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
           if (chunk_end) chunk++;
         }
       }
+      // Whether the loop ran to the end or gave up, every MMA issued above
+      // completes before TMEM is released (a commit with none outstanding
+      // arrives at once).
+      if constexpr (PAIR) tc::mma_commit_pair(tc::smem_u32(drain), 0x1);
+      else tc::mma_commit(tc::smem_u32(drain));
+      tc::mbar_wait_bounded(tc::smem_u32(drain), 0, status, kStatusTimeoutDrain, wc.limit_ns);
     }
     __syncwarp();
   } else {
@@ -337,7 +346,7 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
       for (int c = 0; c < num_chunks; c++, chunk++) {
         const int buf = chunk % NBUF;
         ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / NBUF) & 1, status,
-                                   kStatusTimeoutEpilogue);
+                                   kStatusTimeoutEpilogue, wc.limit_ns);
         ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
         if (!ok) break;
         tc::tc_fence_after();
@@ -624,7 +633,7 @@ cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, cons
     const int grid = std::min(tiles_m * tiles_n, sm_count());
     kern<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(ta, tb, (float *)g.c, g.rso, g.cso, (int)g.M,
                                                (int)g.N, num_kb, tiles_m, tiles_n, vec4, status,
-                                               fb);
+                                               fb, wait_cfg());
   } else {
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
@@ -651,7 +660,8 @@ cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, cons
     pairs = std::min(pairs, tiles_m * tiles_n);
     cfg.gridDim = dim3((unsigned)(CTAS * pairs));
     e = cudaLaunchKernelEx(&cfg, kern, ta, tb, (float *)g.c, (int64_t)g.rso, (int64_t)g.cso,
-                           (int)g.M, (int)g.N, num_kb, tiles_m, tiles_n, vec4, status, fb);
+                           (int)g.M, (int)g.N, num_kb, tiles_m, tiles_n, vec4, status, fb,
+                           wait_cfg());
     if (e != cudaSuccess) return e;
   }
   count_launch();
@@ -849,13 +859,13 @@ cudaError_t run_split(const Gemm &g, const SplitLayout &L, void *ws_v, size_t ws
 
 // ---- allocation-free entry point ---------------------------------------------
 //
-// Some callers of a GEMM may not allocate device memory at call time: code
-// that records work into a CUDA graph or runs from a stream callback (where
-// cudaMalloc is not allowed), real-time services that forbid allocation
-// after start-up, and hosts whose device memory is owned by another
-// framework's allocator.  numc_cuda_sgemm_split_static runs the split-BF16
-// GEMM on a fixed scratch array compiled into this library instead of
-// asking for workspace: the caller passes only inputs and outputs.
+// Some callers of a GEMM may not allocate device memory at call time:
+// real-time services that forbid allocation after start-up, work issued
+// from stream callbacks (where CUDA calls that allocate are not allowed),
+// and hosts whose device memory is owned by another framework's allocator.
+// numc_cuda_sgemm_split_static runs the split-BF16 GEMM on a fixed scratch
+// array compiled into this library instead of asking for workspace: the
+// caller passes only inputs and outputs.
 //
 // The scratch array below is part of this module's device image: every GPU
 // on which the library's kernels are loaded holds its 64 MiB until the
@@ -863,38 +873,51 @@ cudaError_t run_split(const Gemm &g, const SplitLayout &L, void *ws_v, size_t ws
 // (two streams, or two host threads) race on it and must be serialised by
 // the caller.  Its contents persist between calls; nothing in it needs to
 // start at zero (the split planes are rewritten in full, the non-finite
-// flags are tagged with the call's generation number) except the
-// caller's status word, which each call clears.
+// flags are tagged with the call's generation number) except the status
+// word: the caller's, which each call clears, or, when the caller passes
+// none, the library's own word g_static_status, which numc_cuda_check_status
+// reads and clears.
 
 namespace numc_k {
 namespace {
 
 constexpr size_t kStaticScratchBytes = 64ull << 20;
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+static __device__ unsigned g_static_status;
 
-std::mutex g_static_mu;
-void *g_static_addr[64] = {nullptr};
+// Devices on which a call ran with the library's own status word.
+std::atomic<uint64_t> g_static_status_used{0};
 
-// Device address of g_static_scratch on the current device.  Host code may
-// not use the array's name as an address (it names a host-side shadow), so
-// the address is looked up once per device, with that device current.
-cudaError_t static_scratch_address(void **out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+// Device addresses of g_static_scratch and g_static_status on the current
+// device.  Host code may not use the arrays' names as addresses (they name
+// host-side shadows), so the addresses are looked up with the device
+// current, on every call: the lookup is a host-side table read once the
+// module is loaded, and a cached pointer would outlive a context that
+// cudaDeviceReset replaced.
+cudaError_t static_addresses(void **scratch, unsigned **status) {
+  cudaError_t e = cudaGetSymbolAddress(scratch, g_static_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_static_mu);
-  if (!g_static_addr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_static_scratch);
-    if (e != cudaSuccess) return e;
-    g_static_addr[dev] = p;
-  }
-  *out = g_static_addr[dev];
-  return cudaSuccess;
+  return cudaGetSymbolAddress((void **)status, g_static_status);
 }
 
 }  // namespace
+
+int static_status_read_and_clear(unsigned *status, void *stream) {
+  *status = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return (int)e;
+  if (dev < 0 || dev >= 64 || !(g_static_status_used.load() >> dev & 1)) return 0;
+  void *scratch = nullptr;
+  unsigned *word = nullptr;
+  cudaStream_t s = (cudaStream_t)stream;
+  if ((e = static_addresses(&scratch, &word)) != cudaSuccess) return (int)e;
+  if ((e = cudaMemcpyAsync(status, word, sizeof(unsigned), cudaMemcpyDeviceToHost, s)))
+    return (int)e;
+  if ((e = cudaMemsetAsync(word, 0, sizeof(unsigned), s))) return (int)e;
+  return (int)cudaStreamSynchronize(s);
+}
+
 }  // namespace numc_k
 
 extern "C" int numc_cuda_sgemm_split_static(const float *a, const float *b, float *out,
@@ -919,13 +942,23 @@ extern "C" int numc_cuda_sgemm_split_static(const float *a, const float *b, floa
                           "must fit); use numc_cuda_gemm with a workspace instead",
                           M, K, N, L.total, kStaticScratchBytes);
   void *base = nullptr;
-  cudaError_t e = static_scratch_address(&base);
+  unsigned *own_status = nullptr;
+  cudaError_t e = static_addresses(&base, &own_status);
   if (e != cudaSuccess)
     return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "sgemm_split_static: scratch address: %s",
                           cudaGetErrorString(e));
   cudaStream_t s = (cudaStream_t)stream;
-  if (status && (e = cudaMemsetAsync(status, 0, sizeof(unsigned), s)) != cudaSuccess)
+  if (!status) {
+    // The library's word keeps the first failure until numc_cuda_check_status
+    // reads and clears it, so one check covers a run of calls.
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess || dev < 0 || dev >= 64)
+      return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "sgemm_split_static: device %d", dev);
+    g_static_status_used.fetch_or(1ull << dev);
+    status = own_status;
+  } else if ((e = cudaMemsetAsync(status, 0, sizeof(unsigned), s)) != cudaSuccess) {
     return NUMC_SET_ERROR(NUMC_ERR_INTERNAL, "sgemm_split_static: %s", cudaGetErrorString(e));
+  }
   Gemm g;
   g.a = a; g.b = b; g.c = out;
   g.M = (int64_t)M; g.K = (int64_t)K; g.N = (int64_t)N;

@@ -144,6 +144,10 @@ cudaError_t rand_fill(NumcDType dt, void *out, size_t n, cudaStream_t s);
 // Device-side status word set by kernels that give up on a bounded wait.
 cudaError_t read_and_clear_status(unsigned *status, cudaStream_t s);
 
+// Every device allocation of the library goes through here (cudaMalloc,
+// or a simulated out-of-memory failure set by numc_cuda_debug_fail_malloc).
+cudaError_t dev_malloc(void **p, size_t bytes);
+
 // Count of kernel launches issued by this library.
 void count_launch(unsigned n = 1);
 uint64_t launches();

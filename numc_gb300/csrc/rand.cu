@@ -129,7 +129,7 @@ cudaError_t device_tables(uint64_t **out) {
   if (!g_dev_tables[dev]) {
     const Tables &t = tables();
     uint64_t *p = nullptr;
-    if ((e = cudaMalloc(&p, kTableWords * sizeof(uint64_t))) != cudaSuccess) return e;
+    if ((e = dev_malloc((void **)&p, kTableWords * sizeof(uint64_t))) != cudaSuccess) return e;
     if ((e = cudaMemcpy(p, t.row, kTableWords * sizeof(uint64_t), cudaMemcpyHostToDevice)) !=
         cudaSuccess) {
       cudaFree(p);

@@ -14,11 +14,29 @@ namespace numc_k {
 
 namespace {
 std::atomic<uint64_t> g_launches{0};
+std::atomic<unsigned long long> g_wait_limit_ns{2000000000ull};
+std::atomic<int> g_wait_starve{0};
+std::atomic<int> g_fail_mallocs{0};
 std::mutex g_status_mu;
 unsigned *g_status_dev[64] = {nullptr};
 }  // namespace
 
 void count_launch(unsigned n) { g_launches.fetch_add(n); }
+
+WaitCfg wait_cfg() { return WaitCfg{g_wait_limit_ns.load(), g_wait_starve.load()}; }
+
+cudaError_t dev_malloc(void **p, size_t bytes) {
+  // numc_cuda_debug_fail_malloc: fail the next n allocations as the device
+  // would when out of memory.
+  int n = g_fail_mallocs.load();
+  while (n > 0) {
+    if (g_fail_mallocs.compare_exchange_weak(n, n - 1)) {
+      *p = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
+  }
+  return cudaMalloc(p, bytes);
+}
 uint64_t launches() { return g_launches.load(); }
 
 unsigned *status_word() {
@@ -27,7 +45,7 @@ unsigned *status_word() {
   std::lock_guard<std::mutex> lock(g_status_mu);
   if (!g_status_dev[dev]) {
     unsigned *p = nullptr;
-    if (cudaMalloc(&p, sizeof(unsigned)) != cudaSuccess) return nullptr;
+    if (dev_malloc((void **)&p, sizeof(unsigned)) != cudaSuccess) return nullptr;
     if (cudaMemset(p, 0, sizeof(unsigned)) != cudaSuccess) {
       cudaFree(p);
       return nullptr;
@@ -48,3 +66,14 @@ cudaError_t read_and_clear_status(unsigned *status, cudaStream_t s) {
 }
 
 }  // namespace numc_k
+
+extern "C" int numc_cuda_debug_wait_timeout(unsigned long long limit_ns, int starve) {
+  numc_k::g_wait_limit_ns = limit_ns ? limit_ns : 2000000000ull;
+  numc_k::g_wait_starve = limit_ns ? (starve != 0) : 0;
+  return 0;
+}
+
+extern "C" int numc_cuda_debug_fail_malloc(int count) {
+  numc_k::g_fail_mallocs = count > 0 ? count : 0;
+  return 0;
+}

@@ -79,12 +79,27 @@ def _mix(z):
     return z ^ (z >> np.uint64(31))
 
 
-def draws(seed, stream, n):
-    """n consecutive splitmix64 outputs of stream `stream` under `seed`."""
+def draws(seed, stream, n, start=0):
+    """n consecutive splitmix64 outputs of stream `stream` under `seed`,
+    beginning with output number `start`."""
     with np.errstate(over="ignore"):
         base = _mix(np.uint64(seed) ^ (np.uint64(stream) * _STREAM))
-        idx = np.arange(1, n + 1, dtype=np.uint64)
+        idx = np.arange(start + 1, start + n + 1, dtype=np.uint64)
         return _mix(base + idx * GOLDEN)
+
+
+def _parallel_chunks(n, fn):
+    """fn(s, e) for consecutive chunks [s, e) of range(n), on a thread pool
+    (numpy releases the interpreter lock in its array loops)."""
+    spans = [(s, min(n, s + _CHUNK)) for s in range(0, n, _CHUNK)]
+    if len(spans) <= 1:
+        for s, e in spans:
+            fn(s, e)
+        return
+    from concurrent.futures import ThreadPoolExecutor
+    import os
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        list(ex.map(lambda se: fn(*se), spans))
 
 
 def uniform(seed, stream, shape, lo=-1.0, hi=1.0, dtype=np.float32):
@@ -108,14 +123,15 @@ def integers(seed, stream, shape, lo, hi, dtype):
 
 def normal(seed, stream, shape, dtype=np.float32):
     n = int(np.prod(shape))
-    x = draws(seed, stream, 2 * n)
     out = np.empty(n, dtype=dtype)
-    for s in range(0, n, _CHUNK):             # chunks stay in cache
-        xs = x[2 * s: 2 * min(n, s + _CHUNK)]
+
+    def chunk(s, e):                          # element i uses draws 2i, 2i + 1
+        xs = draws(seed, stream, 2 * (e - s), start=2 * s)
         u1 = ((xs[0::2] >> np.uint64(11)).astype(np.float64) + 1.0) * 2.0 ** -53
         u2 = (xs[1::2] >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
         z = np.sqrt(-2.0 * _log01(u1)) * _cos2pi(u2)
-        out[s: s + len(z)] = z.astype(dtype)
+        out[s:e] = z.astype(dtype)
+    _parallel_chunks(n, chunk)
     return out.reshape(shape)
 
 
@@ -186,3 +202,30 @@ def array(kind, shape, seed=42, stream=1, dtype="float32"):
         return uniform(seed, stream, shape, dtype=dt)
     lo, hi = INT_RANGES[dt.name]
     return integers(seed, stream, shape, lo, hi, dt)
+
+
+def grouped_case(torch, dev, seed=42, problems=2048, chains=256):
+    """The batched uneven workload as torch CUDA tensors: `problems`
+    float32 matmuls with M, N, K each log-uniform in [16, 1024] (rounded),
+    entries U[-1, 1), plus `chains` MLP chains X[256,784] -> W1[784,128] ->
+    W2[128,10] with X ~ U[-1, 1) and W ~ N(0, 0.05).  Drawn on the device
+    from torch generators seeded with `seed`.  Returns (dims, probs, chains,
+    algorithmic flops): probs[i] = (a, b, out), chains[i] = (x, w1, w2, h, y)."""
+    rng = np.random.default_rng(seed)
+    dims = np.exp(rng.uniform(np.log(16), np.log(1024), (problems, 3))).round().astype(int)
+    gen = torch.Generator(device=dev).manual_seed(seed)
+    probs = []
+    for (Mi, Ni, Ki) in dims:
+        a = torch.rand((Mi, Ki), device=dev, generator=gen) * 2 - 1
+        b = torch.rand((Ki, Ni), device=dev, generator=gen) * 2 - 1
+        probs.append((a, b, torch.empty((Mi, Ni), device=dev)))
+    mlp = []
+    for _ in range(chains):
+        x = torch.rand((256, 784), device=dev, generator=gen) * 2 - 1
+        w1 = torch.randn((784, 128), device=dev, generator=gen) * 0.05
+        w2 = torch.randn((128, 10), device=dev, generator=gen) * 0.05
+        mlp.append((x, w1, w2, torch.empty((256, 128), device=dev),
+                    torch.empty((256, 10), device=dev)))
+    flops = float(sum(2.0 * m * n * k for m, n, k in dims)) + \
+        chains * 2.0 * 256 * (784 * 128 + 128 * 10)
+    return dims, probs, mlp, flops
