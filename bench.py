@@ -243,6 +243,17 @@ def run_reference(args, world, rank):
 
 # ---- GPU legs ---------------------------------------------------------------
 
+ISA_NAMES = {0: "x86-64 AVX2", 1: "aarch64 NEON", 3: "x86-64 AVX-512"}
+
+
+def oracle_profile(nc):
+    """The oracle profile of the numc build the library reproduces now."""
+    import oracle
+    return {nc.INT8_X86_AVX2: oracle.PROFILE_X86_AVX2,
+            nc.INT8_ARM_NEON: oracle.PROFILE_ARM_NEON,
+            nc.INT8_X86_AVX512: oracle.PROFILE_X86_AVX512}[nc.get_isa_profile()]
+
+
 def time_gemm(nc, torch, a, b, c, algo, param, steps, warmup, ws=None):
     for _ in range(warmup):
         nc.gemm(a, b, c, algo=algo, param=param, workspace=ws)
@@ -465,6 +476,9 @@ def accuracy_summary(r):
         out["int_1024_bitexact"] = all(
             v["bitexact_vs_numc"] for dt in ("int8", "uint8", "int32", "int64")
             for v in ints.get(dt, {}).values())
+        out["int8_1024_bitexact_neon_avx512_builds"] = all(
+            v["bitexact_vs_numc"] for k, d in ints.items()
+            if k.endswith("_neon") or k.endswith("_avx512") for v in d.values())
     return out
 
 
@@ -574,7 +588,8 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
         for _ in range(50):
             nc.matmul(A1, B1, C1)
         e2e_us = (time.perf_counter() - t0) / 50 * 1e6
-        exact = C1.numpy().tobytes() == oracle.matmul(a1, b1).tobytes()
+        # numc_matmul reproduces numc as built for this host (ISA profile)
+        exact = C1.numpy().tobytes() == oracle.matmul(a1, b1, oracle_profile(nc)).tobytes()
     oracle.matmul(a1, b1)
     t0 = time.perf_counter()
     for _ in range(5):
@@ -583,6 +598,7 @@ def side_workloads(nc, torch, oracle, synth, a, b, c, ws, a_h, b_h, dev, args):
     out["f32_512"] = {"plain_tflops": f1 / ms_p / 1e9, "split_tflops": f1 / ms_s / 1e9,
                       "plain_us": ms_p * 1e3, "split_us": ms_s * 1e3,
                       "e2e_numc_matmul_us": e2e_us, "e2e_bitexact_vs_numc": exact,
+                      "isa_profile": ISA_NAMES.get(nc.get_isa_profile()),
                       "cpu_port_us": cpu_us, "cpu_cores": oracle.num_threads(),
                       "note": "L2-resident, latency-bound; device times from 50 calls in a CUDA graph"}
 
@@ -639,9 +655,10 @@ def misc_workload(nc, synth, oracle):
         C.to_device()
         t = per_call(lambda: nc.matmul(A, B, C), 20)
         C.to_host()
-        out["simt_f32_1000_with_edges"] = {"ms": t, "tflops": 2e9 / t / 1e9,
-                                           "bitexact_vs_numc":
-                                               C.numpy().tobytes() == oracle.matmul(a, b).tobytes()}
+        out["simt_f32_1000_with_edges"] = {
+            "ms": t, "tflops": 2e9 / t / 1e9,
+            "bitexact_vs_numc": C.numpy().tobytes() == oracle.matmul(
+                a, b, oracle_profile(nc)).tobytes()}
         # numc_dot 1-D float32: numc's lane order, 4 OpenMP chunks
         n = 16 << 20
         u = synth.array("normal", (n,), seed=5, stream=1, dtype="float32")
@@ -752,6 +769,20 @@ def int_workload(nc, torch, synth, dev):
             h = hashlib.sha256(tc_.cpu().numpy().tobytes()).hexdigest()
             ints.setdefault(dt, {})[name] = {"tops": 2.0 * 1024 ** 3 / ms_ / 1e9, "ms": ms_,
                                              "bitexact_vs_numc": h == want}
+    # the same int8/uint8 inputs under numc's NEON and AVX-512 builds' store
+    # rules, against those builds' own outputs
+    isa_gold = {c["name"]: c for c in json.load(open(os.path.join(
+        ROOT, "tests", "golden", "golden_isa.json")))["cases"]}
+    for variant, profile in (("neon", nc.INT8_ARM_NEON), ("avx512", nc.INT8_X86_AVX512)):
+        for dt in ["int8", "uint8"]:
+            ai_, bi_ = synth.operands("uniform", 1024, 1024, 1024, dtype=dt)
+            ta_, tb_ = torch.from_numpy(ai_).to(dev), torch.from_numpy(bi_).to(dev)
+            tc_ = torch.empty((1024, 1024), dtype=ta_.dtype, device=dev)
+            want = isa_gold[f"{variant}_uniform_{dt}_1024x1024x1024"]["sha256"]
+            ms_ = time_gemm(nc, torch, ta_, tb_, tc_, nc.ALGO_TC_INT8, profile, steps=20, warmup=2)
+            h = hashlib.sha256(tc_.cpu().numpy().tobytes()).hexdigest()
+            ints.setdefault(f"{dt}_{variant}", {})["tensor"] = {
+                "tops": 2.0 * 1024 ** 3 / ms_ / 1e9, "ms": ms_, "bitexact_vs_numc": h == want}
     # int8 4096^3 on the tensor path (128 x 128 tiles), checked against the
     # CUDA-core path, which follows numc's arithmetic independently
     ai_, bi_ = synth.operands("uniform", 4096, 4096, 4096, dtype="int8")

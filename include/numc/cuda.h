@@ -60,12 +60,21 @@ typedef enum {
                                     (0 = default) */
 } NumcCudaAlgo;
 
-/* Which numc build's int8/uint8 results to reproduce (the store rules of
- * numc's packed integer kernels differ by ISA). */
+/* Which numc build's results to reproduce where numc's arithmetic depends
+ * on the ISA it was compiled for: the store rules of its packed int8/uint8
+ * kernels, and the register-tile geometry of its float32/float64 kernels
+ * (which outputs are one FMA chain and which sum per-256 K-block chains, or
+ * mix vector and scalar columns).  Used as `param` of int8/uint8 (every
+ * algorithm) and of float32/float64 with NUMC_CUDA_ALGO_SIMT; -1 there
+ * means the process-wide profile (numc_cuda_set_isa_profile). */
 typedef enum {
-  NUMC_INT8_X86_AVX2 = 0, /* numc built for x86-64 AVX2 (default) */
-  NUMC_INT8_ARM_NEON = 1, /* numc built for aarch64 NEON */
-  NUMC_INT8_WRAP = 2      /* numc_matmul_naive: truncate the sum to 8 bits */
+  NUMC_INT8_X86_AVX2 = 0,  /* numc built for x86-64 AVX2 */
+  NUMC_INT8_ARM_NEON = 1,  /* numc built for aarch64 NEON (-march=armv8-a) */
+  NUMC_INT8_WRAP = 2,      /* numc_matmul_naive: int8 sums truncated to 8
+                              bits, floats `acc += a * b` unfused */
+  NUMC_INT8_X86_AVX512 = 3 /* numc built for x86-64 with AVX-512 (its
+                              -march=native on such hosts): int8/uint8 only;
+                              floats keep the AVX2 tiles */
 } NumcInt8Profile;
 
 /* Number of usable CUDA devices (0 when none). */
@@ -73,11 +82,23 @@ NUMC_API int numc_cuda_device_count(void);
 
 /* Process-wide algorithm per dtype used by numc_matmul and by
  * NUMC_CUDA_ALGO_DEFAULT.  For float64 OZAKI, `param` is the slice count;
- * for int8/uint8, `param` is a NumcInt8Profile.  Environment defaults:
- * NUMC_CUDA_F32_ALGO (simt|split|split6|split16|auto), NUMC_CUDA_F64_ALGO (simt|dmma|
- * ozaki[:slices]), NUMC_CUDA_INT8_PROFILE (x86|neon|wrap). */
+ * for int8/uint8 and for SIMT float32/float64, `param` is a NumcInt8Profile
+ * or -1 (the process-wide ISA profile, the default).  Environment
+ * defaults: NUMC_CUDA_F32_ALGO (simt|split|split6|split16|auto),
+ * NUMC_CUDA_F64_ALGO (simt|dmma|ozaki[:slices]), NUMC_CUDA_INT8_PROFILE
+ * (x86|neon|avx512|wrap: int8/uint8 only). */
 NUMC_API int numc_cuda_set_algo(NumcDType dtype, int algo, int param);
 NUMC_API int numc_cuda_get_algo(NumcDType dtype, int *algo, int *param);
+
+/* The process-wide ISA profile: NUMC_INT8_X86_AVX2, NUMC_INT8_ARM_NEON or
+ * NUMC_INT8_X86_AVX512.  numc selects its kernels when it is compiled, for
+ * the host it is compiled on, so the default is this host's build: NEON on
+ * aarch64 (numc's -march=armv8-a build; no SVE), AVX2 on x86-64.
+ * Environment: NUMC_CUDA_ISA_PROFILE (x86|neon|avx512).  numc_dot follows
+ * it too: its GEMM branch calls numc's AVX2 kernels on x86 builds and its
+ * naive kernels on NEON builds. */
+NUMC_API int numc_cuda_set_isa_profile(int profile);
+NUMC_API int numc_cuda_get_isa_profile(void);
 
 /* --- device residency --------------------------------------------------- */
 

@@ -28,7 +28,7 @@ ERR_TYPE, ERR_BOUNDS, ERR_VALUE, ERR_INTERNAL = -4, -5, -6, -99
 # NumcCudaAlgo (include/numc/cuda.h)
 (ALGO_DEFAULT, ALGO_SIMT, ALGO_SPLIT_BF16, ALGO_DMMA, ALGO_OZAKI, ALGO_AUTO, ALGO_TC_INT8,
  ALGO_SPLIT_FP16) = range(8)
-INT8_X86_AVX2, INT8_ARM_NEON, INT8_WRAP = 0, 1, 2
+INT8_X86_AVX2, INT8_ARM_NEON, INT8_WRAP, INT8_X86_AVX512 = 0, 1, 2, 3
 
 
 class NumcLibraryMissing(RuntimeError):
@@ -94,6 +94,8 @@ SIGNATURES = [
     ("numc_cuda_device_count", _I, []),
     ("numc_cuda_set_algo", _I, [_I, _I, _I]),
     ("numc_cuda_get_algo", _I, [_I, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    ("numc_cuda_set_isa_profile", _I, [_I]),
+    ("numc_cuda_get_isa_profile", _I, []),
     ("numc_cuda_array_to_device", _I, [_VP]),
     ("numc_cuda_array_to_host", _I, [_VP]),
     ("numc_cuda_array_device_data", _VP, [_VP]),
@@ -168,6 +170,16 @@ def get_algo(dtype):
     a, p = ctypes.c_int(), ctypes.c_int()
     check(lib().numc_cuda_get_algo(CODE[np.dtype(dtype).name], ctypes.byref(a), ctypes.byref(p)))
     return a.value, p.value
+
+
+def set_isa_profile(profile):
+    """Which numc build's results to reproduce (INT8_X86_AVX2, INT8_ARM_NEON
+    or INT8_X86_AVX512) where numc's arithmetic depends on its ISA."""
+    check(lib().numc_cuda_set_isa_profile(profile))
+
+
+def get_isa_profile():
+    return lib().numc_cuda_get_isa_profile()
 
 
 def launch_count():

@@ -34,13 +34,40 @@ struct AlgoChoice {
 AlgoChoice g_algo[NUMC_DTYPE_COUNT];
 std::once_flag g_algo_once;
 
+// Which numc build's results to reproduce where numc's arithmetic depends
+// on the ISA it was compiled for (int8/uint8 store rules, float register
+// tiles): numc_cuda_set_isa_profile.  numc picks its kernels at compile
+// time for the host it is built on (src/arch_dispatch.h), so the default is
+// this host's: the NEON build on aarch64, the AVX2 build on x86-64.
+std::atomic<int> g_isa_profile{
+#if defined(__aarch64__)
+    NUMC_INT8_ARM_NEON
+#else
+    NUMC_INT8_X86_AVX2
+#endif
+};
+
+int parse_profile(const std::string &v) {
+  if (v == "neon") return NUMC_INT8_ARM_NEON;
+  if (v == "avx512") return NUMC_INT8_X86_AVX512;
+  if (v == "wrap") return NUMC_INT8_WRAP;
+  if (v == "x86" || v == "avx2") return NUMC_INT8_X86_AVX2;
+  return -1;
+}
+
 void init_algos_from_env() {
   for (int d = 0; d < NUMC_DTYPE_COUNT; d++) {
     g_algo[d].algo = NUMC_CUDA_ALGO_SIMT;
     g_algo[d].param = 0;
   }
-  g_algo[NUMC_DTYPE_INT8].param = NUMC_INT8_X86_AVX2;
-  g_algo[NUMC_DTYPE_UINT8].param = NUMC_INT8_X86_AVX2;
+  // int8/uint8 and the CUDA-core float kernels follow the ISA profile
+  for (NumcDType d : {NUMC_DTYPE_INT8, NUMC_DTYPE_UINT8, NUMC_DTYPE_FLOAT32, NUMC_DTYPE_FLOAT64})
+    g_algo[d].param = -1;
+  if (const char *e = getenv("NUMC_CUDA_ISA_PROFILE")) {
+    const int p = parse_profile(e);
+    if (p == NUMC_INT8_X86_AVX2 || p == NUMC_INT8_ARM_NEON || p == NUMC_INT8_X86_AVX512)
+      g_isa_profile = p;
+  }
   // int8/uint8: the tensor path is bit-exact and faster beyond tiny sizes.
   g_algo[NUMC_DTYPE_INT8].algo = NUMC_CUDA_ALGO_AUTO;
   g_algo[NUMC_DTYPE_UINT8].algo = NUMC_CUDA_ALGO_AUTO;
@@ -64,10 +91,11 @@ void init_algos_from_env() {
     }
   }
   if (const char *e = getenv("NUMC_CUDA_INT8_PROFILE")) {
-    std::string v(e);
-    int p = v == "neon" ? NUMC_INT8_ARM_NEON : v == "wrap" ? NUMC_INT8_WRAP : NUMC_INT8_X86_AVX2;
-    g_algo[NUMC_DTYPE_INT8].param = p;
-    g_algo[NUMC_DTYPE_UINT8].param = p;
+    const int p = parse_profile(e);
+    if (p >= 0) {
+      g_algo[NUMC_DTYPE_INT8].param = p;
+      g_algo[NUMC_DTYPE_UINT8].param = p;
+    }
   }
 }
 
@@ -147,20 +175,26 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct Plan {
   int algo;     // concrete algorithm
-  int param;    // rule8 for int8/uint8, slices for Ozaki
+  int param;    // Rule8 for int8/uint8, FloatSimt for SIMT floats, slices for Ozaki
 };
 
-// `packed_only`: numc's packed kernels are called directly (numc_dot), so
-// the x86 int8/uint8 rule has no small-size unpacked branch.
+// numc_matmul_naive's arithmetic, passed as `param` by the library itself.
+constexpr int kParamNaive = -1000;
+
+// `packed_only`: numc_dot's GEMM branch (src/reduction/dot.c:386-400), which
+// calls numc's x86 AVX2 packed kernels directly — no small-size unpacked
+// branch — and on NEON builds, whose dot has no GEMM table (dot.c:275-288),
+// numc's naive kernels.
 int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Plan *p,
             bool packed_only = false) {
   ensure_algos();
   if (algo == NUMC_CUDA_ALGO_DEFAULT) {
     algo = g_algo[dt].algo.load();
-    if (param < 0) param = g_algo[dt].param.load();
+    if (param == -1) param = g_algo[dt].param.load();
   }
-  if (param < 0) param = 0;   // 0 = x86 profile for int8/uint8, default slices
-  if (algo == NUMC_CUDA_ALGO_AUTO && (dt == NUMC_DTYPE_INT8 || dt == NUMC_DTYPE_UINT8)) {
+  const bool is8 = dt == NUMC_DTYPE_INT8 || dt == NUMC_DTYPE_UINT8;
+  const bool isf = dt == NUMC_DTYPE_FLOAT32 || dt == NUMC_DTYPE_FLOAT64;
+  if (algo == NUMC_CUDA_ALGO_AUTO && is8) {
     algo = ((double)M * K * N >= (double)(1 << 21)) ? NUMC_CUDA_ALGO_TC_INT8 : NUMC_CUDA_ALGO_SIMT;
   } else if (algo == NUMC_CUDA_ALGO_AUTO) {
     if (dt != NUMC_DTYPE_FLOAT32)
@@ -168,10 +202,14 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
     // The scaled float16 split (float32-level error) pays for its scale
     // and split passes once each output sums enough terms and the grid
     // fills the GPU.
-    algo = ((uint64_t)M * N >= (1u << 16) && K >= 128) ? NUMC_CUDA_ALGO_SPLIT_FP16
-                                                      : NUMC_CUDA_ALGO_SIMT;
-    param = 0;
+    const bool split = (uint64_t)M * N >= (1u << 16) && K >= 128;
+    algo = split ? NUMC_CUDA_ALGO_SPLIT_FP16 : NUMC_CUDA_ALGO_SIMT;
+    param = split ? 0 : -1;
   }
+  // int8/uint8 and CUDA-core floats: `param` names the numc build (profile)
+  const bool profiled = is8 || (isf && algo == NUMC_CUDA_ALGO_SIMT);
+  if (profiled && param == -1) param = g_isa_profile.load();
+  if (!profiled && param < 0) param = 0;   // default slices / passes / flush
   switch (algo) {
   case NUMC_CUDA_ALGO_SIMT: break;
   case NUMC_CUDA_ALGO_SPLIT_BF16:
@@ -193,7 +231,7 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
       return NUMC_SET_ERROR(NUMC_ERR_TYPE, "DMMA GEMM is float64 only");
     break;
   case NUMC_CUDA_ALGO_TC_INT8:
-    if (dt != NUMC_DTYPE_INT8 && dt != NUMC_DTYPE_UINT8)
+    if (!is8)
       return NUMC_SET_ERROR(NUMC_ERR_TYPE, "the int8 tensor path is int8/uint8 only");
     break;
   case NUMC_CUDA_ALGO_OZAKI:
@@ -206,22 +244,38 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
   default:
     return NUMC_SET_ERROR(NUMC_ERR_VALUE, "unknown algorithm %d", algo);
   }
-  if (algo == NUMC_CUDA_ALGO_SIMT && packed_only &&
-      (dt == NUMC_DTYPE_FLOAT32 || dt == NUMC_DTYPE_FLOAT64) && param == numc_k::kFloatNumc)
-    param = numc_k::kFloatNumcPacked;
   p->algo = algo;
   p->param = param;
-  if (dt == NUMC_DTYPE_INT8 || dt == NUMC_DTYPE_UINT8) {
-    int profile = param;
-    if (profile == NUMC_INT8_ARM_NEON) p->param = numc_k::kRuleNeon;
-    else if (profile == NUMC_INT8_WRAP) p->param = numc_k::kRuleWrap;
-    else if (profile == NUMC_INT8_X86_AVX2)
+  if (isf && algo == NUMC_CUDA_ALGO_SIMT) {
+    // numc's AVX-512 float kernels are not reproduced (their float64 packed
+    // path overflows its stack buffer, gemm_avx512.h:278,797): the AVX-512
+    // profile keeps the AVX2 tiles for floats, as numc_dot does there.
+    const bool naive = param == kParamNaive || param == NUMC_INT8_WRAP ||
+                       (packed_only && param == NUMC_INT8_ARM_NEON);
+    if (naive) p->param = numc_k::kFloatNaive;
+    else if (param == NUMC_INT8_X86_AVX2 || param == NUMC_INT8_X86_AVX512)
+      p->param = packed_only ? numc_k::kFloatNumcPacked : numc_k::kFloatNumc;
+    else if (param == NUMC_INT8_ARM_NEON)
+      p->param = numc_k::kFloatNumc | numc_k::kFloatIsaNeon;
+    else return NUMC_SET_ERROR(NUMC_ERR_VALUE, "unknown float profile %d", param);
+  }
+  if (is8) {
+    const bool sup = !packed_only && (uint64_t)M * K * N <= 192ull * 192 * 192;
+    if (param == kParamNaive || param == NUMC_INT8_WRAP) p->param = numc_k::kRuleWrap;
+    else if (param == NUMC_INT8_ARM_NEON)
+      // NEON builds have no integer gemmsup (matmul.c:187-205) and numc_dot
+      // falls to its naive kernels there
+      p->param = packed_only ? numc_k::kRuleWrap : numc_k::kRuleNeon;
+    else if (param == NUMC_INT8_X86_AVX2)
       // numc's x86 build sends M*K*N <= 192^3 to its unpacked kernels, which
       // truncate (src/matmul/matmul.c:241-256, gemmsup_avx2.h:744-756).
-      p->param = (!packed_only && (uint64_t)M * K * N <= 192ull * 192 * 192)
-                     ? numc_k::kRuleWrap
-                     : numc_k::kRuleX86Packed;
-    else return NUMC_SET_ERROR(NUMC_ERR_VALUE, "unknown int8 profile %d", profile);
+      p->param = sup ? numc_k::kRuleWrap : numc_k::kRuleX86Packed;
+    else if (param == NUMC_INT8_X86_AVX512)
+      // the AVX-512 build keeps AVX2's integer gemmsup and numc_dot's AVX2
+      // GEMM table; numc_matmul's packed int8 is gemm_i8_avx512
+      p->param = sup ? numc_k::kRuleWrap
+                     : packed_only ? numc_k::kRuleX86Packed : numc_k::kRuleAvx512;
+    else return NUMC_SET_ERROR(NUMC_ERR_VALUE, "unknown int8 profile %d", param);
   }
   return 0;
 }
@@ -676,11 +730,7 @@ extern "C" int numc_matmul_naive(const NumcArray *a, const NumcArray *b, NumcArr
   // numc's naive kernels (kernel.h:18-62): integers accumulate in the
   // storage type (8-bit through 32 bits, truncated), floats `acc += a * b`
   // without contraction.
-  int param = 0;
-  if (a && (a->dtype == NUMC_DTYPE_INT8 || a->dtype == NUMC_DTYPE_UINT8)) param = NUMC_INT8_WRAP;
-  if (a && (a->dtype == NUMC_DTYPE_FLOAT32 || a->dtype == NUMC_DTYPE_FLOAT64))
-    param = numc_k::kFloatNaive;
-  return matmul_impl(a, b, out, NUMC_CUDA_ALGO_SIMT, param);
+  return matmul_impl(a, b, out, NUMC_CUDA_ALGO_SIMT, kParamNaive);
 }
 
 // ---- numc_linear / numc_bmm (numc's ROADMAP.md, "Linear algebra") -------------
@@ -1081,6 +1131,24 @@ extern "C" int numc_cuda_set_algo(NumcDType dt, int algo, int param) {
   g_algo[dt].param = param;
   return 0;
 }
+
+extern "C" int numc_cuda_set_isa_profile(int profile) {
+  ensure_algos();
+  if (profile != NUMC_INT8_X86_AVX2 && profile != NUMC_INT8_ARM_NEON &&
+      profile != NUMC_INT8_X86_AVX512)
+    return NUMC_SET_ERROR(NUMC_ERR_VALUE, "unknown ISA profile %d", profile);
+  g_isa_profile = profile;
+  return 0;
+}
+
+extern "C" int numc_cuda_get_isa_profile(void) {
+  ensure_algos();
+  return g_isa_profile.load();
+}
+
+namespace numc_k {
+int float_isa() { return numc_cuda_get_isa_profile() == NUMC_INT8_ARM_NEON ? kIsaNeon : kIsaX86; }
+}  // namespace numc_k
 
 extern "C" int numc_cuda_get_algo(NumcDType dt, int *algo, int *param) {
   ensure_algos();

@@ -58,6 +58,7 @@ struct Prob {
   int64_t rsa, csa, rsb, csb, rso, cso;
   int M, N, K, num_kb, Kp;
   int split_mode_a, split_mode_b;
+  int isa;                                // CUDA-core problems: numc's tile geometry
   uint16_t *pa, *pb;                      // planes (2 x M x Kp, 2 x N x Kp)
   unsigned long long *flags_a, *flags_b;  // per 128 rows of A, per 64 columns of B
   unsigned *max_a, *max_b;                // float16 planes: row / column maxima
@@ -463,6 +464,7 @@ grouped_simt(const Prob *__restrict__ probs, const Tile *__restrict__ tiles) {
   g.a = P.A; g.b = P.B; g.c = P.C;
   g.M = P.M; g.K = P.K; g.N = P.N;
   g.rsa = P.rsa; g.csa = P.csa; g.rsb = P.rsb; g.csb = P.csb; g.rso = P.rso; g.cso = P.cso;
+  g.isa = P.isa;
   simt::simt_tile<float, kSimtBM, kSimtBN, 8, 8, 8, KIND>(g, 0, tl.m0, tl.n0);
 }
 
@@ -478,8 +480,9 @@ grouped_float_edges(const Prob *__restrict__ probs, const int *__restrict__ prob
   g.a = P.A; g.b = P.B; g.c = P.C;
   g.M = P.M; g.K = P.K; g.N = P.N;
   g.rsa = P.rsa; g.csa = P.csa; g.rsb = P.rsb; g.csb = P.csb; g.rso = P.rso; g.cso = P.cso;
-  const int64_t r0 = simt::edge_row<float>(g.M), c0 = simt::edge_col<float>(g.N);
-  const int64_t n = simt::float_edge_groups<float>(g.M, g.N);
+  g.isa = P.isa;
+  const int64_t r0 = simt::edge_row<float>(g.M, g.isa), c0 = simt::edge_col<float>(g.N, g.isa);
+  const int64_t n = simt::float_edge_groups<float>(g.M, g.N, g.isa);
   const int64_t gi = (int64_t)job.y * 16 + threadIdx.x / 16;
   if (gi < n) simt::float_edge_output<float>(g, gi, threadIdx.x % 16, r0, c0);
 }
@@ -739,6 +742,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   std::vector<size_t> plane_off(count, 0), flag_off(count, 0);
   size_t planes_bytes = 0, flags_bytes = 0;
   p->probs.resize(count);
+  const int isa = float_isa();   // numc build whose CUDA-core arithmetic to follow
   p->variant.resize(count);
   for (size_t i = 0; i < count; i++) {
     const NumcCudaGemmDesc &d = descs[i];
@@ -754,6 +758,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
     P.A = (const float *)d.a; P.B = (const float *)d.b; P.C = (float *)d.out;
     P.rsa = d.rsa; P.csa = d.csa; P.rsb = d.rsb; P.csb = d.csb; P.rso = d.rso; P.cso = d.cso;
     P.M = (int)d.M; P.N = (int)d.N; P.K = (int)d.K;
+    P.isa = isa;
     P.Kp = (int)align_up(d.K ? d.K : 1, kBK);
     P.num_kb = P.Kp / kBK;
     int v = algo == NUMC_CUDA_ALGO_SIMT ? kVarSimt
@@ -784,7 +789,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
     const int v = p->variant[i];
     if (v < 0) continue;
     if (v == kVarSimt && simt::float_edges_needed<float>(p->probs[i].K) && numc_packed(p->probs[i]) &&
-        simt::float_edge_count<float>(p->probs[i].M, p->probs[i].N) > 0)
+        simt::float_edge_count<float>(p->probs[i].M, p->probs[i].N, p->probs[i].isa) > 0)
       edge_idx.push_back((int)i);
     const int bn = v == kVarTc128 ? 128 : v == kVarTc64 ? 64 : kSimtBN;
     const int bm = v == kVarSimt ? kSimtBM : kBM;
@@ -822,7 +827,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   }
   for (size_t q = 0; q < edge_idx.size(); q++) {
     const Prob &P = p->probs[edge_idx[q]];
-    const long long n = (simt::float_edge_groups<float>(P.M, P.N) + 15) / 16;
+    const long long n = (simt::float_edge_groups<float>(P.M, P.N, P.isa) + 15) / 16;
     for (long long j = 0; j < n; j++) edge_jobs.push_back(make_int2((int)q, (int)j));
   }
   p->split_jobs = (long long)split_jobs.size();

@@ -279,7 +279,7 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
       if (lane == 0) tc::mbar_arrive(tc::smem_u32(&tempty[buf]));
       if (chunk % CHUNKS_PER_BLOCK == CHUNKS_PER_BLOCK - 1) {
         const int b = chunk / CHUNKS_PER_BLOCK;
-        if (rule == kRuleNeon || rule == kRuleWrap) {
+        if (rule != kRuleX86Packed) {
           // one block over all K: accumulate the wrapped int32 sum
 #pragma unroll
           for (int j = 0; j < CW; j++) d[j] = (int32_t)((uint32_t)d[j] + (uint32_t)part[j]);
@@ -291,7 +291,7 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
       }
     }
     if (ok && row < M) {
-      if (rule == kRuleNeon || rule == kRuleWrap) {
+      if (rule != kRuleX86Packed) {
 #pragma unroll
         for (int j = 0; j < CW; j++)
           d[j] = simt::fold8(0, d[j], true, rule, SIGNED, row, n0 + cbase + j, M, N);

@@ -54,18 +54,18 @@ __global__ void __launch_bounds__(256) float_edges_lanes(Gemm g, int64_t r0, int
 template <typename T>
 cudaError_t launch_float_edges(const Gemm &g, cudaStream_t s) {
   if (!simt::float_edges_needed<T>(g.K)) return cudaSuccess;
-  const int64_t r0 = simt::edge_row<T>(g.M), c0 = simt::edge_col<T>(g.N);
+  const int64_t r0 = simt::edge_row<T>(g.M, g.isa), c0 = simt::edge_col<T>(g.N, g.isa);
   // K blocks on separate lanes when there are enough of them, or when the
   // outputs are too few to fill the GPU one lane each (the chains are then
   // the whole latency)
   const int64_t nkb = (g.K + simt::kNumcKC - 1) / simt::kNumcKC;
-  if (nkb >= 4 || simt::float_edge_count<T>(g.M, g.N) <= 152 * 128) {
-    const int64_t n = simt::float_edge_count<T>(g.M, g.N);
+  if (nkb >= 4 || simt::float_edge_count<T>(g.M, g.N, g.isa) <= 152 * 128) {
+    const int64_t n = simt::float_edge_count<T>(g.M, g.N, g.isa);
     if (n == 0) return cudaSuccess;
     const int64_t blocks = std::min<int64_t>((n + 31) / 32, 152 * 16);
     float_edges_lanes<T><<<(unsigned)blocks, 256, 0, s>>>(g, r0, c0, n);
   } else {
-    const int64_t n = simt::float_edge_groups<T>(g.M, g.N);
+    const int64_t n = simt::float_edge_groups<T>(g.M, g.N, g.isa);
     if (n == 0) return cudaSuccess;
     const int64_t blocks = std::min<int64_t>((n + 15) / 16, 152 * 16);
     float_edges<T><<<(unsigned)blocks, 256, 0, s>>>(g, r0, c0, n);
@@ -133,22 +133,31 @@ cudaError_t launch_float_packed(const Gemm &g, cudaStream_t s) {
 }  // namespace
 
 int float_rule(NumcDType dt, const Gemm &g, int rule) {
-  if (rule != kFloatNumc) return rule;
-  // numc_matmul's gemmsup threshold (src/matmul/matmul.c:241-256)
+  const int kind = rule & kFloatKindMask;
+  if (kind != kFloatNumc) return rule;
+  // numc_matmul's gemmsup threshold (src/matmul/matmul.c:241-256; the same
+  // table on every ISA)
   const double thr = dt == NUMC_DTYPE_FLOAT32 ? 96.0 * 96 * 96 : 48.0 * 48 * 48;
-  return (double)g.M * g.K * g.N > thr ? kFloatNumcPacked : kFloatNumcSmall;
+  return (rule & ~kFloatKindMask) |
+         ((double)g.M * g.K * g.N > thr ? kFloatNumcPacked : kFloatNumcSmall);
 }
 
-cudaError_t launch_simt(NumcDType dt, const Gemm &g, int rule8, cudaStream_t s) {
+cudaError_t launch_simt(NumcDType dt, const Gemm &g_in, int rule8, cudaStream_t s) {
+  Gemm g = g_in;
+  if (dt == NUMC_DTYPE_FLOAT32 || dt == NUMC_DTYPE_FLOAT64) {
+    // the float variant's ISA bit selects numc's tile geometry
+    g.isa = (rule8 & kFloatIsaNeon) ? kIsaNeon : kIsaX86;
+    rule8 = float_rule(dt, g, rule8) & kFloatKindMask;
+  }
   switch (dt) {
   case NUMC_DTYPE_FLOAT32:
-    switch (float_rule(dt, g, rule8)) {
+    switch (rule8) {
     case kFloatNaive: return launch_sized<float, simt::kFloatUnfused, 128>(g, 0, s);
     case kFloatNumcSmall: return launch_sized<float, simt::kFloatSmall, 128>(g, 0, s);
     default: return launch_float_packed<float, 128>(g, s);
     }
   case NUMC_DTYPE_FLOAT64:
-    switch (float_rule(dt, g, rule8)) {
+    switch (rule8) {
     case kFloatNaive: return launch_sized<double, simt::kFloatUnfused, 64>(g, 0, s);
     case kFloatNumcSmall: return launch_sized<double, simt::kFloatSmall, 64>(g, 0, s);
     default: return launch_float_packed<double, 64>(g, s);

@@ -22,7 +22,11 @@ struct Gemm {
   // 2^bits), folded into the store of the kernels that support it.
   const void *bias = nullptr;
   int64_t bias_stride = 1;
+  // CUDA-core float kernels: which numc build's register-tile geometry to
+  // follow (kIsaX86: x86-64 AVX2, kIsaNeon: aarch64 NEON).
+  int isa = 0;
 };
+enum NumcIsa : int { kIsaX86 = 0, kIsaNeon = 1 };
 
 // Whether `algo` adds Gemm::bias in its own epilogue (else the caller runs
 // launch_bias_add after the GEMM).
@@ -34,7 +38,8 @@ cudaError_t launch_bias_add(NumcDType dt, const Gemm &g, cudaStream_t s);
 enum Rule8 : int {
   kRuleWrap = 0,      // truncate the full sum to 8 bits
   kRuleX86Packed = 1, // numc x86 AVX2 packed path (K blocks of 512)
-  kRuleNeon = 2,      // numc aarch64 NEON path (one block over all K)
+  kRuleNeon = 2,      // numc aarch64 NEON path (one block over all K, 6x8 tiles)
+  kRuleAvx512 = 3,    // numc x86-64 AVX-512 path (one block over all K, 12x16 tiles)
 };
 
 // float32/float64 SIMT variant (numc's x86 AVX2 arithmetic, bit-exact):
@@ -46,8 +51,11 @@ enum Rule8 : int {
 //   kFloatNumcSmall  the unpacked (gemmsup) path at every size.
 // Full register tiles are one FMA chain per output in k order on both
 // paths; remainder tiles differ (see simt_common.cuh).
+// kFloatIsaNeon, or'ed in, follows numc's aarch64 NEON tile geometry
+// instead of x86 AVX2's.
 enum FloatSimt : int {
-  kFloatNumc = 0, kFloatNaive = 1, kFloatNumcPacked = 2, kFloatNumcSmall = 3
+  kFloatNumc = 0, kFloatNaive = 1, kFloatNumcPacked = 2, kFloatNumcSmall = 3,
+  kFloatKindMask = 15, kFloatIsaNeon = 16
 };
 
 // CUDA-core kernels for every dtype.  `rule8` is the Rule8 for int8/uint8,
@@ -55,6 +63,8 @@ enum FloatSimt : int {
 cudaError_t launch_simt(NumcDType dt, const Gemm &g, int rule8, cudaStream_t s);
 // The float variant kFloatNumc resolves to for problem g.
 int float_rule(NumcDType dt, const Gemm &g, int rule);
+// The float tile geometry (NumcIsa) of the process-wide ISA profile.
+int float_isa();
 
 // numc_dot's non-GEMM cases (dot_kernels.cu), all on device pointers:
 // out[i] = x[i] * scalar over an N-D strided array (scalar read from

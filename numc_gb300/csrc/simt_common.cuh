@@ -45,43 +45,59 @@ constexpr int kThreads = 256;
 enum Kind : int { kFloat = 0, kWrapInt = 1, kByte = 2, kFloatUnfused = 3, kFloatSmall = 4,
                   kFloatEdges = 5 };
 
-// ---- numc's float register tiles (x86 AVX2 build) --------------------------
+// ---- numc's float register tiles ------------------------------------------
 //
-// Packed path (gemm_avx2.h:852-950 float32, 1377-1475 float64): M in blocks
-// of MC rows (144 / 72) cut into 6-row register tiles, N in panels of 4080
-// columns cut into NR-column tiles (16 / 8), K in blocks of 256.  An output
-// of a full 6 x NR tile is one FMA chain over all K (the micro-kernel
-// reloads C between K blocks); an output of a remainder tile sums each K
-// block as an FMA chain from zero and adds it to the stored value.
-// Unpacked path (gemmsup_avx2.h:97-147, 221-270; M K N at most 96^3 /
-// 48^3): 6 x NR tiles from the origin; in a tile narrower than NR the first
+// Packed path: M in blocks of MC rows cut into MR-row register tiles, N in
+// panels of NC columns cut into NR-column tiles, K in blocks of 256.  An
+// output of a full MR x NR tile is one FMA chain over all K (the
+// micro-kernel reloads C between K blocks); an output of a remainder tile
+// sums each K block as an FMA chain from zero and adds it to the stored
+// value.  Unpacked path (M K N at most 96^3 float32 / 48^3 float64): 6 x NR
+// tiles from the origin; in a tile narrower than NR the first
 // (width / VW) x VW columns are vector FMA chains and the rest scalar
 // `c += a * b`, unfused (numc is ISO C without contraction).
-template <typename T> struct NumcTiles;
-template <> struct NumcTiles<float> { static constexpr int MC = 144, NR = 16, VW = 8; };
-template <> struct NumcTiles<double> { static constexpr int MC = 72, NR = 8, VW = 4; };
-constexpr int kNumcMR = 6, kNumcNC = 4080, kNumcKC = 256;
+// The geometry depends on the ISA numc was built for (Gemm::isa):
+//   x86-64 AVX2 (gemm_avx2.h:852-950, 1377-1475; gemmsup_avx2.h:97-147,
+//   221-270): float32 MC 144, MR 6, NR 16, NC 4080, VW 8; float64 MC 72,
+//   MR 6, NR 8, NC 4080, VW 4;
+//   aarch64 NEON (gemm_neon.h:610-740, 951-1080; gemmsup_neon.h:28-155,
+//   163-300): float32 MC 128, MR 8, NR 12, NC 4080, VW 4; float64 MC 96,
+//   MR 6, NR 8, NC 2048, VW 2.
+struct FloatGeom {
+  int mc, mr, nc, nr, vw;
+};
+template <typename T> __host__ __device__ inline FloatGeom numc_geom(int isa) {
+  if constexpr (std::is_same<T, float>::value)
+    return isa == kIsaNeon ? FloatGeom{128, 8, 4080, 12, 4} : FloatGeom{144, 6, 4080, 16, 8};
+  else
+    return isa == kIsaNeon ? FloatGeom{96, 6, 2048, 8, 2} : FloatGeom{72, 6, 4080, 8, 4};
+}
+constexpr int kNumcKC = 256;
 
 // First row / column of numc's remainder register tiles: rows from
 // edge_row(M) (the last MC block's partial MR tile), and, above them,
-// columns from edge_col(N) (the last 4080-column panel's partial NR tile).
-template <typename T> __host__ __device__ inline int64_t edge_row(int64_t M) {
+// columns from edge_col(N) (the last NC-column panel's partial NR tile).
+// MC and NC are multiples of MR and NR on every ISA, so no other tile is
+// partial.
+template <typename T> __host__ __device__ inline int64_t edge_row(int64_t M, int isa) {
   if (M == 0) return 0;
-  const int64_t ic = ((M - 1) / NumcTiles<T>::MC) * NumcTiles<T>::MC;
-  return ic + ((M - ic) / kNumcMR) * kNumcMR;
+  const FloatGeom G = numc_geom<T>(isa);
+  const int64_t ic = ((M - 1) / G.mc) * G.mc;
+  return ic + ((M - ic) / G.mr) * G.mr;
 }
-template <typename T> __host__ __device__ inline int64_t edge_col(int64_t N) {
+template <typename T> __host__ __device__ inline int64_t edge_col(int64_t N, int isa) {
   if (N == 0) return 0;
-  const int64_t jc = ((N - 1) / kNumcNC) * kNumcNC;
-  return jc + ((N - jc) / NumcTiles<T>::NR) * NumcTiles<T>::NR;
+  const FloatGeom G = numc_geom<T>(isa);
+  const int64_t jc = ((N - 1) / G.nc) * G.nc;
+  return jc + ((N - jc) / G.nr) * G.nr;
 }
 
 // Unpacked path: column j is one of a narrow tile's scalar (unfused) columns.
 template <typename T>
-__device__ __forceinline__ bool small_col_unfused(int64_t j, int64_t N) {
-  constexpr int NR = NumcTiles<T>::NR, VW = NumcTiles<T>::VW;
-  const int64_t j0 = (j / NR) * NR, nr = min((int64_t)NR, N - j0);
-  return nr < NR && (j - j0) >= (nr / VW) * VW;
+__device__ __forceinline__ bool small_col_unfused(int64_t j, int64_t N, int isa) {
+  const FloatGeom G = numc_geom<T>(isa);
+  const int64_t j0 = (j / G.nr) * G.nr, nr = min((int64_t)G.nr, N - j0);
+  return nr < G.nr && (j - j0) >= (nr / G.vw) * G.vw;
 }
 
 // ---- numc's int8/uint8 store rules ---------------------------------------
@@ -110,11 +126,16 @@ __device__ __forceinline__ bool x86_full(int64_t i, int64_t j, int64_t M,
   int64_t jr = ((j - jc) / 16) * 16, nr = min((int64_t)16, nc - jr);
   return mr == 6 && nr == 16;
 }
-// Full 6x8 tile of numc's NEON int8 path (gemm_neon.h:1509-1535).
-__device__ __forceinline__ bool neon_full(int64_t i, int64_t j, int64_t M,
-                                          int64_t N) {
-  int64_t ic = (i / 72) * 72, mc = min((int64_t)72, M - ic);
-  return (i - ic) < (mc / 6) * 6 && j < (N / 8) * 8;
+// Full MR x NR tile of a clamp-once int8 path that blocks M by MC (a
+// multiple of MR) and N by NR from column 0: numc's NEON build (72, 6, 8;
+// gemm_neon.h:1509-1535) and its AVX-512 build (240, 12, 16;
+// gemm_avx512.h:1315-1341).
+__device__ __forceinline__ bool clamp_full(int64_t i, int64_t j, int64_t M, int64_t N,
+                                           int rule) {
+  const int64_t MC = rule == kRuleNeon ? 72 : 240, MR = rule == kRuleNeon ? 6 : 12;
+  const int64_t NR = rule == kRuleNeon ? 8 : 16;
+  int64_t ic = (i / MC) * MC, mc = min(MC, M - ic);
+  return (i - ic) < (mc / MR) * MR && j < (N / NR) * NR;
 }
 
 // One K-block end for element (i, j): fold the block's partial sum P into
@@ -135,8 +156,11 @@ __device__ __forceinline__ int32_t fold8(int32_t d, int32_t P, bool first,
                                          int64_t j, int64_t M, int64_t N) {
   if (rule == kRuleX86Packed)
     return fold8_x86(d, P, first, x86_full(i, j, M, N), is_signed);
-  if (rule == kRuleNeon) {
-    if (neon_full(i, j, M, N))
+  if (rule == kRuleNeon || rule == kRuleAvx512) {
+    // one block over all K: the wrapped int32 sum narrowed once with
+    // saturation (uint8: the lane read as unsigned, min(u32, 255)), or
+    // truncated in remainder tiles
+    if (clamp_full(i, j, M, N, rule))
       return is_signed ? sat_s8(P) : ((uint32_t)P > 255u ? 255 : P);
     return wrap8(P, is_signed);
   }
@@ -299,7 +323,7 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
   uint32_t edge_mask = 0;
   if constexpr (kEdges) {
     if (g.K > kNumcKC) {
-      const int64_t er = edge_row<T>(g.M), ec = edge_col<T>(g.N);
+      const int64_t er = edge_row<T>(g.M, g.isa), ec = edge_col<T>(g.N, g.isa);
 #pragma unroll
       for (int i = 0; i < TM; i++)
 #pragma unroll
@@ -315,7 +339,7 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
   if constexpr (KIND == kFloatSmall) {
 #pragma unroll
     for (int j = 0; j < TN; j++)
-      if (small_col_unfused<T>(n0 + col_of(j), g.N)) unf_mask |= 1u << j;
+      if (small_col_unfused<T>(n0 + col_of(j), g.N, g.isa)) unf_mask |= 1u << j;
   }
 
   load_tiles(0);
@@ -407,9 +431,8 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
 // ---- numc's packed-path remainder tiles (floats) --------------------------
 //
 // Only the last, partial MC block of rows and the last, partial NR tile of
-// the last 4080-column panel hold remainder tiles (MC and 4080 are
-// multiples of the tile sizes): rows from edge_row(M), columns from
-// edge_col(N).  Their outputs are recomputed after the GEMM kernel: each
+// the last NC-column panel hold remainder tiles (MC and NC are multiples of
+// the tile sizes): rows from edge_row(M), columns from edge_col(N).  Their outputs are recomputed after the GEMM kernel: each
 // 256-deep K block as an FMA chain from zero, added to the running value.
 
 // Short K or many problems: remainder outputs in groups of 16 consecutive
@@ -419,8 +442,8 @@ __device__ __forceinline__ void simt_tile(const Gemm &g, int rule8, int64_t m0, 
 // group, one output a lane, so its loads of B are consecutive and its loads
 // of A one address.
 template <typename T>
-__host__ __device__ inline int64_t float_edge_groups(int64_t M, int64_t N) {
-  const int64_t r0 = edge_row<T>(M), c0 = edge_col<T>(N);
+__host__ __device__ inline int64_t float_edge_groups(int64_t M, int64_t N, int isa) {
+  const int64_t r0 = edge_row<T>(M, isa), c0 = edge_col<T>(N, isa);
   return (M - r0) * ((N + 15) / 16) + (c0 < N ? r0 : 0);
 }
 
@@ -534,8 +557,8 @@ template <typename T>
 __host__ __device__ inline bool float_edges_needed(int64_t K) { return K > kNumcKC; }
 
 template <typename T>
-__host__ __device__ inline int64_t float_edge_count(int64_t M, int64_t N) {
-  const int64_t r0 = edge_row<T>(M), c0 = edge_col<T>(N);
+__host__ __device__ inline int64_t float_edge_count(int64_t M, int64_t N, int isa) {
+  const int64_t r0 = edge_row<T>(M, isa), c0 = edge_col<T>(N, isa);
   return (M - r0) * N + r0 * (N - c0);
 }
 

@@ -162,6 +162,10 @@ def operands(kind, M, K, N, seed=42, dtype="float32"):
     expspread   float64 uniform [-1, 1) times 2^e, e integer U(-20, 20)
                 per element
     smallint    numc's own test fill: A[i] = (i % 7) + 1, B[i] = (i % 5) + 1
+    extreme     integers only: each entry the dtype's maximum with
+                probability 7/8, else its minimum (long K drives the int32
+                sums of 8-bit products past 2^31: saturation and
+                wraparound cases)
     """
     dt = np.dtype(dtype)
     if kind == "smallint":
@@ -177,6 +181,12 @@ def operands(kind, M, K, N, seed=42, dtype="float32"):
                 integers(seed, 2, (K, N), lo, hi, dt))
     if kind == "normal":
         return normal(seed, 3, (M, K), dt), normal(seed, 4, (K, N), dt)
+    if kind == "extreme":
+        info = np.iinfo(dt)
+        pick_a = integers(seed, 13, (M, K), 0, 7, np.int64)
+        pick_b = integers(seed, 14, (K, N), 0, 7, np.int64)
+        return (np.where(pick_a == 0, info.min, info.max).astype(dt),
+                np.where(pick_b == 0, info.min, info.max).astype(dt))
     if kind == "illscaled":
         a, b = normal(seed, 3, (M, K), dt), normal(seed, 4, (K, N), dt)
         u, v = ill_scales(seed, M, N)

@@ -28,9 +28,10 @@ PROFILE_X86_AVX2 = 0
 PROFILE_ARM_NEON = 1
 PROFILE_WRAP = 2          # numc_matmul_naive (floats: unfused chains)
 PROFILE_X86_PACKED = 3    # numc's x86 packed kernels called directly (numc_dot)
+PROFILE_X86_AVX512 = 4    # numc's x86-64 AVX-512 build (int8/uint8 store rule)
 
 _lib = None
-_ref = None
+_refs = {}
 
 
 def _load():
@@ -183,16 +184,15 @@ def rand(dtype, shape, state, max_threads):
 
 # -- the compiled reference ------------------------------------------------
 
-def reference_available():
-    return os.path.exists(_build.REF_SO) or _build.reference_buildable()
+def reference_available(variant="avx2"):
+    return os.path.exists(_build.REF_VARIANTS[variant][1]) or _build.reference_buildable()
 
 
-def _load_ref():
-    global _ref
-    if _ref is None:
-        path = _build.build_reference()
+def _load_ref(variant="avx2"):
+    if variant not in _refs:
+        path = _build.build_reference(variant)
         if path is None:
-            raise RuntimeError("numc reference library not buildable here")
+            raise RuntimeError(f"numc reference library ({variant}) not buildable here")
         lib = ctypes.CDLL(path)
         vp = ctypes.c_void_p
         lib.numc_ctx_create.restype = vp
@@ -212,13 +212,14 @@ def _load_ref():
         lib.numc_manual_seed.argtypes = [ctypes.c_uint64]
         lib.numc_array_rand.restype = vp
         lib.numc_array_rand.argtypes = [vp, vp, ctypes.c_size_t, ctypes.c_int]
-        _ref = lib
-    return _ref
+        _refs[variant] = lib
+    return _refs[variant]
 
 
-def ref_matmul(a, b, naive=False):
-    """Run numc's own numc_matmul (or numc_matmul_naive) on contiguous a, b."""
-    lib = _load_ref()
+def ref_matmul(a, b, naive=False, variant="avx2"):
+    """Run numc's own numc_matmul (or numc_matmul_naive) on contiguous a, b,
+    in numc's build `variant` (avx2, avx512 or neon)."""
+    lib = _load_ref(variant)
     a = np.ascontiguousarray(a)
     b = np.ascontiguousarray(b)
     M, K = a.shape
@@ -249,12 +250,12 @@ def ref_matmul(a, b, naive=False):
         lib.numc_ctx_free(ctx)
 
 
-def ref_dot(a, b, perm_a=None, perm_b=None, perm_out=None):
+def ref_dot(a, b, perm_a=None, perm_b=None, perm_out=None, variant="avx2"):
     """numc's own numc_dot(a, b, out).  Each operand (and out) is created in
     numc as a contiguous array holding x.transpose(inverse(perm)) and then
     viewed with numc_array_transpose(perm), so a perm other than the identity
     gives numc a strided, non-contiguous view equal to x."""
-    lib = _load_ref()
+    lib = _load_ref(variant)
     code = DTYPE_CODE[a.dtype.name]
     oshape = dot_shape(a.shape, b.shape)
     ctx = lib.numc_ctx_create()

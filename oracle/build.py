@@ -2,10 +2,11 @@
 
 ``build_oracle()`` compiles ``oracle/numc_oracle.c`` (the CPU restatement of
 numc's matmul arithmetic) into ``oracle/_build/liboracle.so``.
-``build_reference()`` compiles the unmodified numc sources from a local
-reference checkout into ``oracle/_ref/libnumc_ref.so`` through
-``oracle/Makefile.ref``; it only runs where that checkout exists and the host
-is x86-64 (the recipe pins AVX2).
+``build_reference(variant)`` compiles the unmodified numc sources from a
+local reference checkout into ``oracle/_ref/`` through ``oracle/Makefile.ref``
+(the AVX2 build, the AVX-512 build, or the NEON matmul on the intrinsic model
+in ``oracle/neon_shim``); it only runs where that checkout exists and the
+host is x86-64.
 """
 import os
 import platform
@@ -17,6 +18,12 @@ ROOT = os.path.dirname(HERE)
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libnumc_ref.so")
 REF_SRC = "/root/reference"
+# numc builds the recipe can make: (make target, library)
+REF_VARIANTS = {
+    "avx2": ("all", REF_SO),
+    "avx512": ("avx512", os.path.join(HERE, "_ref", "libnumc_ref_avx512.so")),
+    "neon": ("neon", os.path.join(HERE, "_ref", "libnumc_ref_neon.so")),
+}
 
 
 def build_oracle(force=False):
@@ -50,17 +57,20 @@ def reference_buildable():
             and shutil.which("make") is not None)
 
 
-def build_reference():
-    """Returns the path of the compiled reference, or None if not buildable."""
-    if os.path.exists(REF_SO):
-        return REF_SO
+def build_reference(variant="avx2"):
+    """Returns the path of the compiled reference build `variant` (avx2:
+    numc's x86-64 AVX2 build; avx512: its AVX-512 build; neon: its aarch64
+    NEON matmul through oracle/neon_shim), or None if not buildable."""
+    target, path = REF_VARIANTS[variant]
+    if os.path.exists(path):
+        return path
     if not reference_buildable():
         return None
     subprocess.check_call(
         ["make", "-f", os.path.join("oracle", "Makefile.ref"),
-         f"-j{os.cpu_count() or 4}", f"REF={REF_SRC}"],
+         f"-j{os.cpu_count() or 4}", f"REF={REF_SRC}", target],
         cwd=ROOT, stdout=subprocess.DEVNULL)
-    return REF_SO if os.path.exists(REF_SO) else None
+    return path if os.path.exists(path) else None
 
 
 if __name__ == "__main__":

@@ -43,6 +43,17 @@
  *      with vqmovn twice (int8: clamp to [-128,127]; uint8: min(u32, 255));
  *      remainder tiles truncate to 8 bits.  Restated from source only.
  *
+ *    ORACLE_I8_X86_AVX512 (the x86-64 build on an AVX-512 host, numc's
+ *      default -march=native there): M*K*N <= 192^3 keeps AVX2's unpacked
+ *      path (truncation; src/matmul/matmul.c:210-226 gives AVX-512 no integer
+ *      gemmsup of its own); larger products use gemm_i8_avx512 /
+ *      gemm_u8_avx512 (src/intrinsics/gemm_avx512.h:1263-1414): no K
+ *      blocking, M blocked by 240 (MR 12) and N by NR 16 from column 0.
+ *      Full 12x16 tiles narrow the wrapped int32 sum once with
+ *      _mm512_cvtsepi32_epi8 (int8: clamp to [-128,127]) or
+ *      _mm512_cvtusepi32_epi8 (uint8: the lane read as unsigned, min(u32,
+ *      255)); remainder tiles truncate to 8 bits.
+ *
  *    ORACLE_I8_WRAP (numc_matmul_naive, src/matmul/kernel.h:35-62): the sum
  *      truncated to 8 bits.
  *
@@ -71,7 +82,7 @@ enum {
  * differ for int8/uint8 (store rules) and, in the last bits, for the
  * remainder tiles of float32/float64. */
 enum { ORACLE_I8_X86_AVX2 = 0, ORACLE_I8_ARM_NEON = 1, ORACLE_I8_WRAP = 2,
-       ORACLE_X86_PACKED = 3 };
+       ORACLE_X86_PACKED = 3, ORACLE_I8_X86_AVX512 = 4 };
 
 static const size_t k_elem[] = {1, 2, 4, 8, 1, 2, 4, 8, 4, 8};
 
@@ -180,18 +191,23 @@ static void scatter(void *dstv, const void *src, int64_t rows, int64_t cols,
 DEFINE_FLOAT_KERNEL(kern_f32, float, oracle_micro_f32, ORACLE_MR, ORACLE_NR_F32)
 DEFINE_FLOAT_KERNEL(kern_f64, double, oracle_micro_f64, ORACLE_MR, ORACLE_NR_F64)
 
-/* Outputs of the x86 AVX2 build that are not a plain FMA chain.
+/* Outputs of numc's float kernels that are not a plain FMA chain.
  *
- * Unpacked path (M*K*N <= THR; gemmsup_avx2.h:97-147 and 221-270): 6 x NR
- * tiles from the origin; inside a remainder tile the first (nr / VW) * VW
- * columns use vector FMA and the rest scalar `c += a * b`, which the
- * reference's ISO C build (-std=c2x, no FP contraction) rounds twice.
+ * Unpacked path (M*K*N <= THR): 6 x NR tiles from the origin; inside a
+ * remainder tile the first (nr / VW) * VW columns use vector FMA and the
+ * rest scalar `c += a * b`, which the reference's ISO C build (-std=c2x, no
+ * FP contraction) rounds twice.  x86 AVX2: gemmsup_avx2.h:97-147 and
+ * 221-270 (NR 16 / 8, VW 8 / 4); aarch64 NEON: gemmsup_neon.h:28-155 and
+ * 163-300 (NR 12 / 8, VW 4 / 2).
  *
- * Packed path (gemm_avx2.h:852-950 for f32, 1377-1475 for f64): a remainder
- * tile computes each KC=256 block as an FMA chain from zero and adds it to
- * the stored value.  The tile grid is MC x NR inside NC=4080 column panels.
+ * Packed path: a remainder tile computes each KC=256 block as an FMA chain
+ * from zero and adds it to the stored value; full tiles reload C and keep
+ * one chain.  The tile grid is MC x MR rows, NR columns inside NC-column
+ * panels.  x86 AVX2 (gemm_avx2.h:852-950 f32, 1377-1475 f64): MC 144 / 72,
+ * MR 6, NR 16 / 8, NC 4080.  aarch64 NEON (gemm_neon.h:610-740 f32,
+ * 951-1080 f64): MC 128 / 96, MR 8 / 6, NR 12 / 8, NC 4080 / 2048.
  */
-#define DEFINE_FLOAT_EDGES(NAME, T, FMA, THR, NR, VW, MC)                     \
+#define DEFINE_FLOAT_EDGES(NAME, T, FMA, THR, NR, VW, MC, MR, NC)             \
   /* Packed-path remainder output (i, j): per-KC chains summed in order. */   \
   static T NAME##_packed_one(const T *a, const T *b, int64_t i, int64_t j,   \
                              int64_t K, int64_t N) {                          \
@@ -217,8 +233,8 @@ DEFINE_FLOAT_KERNEL(kern_f64, double, oracle_micro_f64, ORACLE_MR, ORACLE_NR_F64
         _Pragma("omp for schedule(dynamic, 1)")                               \
         for (int64_t i = 0; i < M; i++) {                                     \
           int64_t ic = (i / (MC)) * (MC), mc = MIN((MC), M - ic);             \
-          int64_t ir = ((i - ic) / 6) * 6, mr = MIN(6, mc - ir);              \
-          if (mr < 6) {                                                       \
+          int64_t ir = ((i - ic) / (MR)) * (MR), mr = MIN((MR), mc - ir);     \
+          if (mr < (MR)) {                                                    \
             for (int64_t pc = 0; pc < K; pc += 256) {                         \
               int64_t pe = MIN(pc + 256, K);                                  \
               for (int64_t j = 0; j < N; j++) t[j] = (T)0;                    \
@@ -232,8 +248,8 @@ DEFINE_FLOAT_KERNEL(kern_f64, double, oracle_micro_f64, ORACLE_MR, ORACLE_NR_F64
             for (int64_t j = 0; j < N; j++) c[i * N + j] = K ? d[j] : (T)0;   \
             continue;                                                         \
           }                                                                   \
-          for (int64_t jc = 0; jc < N; jc += 4080) {                          \
-            int64_t nc = MIN(4080, N - jc);                                   \
+          for (int64_t jc = 0; jc < N; jc += (NC)) {                          \
+            int64_t nc = MIN((NC), N - jc);                                   \
             for (int64_t j = jc + (nc / (NR)) * (NR); j < jc + nc; j++)       \
               c[i * N + j] = NAME##_packed_one(a, b, i, j, K, N);             \
           }                                                                   \
@@ -260,8 +276,10 @@ DEFINE_FLOAT_KERNEL(kern_f64, double, oracle_micro_f64, ORACLE_MR, ORACLE_NR_F64
     }                                                                         \
   }
 
-DEFINE_FLOAT_EDGES(edges_f32, float, fmaf, 96ULL * 96 * 96, 16, 8, 144)
-DEFINE_FLOAT_EDGES(edges_f64, double, fma, 48ULL * 48 * 48, 8, 4, 72)
+DEFINE_FLOAT_EDGES(edges_f32, float, fmaf, 96ULL * 96 * 96, 16, 8, 144, 6, 4080)
+DEFINE_FLOAT_EDGES(edges_f64, double, fma, 48ULL * 48 * 48, 8, 4, 72, 6, 4080)
+DEFINE_FLOAT_EDGES(edges_f32_neon, float, fmaf, 96ULL * 96 * 96, 12, 4, 128, 8, 4080)
+DEFINE_FLOAT_EDGES(edges_f64_neon, double, fma, 48ULL * 48 * 48, 8, 2, 96, 6, 2048)
 
 /* Naive float kernels: per output `acc = acc + a * b` from 0 in k order,
  * product and sum each rounded (this file is built without contraction). */
@@ -350,10 +368,15 @@ static inline int x86_full_tile(int64_t i, int64_t j, int64_t M, int64_t N) {
   return mr == 6 && nr == 16;
 }
 
-static inline int neon_full_tile(int64_t i, int64_t j, int64_t M, int64_t N) {
-  int64_t ic = (i / 72) * 72, mc = MIN(72, M - ic);
-  int64_t full_rows = (mc / 6) * 6;
-  int64_t full_cols = (N / 8) * 8;
+/* 1 when (i, j) lies in a full MR x NR tile of a clamp-once path that
+ * blocks M by MC (a multiple of MR) and N by NR from column 0: NEON
+ * (72, 6, 8; gemm_neon.h:1509-1535) and AVX-512 (240, 12, 16;
+ * gemm_avx512.h:1315-1341). */
+static inline int clamp_full_tile(int64_t i, int64_t j, int64_t M, int64_t N,
+                                  int64_t MC, int64_t MR, int64_t NR) {
+  int64_t ic = (i / MC) * MC, mc = MIN(MC, M - ic);
+  int64_t full_rows = (mc / MR) * MR;
+  int64_t full_cols = (N / NR) * NR;
   return (i - ic) < full_rows && j < full_cols;
 }
 
@@ -361,10 +384,11 @@ static void kern_8bit(const void *av, const void *bv, void *cv, int64_t M,
                       int64_t K, int64_t N, int is_signed, int profile) {
   const int8_t *as = (const int8_t *)av, *bs = (const int8_t *)bv;
   const uint8_t *au = (const uint8_t *)av, *bu = (const uint8_t *)bv;
+  const int above_sup = (uint64_t)M * (uint64_t)K * (uint64_t)N > 192ULL * 192 * 192;
   int x86_packed = profile == ORACLE_X86_PACKED ||
-                   (profile == ORACLE_I8_X86_AVX2 &&
-                    (uint64_t)M * (uint64_t)K * (uint64_t)N > 192ULL * 192 * 192);
+                   (profile == ORACLE_I8_X86_AVX2 && above_sup);
   if (profile == ORACLE_X86_PACKED) profile = ORACLE_I8_X86_AVX2;
+  if (profile == ORACLE_I8_X86_AVX512 && !above_sup) profile = ORACLE_I8_WRAP;
   /* x86 packed blocks K by 512; everything else sums all K in one block. */
   int64_t kblk = x86_packed ? 512 : (K > 0 ? K : 1);
 #pragma omp parallel for schedule(dynamic, 1)
@@ -410,8 +434,9 @@ static void kern_8bit(const void *av, const void *bv, void *cv, int64_t M,
               int32_t t = is_signed ? sat_s8(P) : sat_u8_x86(P);
               *dij = (b == 0) ? t : wrap8(*dij + t, is_signed);
             }
-          } else { /* ORACLE_I8_ARM_NEON: one block over all K */
-            if (neon_full_tile(i, j, M, N)) {
+          } else { /* NEON or AVX-512: one block over all K, clamp once */
+            const int neon = profile == ORACLE_I8_ARM_NEON;
+            if (clamp_full_tile(i, j, M, N, neon ? 72 : 240, neon ? 6 : 12, neon ? 8 : 16)) {
               if (is_signed) *dij = sat_s8(P);
               else *dij = (uint32_t)P > 255u ? 255 : P;
             } else {
@@ -456,7 +481,9 @@ int oracle_matmul(int dtype, const void *a, const void *b, void *out,
     free(ad); free(bd); free(cd);
     return -1;
   }
-  const int x86 = profile == ORACLE_I8_X86_AVX2 || profile == ORACLE_X86_PACKED;
+  /* the AVX-512 profile is an int8/uint8 rule: its floats keep AVX2's tiles */
+  const int x86 = profile == ORACLE_I8_X86_AVX2 || profile == ORACLE_X86_PACKED ||
+                  profile == ORACLE_I8_X86_AVX512;
   switch (dtype) {
   case DT_F32:
     if (profile == ORACLE_I8_WRAP) {
@@ -465,6 +492,7 @@ int oracle_matmul(int dtype, const void *a, const void *b, void *out,
     }
     kern_f32(ad, bd, cd, M, K, N);
     if (x86) edges_f32(ad, bd, cd, M, K, N, profile == ORACLE_X86_PACKED);
+    else if (profile == ORACLE_I8_ARM_NEON) edges_f32_neon(ad, bd, cd, M, K, N, 0);
     break;
   case DT_F64:
     if (profile == ORACLE_I8_WRAP) {
@@ -473,6 +501,7 @@ int oracle_matmul(int dtype, const void *a, const void *b, void *out,
     }
     kern_f64(ad, bd, cd, M, K, N);
     if (x86) edges_f64(ad, bd, cd, M, K, N, profile == ORACLE_X86_PACKED);
+    else if (profile == ORACLE_I8_ARM_NEON) edges_f64_neon(ad, bd, cd, M, K, N, 0);
     break;
   case DT_I16: kern_i16(ad, bd, cd, M, K, N); break;
   case DT_U16: kern_u16(ad, bd, cd, M, K, N); break;

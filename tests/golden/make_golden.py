@@ -7,8 +7,10 @@ numc_gb300.synth and records its outputs.  Small outputs are stored whole;
 large ones as a SHA-256 of the output bytes plus a seeded sample of entries.
 
     python tests/golden/make_golden.py      (needs the reference checkout)
+    python tests/golden/make_golden.py isa  (numc's NEON and AVX-512 builds)
 
-Writes tests/golden/golden.json and tests/golden/golden.npz.
+Writes tests/golden/golden.json and tests/golden/golden.npz, or
+tests/golden/golden_isa.json and tests/golden/golden_isa.npz.
 """
 import hashlib
 import json
@@ -129,7 +131,70 @@ def record(cases, arrays, name, dt, kind, shape, seed=42):
     cases.append(entry)
 
 
+# numc's other ISA builds (oracle/Makefile.ref targets avx512 and neon):
+# tests/golden/golden_isa.{json,npz}.  NEON: every dtype through numc's
+# aarch64 matmul (packed and unpacked float tiles, several column panels,
+# the int8/uint8 clamp-once rule with its remainder tiles, sums past
+# 2^31); AVX-512: int8/uint8 (its float64 path is the crashing one).
+ISA_SHAPES = [(5, 3, 4), (5, 3, 7), (6, 9, 14), (33, 70, 17), (47, 40, 45),
+              (97, 300, 103), (129, 257, 131), (200, 200, 200), (150, 513, 300),
+              (241, 300, 250)]
+ISA_CASES = (
+    [("neon", dt, "uniform", sh) for dt in ALL for sh in ISA_SHAPES] +
+    [("neon", "float32", "normal", sh) for sh in ISA_SHAPES] +
+    [("neon", "float64", "normal", sh) for sh in ISA_SHAPES] +
+    [("neon", "float32", "normal", (130, 700, 4100)),
+     ("neon", "float64", "normal", (257, 300, 2050)),
+     ("neon", "float32", "uniform", (512, 512, 512)),
+     ("neon", "int8", "uniform", (1024, 1024, 1024)),
+     ("neon", "uint8", "uniform", (1024, 1024, 1024)),
+     ("neon", "int8", "uniform", (479, 1030, 33)),
+     ("neon", "uint8", "uniform", (479, 1030, 33)),
+     ("neon", "int8", "extreme", (7, 300000, 17)),
+     ("neon", "uint8", "extreme", (7, 40000, 17)),
+     ("neon", "int8", "extreme", (80, 2000, 70))] +
+    [("avx512", dt, "uniform", sh) for dt in ("int8", "uint8") for sh in
+     ISA_SHAPES + [(479, 1030, 33), (1024, 1024, 1024), (300, 4100, 4200)]] +
+    [("avx512", "int8", "extreme", (13, 300000, 35)),
+     ("avx512", "uint8", "extreme", (13, 40000, 35)),
+     ("avx512", "int8", "extreme", (250, 2000, 70)),
+     ("avx512", "uint8", "extreme", (250, 2000, 70))]
+)
+
+
+def make_isa_goldens():
+    cases, arrays = [], {}
+    for variant, dt, kind, (M, K, N) in ISA_CASES:
+        name = f"{variant}_{kind}_{dt}_{M}x{K}x{N}"
+        a, b = synth.operands(kind, M, K, N, seed=42, dtype=dt)
+        record_op(cases, arrays, name, oracle.ref_matmul(a, b, variant=variant),
+                  {"variant": variant, "dtype": dt, "kind": kind, "shape": [M, K, N],
+                   "seed": 42})
+        print(name, flush=True)
+    # numc_dot's N-D GEMM branch of the NEON build: numc's dot.c has no GEMM
+    # table there (dot.c:275-288) and runs its naive kernels; dot.c holds no
+    # NEON code on that branch, so the build's scalar dot.c is numc's.
+    dot_cases = []
+    for dt in ("int8", "uint8", "int32", "float32", "float64"):
+        for tag, ashape, bshape in (("2d_x_2d", (97, 300), (300, 103)),
+                                    ("2d_x_2d_small", (5, 7), (7, 3)),
+                                    ("2d_x_2d_panels", (40, 600), (600, 4100))):
+            name = f"neon_dot_{tag}_{dt}"
+            a, b = dot_operands(dt, ashape, bshape, 42)
+            record_op(dot_cases, arrays, name, oracle.ref_dot(a, b, variant="neon"),
+                      {"variant": "neon", "dtype": dt, "a_shape": list(ashape),
+                       "b_shape": list(bshape), "seed": 42})
+    with open(os.path.join(HERE, "golden_isa.json"), "w") as f:
+        json.dump({"generator": "numc_matmul and numc_dot of numc's aarch64 NEON build "
+                                "(matmul.c compiled against oracle/neon_shim) and "
+                                "numc_matmul of its x86-64 AVX-512 build",
+                   "cases": cases, "dot_cases": dot_cases}, f, indent=1)
+    np.savez_compressed(os.path.join(HERE, "golden_isa.npz"), **arrays)
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "isa":
+        return make_isa_goldens()
     if not oracle.reference_available():
         sys.exit("numc reference library cannot be built on this host")
     cases, arrays = [], {}
