@@ -157,6 +157,20 @@ NUMC_API int numc_cuda_gemm(NumcDType dtype, int algo, int param,
                             intptr_t rso, intptr_t cso, void *workspace,
                             size_t workspace_bytes, void *stream);
 
+/* numc's per-dtype kernel-table entry (GemmSimdKernel, src/matmul/
+ * matmul.c:84-86) with the dtype as first argument, on HOST memory: what
+ * numc's own numc_matmul would call in place of gemm_simd_table[dtype]
+ * (the in-tree binding).  out[i*rso + j] = sum_k a[i*rsa + k*csa] *
+ * b[k*rsb + j] with the default algorithm of `dtype` (numc_cuda_set_algo);
+ * b and out have unit column stride, as numc assumes.  Stages the operands
+ * to the GPU, runs, copies the result back and returns when `out` holds it
+ * (0, or a negative NumcErrorCode).  Device scratch comes from a context
+ * kept per calling thread. */
+NUMC_API int numc_cuda_gemm_host(NumcDType dtype, const void *a, const void *b,
+                                 void *out, size_t M, size_t K, size_t N,
+                                 intptr_t rsa, intptr_t csa, intptr_t rsb,
+                                 intptr_t rso);
+
 /* Waits for `stream` and reports any kernel that gave up on a bounded
  * wait (NUMC_ERR_INTERNAL); clears the flag. */
 NUMC_API int numc_cuda_check_status(void *stream);

@@ -726,6 +726,58 @@ extern "C" int numc_matmul(const NumcArray *a, const NumcArray *b, NumcArray *ou
   return matmul_impl(a, b, out, NUMC_CUDA_ALGO_DEFAULT, -1);
 }
 
+// numc's GemmSimdKernel on host memory: views of the caller's buffers on a
+// per-thread context, run through numc_matmul's host-operand path.
+namespace {
+struct ThreadCtx {
+  NumcCtx *ctx = nullptr;
+  ~ThreadCtx() {
+    if (ctx) numc_ctx_free(ctx);
+  }
+};
+thread_local ThreadCtx t_host_ctx;
+
+void host_view(NumcArray *v, NumcCtx *ctx, NumcDType dt, const void *data, size_t rows,
+               size_t cols, intptr_t rs, intptr_t cs) {
+  memset(v, 0, sizeof *v);
+  const size_t es = numc_dtype_size(dt);
+  v->ctx = ctx;
+  v->data = const_cast<void *>(data);
+  v->dim = 2;
+  v->shape = v->shape_buf;
+  v->strides = v->strides_buf;
+  v->shape[0] = rows;
+  v->shape[1] = cols;
+  v->strides[0] = (size_t)rs * es;
+  v->strides[1] = (size_t)cs * es;
+  v->elem_size = es;
+  v->size = rows * cols;
+  v->capacity = rows && cols ? ((rows - 1) * (size_t)rs + (cols - 1) * (size_t)cs + 1) * es : 0;
+  v->is_contiguous = cs == 1 && (size_t)rs == cols;
+  v->dtype = dt;
+  v->residency = kHostOnly;
+}
+}  // namespace
+
+extern "C" int numc_cuda_gemm_host(NumcDType dt, const void *a, const void *b, void *out,
+                                   size_t M, size_t K, size_t N, intptr_t rsa, intptr_t csa,
+                                   intptr_t rsb, intptr_t rso) {
+  if ((int)dt < 0 || (int)dt >= NUMC_DTYPE_COUNT)
+    return NUMC_SET_ERROR(NUMC_ERR_TYPE, "gemm_host: unknown dtype %d", (int)dt);
+  if (M == 0 || N == 0) return 0;
+  if (!out || (K > 0 && (!a || !b)))
+    return NUMC_SET_ERROR(NUMC_ERR_NULL, "gemm_host: NULL operand (a=%p b=%p out=%p)", a, b, out);
+  if (rsa < 0 || csa < 0 || rsb < 0 || rso < 0)
+    return NUMC_SET_ERROR(NUMC_ERR_VALUE, "gemm_host: negative stride");
+  if (!t_host_ctx.ctx && !(t_host_ctx.ctx = numc_ctx_create()))
+    return NUMC_SET_ERROR(NUMC_ERR_MALLOC, "gemm_host: context creation failed");
+  NumcArray va, vb, vo;
+  host_view(&va, t_host_ctx.ctx, dt, a, M, K, rsa, csa);
+  host_view(&vb, t_host_ctx.ctx, dt, b, K, N, rsb, 1);   // numc: unit column strides
+  host_view(&vo, t_host_ctx.ctx, dt, out, M, N, rso, 1);
+  return matmul_impl(&va, &vb, &vo, NUMC_CUDA_ALGO_DEFAULT, -1);
+}
+
 extern "C" int numc_matmul_naive(const NumcArray *a, const NumcArray *b, NumcArray *out) {
   // numc's naive kernels (kernel.h:18-62): integers accumulate in the
   // storage type (8-bit through 32 bits, truncated), floats `acc += a * b`
