@@ -106,6 +106,7 @@ SIGNATURES = [
     ("numc_cuda_gemm", _I, [_I, _I, _I, _VP, _VP, _VP, _SZ, _SZ, _SZ,
                             _IP, _IP, _IP, _IP, _IP, _IP, _VP, _SZ, _VP]),
     ("numc_cuda_check_status", _I, [_VP]),
+    ("numc_cuda_gemm_host", _I, [_I, _VP, _VP, _VP, _SZ, _SZ, _SZ, _IP, _IP, _IP, _IP]),
     ("numc_cuda_debug_fail_malloc", _I, [_I]),
     ("numc_cuda_debug_wait_timeout", _I, [ctypes.c_ulonglong, _I]),
     ("numc_cuda_launch_count", ctypes.c_uint64, []),
