@@ -126,7 +126,7 @@ grouped_split(const Prob *__restrict__ probs, const int2 *__restrict__ jobs,
 // planes — one read of the operand instead of two.  jobs[b] = (problem,
 // block), A's blocks first.  Problems with Kp above kFusedMaxKp use the
 // separate passes.
-constexpr int kFusedRows = 16, kFusedMaxKp = 1024;
+// kFusedRows, kFusedMaxKp and the block body: split_common.cuh
 
 __global__ void __launch_bounds__(256)
 grouped_scale_split(const Prob *__restrict__ probs, const int2 *__restrict__ jobs,
@@ -136,98 +136,11 @@ grouped_scale_split(const Prob *__restrict__ probs, const int2 *__restrict__ job
   const Prob &P = probs[job.x];
   const int a_blocks = (P.M + kFusedRows - 1) / kFusedRows;
   const bool is_a = job.y < a_blocks;
-  const float *src = is_a ? P.A : P.B;
-  const int64_t rs_row = is_a ? P.rsa : P.csb, rs_k = is_a ? P.csa : P.rsb;
-  const int R = is_a ? P.M : P.N, K = P.K, Kp = P.Kp;
-  const int r0 = (is_a ? job.y : job.y - a_blocks) * kFusedRows;
-  uint16_t *planes = is_a ? P.pa : P.pb;
-  unsigned long long *flags = is_a ? P.flags_a : P.flags_b;
-  const int flag_rows = is_a ? kBM : 64;
-  unsigned *maxbits = is_a ? P.max_a : P.max_b;
-  const int tid = threadIdx.x;
-
-  // Load the rows (zero past K and past R), 16 threads a row.
-  bool bad = false;
-  if (rs_k == 1) {           // along k: 16 consecutive k a row per step
-    const int r = tid / 16, sub = tid % 16;
-    const float *p = src + (int64_t)(r0 + r) * rs_row;
-    const bool live = r0 + r < R;
-    for (int k = sub; k < Kp; k += 16 * 8) {
-      float x[8];
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int kk = k + 16 * u;
-        x[u] = (live && kk < K) ? p[kk] : 0.0f;
-      }
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int kk = k + 16 * u;
-        if (kk < Kp) {
-          bad |= !isfinite(x[u]);
-          rowbuf[r * Kp + kk] = x[u];
-        }
-      }
-    }
-  } else {                   // across rows: 16 consecutive rows per k
-    const int r = tid % 16, sub = tid / 16;
-    const float *p = src + (int64_t)(r0 + r) * rs_row;
-    const bool live = r0 + r < R;
-    for (int k = sub; k < Kp; k += 16 * 8) {
-      float x[8];
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int kk = k + 16 * u;
-        x[u] = (live && kk < K) ? p[(int64_t)kk * rs_k] : 0.0f;
-      }
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int kk = k + 16 * u;
-        if (kk < Kp) {
-          bad |= !isfinite(x[u]);
-          rowbuf[r * Kp + kk] = x[u];
-        }
-      }
-    }
-  }
-  if (__syncthreads_or(bad) && tid == 0) flags[r0 / flag_rows] = gen;
-
-  // Row maxima: the 16 threads of a row (one half-warp) reduce its k range.
-  const int r = tid / 16, sub = tid % 16;
-  unsigned m = 0;
-  for (int k = sub; k < Kp; k += 16) m = max(m, absbits(rowbuf[r * Kp + k]));
-#pragma unroll
-  for (int o = 8; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-  const bool live = r0 + r < R;
-  if (live && sub == 0) maxbits[r0 + r] = m;
-
-  // Split: thread (r, sub) converts k = 4 sub + 64 i .. +3 of row r.
-  if (live) {
-    const int sexp = f16_scale_exp(m);
-    const int64_t plane_elems = (int64_t)R * Kp;
-    for (int k = 4 * sub; k < Kp; k += 64) {
-      const float4 v = *reinterpret_cast<const float4 *>(&rowbuf[r * Kp + k]);
-      const float rem[4] = {v.x, v.y, v.z, v.w};
-      uint16_t out[kPlanes][4];
-#pragma unroll
-      for (int t = 0; t < 4; t++) {
-        float x = isfinite(rem[t]) ? scale_pow2(rem[t], sexp) : 0.0f;
-#pragma unroll
-        for (int pl = 0; pl < kPlanes; pl++) {
-          const __half h = __float2half_rn(x);
-          out[pl][t] = __half_as_ushort(h);
-          x -= __half2float(h);
-        }
-      }
-      const int64_t off = (int64_t)(r0 + r) * Kp + k;
-#pragma unroll
-      for (int pl = 0; pl < kPlanes; pl++) {
-        uint2 w;
-        w.x = (uint32_t)out[pl][0] | ((uint32_t)out[pl][1] << 16);
-        w.y = (uint32_t)out[pl][2] | ((uint32_t)out[pl][3] << 16);
-        *reinterpret_cast<uint2 *>(planes + pl * plane_elems + off) = w;
-      }
-    }
-  }
+  fused_scale_split_rows(is_a ? P.A : P.B, is_a ? P.rsa : P.csb, is_a ? P.csa : P.rsb,
+                         is_a ? P.M : P.N, P.K, P.Kp,
+                         (is_a ? job.y : job.y - a_blocks) * kFusedRows,
+                         is_a ? P.pa : P.pb, is_a ? P.flags_a : P.flags_b, is_a ? kBM : 64,
+                         is_a ? P.max_a : P.max_b, gen, rowbuf);
 }
 
 // ---- persistent grouped split GEMM ----------------------------------------------
@@ -401,6 +314,20 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
       bool nonfinite = P.flags_a[tl.m0 / kBM] == gen;
       for (int c = tl.n0 / 64; c < (tl.n0 + BN) / 64 && c * 64 < P.N; c++)
         nonfinite |= P.flags_b[c] == gen;
+      if (F16 && !nonfinite) {
+        // acc * 2^-(s_row + s_col), correctly rounded (see gemm_tc.cu); the
+        // warp's column exponents are loaded once and broadcast (every lane
+        // runs this, rows past M included: nonfinite is the warp's tile's)
+        const int lc = tl.n0 + cbase + lane;
+        const int eb_lo = lc < P.N ? f16_scale_exp(P.max_b[lc]) : 0;
+        const int eb_hi = (CW > 32 && lc + 32 < P.N) ? f16_scale_exp(P.max_b[lc + 32]) : 0;
+        const int sa = row < P.M ? f16_scale_exp(P.max_a[row]) : 0;
+#pragma unroll
+        for (int j = 0; j < CW; j++) {
+          const int e = -(sa + __shfl_sync(0xffffffffu, j < 32 ? eb_lo : eb_hi, j & 31));
+          acc[j] = (e >= -126 && e <= 127) ? acc[j] * exp2_int(e) : ldexpf(acc[j], e);
+        }
+      }
       if (row >= P.M) {
         // rows past M: nothing to store
       } else if (nonfinite) {
@@ -416,16 +343,6 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
           P.C[(int64_t)row * P.rso + (int64_t)col * P.cso] = f;
         }
       } else {
-        if (F16) {
-          // acc * 2^-(s_row + s_col), correctly rounded (see gemm_tc.cu).
-          const int sa = f16_scale_exp(P.max_a[row]);
-#pragma unroll
-          for (int j = 0; j < CW; j++) {
-            const int col = tl.n0 + cbase + j;
-            const int e = -(sa + (col < P.N ? f16_scale_exp(P.max_b[col]) : 0));
-            acc[j] = (e >= -126 && e <= 127) ? acc[j] * exp2_int(e) : ldexpf(acc[j], e);
-          }
-        }
         float *crow = P.C + (int64_t)row * P.rso;
 #pragma unroll
         for (int j = 0; j < CW; j++) {

@@ -88,6 +88,24 @@ void launch_split_planes(dim3 grid, cudaStream_t s, int mode, const float *src, 
                                                       flags, flag_rows, gen, maxbits);
 }
 
+// Both operands of one float16-plane split through fused_scale_split_rows
+// (K up to kFusedMaxKp): blocks [0, a_blocks) take 16 rows of A each, the
+// rest 16 columns of B.  One launch replaces two zeroings of the maxima,
+// two absmax passes and two split passes.
+__global__ void __launch_bounds__(256)
+scale_split_pair(const float *A, int64_t rsa, int64_t csa, int M, const float *B,
+                 int64_t rsb, int64_t csb, int N, int K, int Kp, uint16_t *pa, uint16_t *pb,
+                 unsigned long long *fa, unsigned long long *fbl, unsigned *max_a,
+                 unsigned *max_b, unsigned long long gen) {
+  extern __shared__ __align__(16) float rowbuf[];   // [kFusedRows][Kp]
+  const int a_blocks = (M + kFusedRows - 1) / kFusedRows;
+  const bool is_a = (int)blockIdx.x < a_blocks;
+  fused_scale_split_rows(is_a ? A : B, is_a ? rsa : csb, is_a ? csa : rsb, is_a ? M : N, K, Kp,
+                         (is_a ? (int)blockIdx.x : (int)blockIdx.x - a_blocks) * kFusedRows,
+                         is_a ? pa : pb, is_a ? fa : fbl, is_a ? kBM : 64, is_a ? max_a : max_b,
+                         gen, rowbuf);
+}
+
 // ---- pass 2: the tcgen05 GEMM ------------------------------------------------
 
 // Original operands and the non-finite flags, for tiles that must be
@@ -408,36 +426,38 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
               C[(int64_t)row * rso + (int64_t)(n0 + c0 + j) * cso] =
                   fb.bias ? __fadd_rn(f[j], fb.bias[(int64_t)(n0 + c0 + j) * fb.bias_stride]) : f[j];
         }
-      } else if (row < M) {
+      } else {
         if (F16) {
           // Undo the row and column scaling, acc * 2^-(sa + sb) correctly
           // rounded: one multiply by a power of two when the exponent is a
           // normal float32's (the product then rounds once, if at all),
-          // ldexpf otherwise.
-          const int sa = f16_scale_exp(fb.max_a[row]);
-          bool in_range = true;
-#pragma unroll 4
-          for (int j = 0; j < CW; j++) {
-            const int col = n0 + cbase + j;
-            const int e = -(sa + (col < N ? f16_scale_exp(fb.max_b[col]) : 0));
-            in_range &= e >= -126 && e <= 127;
-          }
+          // ldexpf otherwise.  The warp's 64 column exponents are loaded
+          // once, one per lane and half-warp pass, and broadcast.
+          const int lc = n0 + cbase + lane;
+          const int eb_lo = lc < N ? f16_scale_exp(fb.max_b[lc]) : 0;
+          const int eb_hi = lc + 32 < N ? f16_scale_exp(fb.max_b[lc + 32]) : 0;
+          const int sa = row < M ? f16_scale_exp(fb.max_a[row]) : 0;
+          // e = -(sa + eb) over the warp's rows and columns: all normal
+          // float32 exponents (the usual case) -> float multiplies; else the
+          // product in double (exact: acc has 24 bits) rounded once to float
+          const int eb_min = __reduce_min_sync(0xffffffffu, min(eb_lo, eb_hi));
+          const int eb_max = __reduce_max_sync(0xffffffffu, max(eb_lo, eb_hi));
+          const bool in_range = __all_sync(0xffffffffu, -(sa + eb_max) >= -126 &&
+                                                          -(sa + eb_min) <= 127);
           if (in_range) {
 #pragma unroll
-            for (int j = 0; j < CW; j++) {
-              const int col = n0 + cbase + j;
-              const int e = -(sa + (col < N ? f16_scale_exp(fb.max_b[col]) : 0));
-              acc[j] *= exp2_int(e);
-            }
+            for (int j = 0; j < CW; j++)
+              acc[j] *= exp2_int(-(sa + __shfl_sync(0xffffffffu, j < 32 ? eb_lo : eb_hi, j & 31)));
           } else {
 #pragma unroll
             for (int j = 0; j < CW; j++) {
-              const int col = n0 + cbase + j;
-              const int e = -(sa + (col < N ? f16_scale_exp(fb.max_b[col]) : 0));
-              acc[j] = ldexpf(acc[j], e);
+              const int e = -(sa + __shfl_sync(0xffffffffu, j < 32 ? eb_lo : eb_hi, j & 31));
+              acc[j] = (float)((double)acc[j] * exp2_dbl(e));
             }
           }
         }
+      }
+      if (!nonfinite && row < M) {
         if (fb.bias) {
 #pragma unroll
           for (int j = 0; j < CW; j++) {
@@ -584,9 +604,28 @@ cudaError_t split_b(const SplitLayout &L, const SplitBufs &b, const Gemm &g,
                        b.max_b, gen, s);
 }
 
-// Launch the split pass of both operands.
+// Launch the split pass of both operands: for float16 planes with K up to
+// kFusedMaxKp one fused scale + split launch over both, else a scale pass
+// and a split pass per operand.
 cudaError_t launch_split_pass(const SplitLayout &L, const SplitBufs &b, const Gemm &g,
                               unsigned long long gen, cudaStream_t s) {
+  if (L.f16 && L.Kp <= kFusedMaxKp && g.M < (1ll << 30) && g.N < (1ll << 30)) {
+    const int64_t blocks = (g.M + kFusedRows - 1) / kFusedRows + (g.N + kFusedRows - 1) / kFusedRows;
+    const size_t smem = (size_t)kFusedRows * L.Kp * sizeof(float);
+    static bool attr_set = false;   // per process; the attribute is per function
+    cudaError_t e = cudaSuccess;
+    if (!attr_set) {
+      e = cudaFuncSetAttribute(scale_split_pair, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(kFusedRows * kFusedMaxKp * sizeof(float)));
+      if (e != cudaSuccess) return e;
+      attr_set = true;
+    }
+    scale_split_pair<<<(unsigned)blocks, 256, smem, s>>>(
+        (const float *)g.a, g.rsa, g.csa, (int)g.M, (const float *)g.b, g.rsb, g.csb, (int)g.N,
+        (int)g.K, (int)L.Kp, b.pa, b.pb, b.flags_a, b.flags_b, b.max_a, b.max_b, gen);
+    count_launch();
+    return cudaGetLastError();
+  }
   cudaError_t e = split_a(L, b, g, gen, s);
   return e != cudaSuccess ? e : split_b(L, b, g, gen, s);
 }

@@ -21,6 +21,11 @@ namespace numc_k {
 // Scale exponent of a row whose largest magnitude has float32 bits
 // `maxbits`: s with max * 2^s in [2^14, 2^15), or 0 for an all-zero or
 // non-finite row (a non-finite row is recomputed by the fallback anyway).
+// 2^e as a double, exactly, for |e| <= 1022.
+__device__ __forceinline__ double exp2_dbl(int e) {
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
 __host__ __device__ inline int f16_scale_exp(unsigned maxbits) {
   if (maxbits == 0 || maxbits >= 0x7f800000u) return 0;
   int e;   // floor(log2(max))
@@ -59,6 +64,15 @@ constexpr int kMaxRows1 = 8, kMaxK1 = 1024, kMaxRows2 = 1024, kMaxK2 = 64, kMaxR
               kMaxK0 = 64;
 
 __device__ __forceinline__ unsigned absbits(float x) { return __float_as_uint(x) & 0x7fffffffu; }
+
+// K extent of a block in read mode 2 (rows contiguous, 1024 rows a block):
+// 64 on large operands; on small ones halved down to 8 until the grid has
+// about four blocks per SM, so the pass is not a few long load chains.
+__host__ __device__ inline int64_t absmax_k2(int64_t R, int64_t K) {
+  int64_t kk = kMaxK2;
+  while (kk > 8 && ((K + kk - 1) / kk) * ((R + kMaxRows2 - 1) / kMaxRows2) < 608) kk /= 2;
+  return kk;
+}
 
 // Block (bk, br) of the grid below, executed by a 256-thread block.
 __device__ __forceinline__ void absmax_block(const float *__restrict__ src, int64_t rs_row,
@@ -102,10 +116,11 @@ __device__ __forceinline__ void absmax_block(const float *__restrict__ src, int6
     if (lane == 0 && r < R && m) atomicMax(&maxbits[r], m);
   } else if (mode == 2) {
     const int64_t r = br * kMaxRows2 + 4 * tid;
-    const int64_t k0 = bk * kMaxK2;
+    const int64_t kk = absmax_k2(R, K);
+    const int64_t k0 = bk * kk;
     unsigned m[4] = {0, 0, 0, 0};
     if (r < R) {
-      const int64_t k1 = k0 + kMaxK2 < K ? k0 + kMaxK2 : K;
+      const int64_t k1 = k0 + kk < K ? k0 + kk : K;
       for (int64_t k = k0; k < k1; k++) {
         const float *p = src + r + k * rs_k;
         if (r + 3 < R) {
@@ -145,7 +160,7 @@ absmax_rows_f32(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int
 // Grid of absmax_rows_f32 for R rows, K columns, read mode `mode`.
 __host__ __device__ inline dim3 absmax_grid(int64_t R, int64_t K, int mode) {
   const bool rowwise = mode == 1 || mode == 3;
-  const int64_t kk = rowwise ? kMaxK1 : mode == 2 ? kMaxK2 : kMaxK0;
+  const int64_t kk = rowwise ? kMaxK1 : mode == 2 ? absmax_k2(R, K) : kMaxK0;
   const int64_t rr = rowwise ? kMaxRows1 : mode == 2 ? kMaxRows2 : kMaxRows0;
   return dim3((unsigned)((K + kk - 1) / kk), (unsigned)((R + rr - 1) / rr));
 }
@@ -319,6 +334,107 @@ __device__ __forceinline__ void split_tile(const float *__restrict__ src, int64_
 // Read mode of the scale pass for a source of split mode `mode`: k-contiguous
 // rows that are not 16-byte aligned are read one warp per row (3), not one
 // thread per row.
+// ---- fused scale and split (float16 planes, K up to kFusedMaxKp) --------------
+//
+// One 256-thread block: kFusedRows rows of one operand (A's rows, or B's
+// columns as B^T's rows), staged whole in shared memory `rowbuf` (at least
+// kFusedRows x Kp floats): the row maxima, then the two float16 planes, from
+// one read of the operand instead of the two of the absmax and split passes.
+// Writes maxbits[row] directly (no zeroing first) and, for a non-finite
+// value, flags[r0 / flag_rows] = gen.  Same arithmetic as split_tile<2, true>.
+constexpr int kFusedRows = 16, kFusedMaxKp = 1024;
+
+__device__ __forceinline__ void fused_scale_split_rows(
+    const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int R, int K, int Kp, int r0,
+    uint16_t *__restrict__ planes, unsigned long long *flags, int flag_rows,
+    unsigned *__restrict__ maxbits, unsigned long long gen, float *rowbuf) {
+  constexpr int kPlanes = 2;
+  const int tid = threadIdx.x;
+
+  // Load the rows (zero past K and past R), 16 threads a row.
+  bool bad = false;
+  if (rs_k == 1) {           // along k: 16 consecutive k a row per step
+    const int r = tid / 16, sub = tid % 16;
+    const float *p = src + (int64_t)(r0 + r) * rs_row;
+    const bool live = r0 + r < R;
+    for (int k = sub; k < Kp; k += 16 * 8) {
+      float x[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int kk = k + 16 * u;
+        x[u] = (live && kk < K) ? p[kk] : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int kk = k + 16 * u;
+        if (kk < Kp) {
+          bad |= !isfinite(x[u]);
+          rowbuf[r * Kp + kk] = x[u];
+        }
+      }
+    }
+  } else {                   // across rows: 16 consecutive rows per k
+    const int r = tid % 16, sub = tid / 16;
+    const float *p = src + (int64_t)(r0 + r) * rs_row;
+    const bool live = r0 + r < R;
+    for (int k = sub; k < Kp; k += 16 * 8) {
+      float x[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int kk = k + 16 * u;
+        x[u] = (live && kk < K) ? p[(int64_t)kk * rs_k] : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int kk = k + 16 * u;
+        if (kk < Kp) {
+          bad |= !isfinite(x[u]);
+          rowbuf[r * Kp + kk] = x[u];
+        }
+      }
+    }
+  }
+  if (__syncthreads_or(bad) && tid == 0) flags[r0 / flag_rows] = gen;
+
+  // Row maxima: the 16 threads of a row (one half-warp) reduce its k range.
+  const int r = tid / 16, sub = tid % 16;
+  unsigned m = 0;
+  for (int k = sub; k < Kp; k += 16) m = max(m, absbits(rowbuf[r * Kp + k]));
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  const bool live = r0 + r < R;
+  if (live && sub == 0) maxbits[r0 + r] = m;
+
+  // Split: thread (r, sub) converts k = 4 sub + 64 i .. +3 of row r.
+  if (live) {
+    const int sexp = f16_scale_exp(m);
+    const int64_t plane_elems = (int64_t)R * Kp;
+    for (int k = 4 * sub; k < Kp; k += 64) {
+      const float4 v = *reinterpret_cast<const float4 *>(&rowbuf[r * Kp + k]);
+      const float rem[4] = {v.x, v.y, v.z, v.w};
+      uint16_t out[kPlanes][4];
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        float x = isfinite(rem[t]) ? scale_pow2(rem[t], sexp) : 0.0f;
+#pragma unroll
+        for (int pl = 0; pl < kPlanes; pl++) {
+          const __half h = __float2half_rn(x);
+          out[pl][t] = __half_as_ushort(h);
+          x -= __half2float(h);
+        }
+      }
+      const int64_t off = (int64_t)(r0 + r) * Kp + k;
+#pragma unroll
+      for (int pl = 0; pl < kPlanes; pl++) {
+        uint2 w;
+        w.x = (uint32_t)out[pl][0] | ((uint32_t)out[pl][1] << 16);
+        w.y = (uint32_t)out[pl][2] | ((uint32_t)out[pl][3] << 16);
+        *reinterpret_cast<uint2 *>(planes + pl * plane_elems + off) = w;
+      }
+    }
+  }
+}
+
 __host__ __device__ inline int absmax_mode(int mode, int64_t rs_k) {
   return mode == 0 && rs_k == 1 ? 3 : mode;
 }
