@@ -149,9 +149,12 @@ template <int BN, int STAGES, int FLUSH>
 struct Cfg {
   static constexpr uint32_t A_BYTES = kBM * kBK * 2, B_BYTES = BN * kBK * 2;
   static constexpr uint32_t STAGE_BYTES = kPlanes * (A_BYTES + B_BYTES);
-  static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024 + 256;
-  static constexpr int NBUF = 512 / BN;
   static constexpr int ACC_WARPS = 8;
+  // ring, barriers, and per accumulator warp a staging buffer for coalesced
+  // stores
+  static constexpr uint32_t SMEM =
+      STAGES * STAGE_BYTES + 1024 + 256 + ACC_WARPS * kEpiStageFloats * 4;
+  static constexpr int NBUF = 512 / BN;
   static constexpr int CW = BN / 2;
   static constexpr int THREADS = 64 + 32 * ACC_WARPS;
   static_assert(SMEM <= 232448, "shared memory");
@@ -342,13 +345,20 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
                           P.B[(int64_t)k * P.rsb + (int64_t)col * P.csb], f);
           P.C[(int64_t)row * P.rso + (int64_t)col * P.cso] = f;
         }
-      } else {
+      } else if (P.cso != 1) {
         float *crow = P.C + (int64_t)row * P.rso;
 #pragma unroll
         for (int j = 0; j < CW; j++) {
           const int col = tl.n0 + cbase + j;
           if (col < P.N) crow[(int64_t)col * P.cso] = acc[j];
         }
+      }
+      __syncwarp();
+      if (!nonfinite && P.cso == 1) {   // warp-uniform: every lane stores
+        float *stage =
+            (float *)(smem + STAGES * C_::STAGE_BYTES + 256) + (warp - 2) * kEpiStageFloats;
+        store_rows_coalesced<CW>(acc, stage, P.C, P.rso, tl.m0 + quad * 32, tl.n0 + cbase, P.M,
+                                 P.N, lane);
       }
       __syncwarp();   // reconverge before the next tile's tcgen05.ld
     }

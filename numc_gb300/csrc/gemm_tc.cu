@@ -126,11 +126,16 @@ struct SplitCfg {
   static constexpr uint32_t A_BYTES = kBM * kBK * 2;   // one plane of a K slab of A
   static constexpr uint32_t B_BYTES = BN_CTA * kBK * 2;
   static constexpr uint32_t STAGE_BYTES = PLANES * (A_BYTES + B_BYTES);   // per CTA
-  static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
   static constexpr int NBUF = 512 / BN;           // FP32 accumulator buffers in TMEM
   static constexpr uint32_t TMEM_COLS = NBUF * BN;
   static constexpr int COLS_PER_WARP = 64;
   static constexpr int ACC_WARPS = 4 * BN / COLS_PER_WARP;   // BN / 64 per TMEM lane quadrant
+  // per accumulator warp, a staging buffer for coalesced stores, where the
+  // ring leaves room for it
+  static constexpr uint32_t RING = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+  static constexpr uint32_t EPI_BYTES = ACC_WARPS * kEpiStageFloats * 4;
+  static constexpr bool EPI_STAGE = RING + EPI_BYTES <= 232448;
+  static constexpr uint32_t SMEM = RING + (EPI_STAGE ? EPI_BYTES : 0);
   static constexpr int THREADS = 64 + 32 * ACC_WARPS;   // producer, MMA, accumulators
   static_assert(BN == 128 || BN == 256, "tile width");
   static_assert(CTAS == 1 || CTAS == 2, "one CTA or a CTA pair");
@@ -402,6 +407,21 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
 #pragma unroll 1
       for (int c = n0 / 64; c < (n0 + BN) / 64 && c * 64 < N; c++)
         nonfinite |= fb.flags_b[c] == fb.gen;
+      // The warp's staging buffer: first its 64 column scale exponents
+      // (float16 planes; one load per lane and half, read back as
+      // broadcasts), then the coalesced stores.
+      float *stage = (float *)(smem + STAGES * Cfg::STAGE_BYTES + 256) +
+                     (warp - 2) * kEpiStageFloats;
+      const int *colexp = (const int *)stage;
+      if constexpr (F16) {
+        static_assert(Cfg::EPI_STAGE, "float16 planes stage their epilogue");
+        if (!nonfinite) {
+          const int lc = n0 + cbase + lane;
+          ((int *)stage)[lane] = lc < N ? f16_scale_exp(fb.max_b[lc]) : 0;
+          ((int *)stage)[lane + 32] = lc + 32 < N ? f16_scale_exp(fb.max_b[lc + 32]) : 0;
+          __syncwarp();
+        }
+      }
       if (nonfinite) {
         // numc's arithmetic: one FMA chain per output in k order (slow path).
 #pragma unroll 1
@@ -426,38 +446,29 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
               C[(int64_t)row * rso + (int64_t)(n0 + c0 + j) * cso] =
                   fb.bias ? __fadd_rn(f[j], fb.bias[(int64_t)(n0 + c0 + j) * fb.bias_stride]) : f[j];
         }
-      } else {
-        if (F16) {
+      } else if (row < M) {
+        if constexpr (F16) {
           // Undo the row and column scaling, acc * 2^-(sa + sb) correctly
-          // rounded: one multiply by a power of two when the exponent is a
-          // normal float32's (the product then rounds once, if at all),
-          // ldexpf otherwise.  The warp's 64 column exponents are loaded
-          // once, one per lane and half-warp pass, and broadcast.
-          const int lc = n0 + cbase + lane;
-          const int eb_lo = lc < N ? f16_scale_exp(fb.max_b[lc]) : 0;
-          const int eb_hi = lc + 32 < N ? f16_scale_exp(fb.max_b[lc + 32]) : 0;
-          const int sa = row < M ? f16_scale_exp(fb.max_a[row]) : 0;
-          // e = -(sa + eb) over the warp's rows and columns: all normal
-          // float32 exponents (the usual case) -> float multiplies; else the
-          // product in double (exact: acc has 24 bits) rounded once to float
-          const int eb_min = __reduce_min_sync(0xffffffffu, min(eb_lo, eb_hi));
-          const int eb_max = __reduce_max_sync(0xffffffffu, max(eb_lo, eb_hi));
-          const bool in_range = __all_sync(0xffffffffu, -(sa + eb_max) >= -126 &&
-                                                          -(sa + eb_min) <= 127);
+          // rounded: float multiplies by powers of two when every exponent
+          // is a normal float32's (the product then rounds once, if at all),
+          // else the product in double (exact: acc has 24 bits) rounded
+          // once to float.  Column exponents come from the warp's table.
+          const int sa = f16_scale_exp(fb.max_a[row]);
+          bool in_range = true;
+#pragma unroll 8
+          for (int j = 0; j < CW; j++) {
+            const int e = -(sa + colexp[j]);
+            in_range &= e >= -126 && e <= 127;
+          }
           if (in_range) {
 #pragma unroll
-            for (int j = 0; j < CW; j++)
-              acc[j] *= exp2_int(-(sa + __shfl_sync(0xffffffffu, j < 32 ? eb_lo : eb_hi, j & 31)));
+            for (int j = 0; j < CW; j++) acc[j] *= exp2_int(-(sa + colexp[j]));
           } else {
 #pragma unroll
-            for (int j = 0; j < CW; j++) {
-              const int e = -(sa + __shfl_sync(0xffffffffu, j < 32 ? eb_lo : eb_hi, j & 31));
-              acc[j] = (float)((double)acc[j] * exp2_dbl(e));
-            }
+            for (int j = 0; j < CW; j++)
+              acc[j] = (float)((double)acc[j] * exp2_dbl(-(sa + colexp[j])));
           }
         }
-      }
-      if (!nonfinite && row < M) {
         if (fb.bias) {
 #pragma unroll
           for (int j = 0; j < CW; j++) {
@@ -465,21 +476,29 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
             if (col < N) acc[j] = __fadd_rn(acc[j], fb.bias[(int64_t)col * fb.bias_stride]);
           }
         }
-        float *crow = C + (int64_t)row * rso;
+        if (!(Cfg::EPI_STAGE && cso == 1)) {
+          float *crow = C + (int64_t)row * rso;
 #pragma unroll
-        for (int c0 = 0; c0 < CW; c0 += 32) {
-          const int nb = n0 + cbase + c0;
-          if (vec4 && nb + 32 <= N) {
-            float4 *p = reinterpret_cast<float4 *>(crow + nb);
+          for (int c0 = 0; c0 < CW; c0 += 32) {
+            const int nb = n0 + cbase + c0;
+            if (vec4 && nb + 32 <= N) {
+              float4 *p = reinterpret_cast<float4 *>(crow + nb);
 #pragma unroll
-            for (int j = 0; j < 8; j++)
-              p[j] = make_float4(acc[c0 + 4 * j], acc[c0 + 4 * j + 1], acc[c0 + 4 * j + 2],
-                                 acc[c0 + 4 * j + 3]);
-          } else {
+              for (int j = 0; j < 8; j++)
+                p[j] = make_float4(acc[c0 + 4 * j], acc[c0 + 4 * j + 1], acc[c0 + 4 * j + 2],
+                                   acc[c0 + 4 * j + 3]);
+            } else {
 #pragma unroll
-            for (int j = 0; j < 32; j++)
-              if (nb + j < N) crow[(int64_t)(nb + j) * cso] = acc[c0 + j];
+              for (int j = 0; j < 32; j++)
+                if (nb + j < N) crow[(int64_t)(nb + j) * cso] = acc[c0 + j];
+            }
           }
+        }
+      }
+      if constexpr (Cfg::EPI_STAGE) {
+        if (!nonfinite && cso == 1) {   // warp-uniform: every lane stores
+          __syncwarp();
+          store_rows_coalesced<CW>(acc, stage, C, rso, mr + quad * 32, n0 + cbase, M, N, lane);
         }
       }
       __syncwarp();   // reconverge before the next tile's tcgen05.ld

@@ -435,6 +435,49 @@ __device__ __forceinline__ void fused_scale_split_rows(
   }
 }
 
+// ---- coalesced epilogue stores ------------------------------------------------
+//
+// The tensor-memory drain (tcgen05.ld 32x32b) leaves one output row per lane,
+// so a direct store instruction of a warp touches 32 rows.  This writes the
+// warp's 32 rows x W columns (v[c] of row row0 + lane, column col0 + c) to a
+// row-major C with unit column stride through `stage`, the warp's 2 KiB of
+// shared memory, 16 columns at a time: each lane writes its row's 16 values
+// as four 16-byte chunks (chunk q at position q ^ ((row >> 1) & 3): the 8
+// lanes of a store phase hit 32 distinct banks), then every load / store
+// instruction covers two rows of 16 consecutive columns (two 64-byte
+// segments).  Rows >= M and columns >= N are not written.  All 32 lanes
+// must call it.
+constexpr int kEpiStageFloats = 32 * 16;
+
+template <int W>
+__device__ __forceinline__ void store_rows_coalesced(const float (&v)[W], float *stage, float *C,
+                                                     int64_t rso, int row0, int col0, int M,
+                                                     int N, int lane) {
+  static_assert(W % 16 == 0, "16-column blocks");
+#pragma unroll
+  for (int c0 = 0; c0 < W; c0 += 16) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int qs = q ^ ((lane >> 1) & 3);
+      *reinterpret_cast<float4 *>(stage + lane * 16 + qs * 4) =
+          make_float4(v[c0 + 4 * q], v[c0 + 4 * q + 1], v[c0 + 4 * q + 2], v[c0 + 4 * q + 3]);
+    }
+    __syncwarp();
+    const int c = lane & 15, r1 = lane >> 4;
+    // rows r1, r1 + 2, ...: one running pointer, valid rows counted down
+    float *dst = C + (int64_t)(row0 + r1) * rso + (col0 + c0 + c);
+    int rows_left = M - (row0 + r1);
+    const bool col_ok = col0 + c0 + c < N;
+#pragma unroll 1
+    for (int rr = 0; rr < 32; rr += 2, dst += 2 * rso, rows_left -= 2) {
+      const int r = rr + r1;
+      const float x = stage[r * 16 + (((c >> 2) ^ ((r >> 1) & 3)) << 2) + (c & 3)];
+      if (rows_left > 0 && col_ok) *dst = x;
+    }
+    __syncwarp();
+  }
+}
+
 __host__ __device__ inline int absmax_mode(int mode, int64_t rs_k) {
   return mode == 0 && rs_k == 1 ? 3 : mode;
 }
