@@ -117,21 +117,18 @@ grouped_split(const Prob *__restrict__ probs, const int2 *__restrict__ jobs,
   }
 }
 
-// ---- fused scale and split (float16 planes, K up to kFusedMaxKp) -------------------
+// ---- fused scale and split (float16 planes) --------------------------------------
 
 // One block: kFusedRows rows of one operand (A's rows, or B's columns as the
-// rows of B^T) over the whole of K, staged in shared memory; the block
-// takes each row's largest magnitude (the scale pass's result, stored for
-// the GEMM's final rescale), then splits the rows into the two float16
-// planes — one read of the operand instead of two.  jobs[b] = (problem,
-// block), A's blocks first.  Problems with Kp above kFusedMaxKp use the
-// separate passes.
-// kFusedRows, kFusedMaxKp and the block body: split_common.cuh
+// rows of B^T) over the whole of K: each row's largest magnitude (the scale
+// pass's result, stored for the GEMM's final rescale), then the two float16
+// planes, from one launch and one DRAM read of the operand.  jobs[b] =
+// (problem, block), A's blocks first.  kFusedRows and the block body:
+// split_common.cuh.
 
 __global__ void __launch_bounds__(256)
 grouped_scale_split(const Prob *__restrict__ probs, const int2 *__restrict__ jobs,
                     unsigned long long gen) {
-  extern __shared__ __align__(16) float rowbuf[];   // [kFusedRows][Kp]
   const int2 job = jobs[blockIdx.x];
   const Prob &P = probs[job.x];
   const int a_blocks = (P.M + kFusedRows - 1) / kFusedRows;
@@ -140,7 +137,7 @@ grouped_scale_split(const Prob *__restrict__ probs, const int2 *__restrict__ job
                          is_a ? P.M : P.N, P.K, P.Kp,
                          (is_a ? job.y : job.y - a_blocks) * kFusedRows,
                          is_a ? P.pa : P.pb, is_a ? P.flags_a : P.flags_b, is_a ? kBM : 64,
-                         is_a ? P.max_a : P.max_b, gen, rowbuf);
+                         is_a ? P.max_a : P.max_b, gen);
 }
 
 // ---- persistent grouped split GEMM ----------------------------------------------
@@ -440,7 +437,6 @@ struct NumcCudaGemmPlan {
   int2 *d_max_jobs;               // (problem, job) of each scale block (float16 planes)
   int2 *d_fused_jobs;             // (problem, block) of the fused scale + split pass
   long long fused_jobs;
-  int fused_smem;                 // its shared memory (kFusedRows x the largest Kp)
   long long max_jobs;
   int n_split_probs;
   Prob *d_split_probs;
@@ -570,7 +566,7 @@ int plan_enqueue(NumcCudaGemmPlan *p, cudaStream_t s, unsigned *kernels) {
     ++*kernels;
   }
   if (p->fused_jobs > 0) {
-    grouped_scale_split<<<(unsigned)p->fused_jobs, 256, p->fused_smem, s>>>(
+    grouped_scale_split<<<(unsigned)p->fused_jobs, 256, 0, s>>>(
         p->d_split_probs, p->d_fused_jobs, p->gen);
     if ((e = cudaGetLastError())) return fail(e, "grouped scale and split");
     ++*kernels;
@@ -732,13 +728,11 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   // Job tables: (problem, job within it) for every block of the scale,
   // split and remainder passes, so a block finds its problem in one load.
   std::vector<int2> split_jobs, max_jobs, edge_jobs, fused_jobs;
-  int fused_kp = 0;
   for (size_t q = 0; q < split_idx.size(); q++) {
     const Prob &P = p->probs[split_idx[q]];
-    if (p->f16 && P.Kp <= kFusedMaxKp) {   // one fused scale + split pass
+    if (p->f16) {   // float16 planes: one fused scale + split pass
       const long long n = (P.M + kFusedRows - 1) / kFusedRows + (P.N + kFusedRows - 1) / kFusedRows;
       for (long long j = 0; j < n; j++) fused_jobs.push_back(make_int2((int)q, (int)j));
-      fused_kp = std::max(fused_kp, P.Kp);
       continue;
     }
     const long long kt = (P.Kp + kSplitK - 1) / kSplitK;
@@ -762,7 +756,6 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   p->max_jobs = (long long)max_jobs.size();
   p->edge_jobs = (long long)edge_jobs.size();
   p->fused_jobs = (long long)fused_jobs.size();
-  p->fused_smem = kFusedRows * fused_kp * 4;
   if (p->split_jobs > 0x7FFFFFFFll || p->max_jobs > 0x7FFFFFFFll || p->edge_jobs > 0x7FFFFFFFll ||
       p->fused_jobs > 0x7FFFFFFFll) {
     delete p;
@@ -835,9 +828,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
     }
   }
   // Kernel attributes are set here, not per run, so runs can be captured.
-  if ((e = cudaFuncSetAttribute(grouped_scale_split, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                kFusedRows * kFusedMaxKp * 4)) ||
-      (e = prepare_tc<128, 3, kFlushBf16, false>()) || (e = prepare_tc<64, 4, kFlushBf16, false>()) ||
+  if ((e = prepare_tc<128, 3, kFlushBf16, false>()) || (e = prepare_tc<64, 4, kFlushBf16, false>()) ||
       (e = prepare_tc<128, 3, kFlushF16, true>()) || (e = prepare_tc<64, 4, kFlushF16, true>()) ||
       !status_word()) {
     numc_cuda_gemm_plan_free(p);

@@ -54,6 +54,7 @@ namespace numc_k {
 namespace {
 
 constexpr int kBM = 128, kBK = 64;
+constexpr int kFusedMaxKp = 1024;   // single problems: fused scale + split up to this K
 
 __host__ __device__ inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
@@ -88,8 +89,8 @@ void launch_split_planes(dim3 grid, cudaStream_t s, int mode, const float *src, 
                                                       flags, flag_rows, gen, maxbits);
 }
 
-// Both operands of one float16-plane split through fused_scale_split_rows
-// (K up to kFusedMaxKp): blocks [0, a_blocks) take 16 rows of A each, the
+// Both operands of one float16-plane split through fused_scale_split_rows:
+// blocks [0, a_blocks) take 16 rows of A each, the
 // rest 16 columns of B.  One launch replaces two zeroings of the maxima,
 // two absmax passes and two split passes.
 __global__ void __launch_bounds__(256)
@@ -97,13 +98,12 @@ scale_split_pair(const float *A, int64_t rsa, int64_t csa, int M, const float *B
                  int64_t rsb, int64_t csb, int N, int K, int Kp, uint16_t *pa, uint16_t *pb,
                  unsigned long long *fa, unsigned long long *fbl, unsigned *max_a,
                  unsigned *max_b, unsigned long long gen) {
-  extern __shared__ __align__(16) float rowbuf[];   // [kFusedRows][Kp]
   const int a_blocks = (M + kFusedRows - 1) / kFusedRows;
   const bool is_a = (int)blockIdx.x < a_blocks;
   fused_scale_split_rows(is_a ? A : B, is_a ? rsa : csb, is_a ? csa : rsb, is_a ? M : N, K, Kp,
                          (is_a ? (int)blockIdx.x : (int)blockIdx.x - a_blocks) * kFusedRows,
                          is_a ? pa : pb, is_a ? fa : fbl, is_a ? kBM : 64, is_a ? max_a : max_b,
-                         gen, rowbuf);
+                         gen);
 }
 
 // ---- pass 2: the tcgen05 GEMM ------------------------------------------------
@@ -625,21 +625,14 @@ cudaError_t split_b(const SplitLayout &L, const SplitBufs &b, const Gemm &g,
 
 // Launch the split pass of both operands: for float16 planes with K up to
 // kFusedMaxKp one fused scale + split launch over both, else a scale pass
-// and a split pass per operand.
+// and a split pass per operand (large operands: the fused pass's second read
+// would miss L2 like the split pass's does, and the two-pass kernels move
+// 16-byte vectors).
 cudaError_t launch_split_pass(const SplitLayout &L, const SplitBufs &b, const Gemm &g,
                               unsigned long long gen, cudaStream_t s) {
   if (L.f16 && L.Kp <= kFusedMaxKp && g.M < (1ll << 30) && g.N < (1ll << 30)) {
     const int64_t blocks = (g.M + kFusedRows - 1) / kFusedRows + (g.N + kFusedRows - 1) / kFusedRows;
-    const size_t smem = (size_t)kFusedRows * L.Kp * sizeof(float);
-    static bool attr_set = false;   // per process; the attribute is per function
-    cudaError_t e = cudaSuccess;
-    if (!attr_set) {
-      e = cudaFuncSetAttribute(scale_split_pair, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(kFusedRows * kFusedMaxKp * sizeof(float)));
-      if (e != cudaSuccess) return e;
-      attr_set = true;
-    }
-    scale_split_pair<<<(unsigned)blocks, 256, smem, s>>>(
+    scale_split_pair<<<(unsigned)blocks, 256, 0, s>>>(
         (const float *)g.a, g.rsa, g.csa, (int)g.M, (const float *)g.b, g.rsb, g.csb, (int)g.N,
         (int)g.K, (int)L.Kp, b.pa, b.pb, b.flags_a, b.flags_b, b.max_a, b.max_b, gen);
     count_launch();

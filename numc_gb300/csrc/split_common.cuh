@@ -334,84 +334,76 @@ __device__ __forceinline__ void split_tile(const float *__restrict__ src, int64_
 // Read mode of the scale pass for a source of split mode `mode`: k-contiguous
 // rows that are not 16-byte aligned are read one warp per row (3), not one
 // thread per row.
-// ---- fused scale and split (float16 planes, K up to kFusedMaxKp) --------------
+// ---- fused scale and split (float16 planes) ----------------------------------
 //
 // One 256-thread block: kFusedRows rows of one operand (A's rows, or B's
-// columns as B^T's rows), staged whole in shared memory `rowbuf` (at least
-// kFusedRows x Kp floats): the row maxima, then the two float16 planes, from
-// one read of the operand instead of the two of the absmax and split passes.
-// Writes maxbits[row] directly (no zeroing first) and, for a non-finite
-// value, flags[r0 / flag_rows] = gen.  Same arithmetic as split_tile<2, true>.
-constexpr int kFusedRows = 16, kFusedMaxKp = 1024;
+// columns as B^T's rows).  Pass 1 reads the rows for their maxima; pass 2
+// reads them again (from L2: a block's rows are at most kFusedRows x K
+// elements) and writes the two float16 planes — one launch and one DRAM read
+// of the operand instead of the absmax and split passes.  No shared-memory
+// staging, so many blocks fit on an SM and K is unbounded.  Writes
+// maxbits[row] directly (no zeroing first) and, for a non-finite value,
+// flags[r0 / flag_rows] = gen.  Same arithmetic as split_tile<2, true>.
+// Pass 1 layout: k contiguous (rs_k == 1): 16 threads per row along k;
+// otherwise 16 consecutive rows per k step, 16 k steps a pass (coalesced
+// reads of B's rows; the 16 threads per row reduce through shared memory).
+// Pass 2: 16 threads per row along k for both, so each row's planes are
+// written in 128-byte runs (B's second read comes from L2 in 4-byte pieces).
+constexpr int kFusedRows = 16;
 
 __device__ __forceinline__ void fused_scale_split_rows(
     const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int R, int K, int Kp, int r0,
     uint16_t *__restrict__ planes, unsigned long long *flags, int flag_rows,
-    unsigned *__restrict__ maxbits, unsigned long long gen, float *rowbuf) {
+    unsigned *__restrict__ maxbits, unsigned long long gen) {
   constexpr int kPlanes = 2;
+  __shared__ unsigned red[16][16];
+  __shared__ unsigned rowmax[kFusedRows];
   const int tid = threadIdx.x;
+  const bool along_k = rs_k == 1;
+  const int r = along_k ? tid / 16 : tid % 16, sub = along_k ? tid % 16 : tid / 16;
+  const bool live = r0 + r < R;
+  const float *p = src + (int64_t)(r0 + (live ? r : 0)) * rs_row;
 
-  // Load the rows (zero past K and past R), 16 threads a row.
+  // Pass 1: the row's largest magnitude (float32 bits) and non-finite values.
+  unsigned m = 0;
   bool bad = false;
-  if (rs_k == 1) {           // along k: 16 consecutive k a row per step
-    const int r = tid / 16, sub = tid % 16;
-    const float *p = src + (int64_t)(r0 + r) * rs_row;
-    const bool live = r0 + r < R;
-    for (int k = sub; k < Kp; k += 16 * 8) {
-      float x[8];
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int kk = k + 16 * u;
-        x[u] = (live && kk < K) ? p[kk] : 0.0f;
-      }
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int kk = k + 16 * u;
-        if (kk < Kp) {
-          bad |= !isfinite(x[u]);
-          rowbuf[r * Kp + kk] = x[u];
-        }
-      }
+  if (live) {
+#pragma unroll 8
+    for (int k = sub; k < K; k += 16) {
+      const float x = p[(int64_t)k * rs_k];
+      bad |= !isfinite(x);
+      m = max(m, absbits(x));
     }
-  } else {                   // across rows: 16 consecutive rows per k
-    const int r = tid % 16, sub = tid / 16;
-    const float *p = src + (int64_t)(r0 + r) * rs_row;
-    const bool live = r0 + r < R;
-    for (int k = sub; k < Kp; k += 16 * 8) {
-      float x[8];
+  }
+  if (along_k) {
 #pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int kk = k + 16 * u;
-        x[u] = (live && kk < K) ? p[(int64_t)kk * rs_k] : 0.0f;
-      }
+    for (int o = 8; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  } else {
+    m = max(m, __shfl_xor_sync(0xffffffffu, m, 16));   // lanes r and r + 16
+    if ((tid & 31) < 16) red[tid >> 5][r] = m;
+    __syncthreads();
+    m = 0;
 #pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int kk = k + 16 * u;
-        if (kk < Kp) {
-          bad |= !isfinite(x[u]);
-          rowbuf[r * Kp + kk] = x[u];
-        }
-      }
-    }
+    for (int w = 0; w < 8; w++) m = max(m, red[w][r]);
+  }
+  if (sub == 0) {
+    rowmax[r] = m;
+    if (live) maxbits[r0 + r] = m;
   }
   if (__syncthreads_or(bad) && tid == 0) flags[r0 / flag_rows] = gen;
 
-  // Row maxima: the 16 threads of a row (one half-warp) reduce its k range.
-  const int r = tid / 16, sub = tid % 16;
-  unsigned m = 0;
-  for (int k = sub; k < Kp; k += 16) m = max(m, absbits(rowbuf[r * Kp + k]));
-#pragma unroll
-  for (int o = 8; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-  const bool live = r0 + r < R;
-  if (live && sub == 0) maxbits[r0 + r] = m;
-
-  // Split: thread (r, sub) converts k = 4 sub + 64 i .. +3 of row r.
-  if (live) {
-    const int sexp = f16_scale_exp(m);
+  // Pass 2: thread (r2, q) converts k = 4 q + 64 i .. +3 of row r2.
+  const int r2 = tid / 16, q = tid % 16;
+  if (r0 + r2 < R) {
+    const int sexp = f16_scale_exp(rowmax[r2]);
     const int64_t plane_elems = (int64_t)R * Kp;
-    for (int k = 4 * sub; k < Kp; k += 64) {
-      const float4 v = *reinterpret_cast<const float4 *>(&rowbuf[r * Kp + k]);
-      const float rem[4] = {v.x, v.y, v.z, v.w};
+    const float *p2 = src + (int64_t)(r0 + r2) * rs_row;
+    uint16_t *dst = planes + (int64_t)(r0 + r2) * Kp;
+#pragma unroll 2
+    for (int k = 4 * q; k < Kp; k += 64) {
+      float rem[4];
+#pragma unroll
+      for (int t = 0; t < 4; t++) rem[t] = k + t < K ? p2[(int64_t)(k + t) * rs_k] : 0.0f;
       uint16_t out[kPlanes][4];
 #pragma unroll
       for (int t = 0; t < 4; t++) {
@@ -423,13 +415,12 @@ __device__ __forceinline__ void fused_scale_split_rows(
           x -= __half2float(h);
         }
       }
-      const int64_t off = (int64_t)(r0 + r) * Kp + k;
 #pragma unroll
       for (int pl = 0; pl < kPlanes; pl++) {
         uint2 w;
         w.x = (uint32_t)out[pl][0] | ((uint32_t)out[pl][1] << 16);
         w.y = (uint32_t)out[pl][2] | ((uint32_t)out[pl][3] << 16);
-        *reinterpret_cast<uint2 *>(planes + pl * plane_elems + off) = w;
+        *reinterpret_cast<uint2 *>(dst + pl * plane_elems + k) = w;
       }
     }
   }
