@@ -218,11 +218,13 @@ typedef struct {
 typedef struct NumcCudaGemmPlan NumcCudaGemmPlan;
 
 /* Plan `count` float32 problems once: each problem gets a kernel from the
- * committed autotune table (split-BF16 with 128- or 64-column tiles, or the
- * CUDA-core kernel for small problems; `algo` SIMT sends all to the CUDA
- * cores), the plan allocates its workspace and uploads TMA descriptors and
- * tile lists.  With SPLIT_BF16, `param` 128 or 64 forces that tile width on
- * every problem (0 = table).  Pointers in `descs` are fixed from here on.  numc has no
+ * committed autotune table (the split GEMM with 128- or 64-column tiles and
+ * 1, 2 or 4 K slices, or the CUDA-core kernel for small problems; `algo`
+ * SIMT sends all to the CUDA cores), the plan allocates its workspace and
+ * uploads TMA descriptors and tile lists.  With the split algorithms,
+ * `param` 128 or 64 forces that tile width on every problem, plus 1000 x s
+ * for s K slices (2 or 4; 0 = table).  K slices add their partial sums in K
+ * order in a reduction pass: results are deterministic.  Pointers in `descs` are fixed from here on.  numc has no
  * counterpart: its callers loop numc_matmul (src/matmul/matmul.c:347). */
 NUMC_API NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int algo,
                                                       int param,

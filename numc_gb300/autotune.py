@@ -2,9 +2,11 @@
 
 For every size class of (M, N, K) — classes <=32, <=64, ..., <=1024 — time
 one plan of identical problems on each kernel variant (the split GEMM from
-scaled float16 planes with 128-column tiles, the same with 64-column tiles,
-CUDA-core FMA) and record the fastest in numc_gb300/autotune_table.txt,
-which plans read at creation (for both split plane formats).
+scaled float16 planes with 128-column tiles or with 64-column tiles, each
+with K cut into 1, 2 or 4 slices whose partial sums a reduction pass adds
+in K order; CUDA-core FMA) and record the fastest variant and its slice
+count in numc_gb300/autotune_table.txt, which plans read at creation (for
+both split plane formats).
 
     python -m numc_gb300.autotune [--out PATH]
 """
@@ -16,7 +18,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPRESENTATIVE = [24, 48, 96, 192, 384, 768]        # one size per class 0..5
-VARIANTS = [(0, "split128", 7, 128), (1, "split64", 7, 64), (2, "simt", 1, 0)]   # 7 = SPLIT_FP16
+# (table variant, K slices, name, algo, plan param); 7 = SPLIT_FP16, 1 = SIMT
+VARIANTS = [(0, 1, "split128", 7, 128), (0, 2, "split128k2", 7, 2128),
+            (0, 4, "split128k4", 7, 4128), (1, 1, "split64", 7, 64),
+            (1, 2, "split64k2", 7, 2064), (1, 4, "split64k4", 7, 4064), (2, 1, "simt", 1, 0)]
 
 
 def time_plan(nc, torch, problems, algo, param, reps=5):
@@ -39,10 +44,12 @@ def main():
     args = ap.parse_args()
     import torch
     import numc_gb300 as nc
-    lines = ["# grouped float32 GEMM autotune table: mclass nclass kclass variant",
+    lines = ["# grouped float32 GEMM autotune table: mclass nclass kclass variant splits",
              "# classes: 0 <=32, 1 <=64, 2 <=128, 3 <=256, 4 <=512, 5 <=1024",
-             "# variants: 0 split-BF16 128-column tiles, 1 split-BF16 64-column tiles,",
-             "#           2 CUDA-core FMA; times are ms per plan run (graph replay)",
+             "# variants: 0 split GEMM (scaled float16 planes) 128-column tiles,",
+             "#           1 the same with 64-column tiles, 2 CUDA-core FMA;",
+             "# splits: K slices of the tensor-core variants (k2, k4 below: 2, 4 slices);",
+             "# times are ms per plan run (graph replay)",
              f"# device: {torch.cuda.get_device_name()}, {time.strftime('%Y-%m-%d')}"]
     t0 = time.time()
     for cm, M in enumerate(REPRESENTATIVE):
@@ -54,9 +61,9 @@ def main():
                 c = torch.empty(count, M, N, device="cuda")
                 problems = [(a[i], b[i], c[i]) for i in range(count)]
                 times = {name: time_plan(nc, torch, problems, algo, param)
-                         for _, name, algo, param in VARIANTS}
-                best = min(VARIANTS, key=lambda v: times[v[1]])
-                lines.append(f"{cm} {cn} {ck} {best[0]}   # {M}x{N}x{K} x{count}: " +
+                         for _, _, name, algo, param in VARIANTS}
+                best = min(VARIANTS, key=lambda v: times[v[2]])
+                lines.append(f"{cm} {cn} {ck} {best[0]} {best[1]}   # {M}x{N}x{K} x{count}: " +
                              " ".join(f"{k}={v:.3f}" for k, v in times.items()))
                 del a, b, c
     with open(args.out, "w") as f:

@@ -62,11 +62,20 @@ struct Prob {
   uint16_t *pa, *pb;                      // planes (2 x M x Kp, 2 x N x Kp)
   unsigned long long *flags_a, *flags_b;  // per 128 rows of A, per 64 columns of B
   unsigned *max_a, *max_b;                // float16 planes: row / column maxima
+  int splits;                             // K slices (split-K; 1 = none)
+  float *part;                            // split-K: splits x M x N partial sums
 };
 
+// One output tile; with split-K, slice `ks` of the problem's K slabs.
 struct Tile {
-  int prob, m0, n0, pad;
+  int prob, m0, n0, ks;
 };
+
+// K slabs [kb0, kb1) of slice ks of P (slices differ by at most one slab).
+__host__ __device__ inline void slice_range(const Prob &P, int ks, int &kb0, int &kb1) {
+  kb0 = (int)((int64_t)ks * P.num_kb / P.splits);
+  kb1 = (int)((int64_t)(ks + 1) * P.num_kb / P.splits);
+}
 
 // ---- grouped scale pass (float16 planes) -----------------------------------------
 
@@ -198,11 +207,12 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
       bool live = true;
       for (int t = blockIdx.x; t < ntiles && live; t += gridDim.x) {
         const Tile tl = tiles[t];
-        const int nkb = probs[tl.prob].num_kb;
+        int kb0, kb1;
+        slice_range(probs[tl.prob], tl.ks, kb0, kb1);
         const CUtensorMap *ta = tmaps + 2 * tl.prob, *tb = ta + 1;
         tc::tensormap_acquire(ta);
         tc::tensormap_acquire(tb);
-        for (int kb = 0; kb < nkb; kb++, g++) {
+        for (int kb = kb0; kb < kb1; kb++, g++) {
           const int s = g % STAGES;
           if (g >= STAGES &&
               !tc::mbar_wait_bounded(tc::smem_u32(&empty[s]), ((g / STAGES) & 1) ^ 1, status,
@@ -230,11 +240,12 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
       int g = 0, chunk = 0;
       bool live = true;
       for (int t = blockIdx.x; t < ntiles && live; t += gridDim.x) {
-        const int nkb = probs[tiles[t].prob].num_kb;
-        for (int kb = 0; kb < nkb; kb++, g++) {
+        int kb0, kb1;
+        slice_range(probs[tiles[t].prob], tiles[t].ks, kb0, kb1);
+        for (int kb = kb0; kb < kb1; kb++, g++) {
           const int s = g % STAGES, buf = chunk % NBUF;
-          const bool cstart = kb % FLUSH == 0;
-          const bool cend = kb % FLUSH == FLUSH - 1 || kb == nkb - 1;
+          const bool cstart = (kb - kb0) % FLUSH == 0;
+          const bool cend = (kb - kb0) % FLUSH == FLUSH - 1 || kb == kb1 - 1;
           if (cstart && chunk >= NBUF &&
               !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / NBUF) & 1) ^ 1,
                                      status, kStatusTimeoutMma, wc.limit_ns)) {
@@ -290,7 +301,9 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
       float acc[CW];
 #pragma unroll
       for (int j = 0; j < CW; j++) acc[j] = 0.0f;
-      const int nchunks = (P.num_kb + FLUSH - 1) / FLUSH;
+      int kb0, kb1;
+      slice_range(P, tl.ks, kb0, kb1);
+      const int nchunks = (kb1 - kb0 + FLUSH - 1) / FLUSH;
       for (int c = 0; c < nchunks; c++, chunk++) {
         const int buf = chunk % NBUF;
         ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / NBUF) & 1, status,
@@ -311,6 +324,16 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
         for (int j = 0; j < CW; j++) acc[j] = __fadd_rn(acc[j], __uint_as_float(r[j]));
       }
       if (!ok) break;
+      if (P.splits > 1) {
+        // split-K: this slice's unscaled partial sums; the ordered
+        // reduction adds the slices, rescales and checks the flags
+        float *stage =
+            (float *)(smem + STAGES * C_::STAGE_BYTES + 256) + (warp - 2) * kEpiStageFloats;
+        store_rows_coalesced<CW>(acc, stage, P.part + (int64_t)tl.ks * P.M * P.N, P.N,
+                                 tl.m0 + quad * 32, tl.n0 + cbase, P.M, P.N, lane);
+        __syncwarp();
+        continue;
+      }
       bool nonfinite = P.flags_a[tl.m0 / kBM] == gen;
       for (int c = tl.n0 / 64; c < (tl.n0 + BN) / 64 && c * 64 < P.N; c++)
         nonfinite |= P.flags_b[c] == gen;
@@ -366,6 +389,41 @@ grouped_split_gemm(const CUtensorMap *__restrict__ tmaps, const Prob *__restrict
     tc::tc_fence_after();
     tc::tmem_dealloc(tmem, 512);
   }
+}
+
+// ---- split-K: ordered reduction of the slices ---------------------------------
+//
+// Block b: 256 consecutive outputs (row-major) of split problem
+// probs_idx[jobs[b].x], block jobs[b].y.  Each output is the FP32 sum of its
+// slices' partial sums in slice (K) order — deterministic — then, as in the
+// GEMM's own epilogue, rescaled (float16 planes) or, in a tile with a
+// non-finite input, recomputed as numc's FMA chain.
+template <bool F16>
+__global__ void __launch_bounds__(256)
+grouped_splitk_reduce(const Prob *__restrict__ probs, const int *__restrict__ probs_idx,
+                      const int2 *__restrict__ jobs, unsigned long long gen) {
+  const int2 job = jobs[blockIdx.x];
+  const Prob &P = probs[probs_idx[job.x]];
+  const int64_t e = (int64_t)job.y * 256 + threadIdx.x;
+  const int64_t MN = (int64_t)P.M * P.N;
+  if (e >= MN) return;
+  const int i = (int)(e / P.N), j = (int)(e % P.N);
+  float *dst = P.C + (int64_t)i * P.rso + (int64_t)j * P.cso;
+  if (P.flags_a[i / kBM] == gen || P.flags_b[j / 64] == gen) {
+    float f = 0.0f;
+    for (int k = 0; k < P.K; k++)
+      f = __fmaf_rn(P.A[(int64_t)i * P.rsa + (int64_t)k * P.csa],
+                    P.B[(int64_t)k * P.rsb + (int64_t)j * P.csb], f);
+    *dst = f;
+    return;
+  }
+  float acc = P.part[e];
+  for (int ks = 1; ks < P.splits; ks++) acc = __fadd_rn(acc, P.part[ks * MN + e]);
+  if (F16) {
+    const int ex = -(f16_scale_exp(P.max_a[i]) + f16_scale_exp(P.max_b[j]));
+    acc = (ex >= -126 && ex <= 127) ? acc * exp2_int(ex) : (float)((double)acc * exp2_dbl(ex));
+  }
+  *dst = acc;
 }
 
 // ---- grouped CUDA-core kernel ---------------------------------------------------
@@ -443,6 +501,10 @@ struct NumcCudaGemmPlan {
   Tile *d_tiles[kNumVar];
   int ntiles[kNumVar];
   int nsimt_packed;               // CUDA-core tiles of numc's packed path (listed first)
+  int *d_sk_probs;                // split-K problems (indices into probs)
+  int2 *d_sk_jobs;                // (split-K problem, block) of each reduction block
+  int n_sk_probs;
+  long long sk_jobs;
   int *d_edge_probs;              // CUDA-core problems with packed-path remainders
   int2 *d_edge_jobs;              // (edge problem, block) of each remainder block
   int n_edge_probs;
@@ -468,11 +530,13 @@ int size_class(size_t x) {
   return c;
 }
 
-// The autotune table: "mclass nclass kclass variant" per line (# comments),
-// classes as size_class(); written by numc_gb300/autotune.py on a GB300.
+// The autotune table: "mclass nclass kclass variant [splits]" per line (#
+// comments), classes as size_class(); written by numc_gb300/autotune.py on a
+// GB300.  splits: K slices of the tensor-core variants (1 when absent).
 struct TuneTable {
   bool loaded = false;
   int v[7][7][7];
+  int splits[7][7][7];
 };
 TuneTable g_tune;
 std::once_flag g_tune_once;
@@ -491,6 +555,9 @@ void load_tune_table() {
   for (auto &a : g_tune.v)
     for (auto &b : a)
       for (int &c : b) c = -1;
+  for (auto &a : g_tune.splits)
+    for (auto &b : a)
+      for (int &c : b) c = 1;
   const char *env = getenv("NUMC_CUDA_AUTOTUNE_TABLE");
   std::string path = env ? env : library_dir() + "/autotune_table.txt";
   FILE *f = fopen(path.c_str(), "r");
@@ -498,10 +565,12 @@ void load_tune_table() {
   char line[256];
   while (fgets(line, sizeof line, f)) {
     if (line[0] == '#') continue;
-    int a, b, c, v;
-    if (sscanf(line, "%d %d %d %d", &a, &b, &c, &v) == 4 && a >= 0 && a < 7 && b >= 0 &&
-        b < 7 && c >= 0 && c < 7 && v >= 0 && v < kNumVar) {
+    int a, b, c, v, sp = 1;
+    const int n = sscanf(line, "%d %d %d %d %d", &a, &b, &c, &v, &sp);
+    if (n >= 4 && a >= 0 && a < 7 && b >= 0 && b < 7 && c >= 0 && c < 7 && v >= 0 &&
+        v < kNumVar) {
       g_tune.v[a][b][c] = v;
+      g_tune.splits[a][b][c] = (n == 5 && (sp == 1 || sp == 2 || sp == 4)) ? sp : 1;
       g_tune.loaded = true;
     }
   }
@@ -516,6 +585,14 @@ int pick_variant(size_t M, size_t N, size_t K) {
   if (v >= 0) return v;
   if ((double)M * N * K < (double)(1 << 18)) return kVarSimt;
   return N <= 64 ? kVarTc64 : kVarTc128;
+}
+
+// K slices for a tensor-core problem: the tuned choice (at most one slice
+// per 64-deep slab).
+int pick_splits(size_t M, size_t N, size_t K, int num_kb) {
+  std::call_once(g_tune_once, load_tune_table);
+  const int sp = g_tune.splits[size_class(M)][size_class(N)][size_class(K)];
+  return std::max(1, std::min(sp, num_kb));
 }
 
 int fail(cudaError_t e, const char *what) {
@@ -593,6 +670,16 @@ int plan_enqueue(NumcCudaGemmPlan *p, cudaStream_t s, unsigned *kernels) {
     if (e) return fail(e, "grouped split GEMM (64)");
     ++*kernels;
   }
+  if (p->sk_jobs > 0) {
+    if (p->f16)
+      grouped_splitk_reduce<true><<<(unsigned)p->sk_jobs, 256, 0, s>>>(p->d_probs, p->d_sk_probs,
+                                                                      p->d_sk_jobs, p->gen);
+    else
+      grouped_splitk_reduce<false><<<(unsigned)p->sk_jobs, 256, 0, s>>>(
+          p->d_probs, p->d_sk_probs, p->d_sk_jobs, p->gen);
+    if ((e = cudaGetLastError())) return fail(e, "grouped split-K reduction");
+    ++*kernels;
+  }
   if (p->nsimt_packed) {
     grouped_simt<simt::kFloat><<<p->nsimt_packed, simt::kThreads, 0, s>>>(
         p->d_probs, p->d_tiles[kVarSimt]);
@@ -631,10 +718,14 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
     return nullptr;
   }
   // Split param: 0 (or 3 for SPLIT_BF16) = per-problem choice from the
-  // autotune table, 128 / 64 = every problem on that tile width.
-  if (algo != NUMC_CUDA_ALGO_SIMT && param != 0 && param != 3 && param != -1 && param != 128 &&
-      param != 64) {
-    NUMC_SET_ERROR(NUMC_ERR_VALUE, "grouped split param %d (0, 3, 64 or 128)", param);
+  // autotune table; 128 / 64 = every problem on that tile width, plus
+  // 1000 x s for s K slices (2 or 4; e.g. 2128 = 128 columns, 2 slices).
+  const int force_width = param > 0 ? param % 1000 : 0, force_splits = param > 0 ? param / 1000 : 0;
+  if (algo != NUMC_CUDA_ALGO_SIMT && param != 0 && param != 3 && param != -1 &&
+      !((force_width == 128 || force_width == 64) &&
+        (force_splits == 0 || force_splits == 1 || force_splits == 2 || force_splits == 4))) {
+    NUMC_SET_ERROR(NUMC_ERR_VALUE,
+                   "grouped split param %d (0, 3, or 64 / 128 plus 1000 x 1, 2 or 4)", param);
     return nullptr;
   }
   if (count > 0 && !descs) {
@@ -685,11 +776,15 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
     P.Kp = (int)align_up(d.K ? d.K : 1, kBK);
     P.num_kb = P.Kp / kBK;
     int v = algo == NUMC_CUDA_ALGO_SIMT ? kVarSimt
-            : param == 128             ? (d.K ? kVarTc128 : kVarSimt)
-            : param == 64              ? (d.K ? kVarTc64 : kVarSimt)
-                                       : pick_variant(d.M, d.N, d.K);
+            : force_width == 128        ? (d.K ? kVarTc128 : kVarSimt)
+            : force_width == 64         ? (d.K ? kVarTc64 : kVarSimt)
+                                        : pick_variant(d.M, d.N, d.K);
     if (d.M == 0 || d.N == 0) v = -1;
     p->variant[i] = v;
+    P.splits = 1;
+    if (v == kVarTc128 || v == kVarTc64)
+      P.splits = force_width ? std::max(1, std::min(force_splits ? force_splits : 1, P.num_kb))
+                             : pick_splits(d.M, d.N, d.K, P.num_kb);
     if (v == kVarTc128 || v == kVarTc64) {
       plane_off[i] = planes_bytes;
       planes_bytes += align_up((size_t)kPlanes * P.Kp * (d.M + d.N) * 2, 256);
@@ -703,8 +798,10 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   // Tile lists, problems sorted by K (largest first) within each variant.
   std::vector<size_t> order(count);
   for (size_t i = 0; i < count; i++) order[i] = i;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](size_t x, size_t y) { return p->probs[x].K > p->probs[y].K; });
+  // (split problems by their slices' depth)
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+    return p->probs[x].num_kb / p->probs[x].splits > p->probs[y].num_kb / p->probs[y].splits;
+  });
   std::vector<Tile> tiles[kNumVar], simt_small;
   std::vector<size_t> split_idx;
   std::vector<int> edge_idx;
@@ -719,7 +816,8 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
     // CUDA-core problems on numc's unpacked path go to a list of their own
     std::vector<Tile> &tl = (v == kVarSimt && !numc_packed(p->probs[i])) ? simt_small : tiles[v];
     for (int m0 = 0; m0 < p->probs[i].M; m0 += bm)
-      for (int n0 = 0; n0 < p->probs[i].N; n0 += bn) tl.push_back(Tile{(int)i, m0, n0, 0});
+      for (int n0 = 0; n0 < p->probs[i].N; n0 += bn)
+        for (int ks = 0; ks < p->probs[i].splits; ks++) tl.push_back(Tile{(int)i, m0, n0, ks});
     if (v != kVarSimt) split_idx.push_back(i);
   }
   // the CUDA-core list: numc's packed-path problems, then the unpacked ones
@@ -746,6 +844,21 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
       for (long long j = 0; j < nm; j++) max_jobs.push_back(make_int2((int)q, (int)j));
     }
   }
+  // split-K problems: partial sums (splits x M x N floats each) and the
+  // reduction's blocks
+  std::vector<int> sk_idx;
+  std::vector<int2> sk_jobs;
+  std::vector<size_t> part_off(count, 0);
+  size_t part_bytes = 0;
+  for (size_t i = 0; i < count; i++) {
+    const Prob &P = p->probs[i];
+    if (p->variant[i] < 0 || P.splits <= 1) continue;
+    part_off[i] = part_bytes;
+    part_bytes += align_up((size_t)P.splits * P.M * P.N * 4, 256);
+    const long long n = ((long long)P.M * P.N + 255) / 256;
+    for (long long j = 0; j < n; j++) sk_jobs.push_back(make_int2((int)sk_idx.size(), (int)j));
+    sk_idx.push_back((int)i);
+  }
   for (size_t q = 0; q < edge_idx.size(); q++) {
     const Prob &P = p->probs[edge_idx[q]];
     const long long n = (simt::float_edge_groups<float>(P.M, P.N, P.isa) + 15) / 16;
@@ -756,8 +869,10 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   p->max_jobs = (long long)max_jobs.size();
   p->edge_jobs = (long long)edge_jobs.size();
   p->fused_jobs = (long long)fused_jobs.size();
+  p->sk_jobs = (long long)sk_jobs.size();
+  p->n_sk_probs = (int)sk_idx.size();
   if (p->split_jobs > 0x7FFFFFFFll || p->max_jobs > 0x7FFFFFFFll || p->edge_jobs > 0x7FFFFFFFll ||
-      p->fused_jobs > 0x7FFFFFFFll) {
+      p->fused_jobs > 0x7FFFFFFFll || p->sk_jobs > 0x7FFFFFFFll) {
     delete p;
     NUMC_SET_ERROR(NUMC_ERR_VALUE, "plan_create: too many split blocks");
     return nullptr;
@@ -771,6 +886,8 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   const size_t o_split_jobs = off; off = align_up(off + split_jobs.size() * sizeof(int2), 256);
   const size_t o_max_jobs = off; off = align_up(off + max_jobs.size() * sizeof(int2), 256);
   const size_t o_fused_jobs = off; off = align_up(off + fused_jobs.size() * sizeof(int2), 256);
+  const size_t o_sk = off; off = align_up(off + sk_idx.size() * sizeof(int), 256);
+  const size_t o_sk_jobs = off; off = align_up(off + sk_jobs.size() * sizeof(int2), 256);
   const size_t o_edges = off; off = align_up(off + edge_idx.size() * sizeof(int), 256);
   const size_t o_edge_jobs = off; off = align_up(off + edge_jobs.size() * sizeof(int2), 256);
   size_t o_tiles[kNumVar];
@@ -779,7 +896,8 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
     off = align_up(off + tiles[v].size() * sizeof(Tile), 256);
   }
   const size_t o_flags = off; off = align_up(off + flags_bytes, 256);
-  const size_t o_planes = off; off += planes_bytes;
+  const size_t o_planes = off; off = align_up(off + planes_bytes, 256);
+  const size_t o_part = off; off += part_bytes;
   p->dev_bytes = off;
   cudaError_t e = dev_malloc((void **)&p->dev, off ? off : 256);
   if (e) {
@@ -793,6 +911,8 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
   p->d_split_jobs = (int2 *)(p->dev + o_split_jobs);
   p->d_max_jobs = (int2 *)(p->dev + o_max_jobs);
   p->d_fused_jobs = (int2 *)(p->dev + o_fused_jobs);
+  p->d_sk_probs = (int *)(p->dev + o_sk);
+  p->d_sk_jobs = (int2 *)(p->dev + o_sk_jobs);
   p->d_edge_probs = (int *)(p->dev + o_edges);
   p->d_edge_jobs = (int2 *)(p->dev + o_edge_jobs);
   p->n_edge_probs = (int)edge_idx.size();
@@ -818,6 +938,7 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
                              align_up(((P.M + kBM - 1) / kBM + (P.N + 63) / 64) * 8, 256));
       P.max_b = P.max_a + P.M;
     }
+    if (P.splits > 1) P.part = (float *)(p->dev + o_part + part_off[i]);
     const uint32_t bn = v == kVarTc128 ? 128 : 64;
     const auto dt = p->f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
     if ((e = make_tmap_3d(&tm[2 * i], P.pa, dt, 2, kPlanes, P.M, P.Kp, P.Kp, kBM, kBK)) ||
@@ -849,6 +970,11 @@ extern "C" NumcCudaGemmPlan *numc_cuda_gemm_plan_create(NumcDType dtype, int alg
       (!fused_jobs.empty() &&
        (e = cudaMemcpy(p->d_fused_jobs, fused_jobs.data(), fused_jobs.size() * sizeof(int2),
                        cudaMemcpyHostToDevice))) ||
+      (!sk_idx.empty() &&
+       ((e = cudaMemcpy(p->d_sk_probs, sk_idx.data(), sk_idx.size() * sizeof(int),
+                        cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(p->d_sk_jobs, sk_jobs.data(), sk_jobs.size() * sizeof(int2),
+                        cudaMemcpyHostToDevice)))) ||
       (!edge_idx.empty() &&
        ((e = cudaMemcpy(p->d_edge_probs, edge_idx.data(), edge_idx.size() * sizeof(int),
                         cudaMemcpyHostToDevice)) ||

@@ -231,3 +231,48 @@ def test_f16_plan_across_the_fused_pass_limit():
         assert rel_err_vs_scale(got[rows], ref[rows], a[rows], b) <= \
             max(f16_bound(K), simt_bound(K))
     plan.free()
+
+
+@pytest.mark.parametrize("param", [2128, 4128, 2064, 4064])
+@pytest.mark.parametrize("algo", [nc.ALGO_SPLIT_FP16, nc.ALGO_SPLIT_BF16])
+def test_split_k_plans_match_oracle(param, algo):
+    """K cut into 2 or 4 slices per tile: the slices' partial sums added in
+    K order by the reduction pass, then rescaled — the same bound."""
+    probs = random_problems(24, lo=16, hi=1500, seed=5)
+    plan = nc.GemmPlan([(p[0], p[1], p[2]) for p in probs], algo, param)
+    plan.run()
+    nc.check_status()
+    check_all(probs, BOUND[algo])
+    first = [p[2].clone() for p in probs]
+    plan.run()          # deterministic: the same bits on a second run
+    torch.cuda.synchronize()
+    for (_, _, out, _, _), f in zip(probs, first):
+        assert torch.equal(out, f)
+    plan.free()
+
+
+def test_split_k_strided_output_and_non_finite_inputs():
+    M, K, N = 150, 700, 90
+    a, b = synth.operands("normal", M, K, N, dtype="float32", seed=8)
+    a[3, 5] = np.inf
+    b[10, 70] = np.nan
+    ta, tb = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    out_t = torch.full((N, M), 7.0, device="cuda")
+    out = out_t.t()                                   # column stride != 1
+    plan = nc.GemmPlan([(ta, tb, out)], nc.ALGO_SPLIT_FP16, 4128)
+    plan.run()
+    nc.check_status()
+    got = out.cpu().numpy()
+    want = oracle.matmul(a, b)
+    fin = np.isfinite(want)
+    # rows / columns with a non-finite input: numc's FMA chains exactly
+    np.testing.assert_array_equal(np.isnan(got), np.isnan(want))
+    np.testing.assert_array_equal(got[3, :][~np.isnan(want[3, :])], want[3, :][~np.isnan(want[3, :])])
+    np.testing.assert_array_equal(got[:, 70], want[:, 70])
+    a0, b0 = np.nan_to_num(a, posinf=0.0), np.nan_to_num(b)
+    mask = fin.copy()
+    mask[3, :] = False
+    mask[:, 70] = False
+    err = np.abs(got[mask] - want[mask]) / np.maximum(np.abs(a0) @ np.abs(b0), 1e-30)[mask]
+    assert err.max() <= f16_bound(K)
+    plan.free()
