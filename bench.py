@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip the side workloads")
     ap.add_argument("--only", choices=["f64", "int", "grouped", "plain", "splitvar", "rand",
-                                       "misc"],
+                                       "misc", "small"],
                     help="run one side workload alone (for profiling) and print it")
     return ap.parse_args()
 
@@ -322,6 +322,14 @@ def main():
             part = rand_workload(nc, torch, oracle, dev)
         elif args.only == "misc":
             part = misc_workload(nc, synth, oracle)
+        elif args.only == "small":
+            # float32 512^3 (uniform [-1, 1)): split from float16 planes and
+            # the plain kernel, per call in CUDA graphs
+            a1, b1 = synth.operands("uniform", 512, 512, 512, dtype="float32")
+            ta1, tb1 = torch.from_numpy(a1).to(dev), torch.from_numpy(b1).to(dev)
+            tc1 = torch.empty((512, 512), device=dev)
+            part = {"f32_512_split_us": time_gemm_graph(nc, torch, ta1, tb1, tc1, HEAD_ALGO, 0) * 1e3,
+                    "f32_512_plain_us": time_gemm_graph(nc, torch, ta1, tb1, tc1, nc.ALGO_SIMT, 0) * 1e3}
         elif args.only == "splitvar":
             # the bfloat16-plane variants, two calls each (3 then 6 passes)
             a = torch.from_numpy(synth.normal(SEED, 3, (M, K), np.float32)).to(dev)

@@ -9,6 +9,12 @@ count in numc_gb300/autotune_table.txt, which plans read at creation (for
 both split plane formats).
 
     python -m numc_gb300.autotune [--out PATH]
+
+With --clusters it measures the other axis instead: the split GEMM kernel
+(scaled float16 planes) as clusters of two CTAs sharing 256 x 256 tiles
+(cta_group::2) against single CTAs on 256-column tiles, on square and
+long-K problems of the grouped plans' sizes, GEMM kernel time only (CUDA
+events around the kernel), and writes numc_gb300/cluster_table.txt.
 """
 import argparse
 import os
@@ -38,10 +44,69 @@ def time_plan(nc, torch, problems, algo, param, reps=5):
     return e0.elapsed_time(e1) / reps
 
 
+CLUSTER_SHAPES = [(256, 256, 256), (256, 256, 1024), (512, 512, 512), (512, 512, 1024),
+                  (768, 768, 768), (1024, 1024, 1024), (1024, 256, 1024), (256, 1024, 1024),
+                  (2048, 2048, 2048)]
+
+
+def _time_gemm_kernels():
+    """Child process: GEMM-kernel milliseconds per shape (phase timing)."""
+    import torch
+    import numc_gb300 as nc
+    out = {}
+    for M, N, K in CLUSTER_SHAPES:
+        a = torch.randn(M, K, device="cuda")
+        b = torch.randn(K, N, device="cuda")
+        c = torch.empty(M, N, device="cuda")
+        ws = torch.empty(nc.workspace_size("float32", 7, 0, M, K, N), dtype=torch.uint8,
+                         device="cuda")
+        for _ in range(3):
+            nc.gemm(a, b, c, algo=7, workspace=ws)
+        torch.cuda.synchronize()
+        nc.phase_timing(True)
+        for _ in range(20):
+            nc.gemm(a, b, c, algo=7, workspace=ws)
+        _, gemm_ms, calls = nc.phase_times()
+        nc.phase_timing(False)
+        out[f"{M}x{N}x{K}"] = gemm_ms / calls
+    nc.check_status()
+    print(repr(out))
+
+
+def clusters(path):
+    import ast
+    import subprocess
+    import sys
+    res = {}
+    for ctas in (2, 1):
+        env = dict(os.environ, NUMC_CUDA_SPLIT_CTAS=str(ctas))
+        r = subprocess.run([sys.executable, "-m", "numc_gb300.autotune", "--child"], env=env,
+                           capture_output=True, text=True, check=True)
+        res[ctas] = ast.literal_eval(r.stdout.strip().splitlines()[-1])
+    import torch
+    lines = ["# split GEMM kernel (scaled float16 planes), GEMM kernel time in ms:",
+             "# ctas=2: clusters of two CTAs on 256 x 256 tiles (cta_group::2);",
+             "# ctas=1: single CTAs on 128 x 256 tiles.  MxNxK  ctas=2  ctas=1  faster",
+             f"# device: {torch.cuda.get_device_name()}, {time.strftime('%Y-%m-%d')}"]
+    for key in res[2]:
+        t2, t1 = res[2][key], res[1][key]
+        lines.append(f"{key} {t2:.4f} {t1:.4f} {2 if t2 < t1 else 1}")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    print("\n".join(lines))
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--out", default=os.path.join(HERE, "autotune_table.txt"))
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--clusters", action="store_true")
+    ap.add_argument("--child", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.child:
+        return _time_gemm_kernels()
+    if args.clusters:
+        return clusters(args.out or os.path.join(HERE, "cluster_table.txt"))
+    args.out = args.out or os.path.join(HERE, "autotune_table.txt")
     import torch
     import numc_gb300 as nc
     lines = ["# grouped float32 GEMM autotune table: mclass nclass kclass variant splits",
