@@ -34,6 +34,7 @@ namespace {
 
 constexpr int kBM = 128, kBK = 64;
 constexpr int kBlockK = 512;                 // numc's int8 K block (KC)
+constexpr uint32_t kBarBytes = 512;          // 2*(kStages + kNumBuf) + 1 mbarriers + TMEM slot
 
 // Output tile 128 x BN: BN = 64 (8 accumulator warps, 8 TMEM buffers, 8
 // ring stages of 24 KiB) for problems with few tiles, BN = 128 (16 warps,
@@ -46,6 +47,49 @@ template <int BN> struct I8Cfg {
 
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
+// Coalesced stores of a warp's 32 rows x 32 output bytes (d[j] of row
+// row0 + lane, column col0 + j) to row-major uint8 C (unit column stride,
+// 4-byte aligned rows), through the warp's 1 KiB `stage`: each lane writes
+// its row's two 16-byte chunks (chunk c at position c ^ ((row >> 2) & 1),
+// so the 8 lanes of a store phase hit 32 distinct banks), then each store
+// instruction writes 4 rows x 32 bytes, 4 bytes a lane.  A direct store
+// instruction touched 32 rows.  Rows >= M and columns >= N are not written.
+// All 32 lanes must call it.
+__device__ __forceinline__ void store_bytes_coalesced(const int32_t (&d)[32], uint8_t *stage,
+                                                      uint8_t *C, int64_t rso, int row0,
+                                                      int col0, int M, int N, int lane) {
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      w[q] = (uint32_t)(uint8_t)d[16 * h + 4 * q] | ((uint32_t)(uint8_t)d[16 * h + 4 * q + 1] << 8) |
+             ((uint32_t)(uint8_t)d[16 * h + 4 * q + 2] << 16) |
+             ((uint32_t)(uint8_t)d[16 * h + 4 * q + 3] << 24);
+    const int pos = h ^ ((lane >> 2) & 1);
+    *reinterpret_cast<uint4 *>(stage + lane * 32 + pos * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+  __syncwarp();
+  const int sub = lane & 7, c = col0 + 4 * sub;
+#pragma unroll
+  for (int rr = 0; rr < 32; rr += 4) {
+    const int r = rr + (lane >> 3);
+    const int pos = (sub >> 2) ^ ((r >> 2) & 1);
+    const uint32_t w = *reinterpret_cast<const uint32_t *>(stage + r * 32 + pos * 16 + (sub & 3) * 4);
+    if (row0 + r < M) {
+      uint8_t *dst = C + (int64_t)(row0 + r) * rso + c;
+      if (c + 4 <= N) {
+        *reinterpret_cast<uint32_t *>(dst) = w;
+      } else {
+#pragma unroll
+        for (int b = 0; b < 4; b++)
+          if (c + b < N) dst[b] = (uint8_t)(w >> (8 * b));
+      }
+    }
+  }
+  __syncwarp();
+}
+
 // One operand of the conversion pass: dst(row, k) = bf16(src[row * rs_row +
 // k * rs_k]) for row < R, k < K, zero for K <= k < Kp.
 struct I8Operand {
@@ -56,15 +100,35 @@ struct I8Operand {
 
 constexpr int kCvtRows = 64, kCvtK = 128;
 
+// Four 8-bit integers (bytes of w, low first) as four bfloat16, packed two
+// a word.  Integers of 8 bits are exact in bfloat16: the value's float32
+// bits with the low 16 (zero) dropped.
+template <bool SIGNED>
+__device__ __forceinline__ uint2 bytes_to_bf16x4(uint32_t w) {
+  uint32_t h[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const uint32_t byte = (w >> (8 * i)) & 0xFFu;
+    const int v = SIGNED ? (int)(int8_t)byte : (int)byte;
+    h[i] = __float_as_uint((float)v) >> 16;
+  }
+  return make_uint2(h[0] | (h[1] << 16), h[2] | (h[3] << 16));
+}
+
 // Both operands in one launch (A's tiles first, then B^T's), 64 rows x 128 k
-// a block staged in shared memory: 16-byte loads along whichever source
-// axis is contiguous (k for row-major A, rows for row-major B), 16-byte
-// stores of 8 bfloat16 along k.  Integers of 8 bits are exact in bfloat16:
-// the value's float32 bits with the low 16 (zero) dropped.
+// a block.  Each source layout gets its own mapping, all of them writing
+// whole 32-byte sectors of the destination:
+//   * k contiguous (row-major A): 16 bytes a thread along k, converted in
+//     registers, two 16-byte stores;
+//   * rows contiguous (row-major B, read as B^T): a 4 x 4 byte block a
+//     thread (four 4-byte loads, one per k, each warp load covering four
+//     whole 32-byte sectors), transposed with byte permutes, four 8-byte
+//     stores of 4 bfloat16 along k (8 rows x 32 bytes a warp store);
+//   * any other strides: byte gathers staged in shared memory.
 template <bool SIGNED>
 __global__ void __launch_bounds__(256)
 int8_pair_to_bf16(I8Operand a, I8Operand b, int64_t K, int64_t Kp, int64_t blocks_a) {
-  __shared__ uint8_t tile[kCvtRows][kCvtK + 16];
+  __shared__ __align__(16) uint8_t tile[kCvtRows][kCvtK + 16];
   int64_t blk = blockIdx.x;
   const I8Operand &op = blk < blocks_a ? a : b;
   if (blk >= blocks_a) blk -= blocks_a;
@@ -74,51 +138,71 @@ int8_pair_to_bf16(I8Operand a, I8Operand b, int64_t K, int64_t Kp, int64_t block
   const uint8_t *src = op.src;
   if (op.rs_k == 1) {
 #pragma unroll
-    for (int it = 0; it < 2; it++) {   // 8 threads a row, 16 bytes each
+    for (int it = 0; it < 2; it++) {   // 8 threads a row, 16 k each
       const int r = (tid >> 3) + 32 * it, kk = (tid & 7) * 16;
       const int64_t gr = r0 + r, gk = k0 + kk;
+      if (gr >= op.R) continue;
       uint4 v = make_uint4(0, 0, 0, 0);
-      if (gr < op.R && gk < K) {
+      if (gk < K) {
         const uint8_t *p = src + gr * op.rs_row + gk;
         if (gk + 16 <= K && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
           v = *reinterpret_cast<const uint4 *>(p);
         } else {
-          alignas(16) uint8_t t[16];
+          uint32_t w[4] = {0, 0, 0, 0};
 #pragma unroll
-          for (int i = 0; i < 16; i++) t[i] = gk + i < K ? p[i] : 0;
-          v = *reinterpret_cast<uint4 *>(t);
+          for (int i = 0; i < 16; i++)
+            if (gk + i < K) w[i >> 2] |= (uint32_t)p[i] << (8 * (i & 3));
+          v = make_uint4(w[0], w[1], w[2], w[3]);
         }
       }
-      *reinterpret_cast<uint4 *>(&tile[r][kk]) = v;
+      const uint2 c0 = bytes_to_bf16x4<SIGNED>(v.x), c1 = bytes_to_bf16x4<SIGNED>(v.y);
+      const uint2 c2 = bytes_to_bf16x4<SIGNED>(v.z), c3 = bytes_to_bf16x4<SIGNED>(v.w);
+      uint4 *d = reinterpret_cast<uint4 *>(op.dst + gr * Kp + gk);
+      d[0] = make_uint4(c0.x, c0.y, c1.x, c1.y);
+      d[1] = make_uint4(c2.x, c2.y, c3.x, c3.y);
     }
-  } else if (op.rs_row == 1) {
+    return;
+  }
+  if (op.rs_row == 1) {
+    const int warp = tid >> 5, lane = tid & 31;
 #pragma unroll
-    for (int it = 0; it < 2; it++) {   // 4 threads a k, 16 rows each
-      const int kk = (tid >> 2) + 64 * it, r = (tid & 3) * 16;
-      const int64_t gr = r0 + r, gk = k0 + kk;
-      alignas(16) uint8_t t[16];
-      if (gk < K && gr < op.R) {
-        const uint8_t *p = src + gk * op.rs_k + gr;
-        if (gr + 16 <= op.R && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
-          *reinterpret_cast<uint4 *>(t) = *reinterpret_cast<const uint4 *>(p);
-        } else {
+    for (int it = 0; it < 2; it++) {   // a warp: 8 row quads x 4 k quads
+      const int grp = warp + 8 * it;
+      const int rq = (grp & 1) * 8 + (lane & 7), kq = (grp >> 1) * 4 + (lane >> 3);
+      const int64_t gr = r0 + 4 * rq, gk = k0 + 4 * kq;
+      if (gr >= op.R) continue;
+      uint32_t w[4];
 #pragma unroll
-          for (int i = 0; i < 16; i++) t[i] = gr + i < op.R ? p[i] : 0;
+      for (int i = 0; i < 4; i++) {
+        w[i] = 0;
+        if (gk + i < K) {
+          const uint8_t *p = src + (gk + i) * op.rs_k + gr;
+          if (gr + 4 <= op.R && (reinterpret_cast<uintptr_t>(p) & 3) == 0) {
+            w[i] = *reinterpret_cast<const uint32_t *>(p);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+              if (gr + j < op.R) w[i] |= (uint32_t)p[j] << (8 * j);
+          }
         }
-      } else {
-#pragma unroll
-        for (int i = 0; i < 16; i++) t[i] = 0;
       }
+      // w[i] holds rows gr..gr+3 at k = gk + i; o[j] holds k = gk..gk+3 of row gr + j
+      const uint32_t lo01 = __byte_perm(w[0], w[1], 0x5140), hi01 = __byte_perm(w[0], w[1], 0x7362);
+      const uint32_t lo23 = __byte_perm(w[2], w[3], 0x5140), hi23 = __byte_perm(w[2], w[3], 0x7362);
+      const uint32_t o[4] = {__byte_perm(lo01, lo23, 0x5410), __byte_perm(lo01, lo23, 0x7632),
+                             __byte_perm(hi01, hi23, 0x5410), __byte_perm(hi01, hi23, 0x7632)};
 #pragma unroll
-      for (int i = 0; i < 16; i++) tile[r + i][kk] = t[i];
+      for (int j = 0; j < 4; j++)
+        if (gr + j < op.R)
+          *reinterpret_cast<uint2 *>(op.dst + (gr + j) * Kp + gk) = bytes_to_bf16x4<SIGNED>(o[j]);
     }
-  } else {
+    return;
+  }
 #pragma unroll 4
-    for (int q = 0; q < kCvtRows * kCvtK / 256; q++) {
-      const int e = tid + 256 * q, r = e / kCvtK, kk = e % kCvtK;
-      const int64_t gr = r0 + r, gk = k0 + kk;
-      tile[r][kk] = (gr < op.R && gk < K) ? src[gr * op.rs_row + gk * op.rs_k] : 0;
-    }
+  for (int q = 0; q < kCvtRows * kCvtK / 256; q++) {
+    const int e = tid + 256 * q, r = e / kCvtK, kk = e % kCvtK;
+    const int64_t gr = r0 + r, gk = k0 + kk;
+    tile[r][kk] = (gr < op.R && gk < K) ? src[gr * op.rs_row + gk * op.rs_k] : 0;
   }
   __syncthreads();
 #pragma unroll
@@ -127,20 +211,8 @@ int8_pair_to_bf16(I8Operand a, I8Operand b, int64_t K, int64_t Kp, int64_t block
     const int64_t gr = r0 + r;
     if (gr >= op.R) continue;
     const uint2 raw = *reinterpret_cast<const uint2 *>(&tile[r][kk]);
-    uint32_t w[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const uint32_t word = q < 2 ? raw.x : raw.y;
-      uint32_t h[2];
-#pragma unroll
-      for (int i = 0; i < 2; i++) {
-        const uint32_t byte = (word >> (8 * (2 * (q & 1) + i))) & 0xFFu;
-        const int v = SIGNED ? (int)(int8_t)byte : (int)byte;
-        h[i] = __float_as_uint((float)v) >> 16;
-      }
-      w[q] = h[0] | (h[1] << 16);
-    }
-    *reinterpret_cast<uint4 *>(op.dst + gr * Kp + k0 + kk) = make_uint4(w[0], w[1], w[2], w[3]);
+    const uint2 c0 = bytes_to_bf16x4<SIGNED>(raw.x), c1 = bytes_to_bf16x4<SIGNED>(raw.y);
+    *reinterpret_cast<uint4 *>(op.dst + gr * Kp + k0 + kk) = make_uint4(c0.x, c0.y, c1.x, c1.y);
   }
 }
 
@@ -290,12 +362,16 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
         }
       }
     }
-    if (ok && row < M) {
-      if (rule != kRuleX86Packed) {
+    const bool staged = cso == 1 && (rso & 3) == 0 && (reinterpret_cast<uintptr_t>(C) & 3) == 0;
+    if (ok && row < M && rule != kRuleX86Packed) {
 #pragma unroll
-        for (int j = 0; j < CW; j++)
-          d[j] = simt::fold8(0, d[j], true, rule, SIGNED, row, n0 + cbase + j, M, N);
-      }
+      for (int j = 0; j < CW; j++)
+        d[j] = simt::fold8(0, d[j], true, rule, SIGNED, row, n0 + cbase + j, M, N);
+    }
+    if (ok && staged) {   // warp-uniform
+      uint8_t *stage = smem + kStages * STAGE_BYTES + kBarBytes + (warp - 2) * 1024;
+      store_bytes_coalesced(d, stage, C, rso, m0 + quad * 32, n0 + cbase, M, N, lane);
+    } else if (ok && row < M) {
       const int col0 = n0 + cbase;
       uint8_t *dst = C + (int64_t)row * rso + (int64_t)col0 * cso;
       if (cso == 1 && ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) && col0 + CW <= N) {
@@ -351,9 +427,10 @@ cudaError_t launch_i8_gemm(const Gemm &g, int rule, const I8Layout &L, __nv_bflo
     return e;
   if ((e = make_tmap_2d(&tb, pb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, g.N, L.Kp, L.Kp, kBN, kBK)))
     return e;
-  constexpr uint32_t kBarBytes = 512;   // 2*(kStages + kNumBuf) mbarriers + TMEM slot
   static_assert((2 * Cfg::kStages + 2 * Cfg::kNumBuf + 1) * 8 + 4 <= kBarBytes, "barrier space");
-  constexpr uint32_t SMEM = Cfg::kStages * (kBM + kBN) * kBK * 2 + 1024 + kBarBytes;
+  // ring, alignment, barriers, and 1 KiB of store staging per accumulator warp
+  constexpr uint32_t SMEM =
+      Cfg::kStages * (kBM + kBN) * kBK * 2 + 1024 + kBarBytes + Cfg::kAccWarps * 1024;
   static_assert(SMEM <= 232448, "shared memory");
   if ((e = cudaFuncSetAttribute(int8_tc_gemm<SIGNED, kBN>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM)))
