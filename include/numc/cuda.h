@@ -47,7 +47,8 @@ typedef enum {
   NUMC_CUDA_ALGO_TC_INT8 = 6,    /* int8/uint8 on tcgen05 (values exact in
                                     bfloat16, exact FP32 sums per numc K
                                     block) with numc's store rules; `param`
-                                    is a NumcInt8Profile */
+                                    is a NumcInt8Profile, plus 16 x a
+                                    NumcInt8Tile to pin the tile schedule */
   NUMC_CUDA_ALGO_SPLIT_FP16 = 7  /* float32 on tcgen05 from float16 planes:
                                     each row of A and column of B scaled by
                                     a power of two, x 2^s = h0 + h1 (22
@@ -76,6 +77,15 @@ typedef enum {
                               -march=native on such hosts): int8/uint8 only;
                               floats keep the AVX2 tiles */
 } NumcInt8Profile;
+
+/* Tile schedules of NUMC_CUDA_ALGO_TC_INT8 (16 x the schedule is added to
+ * the profile in `param`).  Every schedule stores the same bytes. */
+typedef enum {
+  NUMC_INT8_TILE_AUTO = 0,    /* by problem size (the default) */
+  NUMC_INT8_TILE_SINGLE = 1,  /* one CTA per 128 x 128 or 128 x 64 tile */
+  NUMC_INT8_TILE_PAIR128 = 2, /* CTA pairs, persistent, 256 x 128 tiles */
+  NUMC_INT8_TILE_PAIR256 = 3  /* CTA pairs, persistent, 256 x 256 tiles */
+} NumcInt8Tile;
 
 /* Number of usable CUDA devices (0 when none). */
 NUMC_API int numc_cuda_device_count(void);

@@ -29,6 +29,7 @@ ERR_TYPE, ERR_BOUNDS, ERR_VALUE, ERR_INTERNAL = -4, -5, -6, -99
 (ALGO_DEFAULT, ALGO_SIMT, ALGO_SPLIT_BF16, ALGO_DMMA, ALGO_OZAKI, ALGO_AUTO, ALGO_TC_INT8,
  ALGO_SPLIT_FP16) = range(8)
 INT8_X86_AVX2, INT8_ARM_NEON, INT8_WRAP, INT8_X86_AVX512 = 0, 1, 2, 3
+INT8_TILE_AUTO, INT8_TILE_SINGLE, INT8_TILE_PAIR128, INT8_TILE_PAIR256 = 0, 1, 2, 3
 
 
 class NumcLibraryMissing(RuntimeError):

@@ -206,6 +206,14 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
     algo = split ? NUMC_CUDA_ALGO_SPLIT_FP16 : NUMC_CUDA_ALGO_SIMT;
     param = split ? 0 : -1;
   }
+  // int8 tensor path: 16 x the tile schedule on top of the profile
+  int i8_tile = 0;
+  if (is8 && algo == NUMC_CUDA_ALGO_TC_INT8 && param >= 16) {
+    i8_tile = param >> 4;
+    param &= 15;
+    if (i8_tile > NUMC_INT8_TILE_PAIR256)
+      return NUMC_SET_ERROR(NUMC_ERR_VALUE, "int8 tile schedule %d outside 0..3", i8_tile);
+  }
   // int8/uint8 and CUDA-core floats: `param` names the numc build (profile)
   const bool profiled = is8 || (isf && algo == NUMC_CUDA_ALGO_SIMT);
   if (profiled && param == -1) param = g_isa_profile.load();
@@ -276,6 +284,7 @@ int resolve(NumcDType dt, int algo, int param, size_t M, size_t K, size_t N, Pla
       p->param = sup ? numc_k::kRuleWrap
                      : packed_only ? numc_k::kRuleX86Packed : numc_k::kRuleAvx512;
     else return NUMC_SET_ERROR(NUMC_ERR_VALUE, "unknown int8 profile %d", param);
+    if (algo == NUMC_CUDA_ALGO_TC_INT8) p->param |= i8_tile << 8;
   }
   return 0;
 }

@@ -47,43 +47,54 @@ template <int BN> struct I8Cfg {
 
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
-// Coalesced stores of a warp's 32 rows x 32 output bytes (d[j] of row
-// row0 + lane, column col0 + j) to row-major uint8 C (unit column stride,
-// 4-byte aligned rows), through the warp's 1 KiB `stage`: each lane writes
-// its row's two 16-byte chunks (chunk c at position c ^ ((row >> 2) & 1),
-// so the 8 lanes of a store phase hit 32 distinct banks), then each store
-// instruction writes 4 rows x 32 bytes, 4 bytes a lane.  A direct store
-// instruction touched 32 rows.  Rows >= M and columns >= N are not written.
-// All 32 lanes must call it.
-__device__ __forceinline__ void store_bytes_coalesced(const int32_t (&d)[32], uint8_t *stage,
+// Coalesced stores of a warp's 32 rows x CW output bytes (d[j] of row
+// row0 + lane, column col0 + j; CW = 32 or 64) to row-major uint8 C (unit
+// column stride, 4-byte aligned rows), through the warp's 32 * CW byte
+// `stage`: each lane writes its row's 16-byte chunks (chunk c of row r at
+// position c ^ ((r / (8 / chunks)) % chunks), so the 8 lanes of a store
+// phase hit 32 distinct banks), then each store instruction writes
+// 128 / CW whole rows, 4 bytes a lane.  A direct store instruction touched
+// 32 rows.  Rows >= M and columns >= N are not written.  All 32 lanes must
+// call it.
+// The low bytes of four values, first in the low byte.
+__device__ __forceinline__ uint32_t pack4(int32_t a, int32_t b, int32_t c, int32_t d) {
+  return __byte_perm(__byte_perm((uint32_t)a, (uint32_t)b, 0x0040),
+                     __byte_perm((uint32_t)c, (uint32_t)d, 0x0040), 0x5410);
+}
+
+template <int CW>
+__device__ __forceinline__ void pack_bytes(const int32_t (&d)[CW], uint32_t (&w)[CW / 4]) {
+#pragma unroll
+  for (int q = 0; q < CW / 4; q++) w[q] = pack4(d[4 * q], d[4 * q + 1], d[4 * q + 2], d[4 * q + 3]);
+}
+
+// w: the row's CW bytes packed four a word, column col0 first.
+template <int CW>
+__device__ __forceinline__ void store_bytes_coalesced(const uint32_t (&w)[CW / 4], uint8_t *stage,
                                                       uint8_t *C, int64_t rso, int row0,
                                                       int col0, int M, int N, int lane) {
+  constexpr int CH = CW / 16, LPR = CW / 4, RPI = 32 / LPR;
+  static_assert(CW == 32 || CW == 64, "row width");
+  auto swz = [](int r) { return (r / (8 / CH)) % CH; };
 #pragma unroll
-  for (int h = 0; h < 2; h++) {
-    uint32_t w[4];
-#pragma unroll
-    for (int q = 0; q < 4; q++)
-      w[q] = (uint32_t)(uint8_t)d[16 * h + 4 * q] | ((uint32_t)(uint8_t)d[16 * h + 4 * q + 1] << 8) |
-             ((uint32_t)(uint8_t)d[16 * h + 4 * q + 2] << 16) |
-             ((uint32_t)(uint8_t)d[16 * h + 4 * q + 3] << 24);
-    const int pos = h ^ ((lane >> 2) & 1);
-    *reinterpret_cast<uint4 *>(stage + lane * 32 + pos * 16) = make_uint4(w[0], w[1], w[2], w[3]);
-  }
+  for (int h = 0; h < CH; h++)
+    *reinterpret_cast<uint4 *>(stage + lane * CW + (h ^ swz(lane)) * 16) =
+        make_uint4(w[4 * h], w[4 * h + 1], w[4 * h + 2], w[4 * h + 3]);
   __syncwarp();
-  const int sub = lane & 7, c = col0 + 4 * sub;
+  const int sub = lane % LPR, c = col0 + 4 * sub;
 #pragma unroll
-  for (int rr = 0; rr < 32; rr += 4) {
-    const int r = rr + (lane >> 3);
-    const int pos = (sub >> 2) ^ ((r >> 2) & 1);
-    const uint32_t w = *reinterpret_cast<const uint32_t *>(stage + r * 32 + pos * 16 + (sub & 3) * 4);
+  for (int rr = 0; rr < 32; rr += RPI) {
+    const int r = rr + lane / LPR;
+    const uint32_t v = *reinterpret_cast<const uint32_t *>(
+        stage + r * CW + (((sub >> 2) ^ swz(r)) * 16) + (sub & 3) * 4);
     if (row0 + r < M) {
       uint8_t *dst = C + (int64_t)(row0 + r) * rso + c;
       if (c + 4 <= N) {
-        *reinterpret_cast<uint32_t *>(dst) = w;
+        *reinterpret_cast<uint32_t *>(dst) = v;
       } else {
 #pragma unroll
         for (int b = 0; b < 4; b++)
-          if (c + b < N) dst[b] = (uint8_t)(w >> (8 * b));
+          if (c + b < N) dst[b] = (uint8_t)(v >> (8 * b));
       }
     }
   }
@@ -319,10 +330,11 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     int32_t d[CW], part[CW];
     uint32_t fullmask = 0;   // x86 rule: columns inside numc's full 6x16 tiles
+    const bool row_full = simt::x86_row_full(row, M);
 #pragma unroll
     for (int j = 0; j < CW; j++) {
       d[j] = 0;
-      if (rule == kRuleX86Packed && simt::x86_full(row, n0 + cbase + j, M, N))
+      if (rule == kRuleX86Packed && row_full && simt::x86_col_full(n0 + cbase + j, N))
         fullmask |= 1u << j;
     }
     const int nchunks = num_kb / CHUNK;   // num_kb is a multiple of the block size
@@ -370,7 +382,9 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
     }
     if (ok && staged) {   // warp-uniform
       uint8_t *stage = smem + kStages * STAGE_BYTES + kBarBytes + (warp - 2) * 1024;
-      store_bytes_coalesced(d, stage, C, rso, m0 + quad * 32, n0 + cbase, M, N, lane);
+      uint32_t w[CW / 4];
+      pack_bytes<CW>(d, w);
+      store_bytes_coalesced<CW>(w, stage, C, rso, m0 + quad * 32, n0 + cbase, M, N, lane);
     } else if (ok && row < M) {
       const int col0 = n0 + cbase;
       uint8_t *dst = C + (int64_t)row * rso + (int64_t)col0 * cso;
@@ -400,6 +414,321 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
   if (warp == 1) {
     tc::tc_fence_after();
     tc::tmem_dealloc(tmem, kNumBuf * kBN);
+  }
+}
+
+// ---- CTA pairs for large problems -------------------------------------------
+//
+// Clusters of two CTAs on neighbouring SMs walk 256 x BN output tiles
+// persistently (tiles rasterised in groups of 2048 rows).  Each CTA loads
+// its own 128 rows of A and BN/2 rows of B^T per 64-deep slab; the even
+// CTA's MMA thread multiplies both halves with cta_group::2 MMAs into TMEM
+// of both CTAs, so an SM fetches (128 + BN/2) x 64 operand elements per
+// 128 x BN x 64 multiply-adds: at BN = 256 half the bytes per MMA of the
+// single-CTA 128 x 128 tiles.  TMEM holds two (BN = 256) or four (BN = 128)
+// chunk buffers of 128 lanes x BN FP32 columns; 16 accumulator warps per CTA
+// (4 per TMEM lane quarter, BN / 4 columns each) fold every finished chunk
+// into numc's stored bytes while the next chunk is multiplied.
+//
+// X86 selects numc's x86 packed rule at compile time: a fold per 512-deep
+// block, done in FP32 on the block's sum (fold8_x86_f).  For uint8 that sum
+// may exceed 2^24, where FP32 accumulation rounds; but uint8 products are
+// non-negative, so the partial sums only grow, the accumulation is exact as
+// long as the true sum is at most 2^24, and past that the rounded sum stays
+// far above the rule's largest threshold (32767): every stored byte is
+// decided exactly, and the block needs one TMEM chunk.  The other rules
+// add the chunks' exact sums (uint8: two 256-deep halves) into a wrapped
+// int32 and narrow once at the end.
+
+// numc's x86 packed int8/uint8 fold (simt::fold8_x86) in FP32 on the block
+// sums read from TMEM, without a float-to-int conversion per block.  d: the
+// byte stored so far as a float; P: the block's sum.
+template <bool SIGNED>
+__device__ __forceinline__ float sat8_f(float x) {
+  if constexpr (SIGNED) return fminf(fmaxf(x, -128.0f), 127.0f);
+  // packusdw then packuswb: [0,255] kept, (255, 32767] -> 255, else 0
+  return x <= 255.0f ? fmaxf(x, 0.0f) : (x <= 32767.0f ? 255.0f : 0.0f);
+}
+template <bool SIGNED>
+__device__ __forceinline__ float fold8_x86_f(float d, float P, bool first, bool full) {
+  if (full) return sat8_f<SIGNED>(d + P);
+  const float t = sat8_f<SIGNED>(P);
+  if (first) return t;
+  const float x = d + t;   // wrap to 8 bits
+  if constexpr (SIGNED) return x > 127.0f ? x - 256.0f : (x < -128.0f ? x + 256.0f : x);
+  return x > 255.0f ? x - 256.0f : x;
+}
+// Stored bytes packed four a word as offset binary (int8: value + 128), so
+// that a byte turns into a float with one byte permute and one add:
+// 2^23 + byte has the byte as its low mantissa bits.
+template <bool SIGNED>
+__device__ __forceinline__ float byte_to_f(uint32_t word, int k) {
+  constexpr float kBias = 8388608.0f + (SIGNED ? 128.0f : 0.0f);
+  return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7540u + (uint32_t)k)) - kBias;
+}
+// f integral in [-128, 255]: 1.5 x 2^23 + bias + f keeps f + bias in the
+// low mantissa byte.
+template <bool SIGNED>
+__device__ __forceinline__ uint32_t f_to_bits(float f) {
+  constexpr float kMagic = 12582912.0f + (SIGNED ? 128.0f : 0.0f);
+  return __float_as_uint(f + kMagic);
+}
+
+template <int BN> struct I8PairCfg {
+  static constexpr int BN_CTA = BN / 2;
+  static constexpr uint32_t A_BYTES = kBM * kBK * 2, B_BYTES = BN_CTA * kBK * 2;
+  static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int STAGES = BN == 256 ? 6 : 8;
+  static constexpr int NBUF = 512 / BN;
+  static constexpr uint32_t TMEM_COLS = 512;
+  static constexpr int CW = BN / 4;            // columns per accumulator thread
+  static constexpr int ACC_WARPS = 16, THREADS = 64 + 32 * ACC_WARPS;
+  static constexpr uint32_t BAR_BYTES = 256;
+  static constexpr uint32_t EPI_BYTES = ACC_WARPS * 32 * CW;   // byte staging per warp
+  static constexpr uint32_t SMEM = STAGES * STAGE_BYTES + 1024 + BAR_BYTES + EPI_BYTES;
+  static_assert(SMEM <= 232448, "shared memory");
+  static_assert((2 * STAGES + 2 * NBUF + 1) * 8 + 4 <= BAR_BYTES, "barrier space");
+};
+
+template <bool SIGNED, int BN, bool X86>
+__global__ void __launch_bounds__(I8PairCfg<BN>::THREADS, 1)
+int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB,
+               uint8_t *__restrict__ C, int64_t rso, int64_t cso, int M, int N, int num_kb,
+               int tiles_m, int tiles_n, int rule, unsigned *status, WaitCfg wc) {
+  using Cfg = I8PairCfg<BN>;
+  constexpr int STAGES = Cfg::STAGES, NBUF = Cfg::NBUF, CW = Cfg::CW;
+  // slabs per TMEM chunk: a whole 512-deep block, except for uint8 under
+  // the rules that need its exact sum (two 256-deep halves)
+  constexpr int CHUNK = (SIGNED || X86) ? kBlockK / kBK : kBlockK / kBK / 2;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *bars = (uint64_t *)(smem + STAGES * Cfg::STAGE_BYTES);
+  uint64_t *full = bars, *empty = bars + STAGES;
+  uint64_t *tfull = bars + 2 * STAGES, *tempty = tfull + NBUF;
+  uint64_t *drain = tempty + NBUF;   // all issued MMAs complete
+  uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = tiles_m * tiles_n;
+  const uint32_t rank = tc::cluster_ctarank();
+  const bool leader = rank == 0;
+  const int first_tile = blockIdx.x / 2, tile_step = gridDim.x / 2;
+  auto tile_origin = [&](int t, int &m0, int &n0) {
+    constexpr int GM = 8;   // 2048 rows of pair tiles
+    const int group = t / (GM * tiles_n);
+    const int first_m = group * GM;
+    const int gm = min(tiles_m - first_m, GM);
+    const int local = t - group * GM * tiles_n;
+    m0 = (first_m + local % gm) * (2 * kBM);
+    n0 = (local / gm) * BN;
+  };
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      tc::mbar_init(tc::smem_u32(&full[s]), 1);
+      tc::mbar_init(tc::smem_u32(&empty[s]), 1);
+    }
+    for (int b = 0; b < NBUF; b++) {
+      tc::mbar_init(tc::smem_u32(&tfull[b]), 1);
+      tc::mbar_init(tc::smem_u32(&tempty[b]), Cfg::ACC_WARPS * 2);   // both CTAs' warps
+    }
+    tc::mbar_init(tc::smem_u32(drain), 1);
+    tc::fence_barrier_init();
+    tc::tma_prefetch_desc(&tA);
+    tc::tma_prefetch_desc(&tB);
+  }
+  if (warp == 1) tc::tmem_alloc_pair(tc::smem_u32(tmem_slot), Cfg::TMEM_COLS);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::cluster_sync();   // peer barriers initialised
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const int nchunks = num_kb / CHUNK;   // per tile; num_kb is a multiple of the block
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int g = 0;   // stage counter across tiles
+      bool live = true;
+      for (int t = first_tile; t < ntiles && live; t += tile_step) {
+        int m0, n0;
+        tile_origin(t, m0, n0);
+        const int ma = m0 + (int)rank * kBM, nb = n0 + (int)rank * Cfg::BN_CTA;
+        for (int kb = 0; kb < num_kb; kb++, g++) {
+          const int s = g % STAGES;
+          if (g >= STAGES &&
+              !tc::mbar_wait_bounded(tc::smem_u32(&empty[s]), ((g / STAGES) & 1) ^ 1, status,
+                                     kStatusTimeoutProducer, wc.limit_ns)) {
+            live = false;
+            break;
+          }
+          if (wc.starve) continue;   // give-up test: no load, no barrier ever completes
+          const uint32_t fbar = tc::smem_u32(&full[s]);
+          const uint32_t st = tc::smem_u32(smem + s * Cfg::STAGE_BYTES);
+          // the even CTA's full barrier counts the bytes of both CTAs
+          if (leader) tc::mbar_arrive_expect_tx(fbar, 2 * Cfg::STAGE_BYTES);
+          const uint32_t fbar_leader = tc::mapa_shared(fbar, 0);
+          tc::tma_load_3d_pair(st, &tA, fbar_leader, kb * kBK, ma, 0);
+          tc::tma_load_3d_pair(st + Cfg::A_BYTES, &tB, fbar_leader, kb * kBK, nb, 0);
+        }
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0 && leader) {
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(2 * kBM, BN);
+      int g = 0, chunk = 0;   // stage and chunk counters across tiles
+      bool live = true;
+      for (int t = first_tile; t < ntiles && live; t += tile_step) {
+        for (int kb = 0; kb < num_kb; kb++, g++) {
+          const int s = g % STAGES, buf = chunk % NBUF;
+          const bool cstart = kb % CHUNK == 0, cend = kb % CHUNK == CHUNK - 1;
+          if (cstart && chunk >= NBUF &&
+              !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / NBUF) & 1) ^ 1,
+                                     status, kStatusTimeoutMma, wc.limit_ns)) {
+            live = false;
+            break;
+          }
+          if (!tc::mbar_wait_bounded(tc::smem_u32(&full[s]), (g / STAGES) & 1, status,
+                                     kStatusTimeoutMma, wc.limit_ns)) {
+            live = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint32_t sa = tc::smem_u32(smem + s * Cfg::STAGE_BYTES), sb = sa + Cfg::A_BYTES;
+#pragma unroll
+          for (int kk = 0; kk < kBK / 16; kk++)
+            tc::mma_f16_pair(tmem + buf * BN, tc::sdesc_k128(sa + kk * 32),
+                             tc::sdesc_k128(sb + kk * 32), idesc, (!cstart || kk > 0) ? 1u : 0u);
+          tc::mma_commit_pair(tc::smem_u32(&empty[s]), 0x3);
+          if (cend) {
+            tc::mma_commit_pair(tc::smem_u32(&tfull[buf]), 0x3);
+            chunk++;
+          }
+        }
+      }
+      // Every MMA issued above completes before TMEM is released, also when
+      // the loop gave up (a commit with none outstanding arrives at once).
+      tc::mma_commit_pair(tc::smem_u32(drain), 0x1);
+      tc::mbar_wait_bounded(tc::smem_u32(drain), 0, status, kStatusTimeoutDrain, wc.limit_ns);
+    }
+    __syncwarp();
+  } else {
+    // warp w reads TMEM lanes 32 * (w % 4); the four warps of a lane quarter
+    // split the tile's columns CW apiece
+    const int quad = warp & 3, grp = (warp - 2) >> 2;
+    const int cbase = grp * CW;
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    uint8_t *stage = smem + STAGES * Cfg::STAGE_BYTES + Cfg::BAR_BYTES + (warp - 2) * (32 * CW);
+    const bool staged = cso == 1 && (rso & 3) == 0 && (reinterpret_cast<uintptr_t>(C) & 3) == 0;
+    int chunk = 0;   // across tiles
+    bool ok = true;
+    for (int t = first_tile; t < ntiles && ok; t += tile_step) {
+      int m0, n0;
+      tile_origin(t, m0, n0);
+      const int mr = m0 + (int)rank * kBM;   // this CTA's 128 rows
+      const int row = mr + quad * 32 + lane;
+      // x86 rule: the stored bytes so far, packed four a word (every fold
+      // leaves a byte; int8 as value + 128); other rules: the wrapped int32
+      // sums
+      int32_t d[X86 ? 1 : CW];
+      uint32_t d8[X86 ? CW / 4 : 1];
+      uint64_t fullmask = 0;   // x86 rule: columns inside numc's full 6x16 tiles
+      const bool row_full = X86 && simt::x86_row_full(row, M);
+#pragma unroll
+      for (int j = 0; j < CW; j++) {
+        if constexpr (X86) {
+          if (row_full && simt::x86_col_full(n0 + cbase + j, N)) fullmask |= 1ull << j;
+        } else {
+          d[j] = 0;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < (X86 ? CW / 4 : 1); q++) d8[q] = SIGNED ? 0x80808080u : 0u;
+      // warp-uniform: every column of every lane inside numc's full tiles
+      const bool all_full = X86 && __all_sync(0xffffffffu, fullmask == ~0ull >> (64 - CW));
+      for (int c = 0; c < nchunks; c++, chunk++) {
+        const int buf = chunk % NBUF;
+        ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / NBUF) & 1, status,
+                                   kStatusTimeoutEpilogue, wc.limit_ns);
+        ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
+        if (!ok) break;
+        tc::tc_fence_after();
+        const bool first = c == 0;
+#pragma unroll
+        for (int c0 = 0; c0 < CW; c0 += 16) {
+          uint32_t r[16];
+          tc::tmem_ld_32x32b_x16(tmem + lane_off + buf * BN + cbase + c0, r);
+          tc::tmem_ld_wait();
+          if constexpr (X86) {
+            if (all_full) {   // warp-uniform branch: d = sat(d + P)
+#pragma unroll
+              for (int wq = 0; wq < 4; wq++) {
+                const int q0 = c0 + 4 * wq;
+                uint32_t b[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                  const float P = __uint_as_float(r[4 * wq + k]);
+                  b[k] = f_to_bits<SIGNED>(sat8_f<SIGNED>(byte_to_f<SIGNED>(d8[q0 >> 2], k) + P));
+                }
+                d8[q0 >> 2] = pack4((int32_t)b[0], (int32_t)b[1], (int32_t)b[2], (int32_t)b[3]);
+              }
+            } else {
+#pragma unroll
+              for (int wq = 0; wq < 4; wq++) {
+                const int q0 = c0 + 4 * wq;
+                uint32_t b[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                  const float P = __uint_as_float(r[4 * wq + k]);
+                  const float prev = byte_to_f<SIGNED>(d8[q0 >> 2], k);
+                  b[k] = f_to_bits<SIGNED>(
+                      fold8_x86_f<SIGNED>(prev, P, first, (fullmask >> (q0 + k)) & 1ull));
+                }
+                d8[q0 >> 2] = pack4((int32_t)b[0], (int32_t)b[1], (int32_t)b[2], (int32_t)b[3]);
+              }
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < 16; j++)
+              d[c0 + j] = (int32_t)((uint32_t)d[c0 + j] +
+                                    (uint32_t)__float2int_rn(__uint_as_float(r[j])));   // exact
+          }
+        }
+        tc::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive_cluster(tc::mapa_shared(tc::smem_u32(&tempty[buf]), 0));
+      }
+      if (!ok) break;
+      uint32_t w[CW / 4];
+      if constexpr (X86) {
+#pragma unroll
+        for (int q = 0; q < CW / 4; q++) w[q] = SIGNED ? d8[q] ^ 0x80808080u : d8[q];
+      } else {
+        if (row < M) {
+#pragma unroll
+          for (int j = 0; j < CW; j++)
+            d[j] = simt::fold8(0, d[j], true, rule, SIGNED, row, n0 + cbase + j, M, N);
+        }
+        pack_bytes<CW>(d, w);
+      }
+      if (staged) {   // warp-uniform
+        store_bytes_coalesced<CW>(w, stage, C, rso, mr + quad * 32, n0 + cbase, M, N, lane);
+      } else if (row < M) {
+#pragma unroll
+        for (int j = 0; j < CW; j++)
+          if (n0 + cbase + j < N)
+            C[(int64_t)row * rso + (int64_t)(n0 + cbase + j) * cso] = (uint8_t)(w[j >> 2] >> (8 * (j & 3)));
+      }
+      __syncwarp();   // reconverge before the next tile's tcgen05.ld
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  // Neither CTA of a pair leaves while the other may still signal its
+  // barriers or read its shared memory.
+  tc::cluster_sync();
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc_pair(tmem, Cfg::TMEM_COLS);
   }
 }
 
@@ -443,8 +772,60 @@ cudaError_t launch_i8_gemm(const Gemm &g, int rule, const I8Layout &L, __nv_bflo
   return cudaGetLastError();
 }
 
+template <bool SIGNED, int BN, bool X86>
+cudaError_t launch_i8_pair(const Gemm &g, int rule, const I8Layout &L, const __nv_bfloat16 *pa,
+                           const __nv_bfloat16 *pb, unsigned *status, cudaStream_t s) {
+  using Cfg = I8PairCfg<BN>;
+  CUtensorMap ta, tb;
+  cudaError_t e;
+  if ((e = make_tmap_3d(&ta, pa, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, 1, g.M, L.Kp, L.Kp, kBM,
+                        kBK)))
+    return e;
+  if ((e = make_tmap_3d(&tb, pb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, 1, g.N, L.Kp, L.Kp,
+                        Cfg::BN_CTA, kBK)))
+    return e;
+  auto kern = int8_pair_gemm<SIGNED, BN, X86>;
+  if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM)))
+    return e;
+  const int tiles_m = (int)((g.M + 2 * kBM - 1) / (2 * kBM));
+  const int tiles_n = (int)((g.N + BN - 1) / BN);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(Cfg::THREADS);
+  cfg.dynamicSmemBytes = Cfg::SMEM;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3((unsigned)(2 * std::max(1, sm_count() / 2)));
+  int pairs = max_active_clusters((const void *)kern, cfg);
+  if (pairs <= 0) pairs = std::max(1, sm_count() / 2);
+  pairs = std::min(pairs, tiles_m * tiles_n);
+  cfg.gridDim = dim3((unsigned)(2 * pairs));
+  e = cudaLaunchKernelEx(&cfg, kern, ta, tb, (uint8_t *)g.c, (int64_t)g.rso, (int64_t)g.cso,
+                         (int)g.M, (int)g.N, (int)(L.Kp / kBK), tiles_m, tiles_n, rule, status,
+                         wait_cfg());
+  if (e != cudaSuccess) return e;
+  count_launch();
+  return cudaGetLastError();
+}
+
+// Tile schedule when the caller names none: CTA pairs with 256 x 256
+// tiles once those give three pairs in four a tile (measured on GB300: at
+// 2048^3 and above they beat the single-CTA tiles by 1.2-1.4x), else
+// single-CTA tiles (128 x 128 while they cover the SMs, else 128 x 64).
+int pick_tile(const Gemm &g) {
+  const int64_t pairs = std::max(1, sm_count() / 2);
+  const int64_t tiles = (g.M + 2 * kBM - 1) / (2 * kBM) * ((g.N + 255) / 256);
+  return 4 * tiles >= 3 * pairs ? kI8TilePair256 : kI8TileSingle;
+}
+
 template <bool SIGNED>
-cudaError_t launch_i8(const Gemm &g, int rule, char *ws, const I8Layout &L, cudaStream_t s) {
+cudaError_t launch_i8(const Gemm &g, int rule, int tile, char *ws, const I8Layout &L,
+                      cudaStream_t s) {
   unsigned *status = status_word();
   if (!status) return cudaErrorMemoryAllocation;
   PhaseMark mark(s);
@@ -461,9 +842,18 @@ cudaError_t launch_i8(const Gemm &g, int rule, char *ws, const I8Layout &L, cuda
   cudaError_t e = cudaGetLastError();
   if (e) return e;
   mark.split_done();
-  const int64_t tiles128 = ((g.M + kBM - 1) / kBM) * ((g.N + 127) / 128);
-  e = tiles128 >= 152 ? launch_i8_gemm<SIGNED, 128>(g, rule, L, pa, pb, status, s)
-                      : launch_i8_gemm<SIGNED, 64>(g, rule, L, pa, pb, status, s);
+  const bool x86 = rule == kRuleX86Packed;
+  if (tile == kI8TileAuto) tile = pick_tile(g);
+  if (tile == kI8TilePair256)
+    e = x86 ? launch_i8_pair<SIGNED, 256, true>(g, rule, L, pa, pb, status, s)
+            : launch_i8_pair<SIGNED, 256, false>(g, rule, L, pa, pb, status, s);
+  else if (tile == kI8TilePair128)
+    e = x86 ? launch_i8_pair<SIGNED, 128, true>(g, rule, L, pa, pb, status, s)
+            : launch_i8_pair<SIGNED, 128, false>(g, rule, L, pa, pb, status, s);
+  else if (((g.M + kBM - 1) / kBM) * ((g.N + 127) / 128) >= sm_count())
+    e = launch_i8_gemm<SIGNED, 128>(g, rule, L, pa, pb, status, s);
+  else
+    e = launch_i8_gemm<SIGNED, 64>(g, rule, L, pa, pb, status, s);
   mark.gemm_done();
   return e;
 }
@@ -472,15 +862,17 @@ cudaError_t launch_i8(const Gemm &g, int rule, char *ws, const I8Layout &L, cuda
 
 size_t int8_tc_workspace(int64_t M, int64_t K, int64_t N) { return i8_layout(M, K, N).total; }
 
-cudaError_t launch_int8_tc(NumcDType dt, const Gemm &g, int rule, void *ws, size_t ws_bytes,
+cudaError_t launch_int8_tc(NumcDType dt, const Gemm &g, int param, void *ws, size_t ws_bytes,
                            cudaStream_t s) {
   if (g.M == 0 || g.N == 0) return cudaSuccess;
-  if (g.K == 0) return launch_simt(dt, g, rule, s);   // C = 0
+  if (g.K == 0) return launch_simt(dt, g, param & 0xff, s);   // C = 0
   if (g.M >= (1ll << 31) || g.N >= (1ll << 31) || g.K >= (1ll << 31)) return cudaErrorInvalidValue;
   const I8Layout L = i8_layout(g.M, g.K, g.N);
   if (ws_bytes < L.total || ((uintptr_t)ws & 255)) return cudaErrorInvalidValue;
-  if (dt == NUMC_DTYPE_INT8) return launch_i8<true>(g, rule, (char *)ws, L, s);
-  if (dt == NUMC_DTYPE_UINT8) return launch_i8<false>(g, rule, (char *)ws, L, s);
+  const int rule = param & 0xff, tile = param >> 8;
+  if (tile < kI8TileAuto || tile > kI8TilePair256) return cudaErrorInvalidValue;
+  if (dt == NUMC_DTYPE_INT8) return launch_i8<true>(g, rule, tile, (char *)ws, L, s);
+  if (dt == NUMC_DTYPE_UINT8) return launch_i8<false>(g, rule, tile, (char *)ws, L, s);
   return cudaErrorInvalidValue;
 }
 

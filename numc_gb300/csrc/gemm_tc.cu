@@ -51,6 +51,30 @@
 #include "tc_common.cuh"
 
 namespace numc_k {
+
+// Streaming multiprocessors of the current device (persistent grid size).
+int sm_count() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+  if (!cached[dev]) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cached[dev] = n > 0 ? n : 148;
+  }
+  return cached[dev];
+}
+
+// Co-resident clusters of `kern` launched with `cfg` (0 if the query fails).
+int max_active_clusters(const void *kern, const cudaLaunchConfig_t &cfg) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
 namespace {
 
 constexpr int kBM = 128, kBK = 64;
@@ -562,19 +586,6 @@ SplitBufs bufs_of(const SplitLayout &L, char *ws) {
   return b;
 }
 
-// Streaming multiprocessors of the current device (persistent grid size).
-int sm_count() {
-  static int cached[64] = {0};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
-  if (!cached[dev]) {
-    int n = 0;
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    cached[dev] = n > 0 ? n : 148;
-  }
-  return cached[dev];
-}
-
 // Generation numbers of split calls (never 0; flags hold the last writer's).
 std::atomic<unsigned long long> g_split_gen{0x5eed000000000000ull};
 
@@ -640,16 +651,6 @@ cudaError_t launch_split_pass(const SplitLayout &L, const SplitBufs &b, const Ge
   }
   cudaError_t e = split_a(L, b, g, gen, s);
   return e != cudaSuccess ? e : split_b(L, b, g, gen, s);
-}
-
-// Co-resident clusters of `kern` launched with `cfg` (0 if the query fails).
-int max_active_clusters(const void *kern, const cudaLaunchConfig_t &cfg) {
-  int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
-    cudaGetLastError();
-    return 0;
-  }
-  return n;
 }
 
 template <int BN, int STAGES, int PLANES, int FLUSH, bool F16, int CTAS>

@@ -131,9 +131,11 @@ cudaError_t launch_split_f16(const Gemm &g, int flush, void *ws, size_t ws_bytes
 cudaError_t launch_split_bf16(const Gemm &g, int passes, void *ws, size_t ws_bytes,
                               cudaStream_t s);
 
-// int8/uint8 on tcgen05 with numc's store rule `rule8`.
+// int8/uint8 on tcgen05: `param` = numc's store rule (kRule*) + 256 x the
+// tile schedule (kI8Tile*; auto picks by problem size).
+enum I8Tile { kI8TileAuto = 0, kI8TileSingle = 1, kI8TilePair128 = 2, kI8TilePair256 = 3 };
 size_t int8_tc_workspace(int64_t M, int64_t K, int64_t N);
-cudaError_t launch_int8_tc(NumcDType dt, const Gemm &g, int rule8, void *ws, size_t ws_bytes,
+cudaError_t launch_int8_tc(NumcDType dt, const Gemm &g, int param, void *ws, size_t ws_bytes,
                            cudaStream_t s);
 
 // float64 Ozaki slicing on tcgen05.
@@ -157,6 +159,11 @@ cudaError_t read_and_clear_status(unsigned *status, cudaStream_t s);
 // Every device allocation of the library goes through here (cudaMalloc,
 // or a simulated out-of-memory failure set by numc_cuda_debug_fail_malloc).
 cudaError_t dev_malloc(void **p, size_t bytes);
+
+// Streaming multiprocessors of the current device (cached per device).
+int sm_count();
+// Co-resident clusters of `kern` launched with `cfg` (0 if the query fails).
+int max_active_clusters(const void *kern, const cudaLaunchConfig_t &cfg);
 
 // Count of kernel launches issued by this library.
 void count_launch(unsigned n = 1);

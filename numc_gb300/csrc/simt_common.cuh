@@ -126,6 +126,16 @@ __device__ __forceinline__ bool x86_full(int64_t i, int64_t j, int64_t M,
   int64_t jr = ((j - jc) / 16) * 16, nr = min((int64_t)16, nc - jr);
   return mr == 6 && nr == 16;
 }
+// x86_full split into its row and column halves, in 32-bit arithmetic
+// (dimensions below 2^31): x86_full(i, j) == x86_row_full(i) && x86_col_full(j).
+__device__ __forceinline__ bool x86_row_full(int i, int M) {
+  const int ic = i / 72 * 72, mc = min(72, M - ic);
+  return i - ic < mc / 6 * 6;
+}
+__device__ __forceinline__ bool x86_col_full(int j, int N) {
+  const int jc = j / 4080 * 4080, nc = min(4080, N - jc);
+  return j - jc < nc / 16 * 16;
+}
 // Full MR x NR tile of a clamp-once int8 path that blocks M by MC (a
 // multiple of MR) and N by NR from column 0: numc's NEON build (72, 6, 8;
 // gemm_neon.h:1509-1535) and its AVX-512 build (240, 12, 16;

@@ -3,8 +3,9 @@
 Every stored byte must equal numc's own (golden SHA-256 at 1024^3 and
 300x4100x4200) and the oracle's for each store-rule profile, including
 shapes with remainder tiles and K not a multiple of numc's 512 block, on
-both tile widths (128 x 64 tiles, and 128 x 128 once those give every SM
-one).
+every tile schedule: single CTAs (128 x 64 tiles, and 128 x 128 once those
+give every SM one) and persistent CTA pairs (256 x 128, 256 x 256), each
+with every store-rule profile.
 """
 import numpy as np
 import pytest
@@ -20,11 +21,11 @@ torch = pytest.importorskip("torch")
 CASES, _ = golden()
 
 
-def _tc(a, b, profile):
+def _tc(a, b, profile, tile=nc.INT8_TILE_AUTO):
     ta = torch.from_numpy(np.ascontiguousarray(a)).cuda()
     tb = torch.from_numpy(np.ascontiguousarray(b)).cuda()
     out = torch.full((a.shape[0], b.shape[1]), 77, dtype=ta.dtype, device="cuda")
-    nc.gemm(ta, tb, out, algo=nc.ALGO_TC_INT8, param=profile)
+    nc.gemm(ta, tb, out, algo=nc.ALGO_TC_INT8, param=profile + 16 * tile)
     nc.check_status()
     return out.cpu().numpy()
 
@@ -39,6 +40,53 @@ def _tc(a, b, profile):
 def test_profiles_vs_oracle(dt, profile, shape):
     a, b = synth.operands("uniform", *shape, dtype=dt, seed=sum(shape))
     np.testing.assert_array_equal(_tc(a, b, profile), oracle.matmul(a, b, profile))
+
+
+ORACLE_PROFILE = {nc.INT8_X86_AVX2: oracle.PROFILE_X86_AVX2, nc.INT8_ARM_NEON: oracle.PROFILE_ARM_NEON,
+                  nc.INT8_WRAP: oracle.PROFILE_WRAP, nc.INT8_X86_AVX512: oracle.PROFILE_X86_AVX512}
+
+
+@pytest.mark.parametrize("dt", ["int8", "uint8"])
+@pytest.mark.parametrize("tile", [nc.INT8_TILE_SINGLE, nc.INT8_TILE_PAIR128, nc.INT8_TILE_PAIR256],
+                         ids=["single", "pair128", "pair256"])
+@pytest.mark.parametrize("profile", [nc.INT8_X86_AVX2, nc.INT8_ARM_NEON, nc.INT8_WRAP,
+                                     nc.INT8_X86_AVX512], ids=["x86", "neon", "wrap", "avx512"])
+@pytest.mark.parametrize("shape", [(5, 3, 4), (300, 1100, 517), (97, 513, 203),
+                                   # several tiles per pair, an odd CTA below the last row
+                                   (1300, 1536, 1100)],
+                         ids=lambda s: "x".join(map(str, s)))
+def test_tile_schedules_vs_oracle(dt, tile, profile, shape):
+    a, b = synth.operands("extreme" if shape[1] > 1000 else "uniform", *shape, dtype=dt,
+                          seed=7 + sum(shape))
+    np.testing.assert_array_equal(_tc(a, b, profile, tile),
+                                  oracle.matmul(a, b, ORACLE_PROFILE[profile]))
+
+
+@pytest.mark.parametrize("dt", ["int8", "uint8"])
+@pytest.mark.parametrize("tile", [nc.INT8_TILE_PAIR128, nc.INT8_TILE_PAIR256])
+def test_pair_schedules_golden_sha_1024(dt, tile):
+    case = [c for c in CASES if c["dtype"] == dt and c["kind"] == "uniform"
+            and tuple(c["shape"]) == (1024, 1024, 1024)][0]
+    a, b = synth.operands("uniform", 1024, 1024, 1024, seed=case["seed"], dtype=dt)
+    assert sha(_tc(a, b, nc.INT8_X86_AVX2, tile)) == case["sha256"]
+
+
+def test_pair_schedule_strided_output():
+    """A transposed (column-major) output takes the byte-store path."""
+    a, b = synth.operands("uniform", 600, 900, 520, dtype="int8", seed=11)
+    ta, tb = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    for tile in (nc.INT8_TILE_PAIR128, nc.INT8_TILE_PAIR256):
+        out = torch.full((520, 600), 77, dtype=torch.int8, device="cuda").t()
+        nc.gemm(ta, tb, out, algo=nc.ALGO_TC_INT8, param=nc.INT8_X86_AVX2 + 16 * tile)
+        nc.check_status()
+        np.testing.assert_array_equal(out.cpu().numpy(), oracle.matmul(a, b))
+
+
+def test_tile_schedule_out_of_range_is_refused():
+    a = torch.zeros((4, 4), dtype=torch.int8, device="cuda")
+    with pytest.raises(nc.NumcError) as ei:
+        nc.gemm(a, a, a.clone(), algo=nc.ALGO_TC_INT8, param=16 * 4)
+    assert ei.value.code == nc.ERR_VALUE
 
 
 @pytest.mark.parametrize("case", [c for c in CASES if c["dtype"] in ("int8", "uint8")
