@@ -22,6 +22,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
 
 #include "kernels.h"
 #include "phase_timing.h"
@@ -109,7 +110,7 @@ struct I8Operand {
   __nv_bfloat16 *dst;
 };
 
-constexpr int kCvtRows = 64, kCvtK = 128;
+constexpr int kCvtRows = 64, kCvtK = 256;
 
 // Four 8-bit integers (bytes of w, low first) as four bfloat16, packed two
 // a word.  Integers of 8 bits are exact in bfloat16: the value's float32
@@ -126,7 +127,7 @@ __device__ __forceinline__ uint2 bytes_to_bf16x4(uint32_t w) {
   return make_uint2(h[0] | (h[1] << 16), h[2] | (h[3] << 16));
 }
 
-// Both operands in one launch (A's tiles first, then B^T's), 64 rows x 128 k
+// Both operands in one launch (A's tiles first, then B^T's), 64 rows x 256 k
 // a block.  Each source layout gets its own mapping, all of them writing
 // whole 32-byte sectors of the destination:
 //   * k contiguous (row-major A): 16 bytes a thread along k, converted in
@@ -147,27 +148,35 @@ int8_pair_to_bf16(I8Operand a, I8Operand b, int64_t K, int64_t Kp, int64_t block
   const int64_t r0 = (blk / kblocks) * kCvtRows, k0 = (blk % kblocks) * kCvtK;
   const int tid = threadIdx.x;
   const uint8_t *src = op.src;
+  // Every load of a thread is issued before its first store (the
+  // destination may alias nothing it reads, but the compiler cannot know).
   if (op.rs_k == 1) {
+    uint4 v[4];
 #pragma unroll
-    for (int it = 0; it < 2; it++) {   // 8 threads a row, 16 k each
-      const int r = (tid >> 3) + 32 * it, kk = (tid & 7) * 16;
+    for (int it = 0; it < 4; it++) {   // 8 threads a row, 16 k each, two 128-k halves
+      const int r = (tid >> 3) + 32 * (it & 1), kk = (tid & 7) * 16 + 128 * (it >> 1);
       const int64_t gr = r0 + r, gk = k0 + kk;
-      if (gr >= op.R) continue;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (gk < K) {
+      v[it] = make_uint4(0, 0, 0, 0);
+      if (gr < op.R && gk < K) {
         const uint8_t *p = src + gr * op.rs_row + gk;
         if (gk + 16 <= K && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
-          v = *reinterpret_cast<const uint4 *>(p);
+          v[it] = __ldg(reinterpret_cast<const uint4 *>(p));
         } else {
           uint32_t w[4] = {0, 0, 0, 0};
 #pragma unroll
           for (int i = 0; i < 16; i++)
             if (gk + i < K) w[i >> 2] |= (uint32_t)p[i] << (8 * (i & 3));
-          v = make_uint4(w[0], w[1], w[2], w[3]);
+          v[it] = make_uint4(w[0], w[1], w[2], w[3]);
         }
       }
-      const uint2 c0 = bytes_to_bf16x4<SIGNED>(v.x), c1 = bytes_to_bf16x4<SIGNED>(v.y);
-      const uint2 c2 = bytes_to_bf16x4<SIGNED>(v.z), c3 = bytes_to_bf16x4<SIGNED>(v.w);
+    }
+#pragma unroll
+    for (int it = 0; it < 4; it++) {
+      const int r = (tid >> 3) + 32 * (it & 1), kk = (tid & 7) * 16 + 128 * (it >> 1);
+      const int64_t gr = r0 + r, gk = k0 + kk;
+      if (gr >= op.R) continue;
+      const uint2 c0 = bytes_to_bf16x4<SIGNED>(v[it].x), c1 = bytes_to_bf16x4<SIGNED>(v[it].y);
+      const uint2 c2 = bytes_to_bf16x4<SIGNED>(v[it].z), c3 = bytes_to_bf16x4<SIGNED>(v[it].w);
       uint4 *d = reinterpret_cast<uint4 *>(op.dst + gr * Kp + gk);
       d[0] = make_uint4(c0.x, c0.y, c1.x, c1.y);
       d[1] = make_uint4(c2.x, c2.y, c3.x, c3.y);
@@ -176,30 +185,37 @@ int8_pair_to_bf16(I8Operand a, I8Operand b, int64_t K, int64_t Kp, int64_t block
   }
   if (op.rs_row == 1) {
     const int warp = tid >> 5, lane = tid & 31;
+    uint32_t w[kCvtK / 64][4];
 #pragma unroll
-    for (int it = 0; it < 2; it++) {   // a warp: 8 row quads x 4 k quads
+    for (int it = 0; it < kCvtK / 64; it++) {   // a warp: 8 row quads x 4 k quads
+      const int grp = warp + 8 * it;
+      const int rq = (grp & 1) * 8 + (lane & 7), kq = (grp >> 1) * 4 + (lane >> 3);
+      const int64_t gr = r0 + 4 * rq, gk = k0 + 4 * kq;
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        w[it][i] = 0;
+        if (gr < op.R && gk + i < K) {
+          const uint8_t *p = src + (gk + i) * op.rs_k + gr;
+          if (gr + 4 <= op.R && (reinterpret_cast<uintptr_t>(p) & 3) == 0) {
+            w[it][i] = __ldg(reinterpret_cast<const uint32_t *>(p));
+          } else {
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+              if (gr + j < op.R) w[it][i] |= (uint32_t)p[j] << (8 * j);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int it = 0; it < kCvtK / 64; it++) {
       const int grp = warp + 8 * it;
       const int rq = (grp & 1) * 8 + (lane & 7), kq = (grp >> 1) * 4 + (lane >> 3);
       const int64_t gr = r0 + 4 * rq, gk = k0 + 4 * kq;
       if (gr >= op.R) continue;
-      uint32_t w[4];
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        w[i] = 0;
-        if (gk + i < K) {
-          const uint8_t *p = src + (gk + i) * op.rs_k + gr;
-          if (gr + 4 <= op.R && (reinterpret_cast<uintptr_t>(p) & 3) == 0) {
-            w[i] = *reinterpret_cast<const uint32_t *>(p);
-          } else {
-#pragma unroll
-            for (int j = 0; j < 4; j++)
-              if (gr + j < op.R) w[i] |= (uint32_t)p[j] << (8 * j);
-          }
-        }
-      }
-      // w[i] holds rows gr..gr+3 at k = gk + i; o[j] holds k = gk..gk+3 of row gr + j
-      const uint32_t lo01 = __byte_perm(w[0], w[1], 0x5140), hi01 = __byte_perm(w[0], w[1], 0x7362);
-      const uint32_t lo23 = __byte_perm(w[2], w[3], 0x5140), hi23 = __byte_perm(w[2], w[3], 0x7362);
+      // w[it][i] holds rows gr..gr+3 at k = gk + i; o[j] holds k = gk..gk+3 of row gr + j
+      const uint32_t *x = w[it];
+      const uint32_t lo01 = __byte_perm(x[0], x[1], 0x5140), hi01 = __byte_perm(x[0], x[1], 0x7362);
+      const uint32_t lo23 = __byte_perm(x[2], x[3], 0x5140), hi23 = __byte_perm(x[2], x[3], 0x7362);
       const uint32_t o[4] = {__byte_perm(lo01, lo23, 0x5410), __byte_perm(lo01, lo23, 0x7632),
                              __byte_perm(hi01, hi23, 0x5410), __byte_perm(hi01, hi23, 0x7632)};
 #pragma unroll
@@ -217,8 +233,8 @@ int8_pair_to_bf16(I8Operand a, I8Operand b, int64_t K, int64_t Kp, int64_t block
   }
   __syncthreads();
 #pragma unroll
-  for (int it = 0; it < 4; it++) {     // 16 threads a row, 8 k each
-    const int r = (tid >> 4) + 16 * it, kk = (tid & 15) * 8;
+  for (int it = 0; it < kCvtRows * kCvtK / 8 / 256; it++) {   // 8 k a thread
+    const int e = tid + 256 * it, r = e / (kCvtK / 8), kk = (e % (kCvtK / 8)) * 8;
     const int64_t gr = r0 + r;
     if (gr >= op.R) continue;
     const uint2 raw = *reinterpret_cast<const uint2 *>(&tile[r][kk]);
@@ -458,21 +474,9 @@ __device__ __forceinline__ float fold8_x86_f(float d, float P, bool first, bool 
   if constexpr (SIGNED) return x > 127.0f ? x - 256.0f : (x < -128.0f ? x + 256.0f : x);
   return x > 255.0f ? x - 256.0f : x;
 }
-// Stored bytes packed four a word as offset binary (int8: value + 128), so
-// that a byte turns into a float with one byte permute and one add:
-// 2^23 + byte has the byte as its low mantissa bits.
-template <bool SIGNED>
-__device__ __forceinline__ float byte_to_f(uint32_t word, int k) {
-  constexpr float kBias = 8388608.0f + (SIGNED ? 128.0f : 0.0f);
-  return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7540u + (uint32_t)k)) - kBias;
-}
-// f integral in [-128, 255]: 1.5 x 2^23 + bias + f keeps f + bias in the
-// low mantissa byte.
-template <bool SIGNED>
-__device__ __forceinline__ uint32_t f_to_bits(float f) {
-  constexpr float kMagic = 12582912.0f + (SIGNED ? 128.0f : 0.0f);
-  return __float_as_uint(f + kMagic);
-}
+// f integral in [-128, 255]: 1.5 x 2^23 + f has f mod 256 as its low
+// mantissa byte.
+__device__ __forceinline__ uint32_t f_to_bits(float f) { return __float_as_uint(f + 12582912.0f); }
 
 template <int BN> struct I8PairCfg {
   static constexpr int BN_CTA = BN / 2;
@@ -497,9 +501,10 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
                int tiles_m, int tiles_n, int rule, unsigned *status, WaitCfg wc) {
   using Cfg = I8PairCfg<BN>;
   constexpr int STAGES = Cfg::STAGES, NBUF = Cfg::NBUF, CW = Cfg::CW;
-  // slabs per TMEM chunk: a whole 512-deep block, except for uint8 under
-  // the rules that need its exact sum (two 256-deep halves)
-  constexpr int CHUNK = (SIGNED || X86) ? kBlockK / kBK : kBlockK / kBK / 2;
+  // slabs per TMEM chunk: the x86 rule folds every 512-deep block; the
+  // other rules need exact sums only, which FP32 keeps up to 2^24 (int8:
+  // 1024-deep chunks, |sum| <= 1024 * 128^2 = 2^24; uint8: 256-deep ones)
+  constexpr int CHUNK = X86 ? kBlockK / kBK : SIGNED ? 2 * kBlockK / kBK : kBlockK / kBK / 2;
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *bars = (uint64_t *)(smem + STAGES * Cfg::STAGE_BYTES);
@@ -542,7 +547,9 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
   tc::cluster_sync();   // peer barriers initialised
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const int nchunks = num_kb / CHUNK;   // per tile; num_kb is a multiple of the block
+  // per tile; num_kb is a multiple of the 512-deep block (8 slabs), and a
+  // 1024-deep chunk may end early at the last slab
+  const int nchunks = (num_kb + CHUNK - 1) / CHUNK;
 
   if (warp == 0) {
     if (lane == 0) {
@@ -580,7 +587,8 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
       for (int t = first_tile; t < ntiles && live; t += tile_step) {
         for (int kb = 0; kb < num_kb; kb++, g++) {
           const int s = g % STAGES, buf = chunk % NBUF;
-          const bool cstart = kb % CHUNK == 0, cend = kb % CHUNK == CHUNK - 1;
+          const bool cstart = kb % CHUNK == 0;
+          const bool cend = kb % CHUNK == CHUNK - 1 || kb == num_kb - 1;
           if (cstart && chunk >= NBUF &&
               !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / NBUF) & 1) ^ 1,
                                      status, kStatusTimeoutMma, wc.limit_ns)) {
@@ -626,11 +634,11 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
       tile_origin(t, m0, n0);
       const int mr = m0 + (int)rank * kBM;   // this CTA's 128 rows
       const int row = mr + quad * 32 + lane;
-      // x86 rule: the stored bytes so far, packed four a word (every fold
-      // leaves a byte; int8 as value + 128); other rules: the wrapped int32
-      // sums
+      // x86 rule: the stored values so far as bfloat16 pairs (every fold
+      // leaves an integer in [-128, 255], exact in bfloat16); other rules:
+      // the wrapped int32 sums
       int32_t d[X86 ? 1 : CW];
-      uint32_t d8[X86 ? CW / 4 : 1];
+      uint32_t d16[X86 ? CW / 2 : 1];
       uint64_t fullmask = 0;   // x86 rule: columns inside numc's full 6x16 tiles
       const bool row_full = X86 && simt::x86_row_full(row, M);
 #pragma unroll
@@ -642,7 +650,7 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
         }
       }
 #pragma unroll
-      for (int q = 0; q < (X86 ? CW / 4 : 1); q++) d8[q] = SIGNED ? 0x80808080u : 0u;
+      for (int q = 0; q < (X86 ? CW / 2 : 1); q++) d16[q] = 0;
       // warp-uniform: every column of every lane inside numc's full tiles
       const bool all_full = X86 && __all_sync(0xffffffffu, fullmask == ~0ull >> (64 - CW));
       for (int c = 0; c < nchunks; c++, chunk++) {
@@ -653,40 +661,43 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
         if (!ok) break;
         tc::tc_fence_after();
         const bool first = c == 0;
+        const uint32_t taddr = tmem + lane_off + buf * BN + cbase;
+        if constexpr (X86) {
+          // 32 columns per TMEM wait; the tile class decided outside the loop
+          auto drain = [&](auto full_tag) {
+            constexpr bool ALL_FULL = decltype(full_tag)::value;
 #pragma unroll
-        for (int c0 = 0; c0 < CW; c0 += 16) {
-          uint32_t r[16];
-          tc::tmem_ld_32x32b_x16(tmem + lane_off + buf * BN + cbase + c0, r);
-          tc::tmem_ld_wait();
-          if constexpr (X86) {
-            if (all_full) {   // warp-uniform branch: d = sat(d + P)
+            for (int c0 = 0; c0 < CW; c0 += 32) {
+              uint32_t r[32];
+              tc::tmem_ld_32x32b_x16(taddr + c0, *reinterpret_cast<uint32_t(*)[16]>(&r[0]));
+              tc::tmem_ld_32x32b_x16(taddr + c0 + 16, *reinterpret_cast<uint32_t(*)[16]>(&r[16]));
+              tc::tmem_ld_wait();
 #pragma unroll
-              for (int wq = 0; wq < 4; wq++) {
-                const int q0 = c0 + 4 * wq;
-                uint32_t b[4];
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                  const float P = __uint_as_float(r[4 * wq + k]);
-                  b[k] = f_to_bits<SIGNED>(sat8_f<SIGNED>(byte_to_f<SIGNED>(d8[q0 >> 2], k) + P));
+              for (int h = 0; h < 16; h++) {
+                const int q = (c0 >> 1) + h;   // bfloat16 pair: columns 2q, 2q + 1
+                const float p0 = __uint_as_float(r[2 * h]), p1 = __uint_as_float(r[2 * h + 1]);
+                const float v0 = __uint_as_float(d16[q] << 16);
+                const float v1 = __uint_as_float(d16[q] & 0xffff0000u);
+                float f0, f1;
+                if constexpr (ALL_FULL) {   // d = sat(d + P)
+                  f0 = sat8_f<SIGNED>(v0 + p0);
+                  f1 = sat8_f<SIGNED>(v1 + p1);
+                } else {
+                  f0 = fold8_x86_f<SIGNED>(v0, p0, first, (fullmask >> (2 * q)) & 1ull);
+                  f1 = fold8_x86_f<SIGNED>(v1, p1, first, (fullmask >> (2 * q + 1)) & 1ull);
                 }
-                d8[q0 >> 2] = pack4((int32_t)b[0], (int32_t)b[1], (int32_t)b[2], (int32_t)b[3]);
-              }
-            } else {
-#pragma unroll
-              for (int wq = 0; wq < 4; wq++) {
-                const int q0 = c0 + 4 * wq;
-                uint32_t b[4];
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                  const float P = __uint_as_float(r[4 * wq + k]);
-                  const float prev = byte_to_f<SIGNED>(d8[q0 >> 2], k);
-                  b[k] = f_to_bits<SIGNED>(
-                      fold8_x86_f<SIGNED>(prev, P, first, (fullmask >> (q0 + k)) & 1ull));
-                }
-                d8[q0 >> 2] = pack4((int32_t)b[0], (int32_t)b[1], (int32_t)b[2], (int32_t)b[3]);
+                d16[q] = __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
               }
             }
-          } else {
+          };
+          if (all_full) drain(std::true_type{});   // warp-uniform
+          else drain(std::false_type{});
+        } else {
+#pragma unroll
+          for (int c0 = 0; c0 < CW; c0 += 16) {
+            uint32_t r[16];
+            tc::tmem_ld_32x32b_x16(taddr + c0, r);
+            tc::tmem_ld_wait();
 #pragma unroll
             for (int j = 0; j < 16; j++)
               d[c0 + j] = (int32_t)((uint32_t)d[c0 + j] +
@@ -701,7 +712,13 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
       uint32_t w[CW / 4];
       if constexpr (X86) {
 #pragma unroll
-        for (int q = 0; q < CW / 4; q++) w[q] = SIGNED ? d8[q] ^ 0x80808080u : d8[q];
+        for (int q = 0; q < CW / 4; q++) {
+          const uint32_t a = d16[2 * q], b = d16[2 * q + 1];
+          w[q] = pack4((int32_t)f_to_bits(__uint_as_float(a << 16)),
+                       (int32_t)f_to_bits(__uint_as_float(a & 0xffff0000u)),
+                       (int32_t)f_to_bits(__uint_as_float(b << 16)),
+                       (int32_t)f_to_bits(__uint_as_float(b & 0xffff0000u)));
+        }
       } else {
         if (row < M) {
 #pragma unroll
