@@ -141,6 +141,7 @@ template <bool SIGNED>
 __global__ void __launch_bounds__(256)
 int8_pair_to_bf16(I8Operand a, I8Operand b, int64_t K, int64_t Kp, int64_t blocks_a) {
   __shared__ __align__(16) uint8_t tile[kCvtRows][kCvtK + 16];
+  tc::griddep_launch_dependents();   // the GEMM may launch and set up meanwhile
   int64_t blk = blockIdx.x;
   const I8Operand &op = blk < blocks_a ? a : b;
   if (blk >= blocks_a) blk -= blocks_a;
@@ -292,6 +293,7 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  tc::griddep_wait();   // the conversion pass has completed
 
   if (warp == 0) {
     if (lane == 0) {
@@ -547,6 +549,7 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
   tc::cluster_sync();   // peer barriers initialised
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  tc::griddep_wait();   // the conversion pass has completed
   // per tile; num_kb is a multiple of the 512-deep block (8 slabs), and a
   // 1024-deep chunk may end early at the last slab
   const int nchunks = (num_kb + CHUNK - 1) / CHUNK;
@@ -782,9 +785,21 @@ cudaError_t launch_i8_gemm(const Gemm &g, int rule, const I8Layout &L, __nv_bflo
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM)))
     return e;
   const int tiles_m = (int)((g.M + kBM - 1) / kBM), tiles_n = (int)((g.N + kBN - 1) / kBN);
-  int8_tc_gemm<SIGNED, kBN><<<tiles_m * tiles_n, Cfg::kThreads, SMEM, s>>>(
-      ta, tb, (uint8_t *)g.c, g.rso, g.cso, (int)g.M, (int)g.N, (int)(L.Kp / kBK), tiles_m,
-      tiles_n, rule, status, wait_cfg());
+  // programmatic dependent launch: set up while the conversion pass ends
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+  cfg.gridDim = dim3((unsigned)(tiles_m * tiles_n));
+  cfg.blockDim = dim3(Cfg::kThreads);
+  cfg.dynamicSmemBytes = SMEM;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if ((e = cudaLaunchKernelEx(&cfg, int8_tc_gemm<SIGNED, kBN>, ta, tb, (uint8_t *)g.c, g.rso,
+                              g.cso, (int)g.M, (int)g.N, (int)(L.Kp / kBK), tiles_m, tiles_n,
+                              rule, status, wait_cfg())))
+    return e;
   count_launch();
   return cudaGetLastError();
 }
@@ -807,11 +822,14 @@ cudaError_t launch_i8_pair(const Gemm &g, int rule, const I8Layout &L, const __n
   const int tiles_m = (int)((g.M + 2 * kBM - 1) / (2 * kBM));
   const int tiles_n = (int)((g.N + BN - 1) / BN);
   cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = 2;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
+  // programmatic dependent launch: set up while the conversion pass ends
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
   cfg.blockDim = dim3(Cfg::THREADS);
   cfg.dynamicSmemBytes = Cfg::SMEM;
   cfg.stream = s;
@@ -822,6 +840,7 @@ cudaError_t launch_i8_pair(const Gemm &g, int rule, const I8Layout &L, const __n
   if (pairs <= 0) pairs = std::max(1, sm_count() / 2);
   pairs = std::min(pairs, tiles_m * tiles_n);
   cfg.gridDim = dim3((unsigned)(2 * pairs));
+  cfg.numAttrs = 2;
   e = cudaLaunchKernelEx(&cfg, kern, ta, tb, (uint8_t *)g.c, (int64_t)g.rso, (int64_t)g.cso,
                          (int)g.M, (int)g.N, (int)(L.Kp / kBK), tiles_m, tiles_n, rule, status,
                          wait_cfg());

@@ -40,6 +40,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdint>
+#include <cstdlib>
 #include <mutex>
 
 #include "kernels.h"
@@ -63,6 +64,16 @@ int sm_count() {
     cached[dev] = n > 0 ? n : 148;
   }
   return cached[dev];
+}
+
+// Programmatic dependent launch of the GEMM kernels after their operand
+// passes (on unless NUMC_CUDA_PDL=0; read once).
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char *v = getenv("NUMC_CUDA_PDL");
+    return !(v && v[0] == '0');
+  }();
+  return on;
 }
 
 // Co-resident clusters of `kern` launched with `cfg` (0 if the query fails).
@@ -91,6 +102,7 @@ split_planes(const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int64_
                unsigned long long *flags, int flag_rows, unsigned long long gen,
                const unsigned *maxbits) {
   __shared__ __align__(16) float tile[kSplitRows][kSplitK + 4];
+  tc::griddep_launch_dependents();   // the GEMM may launch and set up meanwhile
   split_tile<PLANES, F16, MODE>(src, rs_row, rs_k, R, K, Kp, planes, flags, flag_rows, gen,
                                 MODE, (int64_t)blockIdx.y * kSplitRows,
                                 (int64_t)blockIdx.x * kSplitK, tile, maxbits);
@@ -122,6 +134,7 @@ scale_split_pair(const float *A, int64_t rsa, int64_t csa, int M, const float *B
                  int64_t rsb, int64_t csb, int N, int K, int Kp, uint16_t *pa, uint16_t *pb,
                  unsigned long long *fa, unsigned long long *fbl, unsigned *max_a,
                  unsigned *max_b, unsigned long long gen) {
+  tc::griddep_launch_dependents();   // the GEMM may launch and set up meanwhile
   const int a_blocks = (M + kFusedRows - 1) / kFusedRows;
   const bool is_a = (int)blockIdx.x < a_blocks;
   fused_scale_split_rows(is_a ? A : B, is_a ? rsa : csb, is_a ? csa : rsb, is_a ? M : N, K, Kp,
@@ -270,6 +283,7 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
   if constexpr (PAIR) tc::cluster_sync();   // peer barriers initialised
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  tc::griddep_wait();   // the split pass has completed
   const int num_chunks = (num_kb + FLUSH - 1) / FLUSH;   // per tile
 
   if (warp == 0) {
@@ -681,18 +695,30 @@ cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, cons
   fb.bias = (const float *)g.bias;
   fb.bias_stride = g.bias_stride;
   const int num_kb = (int)(L.Kp / kBK);
+  // programmatic dependent launch: the GEMM sets up while the split pass ends
+  cudaLaunchAttribute pdl;
+  pdl.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  pdl.val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
   if (CTAS == 1) {
-    const int grid = std::min(tiles_m * tiles_n, sm_count());
-    kern<<<grid, Cfg::THREADS, Cfg::SMEM, s>>>(ta, tb, (float *)g.c, g.rso, g.cso, (int)g.M,
-                                               (int)g.N, num_kb, tiles_m, tiles_n, vec4, status,
-                                               fb, wait_cfg());
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)std::min(tiles_m * tiles_n, sm_count()));
+    cfg.blockDim = dim3(Cfg::THREADS);
+    cfg.dynamicSmemBytes = Cfg::SMEM;
+    cfg.stream = s;
+    cfg.attrs = &pdl;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, kern, ta, tb, (float *)g.c, (int64_t)g.rso, (int64_t)g.cso,
+                           (int)g.M, (int)g.N, num_kb, tiles_m, tiles_n, vec4, status, fb,
+                           wait_cfg());
+    if (e != cudaSuccess) return e;
   } else {
     cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = CTAS;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
+    attr[1] = pdl;
     cfg.blockDim = dim3(Cfg::THREADS);
     cfg.dynamicSmemBytes = Cfg::SMEM;
     cfg.stream = s;
@@ -711,6 +737,7 @@ cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, cons
     }
     pairs = std::min(pairs, tiles_m * tiles_n);
     cfg.gridDim = dim3((unsigned)(CTAS * pairs));
+    cfg.numAttrs = 2;
     e = cudaLaunchKernelEx(&cfg, kern, ta, tb, (float *)g.c, (int64_t)g.rso, (int64_t)g.cso,
                            (int)g.M, (int)g.N, num_kb, tiles_m, tiles_n, vec4, status, fb,
                            wait_cfg());

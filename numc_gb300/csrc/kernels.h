@@ -162,6 +162,9 @@ cudaError_t dev_malloc(void **p, size_t bytes);
 
 // Streaming multiprocessors of the current device (cached per device).
 int sm_count();
+// Programmatic dependent launch of GEMM kernels after their operand passes
+// (on unless the environment sets NUMC_CUDA_PDL=0).
+bool pdl_enabled();
 // Co-resident clusters of `kern` launched with `cfg` (0 if the query fails).
 int max_active_clusters(const void *kern, const cudaLaunchConfig_t &cfg);
 

@@ -76,6 +76,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
   }
 }
 
+// ---- programmatic dependent launch ---------------------------------------------
+// A kernel launched with cudaLaunchAttributeProgrammaticStreamSerialization
+// may start while the previous kernel in the stream still runs; it calls
+// griddep_wait() before touching anything that kernel writes (the wait
+// returns once that grid has completed and its writes are visible; it is a
+// no-op for a kernel launched without the attribute).  The previous kernel
+// calls griddep_launch_dependents() once all of its blocks are resident, so
+// the dependent grid's launch and prologue overlap its tail.
+__device__ __forceinline__ void griddep_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void griddep_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ---- TMA ----------------------------------------------------------------------
 
 __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap *m) {
