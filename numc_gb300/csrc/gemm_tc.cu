@@ -484,37 +484,43 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
               C[(int64_t)row * rso + (int64_t)(n0 + c0 + j) * cso] =
                   fb.bias ? __fadd_rn(f[j], fb.bias[(int64_t)(n0 + c0 + j) * fb.bias_stride]) : f[j];
         }
-      } else if (row < M) {
-        if constexpr (F16) {
-          // Undo the row and column scaling, acc * 2^-(sa + sb) correctly
-          // rounded: float multiplies by powers of two when every exponent
-          // is a normal float32's (the product then rounds once, if at all),
-          // else the product in double (exact: acc has 24 bits) rounded
-          // once to float.  Column exponents come from the warp's table.
-          const int sa = f16_scale_exp(fb.max_a[row]);
-          bool in_range = true;
+      } else {   // warp-uniform branch (nonfinite is per tile)
+        if (row < M) {
+          if constexpr (F16) {
+            // Undo the row and column scaling, acc * 2^-(sa + sb) correctly
+            // rounded: float multiplies by powers of two when every exponent
+            // is a normal float32's (the product then rounds once, if at
+            // all), else the product in double (exact: acc has 24 bits)
+            // rounded once to float.  Column exponents come from the warp's
+            // table.
+            const int sa = f16_scale_exp(fb.max_a[row]);
+            bool in_range = true;
 #pragma unroll 8
-          for (int j = 0; j < CW; j++) {
-            const int e = -(sa + colexp[j]);
-            in_range &= e >= -126 && e <= 127;
+            for (int j = 0; j < CW; j++) {
+              const int e = -(sa + colexp[j]);
+              in_range &= e >= -126 && e <= 127;
+            }
+            if (in_range) {
+#pragma unroll
+              for (int j = 0; j < CW; j++) acc[j] *= exp2_int(-(sa + colexp[j]));
+            } else {
+#pragma unroll
+              for (int j = 0; j < CW; j++)
+                acc[j] = (float)((double)acc[j] * exp2_dbl(-(sa + colexp[j])));
+            }
           }
-          if (in_range) {
+          if (fb.bias) {
 #pragma unroll
-            for (int j = 0; j < CW; j++) acc[j] *= exp2_int(-(sa + colexp[j]));
-          } else {
-#pragma unroll
-            for (int j = 0; j < CW; j++)
-              acc[j] = (float)((double)acc[j] * exp2_dbl(-(sa + colexp[j])));
+            for (int j = 0; j < CW; j++) {
+              const int col = n0 + cbase + j;
+              if (col < N) acc[j] = __fadd_rn(acc[j], fb.bias[(int64_t)col * fb.bias_stride]);
+            }
           }
         }
-        if (fb.bias) {
-#pragma unroll
-          for (int j = 0; j < CW; j++) {
-            const int col = n0 + cbase + j;
-            if (col < N) acc[j] = __fadd_rn(acc[j], fb.bias[(int64_t)col * fb.bias_stride]);
-          }
-        }
-        if (!(Cfg::EPI_STAGE && cso == 1)) {
+        if (Cfg::EPI_STAGE && cso == 1) {   // warp-uniform: every lane stores
+          __syncwarp();
+          store_rows_coalesced<CW>(acc, stage, C, rso, mr + quad * 32, n0 + cbase, M, N, lane);
+        } else if (row < M) {
           float *crow = C + (int64_t)row * rso;
 #pragma unroll
           for (int c0 = 0; c0 < CW; c0 += 32) {
@@ -531,12 +537,6 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
                 if (nb + j < N) crow[(int64_t)(nb + j) * cso] = acc[c0 + j];
             }
           }
-        }
-      }
-      if constexpr (Cfg::EPI_STAGE) {
-        if (!nonfinite && cso == 1) {   // warp-uniform: every lane stores
-          __syncwarp();
-          store_rows_coalesced<CW>(acc, stage, C, rso, mr + quad * 32, n0 + cbase, M, N, lane);
         }
       }
       __syncwarp();   // reconverge before the next tile's tcgen05.ld
