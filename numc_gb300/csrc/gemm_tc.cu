@@ -89,7 +89,7 @@ int max_active_clusters(const void *kern, const cudaLaunchConfig_t &cfg) {
 namespace {
 
 constexpr int kBM = 128, kBK = 64;
-constexpr int kFusedMaxKp = 1024;   // single problems: fused scale + split up to this K
+constexpr int kFusedMaxKp = kFusedRegKp;   // single problems: fused scale + split up to this K
 
 __host__ __device__ inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
@@ -759,10 +759,43 @@ cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, cons
 // each CTA holding 128 rows of B^T, 3 stages of 64 KiB) or single CTAs
 // (128 x 256, 2 stages of 96 KiB).  Three planes need 128-column tiles to
 // fit a ring of at least two stages.
+// K slabs per TMEM chain for scaled float16 planes.  Measured at 8192^3 on
+// GB300 with CTA pairs and 256 x 256 tiles (N(0,1) and row/column-scaled
+// 10^U(-4,4) inputs, 512 outputs against a float64 reference; max / mean
+// relative error; plain FP32 FMA 1.3e-3 / 5.6e-6, ill-scaled 7.5e-4 /
+// 5.6e-6; TFLOP/s of the whole call):
+//   1 slab  346 TFLOP/s   2.1e-5 / 8.2e-7
+//   2 slabs 485           1.2e-4 / 1.5e-6
+//   4 slabs 519           4.2e-4 / 3.5e-6   (ill-scaled 5.0e-4 / 3.0e-6)
+//   8 slabs 537           6.9e-4 / 5.7e-6   (ill-scaled 1.0e-3 / 6.5e-6)
+// 4 is the fastest that stays at or below the FP32 FMA chain's error on
+// both inputs.
+constexpr int kF16DefaultFlush = 4;
+
+// Output tile width of the float16-plane GEMM: 256 columns, or 128 when
+// the 256-column tiles would leave more than half of the CTA pairs idle
+// (small problems: twice the SMs share the multiply).  Every output is the
+// same either way.  NUMC_CUDA_SPLIT_TILE=128 or 256 pins it (read once).
+int split_tile_width(const Gemm &g, int ctas) {
+  static const int forced = [] {
+    const char *e = getenv("NUMC_CUDA_SPLIT_TILE");
+    return e ? atoi(e) : 0;
+  }();
+  if (forced == 128 || forced == 256) return forced;
+  const int64_t rows = 128 * ctas;
+  const int64_t wide = (g.M + rows - 1) / rows * ((g.N + 255) / 256);
+  return 2 * wide < sm_count() / ctas ? 128 : 256;
+}
+
 template <int CTAS>
 cudaError_t launch_gemm_ctas(const SplitLayout &L, const SplitBufs &ws, const Gemm &g,
-                             unsigned long long gen, unsigned *status, cudaStream_t s) {
+                             unsigned long long gen, unsigned *status, cudaStream_t s,
+                             bool narrow) {
   constexpr int S2 = CTAS == 2 ? 3 : 2;   // stages of the 2-plane ring
+  if (L.f16 && L.flush == kF16DefaultFlush && narrow)
+    // 128-column tiles: 48 KiB (pair) or 64 KiB (single CTA) stages
+    return launch_gemm_status<128, CTAS == 2 ? 4 : 3, 2, kF16DefaultFlush, true, CTAS>(
+        L, ws, g, gen, status, s);
   if (L.f16) {
     switch (L.flush) {
     case 1: return launch_gemm_status<256, S2, 2, 1, true, CTAS>(L, ws, g, gen, status, s);
@@ -788,26 +821,19 @@ int split_ctas() {
   return v;
 }
 
+// Small problems that take 128-column tiles run them on single CTAs
+// (measured on GB300 at 512^3 - 1536^3: 0.5-0.7 us faster than pairs).
 cudaError_t launch_gemm(const SplitLayout &L, const SplitBufs &ws, const Gemm &g, unsigned long long gen,
                         unsigned *status, cudaStream_t s) {
-  if (split_ctas() == 2) return launch_gemm_ctas<2>(L, ws, g, gen, status, s);
-  return launch_gemm_ctas<1>(L, ws, g, gen, status, s);
+  const int ctas = split_ctas();
+  const bool narrow = split_tile_width(g, ctas) == 128;
+  if (ctas == 2 && !(narrow && L.f16 && L.flush == kF16DefaultFlush))
+    return launch_gemm_ctas<2>(L, ws, g, gen, status, s, narrow);
+  return launch_gemm_ctas<1>(L, ws, g, gen, status, s, narrow);
 }
 
 int planes_for(int passes) { return passes == 6 ? 3 : 2; }
 
-// K slabs per TMEM chain for scaled float16 planes.  Measured at 8192^3 on
-// GB300 with CTA pairs and 256 x 256 tiles (N(0,1) and row/column-scaled
-// 10^U(-4,4) inputs, 512 outputs against a float64 reference; max / mean
-// relative error; plain FP32 FMA 1.3e-3 / 5.6e-6, ill-scaled 7.5e-4 /
-// 5.6e-6; TFLOP/s of the whole call):
-//   1 slab  346 TFLOP/s   2.1e-5 / 8.2e-7
-//   2 slabs 485           1.2e-4 / 1.5e-6
-//   4 slabs 519           4.2e-4 / 3.5e-6   (ill-scaled 5.0e-4 / 3.0e-6)
-//   8 slabs 537           6.9e-4 / 5.7e-6   (ill-scaled 1.0e-3 / 6.5e-6)
-// 4 is the fastest that stays at or below the FP32 FMA chain's error on
-// both inputs.
-constexpr int kF16DefaultFlush = 4;
 
 }  // namespace
 

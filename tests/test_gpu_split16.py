@@ -181,3 +181,41 @@ def test_special_values():
     got2 = _run(a2, b)
     assert np.isnan(got2[0]).all()
     np.testing.assert_array_equal(got2[1], oracle.matmul(a2, b)[1])
+
+
+_TILE_SCRIPT = r"""
+import sys
+import numpy as np, torch
+import numc_gb300 as nc
+from numc_gb300 import synth
+out = []
+for (M, K, N), kind in [((512, 512, 512), "normal"), ((300, 1500, 260), "illscaled"),
+                        ((700, 900, 600), "uniform"), ((2000, 300, 1100), "normal")]:
+    a, b = synth.operands(kind, M, K, N, dtype="float32", seed=M + N)
+    c = torch.full((M, N), float("nan"), device="cuda")
+    nc.gemm(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(), c, algo=nc.ALGO_SPLIT_FP16)
+    nc.check_status()
+    out.append(c.cpu().numpy().ravel())
+np.save(sys.argv[1], np.concatenate(out))
+"""
+
+
+@pytest.mark.parametrize("ctas", ["1", "2"])
+def test_tile_widths_store_identical_bits(tmp_path, ctas):
+    """128- and 256-column tiles (single CTAs and CTA pairs) run the same
+    per-output arithmetic: identical bits, including shapes where the
+    default picks either width."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    res = {}
+    for width in ("128", "256"):
+        env = dict(os.environ, NUMC_CUDA_SPLIT_TILE=width, NUMC_CUDA_SPLIT_CTAS=ctas)
+        path = str(tmp_path / f"c{width}.npy")
+        r = subprocess.run([sys.executable, "-c", _TILE_SCRIPT, path], env=env, cwd=root,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        res[width] = np.load(path)
+    assert np.isfinite(res["128"]).all()
+    np.testing.assert_array_equal(res["128"].view(np.uint32), res["256"].view(np.uint32))
