@@ -709,7 +709,8 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
         }
         tc::tc_fence_before();
         __syncwarp();
-        if (lane == 0) tc::mbar_arrive_cluster(tc::mapa_shared(tc::smem_u32(&tempty[buf]), 0));
+        if (lane == 0)   // the buffer's loads completed at tcgen05.wait::ld
+          tc::mbar_arrive_cluster_relaxed(tc::mapa_shared(tc::smem_u32(&tempty[buf]), 0));
       }
       if (!ok) break;
       uint32_t w[CW / 4];

@@ -46,6 +46,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <atomic>
+#include <cstdlib>
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -404,6 +406,308 @@ ozaki_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
   }
 }
 
+// ---- CTA pairs -------------------------------------------------------------------
+//
+// The default GEMM: clusters of two CTAs walk 256 x 128 output tiles
+// persistently; each CTA loads its 128 rows of A_p and 64 rows of B_q^T per
+// 64-deep slab (24 KiB, against 32 KiB for the same multiply-adds on one
+// CTA) and the even CTA's MMA thread multiplies both halves with
+// cta_group::2 MMAs.  TMEM per CTA: two 128-column FP32 chunk buffers and
+// 256 columns holding the 128 x 128 int64 Horner accumulators (low word,
+// high word), so that the accumulator threads keep only a diagonal's
+// partial sums in registers, as two FP32 integers per output: each chunk
+// sum S (an integer below 2^24) is split as S = 4096 h + l with
+// h = round(S / 4096) and |l| <= 2048 (one FMA and one add each, exact),
+// and H += h, L += l stay exact for up to 2048 chunks.  The float-to-int
+// conversions (a quarter of the FP32 rate) run once per diagonal instead
+// of once per chunk.  At a diagonal's end: acc = acc * 2^8 + round((4096 H
+// + L) / 2^drop), with the same bit-drop rule as the single-CTA kernel but
+// rounding the diagonal's sum once (never less accurate).
+constexpr int kPairBN = 128, kPairBNCta = 64;
+constexpr int kPairStages = 8;              // 24 KiB a stage
+constexpr int kPairNumBuf = 2;              // 2 x 128 TMEM columns of chunk sums
+constexpr uint32_t kPairAccCol = 256;       // int64 accumulators: columns 256..511
+constexpr int kPairFlushChunks = 2048;      // H, L exact up to here
+
+__global__ void __launch_bounds__(kThreads, 1)
+ozaki_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB,
+                double *__restrict__ C, int64_t rso, int64_t cso, int M, int N, int num_kb,
+                int tiles_m, int tiles_n, unsigned *status, OzParams op, WaitCfg wc) {
+  constexpr uint32_t A_BYTES = kBM * kBK * 2, B_BYTES = kPairBNCta * kBK * 2;
+  constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+  constexpr int NBUF = kPairNumBuf;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *bars = (uint64_t *)(smem + kPairStages * STAGE_BYTES);
+  uint64_t *full = bars, *empty = bars + kPairStages;
+  uint64_t *tfull = bars + 2 * kPairStages, *tempty = tfull + NBUF;
+  uint64_t *drain = tempty + NBUF;   // all issued MMAs complete
+  uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int s = op.slices;
+  const int ntiles = tiles_m * tiles_n;
+  const uint32_t rank = tc::cluster_ctarank();
+  const bool leader = rank == 0;
+  const int first_tile = blockIdx.x / 2, tile_step = gridDim.x / 2;
+  auto tile_origin = [&](int t, int &m0, int &n0) {
+    constexpr int GM = 8;   // 2048 rows of pair tiles
+    const int group = t / (GM * tiles_n);
+    const int first_m = group * GM;
+    const int gm = min(tiles_m - first_m, GM);
+    const int local = t - group * GM * tiles_n;
+    m0 = (first_m + local % gm) * (2 * kBM);
+    n0 = (local / gm) * kPairBN;
+  };
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kPairStages; i++) {
+      tc::mbar_init(tc::smem_u32(&full[i]), 1);
+      tc::mbar_init(tc::smem_u32(&empty[i]), 1);
+    }
+    for (int b = 0; b < NBUF; b++) {
+      tc::mbar_init(tc::smem_u32(&tfull[b]), 1);
+      tc::mbar_init(tc::smem_u32(&tempty[b]), kAccWarps * 2);   // both CTAs' warps
+    }
+    tc::mbar_init(tc::smem_u32(drain), 1);
+    tc::fence_barrier_init();
+    tc::tma_prefetch_desc(&tA);
+    tc::tma_prefetch_desc(&tB);
+  }
+  if (warp == 1) tc::tmem_alloc_pair(tc::smem_u32(tmem_slot), 512);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::cluster_sync();   // peer barriers initialised
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  tc::griddep_wait();   // the slicing passes have completed
+
+  // Stage sequence per tile: diagonal D = 0..s-1, K slab kb, pair (p, D - p);
+  // a chunk is up to kChunkSlabs consecutive stages of one diagonal.
+  if (warp == 0) {
+    if (lane == 0) {
+      int g = 0;   // stage counter across tiles
+      bool live = true;
+      for (int t = first_tile; t < ntiles && live; t += tile_step) {
+        int m0, n0;
+        tile_origin(t, m0, n0);
+        const int ma = m0 + (int)rank * kBM, nb = n0 + (int)rank * kPairBNCta;
+        for (int D = 0; D < s && live; D++)
+          for (int kb = 0; kb < num_kb && live; kb++)
+            for (int p = 0; p <= D; p++, g++) {
+              const int st = g % kPairStages;
+              if (g >= kPairStages &&
+                  !tc::mbar_wait_bounded(tc::smem_u32(&empty[st]), ((g / kPairStages) & 1) ^ 1,
+                                         status, kStatusTimeoutProducer, wc.limit_ns)) {
+                live = false;
+                break;
+              }
+              if (wc.starve) continue;   // give-up test: no load, no barrier completes
+              const uint32_t fbar = tc::smem_u32(&full[st]);
+              const uint32_t sa = tc::smem_u32(smem + st * STAGE_BYTES);
+              // the even CTA's full barrier counts the bytes of both CTAs
+              if (leader) tc::mbar_arrive_expect_tx(fbar, 2 * STAGE_BYTES);
+              const uint32_t fbar_leader = tc::mapa_shared(fbar, 0);
+              tc::tma_load_3d_pair(sa, &tA, fbar_leader, kb * kBK, ma, p);
+              tc::tma_load_3d_pair(sa + A_BYTES, &tB, fbar_leader, kb * kBK, nb, D - p);
+            }
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0 && leader) {
+      constexpr uint32_t idesc = tc::idesc_bf16_f32(2 * kBM, kPairBN);
+      int g = 0, chunk = 0;
+      bool live = true;
+      for (int t = first_tile; t < ntiles && live; t += tile_step) {
+        for (int D = 0; D < s && live; D++) {
+          const int stages_d = num_kb * (D + 1);
+          for (int i = 0; i < stages_d && live; i++, g++) {
+            const int st = g % kPairStages;
+            const bool cstart = i % kChunkSlabs == 0;
+            const bool cend = i % kChunkSlabs == kChunkSlabs - 1 || i == stages_d - 1;
+            const int buf = chunk % NBUF;
+            if (cstart && chunk >= NBUF &&
+                !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / NBUF) & 1) ^ 1,
+                                       status, kStatusTimeoutMma, wc.limit_ns)) {
+              live = false;
+              break;
+            }
+            if (!tc::mbar_wait_bounded(tc::smem_u32(&full[st]), (g / kPairStages) & 1, status,
+                                       kStatusTimeoutMma, wc.limit_ns)) {
+              live = false;
+              break;
+            }
+            tc::tc_fence_after();
+            const uint32_t sa = tc::smem_u32(smem + st * STAGE_BYTES), sb = sa + A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < kBK / 16; kk++)
+              tc::mma_f16_pair(tmem + buf * kPairBN, tc::sdesc_k128(sa + kk * 32),
+                               tc::sdesc_k128(sb + kk * 32), idesc,
+                               (!cstart || kk > 0) ? 1u : 0u);
+            tc::mma_commit_pair(tc::smem_u32(&empty[st]), 0x3);
+            if (cend) {
+              tc::mma_commit_pair(tc::smem_u32(&tfull[buf]), 0x3);
+              chunk++;
+            }
+          }
+        }
+      }
+      // Every MMA issued above completes before TMEM is released, also when
+      // the loop gave up (a commit with none outstanding arrives at once).
+      tc::mma_commit_pair(tc::smem_u32(drain), 0x1);
+      tc::mbar_wait_bounded(tc::smem_u32(drain), 0, status, kStatusTimeoutDrain, wc.limit_ns);
+    }
+    __syncwarp();
+  } else {
+    constexpr int CW = kPairBN / 4;   // 32 columns per thread (the bit-drop group)
+    const int quad = warp & 3, quarter = (warp - 2) >> 2;
+    const int cbase = quarter * CW;
+    const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
+    const uint32_t acc_addr = tmem + lane_off + kPairAccCol + 2 * cbase;
+    constexpr float kMagic = 12582912.0f;   // 1.5 x 2^23: adding it rounds to an integer
+    int chunk = 0;                          // across tiles
+    bool ok = true;
+    for (int t = first_tile; t < ntiles && ok; t += tile_step) {
+      int m0, n0;
+      tile_origin(t, m0, n0);
+      const int mr = m0 + (int)rank * kBM;   // this CTA's 128 rows
+      const int row = mr + quad * 32 + lane;
+      int drop = 0;                  // low bits dropped so far (acc holds T / 2^drop)
+      unsigned long long mx = 0;     // largest |acc| of the thread after the last update
+      for (int D = 0; D < s && ok; D++) {
+        const int stages_d = num_kb * (D + 1);
+        const int nchunks = (stages_d + kChunkSlabs - 1) / kChunkSlabs;
+        // Horner step: acc *= 2^8 if it stays exact, else drop 8 more bits
+        // of this and every later diagonal.
+        bool mul = D > 0;
+        if (D > 0 && mx >= (1ull << 53)) {
+          mul = false;
+          drop += 8;
+        }
+        const int sh = drop;
+        for (int c0 = 0; c0 < nchunks && ok; c0 += kPairFlushChunks) {
+          float H[CW], L[CW];
+#pragma unroll
+          for (int j = 0; j < CW; j++) H[j] = L[j] = 0.0f;
+          const int c1 = min(nchunks, c0 + kPairFlushChunks);
+          for (int c = c0; c < c1; c++, chunk++) {
+            const int buf = chunk % NBUF;
+            ok = tc::mbar_wait_bounded(tc::smem_u32(&tfull[buf]), (chunk / NBUF) & 1, status,
+                                       kStatusTimeoutEpilogue, wc.limit_ns);
+            ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
+            if (!ok) break;
+            tc::tc_fence_after();
+#pragma unroll
+            for (int q0 = 0; q0 < CW; q0 += 8) {   // 8 columns a load: H, L hold 64 registers
+              uint32_t r[8];
+              tc::tmem_ld_32x32b_x8(tmem + lane_off + buf * kPairBN + cbase + q0, r);
+              tc::tmem_ld_wait();
+#pragma unroll
+              for (int j = 0; j < 8; j++) {
+                const float v = __uint_as_float(r[j]);               // integer, |v| < 2^24
+                const float h = __fmaf_rn(v, 1.0f / 4096.0f, kMagic) - kMagic;
+                L[q0 + j] += __fmaf_rn(-h, 4096.0f, v);               // exact, |.| <= 2048
+                H[q0 + j] += h;
+              }
+            }
+            tc::tc_fence_before();
+            __syncwarp();
+            if (lane == 0)   // the buffer's loads completed at tcgen05.wait::ld
+              tc::mbar_arrive_cluster_relaxed(tc::mapa_shared(tc::smem_u32(&tempty[buf]), 0));
+          }
+          if (!ok) break;
+          // Fold the partial sums into the int64 accumulators held in TMEM
+          // (4 outputs, 8 words, per access); the first fold of a diagonal
+          // applies its Horner step.
+          const bool first_fold = c0 == 0;
+          unsigned long long nmx = 0;
+#pragma unroll
+          for (int g4 = 0; g4 < CW / 4; g4++) {
+            uint32_t w[8];
+            if (D > 0 || !first_fold) {
+              tc::tmem_ld_32x32b_x8(acc_addr + 8 * g4, w);
+              tc::tmem_ld_wait();
+            } else {
+#pragma unroll
+              for (int i = 0; i < 8; i++) w[i] = 0;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              const int q = 4 * g4 + j;
+              long long acc = (long long)(((unsigned long long)w[2 * j + 1] << 32) | w[2 * j]);
+              if (first_fold && mul) acc *= 256;
+              const long long S = (long long)__float2int_rn(H[q]) * 4096 +
+                                  (long long)__float2int_rn(L[q]);
+              acc += sh == 0 ? S : (sh >= 63 ? 0 : ((S + (1ll << (sh - 1))) >> sh));
+              const unsigned long long a = (unsigned long long)(acc < 0 ? -acc : acc);
+              nmx = a > nmx ? a : nmx;
+              w[2 * j] = (uint32_t)acc;
+              w[2 * j + 1] = (uint32_t)((unsigned long long)acc >> 32);
+            }
+            tc::tmem_st_32x32b_x8(acc_addr + 8 * g4, w);
+          }
+          tc::tmem_st_wait();
+          mx = nmx;
+        }
+      }
+      if (!ok) break;
+
+      // (a pair's odd CTA may lie wholly below the last row: no flag there)
+      bool nonfinite = mr < M && op.flags_a[mr / kBM] == op.gen;
+#pragma unroll 1
+      for (int c = n0 / 64; c < (n0 + kPairBN) / 64 && c * 64 < N; c++)
+        nonfinite |= op.flags_b[c] == op.gen;
+      if (nonfinite) {
+        if (row < M) {
+          // numc's arithmetic: one FMA chain per output in k order.
+#pragma unroll 1
+          for (int j = 0; j < CW; j++) {
+            const int col = n0 + cbase + j;
+            if (col >= N) break;
+            double f = 0.0;
+#pragma unroll 1
+            for (int64_t k = 0; k < op.K; k++)
+              f = __fma_rn(op.A[(int64_t)row * op.rsa + k * op.csa],
+                           op.B[k * op.rsb + (int64_t)col * op.csb], f);
+            C[(int64_t)row * rso + (int64_t)col * cso] = f;
+          }
+        }
+      } else {
+        const int base = (row < M ? exponent_of(op.amax[row]) : 0) + drop - 8 * (s + 1);
+#pragma unroll
+        for (int g4 = 0; g4 < CW / 4; g4++) {
+          uint32_t w[8];
+          tc::tmem_ld_32x32b_x8(acc_addr + 8 * g4, w);   // warp-collective
+          tc::tmem_ld_wait();
+          if (row < M) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              const int col = n0 + cbase + 4 * g4 + j;
+              if (col < N) {
+                const long long acc =
+                    (long long)(((unsigned long long)w[2 * j + 1] << 32) | w[2 * j]);
+                C[(int64_t)row * rso + (int64_t)col * cso] =
+                    ldexp(__ll2double_rn(acc), base + exponent_of(op.bmax[col]));
+              }
+            }
+          }
+        }
+      }
+      tc::tc_fence_before();
+      __syncwarp();   // reconverge before the next tile's tcgen05.ld
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  // Neither CTA of a pair leaves while the other may still signal its
+  // barriers or read its shared memory.
+  tc::cluster_sync();
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc_pair(tmem, 512);
+  }
+}
+
 struct OzLayout {
   int64_t Kp;
   size_t amax, bmax, flags_a, flags_b, a, b, total;
@@ -423,6 +727,62 @@ OzLayout oz_layout(int64_t M, int64_t K, int64_t N, int s) {
 }
 
 std::atomic<unsigned long long> g_oz_gen{0x0a2a000000000000ull};
+
+// CTA pairs unless NUMC_CUDA_OZAKI_CTAS=1 asks for the single-CTA kernel
+// (read once).
+int ozaki_ctas() {
+  static const int v = [] {
+    const char *e = getenv("NUMC_CUDA_OZAKI_CTAS");
+    return (e && atoi(e) == 1) ? 1 : 2;
+  }();
+  return v;
+}
+
+cudaError_t launch_ozaki_pair(const Gemm &g, const OzLayout &L, const __nv_bfloat16 *pa,
+                              const __nv_bfloat16 *pb, unsigned *status, const OzParams &op,
+                              cudaStream_t s) {
+  CUtensorMap ta, tb;
+  cudaError_t e;
+  if ((e = make_tmap_3d(&ta, pa, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, op.slices, g.M, L.Kp,
+                        L.Kp, kBM, kBK)))
+    return e;
+  if ((e = make_tmap_3d(&tb, pb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, op.slices, g.N, L.Kp,
+                        L.Kp, kPairBNCta, kBK)))
+    return e;
+  constexpr uint32_t SMEM = kPairStages * (kBM + kPairBNCta) * kBK * 2 + 1024 + 256;
+  static_assert(SMEM <= 232448, "shared memory");
+  static_assert((2 * kPairStages + 2 * kPairNumBuf + 1) * 8 + 4 <= 256, "barrier space");
+  if ((e = cudaFuncSetAttribute(ozaki_pair_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                SMEM)))
+    return e;
+  const int tiles_m = (int)((g.M + 2 * kBM - 1) / (2 * kBM));
+  const int tiles_n = (int)((g.N + kPairBN - 1) / kPairBN);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = SMEM;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3((unsigned)(2 * std::max(1, sm_count() / 2)));
+  int pairs = max_active_clusters((const void *)ozaki_pair_gemm, cfg);
+  if (pairs <= 0) pairs = std::max(1, sm_count() / 2);
+  pairs = std::min(pairs, tiles_m * tiles_n);
+  cfg.gridDim = dim3((unsigned)(2 * pairs));
+  cfg.numAttrs = 2;
+  e = cudaLaunchKernelEx(&cfg, ozaki_pair_gemm, ta, tb, (double *)g.c, (int64_t)g.rso,
+                         (int64_t)g.cso, (int)g.M, (int)g.N, (int)(L.Kp / kBK), tiles_m, tiles_n,
+                         status, op, wait_cfg());
+  if (e != cudaSuccess) return e;
+  count_launch();
+  return cudaGetLastError();
+}
 
 }  // namespace
 
@@ -462,6 +822,15 @@ cudaError_t launch_ozaki(const Gemm &g, int slices, void *ws_v, size_t ws_bytes,
   if ((e = cudaGetLastError())) return e;
   mark.split_done();
 
+  OzParams op;
+  op.amax = amax; op.bmax = bmax; op.flags_a = fa; op.flags_b = fb; op.gen = gen;
+  op.A = A; op.B = B; op.rsa = g.rsa; op.csa = g.csa; op.rsb = g.rsb; op.csb = g.csb;
+  op.K = g.K; op.slices = slices;
+  if (ozaki_ctas() == 2) {
+    e = launch_ozaki_pair(g, L, pa, pb, status, op, s);
+    mark.gemm_done();
+    return e;
+  }
   CUtensorMap ta, tb;
   if ((e = make_tmap_3d(&ta, pa, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, slices, g.M, L.Kp, L.Kp,
                         kBM, kBK)))
@@ -474,10 +843,6 @@ cudaError_t launch_ozaki(const Gemm &g, int slices, void *ws_v, size_t ws_bytes,
   static_assert((2 * kStages + 2 * kNumBuf + 1) * 8 + 4 <= 256, "barrier space");
   if ((e = cudaFuncSetAttribute(ozaki_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM)))
     return e;
-  OzParams op;
-  op.amax = amax; op.bmax = bmax; op.flags_a = fa; op.flags_b = fb; op.gen = gen;
-  op.A = A; op.B = B; op.rsa = g.rsa; op.csa = g.csa; op.rsb = g.rsb; op.csb = g.csb;
-  op.K = g.K; op.slices = slices;
   const int tiles_m = (int)((g.M + kBM - 1) / kBM), tiles_n = (int)((g.N + kBN - 1) / kBN);
   ozaki_gemm<<<tiles_m * tiles_n, kThreads, SMEM, s>>>(ta, tb, (double *)g.c, g.rso, g.cso,
                                                        (int)g.M, (int)g.N, (int)(L.Kp / kBK),

@@ -153,3 +153,44 @@ def test_tiny_and_subnormal_scales():
     assert (np.abs(got - ref) <= bound + 2.0 ** -1074).all()
     nz = ref[3] != 0
     assert np.all(np.signbit(got[3][nz]) == np.signbit(ref[3][nz]))
+
+
+_KERNEL_SCRIPT = r"""
+import sys
+import numpy as np, torch
+import numc_gb300 as nc
+from numc_gb300 import synth
+out = []
+for (M, K, N), s in [((300, 2100, 264), 7), ((520, 700, 130), 8), ((1, 77, 3), 5)]:
+    a, b = synth.operands("expspread", M, K, N, dtype="float64", seed=13)
+    c = torch.full((M, N), float("nan"), dtype=torch.float64, device="cuda")
+    nc.gemm(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(), c, algo=nc.ALGO_OZAKI, param=s)
+    nc.check_status()
+    out.append(c.cpu().numpy().ravel())
+np.save(sys.argv[1], np.concatenate(out))
+"""
+
+
+@pytest.mark.parametrize("ctas", ["1", "2"], ids=["single_cta", "cta_pairs"])
+def test_both_kernels_within_bound(tmp_path, ctas):
+    """The CTA-pair kernel (default) and the single-CTA kernel
+    (NUMC_CUDA_OZAKI_CTAS=1) each meet the error bound; the pair kernel
+    rounds each diagonal's sum once instead of each chunk's."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    path = str(tmp_path / "c.npy")
+    r = subprocess.run([sys.executable, "-c", _KERNEL_SCRIPT, path],
+                       env=dict(os.environ, NUMC_CUDA_OZAKI_CTAS=ctas), cwd=root,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    got_all = np.load(path)
+    off = 0
+    for (M, K, N), s in [((300, 2100, 264), 7), ((520, 700, 130), 8), ((1, 77, 3), 5)]:
+        a, b = synth.operands("expspread", M, K, N, dtype="float64", seed=13)
+        got = got_all[off:off + M * N].reshape(M, N)
+        off += M * N
+        hi, lo = oracle.dot2_f64(a, b, *np.divmod(np.arange(M * N), N))
+        err = np.abs(got - (hi + lo).reshape(M, N))
+        assert (err <= _bound(a, b, s)).all(), (ctas, M, float((err / _bound(a, b, s)).max()))
