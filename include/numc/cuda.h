@@ -204,6 +204,15 @@ NUMC_API uint64_t numc_cuda_launch_count(void);
  * caller check that a chain of device-resident calls makes no round trip. */
 NUMC_API uint64_t numc_cuda_transfer_bytes(void);
 
+/* Device memory of a context's arrays: bump-allocated from slabs of 64 MiB
+ * (an array larger than that gets a slab of its own) in the order arrays
+ * first need device memory.  numc_ctx_restore rewinds each slab to the end
+ * of its last surviving array and keeps the slabs for reuse; numc_ctx_free
+ * releases them.  Reports the slab count, their total size and the bytes
+ * in use (any pointer may be NULL). */
+NUMC_API int numc_cuda_ctx_device_usage(const NumcCtx *ctx, size_t *slabs,
+                                        size_t *reserved_bytes, size_t *used_bytes);
+
 /* Per-phase timing of the tensor-core GEMMs (split-BF16, Ozaki): when
  * enabled, each call records CUDA events on its stream around the operand
  * preparation kernels and around the GEMM kernel.  Enabling resets the

@@ -89,6 +89,9 @@ SIGNATURES = [
     ("numc_linear", _I, [_VP, _VP, _VP, _VP]),
     ("numc_bmm", _I, [_VP, _VP, _VP]),
     ("numc_cuda_transfer_bytes", ctypes.c_uint64, []),
+    ("numc_cuda_ctx_device_usage", _I, [_VP, ctypes.POINTER(ctypes.c_size_t),
+                                        ctypes.POINTER(ctypes.c_size_t),
+                                        ctypes.POINTER(ctypes.c_size_t)]),
     ("numc_set_error", _I, [_I, ctypes.c_char_p]),
     ("numc_get_error", _Err, []),
     ("numc_log_error", None, [_VP]),
@@ -220,6 +223,13 @@ class Ctx:
 
     def stream(self):
         return lib().numc_cuda_ctx_stream(self.ptr)
+
+    def device_usage(self):
+        """(slabs, reserved_bytes, used_bytes) of the context's device arena."""
+        n, r, u = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
+        check(lib().numc_cuda_ctx_device_usage(self.ptr, ctypes.byref(n), ctypes.byref(r),
+                                               ctypes.byref(u)))
+        return n.value, r.value, u.value
 
     def synchronize(self):
         check(lib().numc_cuda_ctx_synchronize(self.ptr))

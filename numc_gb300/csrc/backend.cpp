@@ -668,6 +668,30 @@ void *host_alloc_pinned(size_t bytes) {
 
 void host_free_pinned(void *p) { cudaFreeHost(p); }
 
+// Device memory for an array of `bytes` owned by the header at `owner`:
+// bump allocation from the context's slabs, continuing in slab dev_cur and
+// moving on to a later slab with room, or a new one (kDeviceSlab bytes, or
+// the array's size if larger).
+cudaError_t dev_arena_alloc(NumcCtx *ctx, size_t bytes, const ArenaPos &owner, char **out) {
+  const size_t need = align_up(bytes ? bytes : 1, 256);
+  auto &slabs = *ctx->dev_slabs;
+  size_t i = ctx->dev_cur;
+  while (i < slabs.size() && slabs[i].cap - slabs[i].used < need) i++;
+  if (i == slabs.size()) {
+    void *p = nullptr;
+    const size_t cap = need > kDeviceSlab ? need : kDeviceSlab;
+    cudaError_t e = numc_k::dev_malloc(&p, cap);
+    if (e != cudaSuccess) return e;
+    slabs.push_back(DeviceSlab{(char *)p, cap, 0});
+  }
+  DeviceSlab &sl = slabs[i];
+  ctx->dev_cur = i;
+  *out = sl.base + sl.used;
+  ctx->dev_allocs->push_back(DeviceAlloc{*out, bytes, owner, sl.base});
+  sl.used += need;
+  return cudaSuccess;
+}
+
 int device_copy_contiguous(const NumcArray *src, NumcArray *dst) {
   if (src->dim > (size_t)numc_k::kDotMaxDims)
     return NUMC_SET_ERROR(NUMC_ERR_SHAPE, "device copy: %zu dimensions (at most %d)", src->dim,
@@ -675,13 +699,8 @@ int device_copy_contiguous(const NumcArray *src, NumcArray *dst) {
   cudaStream_t s;
   int err = ctx_stream(dst->ctx, &s);
   if (err) return err;
-  if (!dst->dev_base) {
-    const size_t bytes = dst->capacity;
-    void *p = nullptr;
-    CU(numc_k::dev_malloc(&p, align_up(bytes ? bytes : 1, 256)), "cudaMalloc(array)");
-    dst->ctx->dev_allocs->push_back(DeviceAlloc{p, bytes, dst->pos});
-    dst->dev_base = (char *)p;
-  }
+  if (!dst->dev_base)
+    CU(dev_arena_alloc(dst->ctx, dst->capacity, dst->pos, &dst->dev_base), "cudaMalloc(array)");
   numc_k::DotNd ix;
   ix.dim = (int)src->dim;
   for (size_t d = 0; d < src->dim; d++) {
@@ -702,12 +721,26 @@ void ctx_release_device(NumcCtx *ctx, const ArenaPos *keep_upto) {
   if (ctx->stream && !ctx->dev_allocs->empty())
     cudaStreamSynchronize((cudaStream_t)ctx->stream);
   auto &v = *ctx->dev_allocs;
+  auto &slabs = *ctx->dev_slabs;
   size_t w = 0;
-  for (size_t r = 0; r < v.size(); r++) {
-    if (!keep_upto || v[r].owner.after(*keep_upto)) cudaFree(v[r].ptr);
-    else v[w++] = v[r];
-  }
+  for (size_t r = 0; r < v.size(); r++)
+    if (keep_upto && v[r].owner.before(*keep_upto)) v[w++] = v[r];
   v.resize(w);
+  // Each slab rewinds to the end of its last surviving array.
+  for (auto &sl : slabs) sl.used = 0;
+  for (const auto &a : v)
+    for (auto &sl : slabs)
+      if (sl.base == a.slab) {
+        const size_t end = (size_t)((char *)a.ptr - sl.base) + align_up(a.bytes ? a.bytes : 1, 256);
+        if (end > sl.used) sl.used = end;
+      }
+  ctx->dev_cur = 0;
+  for (size_t i = 0; i < slabs.size(); i++)
+    if (slabs[i].used) ctx->dev_cur = i;
+  if (!keep_upto) {
+    for (auto &sl : slabs) cudaFree(sl.base);
+    slabs.clear();
+  }
   if (!keep_upto) {
     if (ctx->scratch) {
       if (ctx->stream) cudaStreamSynchronize((cudaStream_t)ctx->stream);
@@ -1227,12 +1260,8 @@ extern "C" int numc_cuda_array_to_device(NumcArray *arr) {
   int err = ctx_stream(arr->ctx, &s);
   if (err) return err;
   size_t span = array_span_bytes(arr);
-  if (!arr->dev_base) {
-    void *p = nullptr;
-    CU(numc_k::dev_malloc(&p, align_up(span ? span : 1, 256)), "cudaMalloc(array)");
-    arr->ctx->dev_allocs->push_back(DeviceAlloc{p, span, arr->pos});
-    arr->dev_base = (char *)p;
-  }
+  if (!arr->dev_base)
+    CU(dev_arena_alloc(arr->ctx, span, arr->pos, &arr->dev_base), "cudaMalloc(array)");
   if (span) CU(xfer_async(arr->dev_base, arr->data, span, cudaMemcpyHostToDevice, s), "copy to device");
   CU(cudaStreamSynchronize(s), "cudaStreamSynchronize");
   arr->residency = kBoth;
@@ -1253,6 +1282,22 @@ extern "C" int numc_cuda_array_to_host(NumcArray *arr) {
 }
 
 extern "C" uint64_t numc_cuda_transfer_bytes(void) { return g_transfer_bytes.load(); }
+
+extern "C" int numc_cuda_ctx_device_usage(const NumcCtx *ctx, size_t *slabs,
+                                          size_t *reserved_bytes, size_t *used_bytes) {
+  if (!ctx) return NUMC_SET_ERROR(NUMC_ERR_NULL, "device usage: ctx is NULL");
+  size_t n = 0, res = 0, used = 0;
+  if (ctx->dev_slabs)
+    for (const auto &sl : *ctx->dev_slabs) {
+      n++;
+      res += sl.cap;
+      used += sl.used;
+    }
+  if (slabs) *slabs = n;
+  if (reserved_bytes) *reserved_bytes = res;
+  if (used_bytes) *used_bytes = used;
+  return 0;
+}
 
 // ---- numc_manual_seed / numc_array_rand (numc's src/random/random.c) --------
 
@@ -1276,14 +1321,11 @@ NumcArray *rand_array(NumcCtx *ctx, const size_t *shape, size_t dim, NumcDType d
   if (ctx_stream(ctx, &s)) return nullptr;
   const size_t bytes = arr->capacity;
   if (!arr->dev_base) {
-    void *p = nullptr;
-    cudaError_t e = numc_k::dev_malloc(&p, align_up(bytes ? bytes : 1, 256));
+    cudaError_t e = dev_arena_alloc(ctx, bytes, arr->pos, &arr->dev_base);
     if (e != cudaSuccess) {
       cuda_fail(e, "cudaMalloc(array)");
       return nullptr;
     }
-    ctx->dev_allocs->push_back(DeviceAlloc{p, bytes, arr->pos});
-    arr->dev_base = (char *)p;
   }
   cudaError_t e = numc_k::rand_fill(dtype, arr->dev_base, arr->size, s);
   if (e != cudaSuccess) {

@@ -138,8 +138,11 @@ extern "C" NumcCtx *numc_ctx_create(void) {
   ctx->scratch = nullptr;
   ctx->scratch_bytes = 0;
   ctx->dev_allocs = new (std::nothrow) std::vector<DeviceAlloc>();
-  if (!ctx->dev_allocs || !new_block(ctx, kArenaBlock)) {
+  ctx->dev_slabs = new (std::nothrow) std::vector<DeviceSlab>();
+  ctx->dev_cur = 0;
+  if (!ctx->dev_allocs || !ctx->dev_slabs || !new_block(ctx, kArenaBlock)) {
     delete ctx->dev_allocs;
+    delete ctx->dev_slabs;
     delete ctx;
     NUMC_SET_ERROR(NUMC_ERR_MALLOC, "failed to create arena (%zu bytes)",
                    kArenaBlock);
@@ -158,6 +161,7 @@ extern "C" void numc_ctx_free(NumcCtx *ctx) {
     b = p;
   }
   delete ctx->dev_allocs;
+  delete ctx->dev_slabs;
   delete ctx;
 }
 

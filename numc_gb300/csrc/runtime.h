@@ -32,8 +32,10 @@ struct ArenaBlock {
 struct ArenaPos {
   uint64_t seq;
   size_t off;
-  bool after(const ArenaPos &o) const {
-    return seq > o.seq || (seq == o.seq && off > o.off);
+  // Strictly earlier: a header allocated at a checkpoint's own position
+  // was made after the checkpoint.
+  bool before(const ArenaPos &o) const {
+    return seq < o.seq || (seq == o.seq && off < o.off);
   }
 };
 
@@ -41,6 +43,19 @@ struct DeviceAlloc {
   void *ptr;
   size_t bytes;
   ArenaPos owner;      // arena position of the owning array header
+  char *slab;          // base of the device slab holding it
+};
+
+// Device memory of a context's arrays comes from slabs of kDeviceSlab bytes
+// (an array larger than that gets a slab of its own), handed out by bump
+// allocation in the order the arrays first need device memory.
+// numc_ctx_restore rewinds each slab to the end of its last surviving
+// array and keeps the slabs for reuse; numc_ctx_free releases them.
+constexpr size_t kDeviceSlab = 64u << 20;
+
+struct DeviceSlab {
+  char *base;
+  size_t cap, used;
 };
 
 enum Residency : int {
@@ -62,6 +77,8 @@ struct NumcCtx {
   void *scratch;                      // device scratch (staging, splits)
   size_t scratch_bytes;
   std::vector<numc_rt::DeviceAlloc> *dev_allocs;
+  std::vector<numc_rt::DeviceSlab> *dev_slabs;
+  size_t dev_cur;                     // slab that bump allocation continues in
 };
 
 struct NumcArray {

@@ -174,3 +174,49 @@ def test_checkpoint_frees_device_arrays(ctx):
     out = ctx.zeros((8, 8), "float32")
     nc.matmul(keep, keep, out)
     assert (out.numpy() == 8).all()
+
+
+def test_device_arena_slabs_bump_rewind_and_reuse(ctx):
+    """Device memory comes from 64 MiB slabs by bump allocation: many small
+    resident arrays share one slab, restore rewinds it and the next arrays
+    reuse the space, an array above the slab size gets a slab of its own,
+    and results stay correct throughout."""
+    slab = 64 << 20
+    assert ctx.device_usage() == (0, 0, 0)
+    keep = ctx.from_numpy(np.full((8, 8), 2.0, "float32")).to_device()
+    n0, r0, u0 = ctx.device_usage()
+    assert (n0, r0) == (1, slab) and u0 == 256
+    cp = ctx.checkpoint()
+    arrs = [ctx.from_numpy(np.full((16, 16), float(i), "float32")).to_device() for i in range(200)]
+    n1, r1, u1 = ctx.device_usage()
+    assert (n1, r1) == (1, slab) and u1 == 256 + 200 * 1024   # 16*16*4 bytes each
+    out = ctx.zeros((16, 16), "float32")
+    nc.matmul(arrs[3], arrs[5], out)
+    assert (out.numpy() == 3 * 5 * 16).all()
+    big = ctx.zeros((5000, 4000), "float32").to_device()   # 80 MB: a slab of its own
+    n2, r2, u2 = ctx.device_usage()
+    assert n2 == 2 and r2 == slab + 5000 * 4000 * 4
+    ctx.restore(cp)
+    n3, r3, u3 = ctx.device_usage()
+    assert (n3, r3, u3) == (2, r2, 256)                      # slabs kept, rewound
+    again = [ctx.from_numpy(np.full((16, 16), 1.0, "float32")).to_device() for _ in range(10)]
+    assert ctx.device_usage() == (2, r2, 256 + 10 * 1024)    # space reused, no new slab
+    out = ctx.zeros((8, 8), "float32")
+    nc.matmul(keep, keep, out)
+    assert (out.numpy() == 32).all()
+    out2 = ctx.zeros((16, 16), "float32")
+    nc.matmul(again[0], again[9], out2)
+    assert (out2.numpy() == 16).all()
+
+
+def test_device_arena_released_by_ctx_free():
+    torch = pytest.importorskip("torch")
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    c = nc.Ctx()
+    for _ in range(3):
+        c.zeros((4096, 4096), "float32").to_device()
+    assert c.device_usage()[0] == 3
+    assert torch.cuda.mem_get_info()[0] <= free0 - 3 * (64 << 20)
+    c.free()
+    assert torch.cuda.mem_get_info()[0] >= free0 - (8 << 20)
