@@ -167,7 +167,9 @@ def device_count():
     return lib().numc_cuda_device_count()
 
 
-def set_algo(dtype, algo, param=0):
+def set_algo(dtype, algo, param=-1):
+    """Process-wide algorithm of `dtype`; param -1 = the algorithm's default
+    (for int8/uint8 and CUDA-core floats: the process-wide ISA profile)."""
     check(lib().numc_cuda_set_algo(CODE[np.dtype(dtype).name], algo, param))
 
 

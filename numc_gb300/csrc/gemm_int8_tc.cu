@@ -782,9 +782,8 @@ cudaError_t launch_i8_gemm(const Gemm &g, int rule, const I8Layout &L, __nv_bflo
   constexpr uint32_t SMEM =
       Cfg::kStages * (kBM + kBN) * kBK * 2 + 1024 + kBarBytes + Cfg::kAccWarps * 1024;
   static_assert(SMEM <= 232448, "shared memory");
-  if ((e = cudaFuncSetAttribute(int8_tc_gemm<SIGNED, kBN>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM)))
-    return e;
+  static LaunchCache lc;
+  if ((e = smem_attr_once(lc, (const void *)int8_tc_gemm<SIGNED, kBN>, SMEM))) return e;
   const int tiles_m = (int)((g.M + kBM - 1) / kBM), tiles_n = (int)((g.N + kBN - 1) / kBN);
   // programmatic dependent launch: set up while the conversion pass ends
   cudaLaunchConfig_t cfg = {};
@@ -818,8 +817,8 @@ cudaError_t launch_i8_pair(const Gemm &g, int rule, const I8Layout &L, const __n
                         Cfg::BN_CTA, kBK)))
     return e;
   auto kern = int8_pair_gemm<SIGNED, BN, X86>;
-  if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM)))
-    return e;
+  static LaunchCache lc;
+  if ((e = smem_attr_once(lc, (const void *)kern, Cfg::SMEM))) return e;
   const int tiles_m = (int)((g.M + 2 * kBM - 1) / (2 * kBM));
   const int tiles_n = (int)((g.N + BN - 1) / BN);
   cudaLaunchConfig_t cfg = {};
@@ -837,7 +836,7 @@ cudaError_t launch_i8_pair(const Gemm &g, int rule, const I8Layout &L, const __n
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   cfg.gridDim = dim3((unsigned)(2 * std::max(1, sm_count() / 2)));
-  int pairs = max_active_clusters((const void *)kern, cfg);
+  int pairs = clusters_once(lc, (const void *)kern, cfg);
   if (pairs <= 0) pairs = std::max(1, sm_count() / 2);
   pairs = std::min(pairs, tiles_m * tiles_n);
   cfg.gridDim = dim3((unsigned)(2 * pairs));

@@ -752,9 +752,8 @@ cudaError_t launch_ozaki_pair(const Gemm &g, const OzLayout &L, const __nv_bfloa
   constexpr uint32_t SMEM = kPairStages * (kBM + kPairBNCta) * kBK * 2 + 1024 + 256;
   static_assert(SMEM <= 232448, "shared memory");
   static_assert((2 * kPairStages + 2 * kPairNumBuf + 1) * 8 + 4 <= 256, "barrier space");
-  if ((e = cudaFuncSetAttribute(ozaki_pair_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                SMEM)))
-    return e;
+  static LaunchCache lc;
+  if ((e = smem_attr_once(lc, (const void *)ozaki_pair_gemm, SMEM))) return e;
   const int tiles_m = (int)((g.M + 2 * kBM - 1) / (2 * kBM));
   const int tiles_n = (int)((g.N + kPairBN - 1) / kPairBN);
   cudaLaunchConfig_t cfg = {};
@@ -771,7 +770,7 @@ cudaError_t launch_ozaki_pair(const Gemm &g, const OzLayout &L, const __nv_bfloa
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   cfg.gridDim = dim3((unsigned)(2 * std::max(1, sm_count() / 2)));
-  int pairs = max_active_clusters((const void *)ozaki_pair_gemm, cfg);
+  int pairs = clusters_once(lc, (const void *)ozaki_pair_gemm, cfg);
   if (pairs <= 0) pairs = std::max(1, sm_count() / 2);
   pairs = std::min(pairs, tiles_m * tiles_n);
   cfg.gridDim = dim3((unsigned)(2 * pairs));
@@ -841,8 +840,8 @@ cudaError_t launch_ozaki(const Gemm &g, int slices, void *ws_v, size_t ws_bytes,
   constexpr uint32_t SMEM = kStages * (kBM + kBN) * kBK * 2 + 1024 + 256;
   static_assert(SMEM <= 232448, "shared memory");
   static_assert((2 * kStages + 2 * kNumBuf + 1) * 8 + 4 <= 256, "barrier space");
-  if ((e = cudaFuncSetAttribute(ozaki_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM)))
-    return e;
+  static LaunchCache lc1;
+  if ((e = smem_attr_once(lc1, (const void *)ozaki_gemm, SMEM))) return e;
   const int tiles_m = (int)((g.M + kBM - 1) / kBM), tiles_n = (int)((g.N + kBN - 1) / kBN);
   ozaki_gemm<<<tiles_m * tiles_n, kThreads, SMEM, s>>>(ta, tb, (double *)g.c, g.rso, g.cso,
                                                        (int)g.M, (int)g.N, (int)(L.Kp / kBK),

@@ -86,6 +86,28 @@ int max_active_clusters(const void *kern, const cudaLaunchConfig_t &cfg) {
   return n;
 }
 
+cudaError_t smem_attr_once(LaunchCache &lc, const void *kern, int bytes) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+  const bool cacheable = dev >= 0 && dev < 64;
+  if (cacheable && ((lc.attr_done.load(std::memory_order_acquire) >> dev) & 1)) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && cacheable) lc.attr_done.fetch_or(1ull << dev, std::memory_order_release);
+  return e;
+}
+
+int clusters_once(LaunchCache &lc, const void *kern, const cudaLaunchConfig_t &cfg) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return max_active_clusters(kern, cfg);
+  int n = lc.clusters[dev].load(std::memory_order_relaxed);
+  if (!n) {
+    n = max_active_clusters(kern, cfg);
+    if (n > 0) lc.clusters[dev].store(n, std::memory_order_relaxed);
+  }
+  return n;
+}
+
 namespace {
 
 constexpr int kBM = 128, kBK = 64;
@@ -678,8 +700,8 @@ cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, cons
   if ((e = make_tmap_3d(&tb, bufs.pb, dtype, 2, PLANES, g.N, L.Kp, L.Kp, Cfg::BN_CTA, kBK)))
     return e;
   auto kern = split_gemm<BN, STAGES, PLANES, FLUSH, F16, CTAS>;
-  if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM)))
-    return e;
+  static LaunchCache lc;
+  if ((e = smem_attr_once(lc, (const void *)kern, Cfg::SMEM))) return e;
   const int tiles_m = (int)((g.M + kBM * CTAS - 1) / (kBM * CTAS));
   const int tiles_n = (int)((g.N + BN - 1) / BN);
   const int vec4 = g.cso == 1 && (g.rso % 4) == 0 && ((uintptr_t)g.c % 16) == 0;
@@ -726,15 +748,8 @@ cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, cons
     cfg.numAttrs = 1;
     // One pair per two SMs, capped by how many pairs fit at once.
     cfg.gridDim = dim3((unsigned)(CTAS * std::max(1, sm_count() / CTAS)));
-    static int pairs_cached[64] = {0};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    int pairs = (dev >= 0 && dev < 64) ? pairs_cached[dev] : 0;
-    if (!pairs) {
-      pairs = max_active_clusters((const void *)kern, cfg);
-      if (pairs <= 0) pairs = std::max(1, sm_count() / CTAS);
-      if (dev >= 0 && dev < 64) pairs_cached[dev] = pairs;
-    }
+    int pairs = clusters_once(lc, (const void *)kern, cfg);
+    if (pairs <= 0) pairs = std::max(1, sm_count() / CTAS);
     pairs = std::min(pairs, tiles_m * tiles_n);
     cfg.gridDim = dim3((unsigned)(CTAS * pairs));
     cfg.numAttrs = 2;

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cstddef>
+#include <atomic>
 #include <cstdint>
 
 #include "numc/cuda.h"
@@ -167,6 +168,16 @@ int sm_count();
 bool pdl_enabled();
 // Co-resident clusters of `kern` launched with `cfg` (0 if the query fails).
 int max_active_clusters(const void *kern, const cudaLaunchConfig_t &cfg);
+
+// Launch setup of one kernel, done once per device: its dynamic shared
+// memory limit and its co-resident cluster count (host calls that cost
+// microseconds, against launches of a few microseconds for small problems).
+struct LaunchCache {
+  std::atomic<uint64_t> attr_done{0};   // bit d: attribute set on device d
+  std::atomic<int> clusters[64] = {};   // per device, 0 = not queried yet
+};
+cudaError_t smem_attr_once(LaunchCache &lc, const void *kern, int bytes);
+int clusters_once(LaunchCache &lc, const void *kern, const cudaLaunchConfig_t &cfg);
 
 // Count of kernel launches issued by this library.
 void count_launch(unsigned n = 1);
