@@ -196,7 +196,7 @@ struct SplitCfg {
   static constexpr bool EPI_STAGE = RING + EPI_BYTES <= 232448;
   static constexpr uint32_t SMEM = RING + (EPI_STAGE ? EPI_BYTES : 0);
   static constexpr int THREADS = 64 + 32 * ACC_WARPS;   // producer, MMA, accumulators
-  static_assert(BN == 128 || BN == 256, "tile width");
+  static_assert(BN == 64 || BN == 128 || BN == 256, "tile width");
   static_assert(CTAS == 1 || CTAS == 2, "one CTA or a CTA pair");
   static_assert(SMEM <= 232448, "shared memory");
   static_assert((2 * STAGES + 2 * NBUF + 1) * 8 + 4 <= 256, "barrier space");
@@ -433,7 +433,7 @@ split_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUten
         ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
         if (!ok) break;
         tc::tc_fence_after();
-        if constexpr (BN == 128) {
+        if constexpr (BN <= 128) {
           uint32_t r[CW];
 #pragma unroll
           for (int c0 = 0; c0 < CW; c0 += 32)
@@ -787,27 +787,34 @@ cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, cons
 // both inputs.
 constexpr int kF16DefaultFlush = 4;
 
-// Output tile width of the float16-plane GEMM: 256 columns, or 128 when
-// the 256-column tiles would leave more than half of the CTA pairs idle
-// (small problems: twice the SMs share the multiply).  Every output is the
-// same either way.  NUMC_CUDA_SPLIT_TILE=128 or 256 pins it (read once).
+// Output tile width of the float16-plane GEMM: 256 columns; 128 when the
+// 256-column tiles would leave more than half of the CTA pairs idle, and 64
+// when even single-CTA 128 x 128 tiles would leave more than half of the
+// SMs idle (small problems: more SMs share the multiply).  Every output is
+// the same for every width.  NUMC_CUDA_SPLIT_TILE=64, 128 or 256 pins it
+// (read once).
 int split_tile_width(const Gemm &g, int ctas) {
   static const int forced = [] {
     const char *e = getenv("NUMC_CUDA_SPLIT_TILE");
     return e ? atoi(e) : 0;
   }();
-  if (forced == 128 || forced == 256) return forced;
+  if (forced == 64 || forced == 128 || forced == 256) return forced;
   const int64_t rows = 128 * ctas;
   const int64_t wide = (g.M + rows - 1) / rows * ((g.N + 255) / 256);
-  return 2 * wide < sm_count() / ctas ? 128 : 256;
+  if (2 * wide >= sm_count() / ctas) return 256;
+  const int64_t narrow = (g.M + 127) / 128 * ((g.N + 127) / 128);   // single-CTA tiles
+  return 2 * narrow < sm_count() ? 64 : 128;
 }
 
 template <int CTAS>
 cudaError_t launch_gemm_ctas(const SplitLayout &L, const SplitBufs &ws, const Gemm &g,
                              unsigned long long gen, unsigned *status, cudaStream_t s,
-                             bool narrow) {
+                             int narrow) {
   constexpr int S2 = CTAS == 2 ? 3 : 2;   // stages of the 2-plane ring
-  if (L.f16 && L.flush == kF16DefaultFlush && narrow)
+  if (L.f16 && L.flush == kF16DefaultFlush && narrow == 64)
+    // 64-column single-CTA tiles: 48 KiB stages
+    return launch_gemm_status<64, 4, 2, kF16DefaultFlush, true, 1>(L, ws, g, gen, status, s);
+  if (L.f16 && L.flush == kF16DefaultFlush && narrow == 128)
     // 128-column tiles: 48 KiB (pair) or 64 KiB (single CTA) stages
     return launch_gemm_status<128, CTAS == 2 ? 4 : 3, 2, kF16DefaultFlush, true, CTAS>(
         L, ws, g, gen, status, s);
@@ -841,7 +848,8 @@ int split_ctas() {
 cudaError_t launch_gemm(const SplitLayout &L, const SplitBufs &ws, const Gemm &g, unsigned long long gen,
                         unsigned *status, cudaStream_t s) {
   const int ctas = split_ctas();
-  const bool narrow = split_tile_width(g, ctas) == 128;
+  const int width = split_tile_width(g, ctas);
+  const int narrow = width < 256 ? width : 0;   // 0: the wide tiles
   if (ctas == 2 && !(narrow && L.f16 && L.flush == kF16DefaultFlush))
     return launch_gemm_ctas<2>(L, ws, g, gen, status, s, narrow);
   return launch_gemm_ctas<1>(L, ws, g, gen, status, s, narrow);

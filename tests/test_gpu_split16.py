@@ -202,15 +202,15 @@ np.save(sys.argv[1], np.concatenate(out))
 
 @pytest.mark.parametrize("ctas", ["1", "2"])
 def test_tile_widths_store_identical_bits(tmp_path, ctas):
-    """128- and 256-column tiles (single CTAs and CTA pairs) run the same
-    per-output arithmetic: identical bits, including shapes where the
-    default picks either width."""
+    """64-, 128- and 256-column tiles (single CTAs and CTA pairs) run the
+    same per-output arithmetic: identical bits, including shapes where the
+    default picks each width."""
     import os
     import subprocess
     import sys
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     res = {}
-    for width in ("128", "256"):
+    for width in ("64", "128", "256"):
         env = dict(os.environ, NUMC_CUDA_SPLIT_TILE=width, NUMC_CUDA_SPLIT_CTAS=ctas)
         path = str(tmp_path / f"c{width}.npy")
         r = subprocess.run([sys.executable, "-c", _TILE_SCRIPT, path], env=env, cwd=root,
@@ -219,3 +219,4 @@ def test_tile_widths_store_identical_bits(tmp_path, ctas):
         res[width] = np.load(path)
     assert np.isfinite(res["128"]).all()
     np.testing.assert_array_equal(res["128"].view(np.uint32), res["256"].view(np.uint32))
+    np.testing.assert_array_equal(res["64"].view(np.uint32), res["256"].view(np.uint32))
