@@ -111,7 +111,7 @@ int clusters_once(LaunchCache &lc, const void *kern, const cudaLaunchConfig_t &c
 namespace {
 
 constexpr int kBM = 128, kBK = 64;
-constexpr int kFusedMaxKp = kFusedRegKp;   // single problems: fused scale + split up to this K
+constexpr int kFusedMaxKp = 1024;   // single problems: fused scale + split up to this K
 
 __host__ __device__ inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 

@@ -350,7 +350,6 @@ __device__ __forceinline__ void split_tile(const float *__restrict__ src, int64_
 // Pass 2: 16 threads per row along k for both, so each row's planes are
 // written in 128-byte runs (B's second read comes from L2 in 4-byte pieces).
 constexpr int kFusedRows = 16;
-constexpr int kFusedRegKp = 1024;   // register-resident rows up to this padded K
 
 __device__ __forceinline__ void fused_scale_split_rows(
     const float *__restrict__ src, int64_t rs_row, int64_t rs_k, int R, int K, int Kp, int r0,
@@ -361,71 +360,6 @@ __device__ __forceinline__ void fused_scale_split_rows(
   __shared__ unsigned rowmax[kFusedRows];
   const int tid = threadIdx.x;
   const bool along_k = rs_k == 1;
-  // Rows contiguous along k, 16-byte aligned and K padded to at most
-  // kFusedRegKp: thread (r, q) reads its row's k = 4 q + 64 i .. +3 once,
-  // as float4, keeps them in registers for both passes.
-  if (along_k && Kp <= kFusedRegKp && (rs_row & 3) == 0 &&
-      (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
-    const int r2 = tid / 16, q = tid % 16;
-    const bool live = r0 + r2 < R;
-    const float *p = src + (int64_t)(r0 + (live ? r2 : 0)) * rs_row;
-    float4 v[kFusedRegKp / 64];
-    unsigned m = 0;
-    bool bad = false;
-#pragma unroll
-    for (int i = 0; i < kFusedRegKp / 64; i++) {
-      const int k = 4 * q + 64 * i;
-      v[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      if (live && k < K) {
-        if (k + 4 <= K) {
-          v[i] = *reinterpret_cast<const float4 *>(p + k);
-        } else {
-          v[i].x = p[k];
-          if (k + 1 < K) v[i].y = p[k + 1];
-          if (k + 2 < K) v[i].z = p[k + 2];
-        }
-      }
-      const float x[4] = {v[i].x, v[i].y, v[i].z, v[i].w};
-#pragma unroll
-      for (int t = 0; t < 4; t++) {
-        bad |= !isfinite(x[t]);
-        m = max(m, absbits(x[t]));
-      }
-    }
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (q == 0 && live) maxbits[r0 + r2] = m;
-    if (__syncthreads_or(bad) && tid == 0) flags[r0 / flag_rows] = gen;
-    if (!live) return;
-    const int sexp = f16_scale_exp(m);
-    const int64_t plane_elems = (int64_t)R * Kp;
-    uint16_t *dst = planes + (int64_t)(r0 + r2) * Kp;
-#pragma unroll
-    for (int i = 0; i < kFusedRegKp / 64; i++) {
-      const int k = 4 * q + 64 * i;
-      if (k >= Kp) break;
-      const float x4[4] = {v[i].x, v[i].y, v[i].z, v[i].w};
-      uint16_t out[kPlanes][4];
-#pragma unroll
-      for (int t = 0; t < 4; t++) {
-        float x = isfinite(x4[t]) ? scale_pow2(x4[t], sexp) : 0.0f;
-#pragma unroll
-        for (int pl = 0; pl < kPlanes; pl++) {
-          const __half h = __float2half_rn(x);
-          out[pl][t] = __half_as_ushort(h);
-          x -= __half2float(h);
-        }
-      }
-#pragma unroll
-      for (int pl = 0; pl < kPlanes; pl++) {
-        uint2 w;
-        w.x = (uint32_t)out[pl][0] | ((uint32_t)out[pl][1] << 16);
-        w.y = (uint32_t)out[pl][2] | ((uint32_t)out[pl][3] << 16);
-        *reinterpret_cast<uint2 *>(dst + pl * plane_elems + k) = w;
-      }
-    }
-    return;
-  }
   const int r = along_k ? tid / 16 : tid % 16, sub = along_k ? tid % 16 : tid / 16;
   const bool live = r0 + r < R;
   const float *p = src + (int64_t)(r0 + (live ? r : 0)) * rs_row;
