@@ -142,7 +142,7 @@ grouped_scale_split(const Prob *__restrict__ probs, const int2 *__restrict__ job
   const Prob &P = probs[job.x];
   const int a_blocks = (P.M + kFusedRows - 1) / kFusedRows;
   const bool is_a = job.y < a_blocks;
-  fused_scale_split_rows(is_a ? P.A : P.B, is_a ? P.rsa : P.csb, is_a ? P.csa : P.rsb,
+  fused_scale_split_rows<false>(is_a ? P.A : P.B, is_a ? P.rsa : P.csb, is_a ? P.csa : P.rsb,
                          is_a ? P.M : P.N, P.K, P.Kp,
                          (is_a ? job.y : job.y - a_blocks) * kFusedRows,
                          is_a ? P.pa : P.pb, is_a ? P.flags_a : P.flags_b, is_a ? kBM : 64,

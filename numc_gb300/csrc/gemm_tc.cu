@@ -159,7 +159,7 @@ scale_split_pair(const float *A, int64_t rsa, int64_t csa, int M, const float *B
   tc::griddep_launch_dependents();   // the GEMM may launch and set up meanwhile
   const int a_blocks = (M + kFusedRows - 1) / kFusedRows;
   const bool is_a = (int)blockIdx.x < a_blocks;
-  fused_scale_split_rows(is_a ? A : B, is_a ? rsa : csb, is_a ? csa : rsb, is_a ? M : N, K, Kp,
+  fused_scale_split_rows<true>(is_a ? A : B, is_a ? rsa : csb, is_a ? csa : rsb, is_a ? M : N, K, Kp,
                          (is_a ? (int)blockIdx.x : (int)blockIdx.x - a_blocks) * kFusedRows,
                          is_a ? pa : pb, is_a ? fa : fbl, is_a ? kBM : 64, is_a ? max_a : max_b,
                          gen);
