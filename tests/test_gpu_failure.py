@@ -93,12 +93,16 @@ def _gemm_case(dtype, algo, param, shape, seed):
 
 CASES = [
     # (dtype, algo, param, (M, K, N), bound relative to |A||B|; None = bit-exact vs numc)
-    ("float32", nc.ALGO_SPLIT_FP16, 0, (300, 520, 270), 2e-6),     # CTA-pair kernel
+    ("float32", nc.ALGO_SPLIT_FP16, 0, (2048, 64, 2048), 2e-6),    # CTA pairs, 256 x 256
+    ("float32", nc.ALGO_SPLIT_FP16, 0, (1300, 520, 1100), 2e-6),   # single CTAs, 128 x 128
+    ("float32", nc.ALGO_SPLIT_FP16, 0, (300, 520, 270), 2e-6),     # single CTAs, 128 x 64
     ("float32", nc.ALGO_SPLIT_BF16, 6, (300, 520, 270), 2e-6),     # three planes
     ("float32", nc.ALGO_SPLIT_BF16, 3, (300, 520, 270), 2.0 ** -14),
-    ("float64", nc.ALGO_OZAKI, 7, (200, 300, 150), 1e-13),
+    ("float64", nc.ALGO_OZAKI, 7, (200, 300, 150), 1e-13),         # CTA pairs
     ("int8", nc.ALGO_TC_INT8, nc.INT8_X86_AVX2, (200, 1100, 150), None),
     ("uint8", nc.ALGO_TC_INT8, nc.INT8_X86_AVX2, (200, 1100, 150), None),
+    ("int8", nc.ALGO_TC_INT8, nc.INT8_X86_AVX2 + 16 * nc.INT8_TILE_PAIR256, (600, 1100, 520), None),
+    ("uint8", nc.ALGO_TC_INT8, nc.INT8_ARM_NEON + 16 * nc.INT8_TILE_PAIR128, (600, 1100, 520), None),
 ]
 
 
@@ -117,7 +121,8 @@ def test_abandoned_waits_report_and_recover(dtype, algo, param, shape, tol):
     nc.gemm(ta, tb, out, algo=algo, param=param)
     nc.check_status(s)
     got = out.cpu().numpy()
-    want = oracle.matmul(a, b)
+    want = oracle.matmul(a, b, oracle.PROFILE_ARM_NEON if algo == nc.ALGO_TC_INT8 and
+                         param % 16 == nc.INT8_ARM_NEON else oracle.PROFILE_X86_AVX2)
     if tol is None:
         assert got.tobytes() == want.tobytes()
     else:
