@@ -110,25 +110,27 @@ struct I8Operand {
   __nv_bfloat16 *dst;
 };
 
-constexpr int kCvtRows = 64, kCvtK = 256;
+constexpr int kCvtRows = 64;
 
 // Four 8-bit integers (bytes of w, low first) as four bfloat16, packed two
 // a word.  Integers of 8 bits are exact in bfloat16: the value's float32
 // bits with the low 16 (zero) dropped.
 template <bool SIGNED>
 __device__ __forceinline__ uint2 bytes_to_bf16x4(uint32_t w) {
-  uint32_t h[4];
+  // Without an int-to-float conversion (a quarter of the FP32 rate): the
+  // float with bits 0x4B0000xx is 2^23 + xx, so subtracting 2^23 (int8:
+  // offset binary, 2^23 + 128) leaves the byte's value exactly.
+  if (SIGNED) w ^= 0x80808080u;
+  constexpr float kBias = SIGNED ? 8388736.0f : 8388608.0f;
+  uint32_t f[4];
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const uint32_t byte = (w >> (8 * i)) & 0xFFu;
-    const int v = SIGNED ? (int)(int8_t)byte : (int)byte;
-    h[i] = __float_as_uint((float)v) >> 16;
-  }
-  return make_uint2(h[0] | (h[1] << 16), h[2] | (h[3] << 16));
+  for (int i = 0; i < 4; i++)
+    f[i] = __float_as_uint(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + i)) - kBias);
+  return make_uint2(__byte_perm(f[0], f[1], 0x7632), __byte_perm(f[2], f[3], 0x7632));
 }
 
-// Both operands in one launch (A's tiles first, then B^T's), 64 rows x 256 k
-// a block.  Each source layout gets its own mapping, all of them writing
+// Both operands in one launch (A's tiles first, then B^T's), 64 rows x
+// kCvtK (128 or 256) k a block.  Each source layout gets its own mapping, all of them writing
 // whole 32-byte sectors of the destination:
 //   * k contiguous (row-major A): 16 bytes a thread along k, converted in
 //     registers, two 16-byte stores;
@@ -137,9 +139,10 @@ __device__ __forceinline__ uint2 bytes_to_bf16x4(uint32_t w) {
 //     whole 32-byte sectors), transposed with byte permutes, four 8-byte
 //     stores of 4 bfloat16 along k (8 rows x 32 bytes a warp store);
 //   * any other strides: byte gathers staged in shared memory.
-template <bool SIGNED>
+template <bool SIGNED, int kCvtK>
 __global__ void __launch_bounds__(256)
 int8_pair_to_bf16(I8Operand a, I8Operand b, int64_t K, int64_t Kp, int64_t blocks_a) {
+  static_assert(kCvtK == 128 || kCvtK == 256, "conversion block depth");
   __shared__ __align__(16) uint8_t tile[kCvtRows][kCvtK + 16];
   tc::griddep_launch_dependents();   // the GEMM may launch and set up meanwhile
   int64_t blk = blockIdx.x;
@@ -152,9 +155,9 @@ int8_pair_to_bf16(I8Operand a, I8Operand b, int64_t K, int64_t Kp, int64_t block
   // Every load of a thread is issued before its first store (the
   // destination may alias nothing it reads, but the compiler cannot know).
   if (op.rs_k == 1) {
-    uint4 v[4];
+    uint4 v[kCvtK / 64];
 #pragma unroll
-    for (int it = 0; it < 4; it++) {   // 8 threads a row, 16 k each, two 128-k halves
+    for (int it = 0; it < kCvtK / 64; it++) {   // 8 threads a row, 16 k each, 128-k halves
       const int r = (tid >> 3) + 32 * (it & 1), kk = (tid & 7) * 16 + 128 * (it >> 1);
       const int64_t gr = r0 + r, gk = k0 + kk;
       v[it] = make_uint4(0, 0, 0, 0);
@@ -172,7 +175,7 @@ int8_pair_to_bf16(I8Operand a, I8Operand b, int64_t K, int64_t Kp, int64_t block
       }
     }
 #pragma unroll
-    for (int it = 0; it < 4; it++) {
+    for (int it = 0; it < kCvtK / 64; it++) {
       const int r = (tid >> 3) + 32 * (it & 1), kk = (tid & 7) * 16 + 128 * (it >> 1);
       const int64_t gr = r0 + r, gk = k0 + kk;
       if (gr >= op.R) continue;
@@ -868,12 +871,20 @@ cudaError_t launch_i8(const Gemm &g, int rule, int tile, char *ws, const I8Layou
   auto *pa = (__nv_bfloat16 *)(ws + L.a), *pb = (__nv_bfloat16 *)(ws + L.b);
   const I8Operand oa{(const uint8_t *)g.a, g.rsa, g.csa, g.M, pa};
   const I8Operand ob{(const uint8_t *)g.b, g.csb, g.rsb, g.N, pb};   // B^T
-  const int64_t kblocks = L.Kp / kCvtK;
+  // 64 x 256 blocks, or 64 x 128 while the deeper blocks would not give
+  // every SM two
+  const int64_t rows = (g.M + kCvtRows - 1) / kCvtRows + (g.N + kCvtRows - 1) / kCvtRows;
+  const int kc = rows * (L.Kp / 256) >= 2 * sm_count() ? 256 : 128;
+  const int64_t kblocks = L.Kp / kc;
   const int64_t blocks_a = (g.M + kCvtRows - 1) / kCvtRows * kblocks;
   const int64_t blocks_b = (g.N + kCvtRows - 1) / kCvtRows * kblocks;
   if (blocks_a + blocks_b >= (1ll << 31)) return cudaErrorInvalidConfiguration;
-  int8_pair_to_bf16<SIGNED><<<(unsigned)(blocks_a + blocks_b), 256, 0, s>>>(oa, ob, g.K, L.Kp,
-                                                                          blocks_a);
+  if (kc == 256)
+    int8_pair_to_bf16<SIGNED, 256><<<(unsigned)(blocks_a + blocks_b), 256, 0, s>>>(
+        oa, ob, g.K, L.Kp, blocks_a);
+  else
+    int8_pair_to_bf16<SIGNED, 128><<<(unsigned)(blocks_a + blocks_b), 256, 0, s>>>(
+        oa, ob, g.K, L.Kp, blocks_a);
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e) return e;

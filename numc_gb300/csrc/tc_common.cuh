@@ -93,13 +93,6 @@ __device__ __forceinline__ void griddep_launch_dependents() {
 
 // ---- TMA ----------------------------------------------------------------------
 
-// Makes this thread's ordinary shared-memory writes visible to the async
-// proxy (TMA stores, tcgen05.mma operand reads) once the consumer has
-// synchronised with it.
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
 __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap *m) {
   asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)m) : "memory");
 }
@@ -367,12 +360,6 @@ __device__ __forceinline__ void mma_commit_pair(uint32_t bar, uint16_t cta_mask)
 cudaError_t make_tmap_2d(CUtensorMap *m, const void *base, CUtensorMapDataType dtype,
                          int elem_bytes, uint64_t rows, uint64_t cols, uint64_t pitch_elems,
                          uint32_t box_rows, uint32_t box_cols);
-
-// Host: the same without swizzle (box rows stored densely, box_cols
-// elements each).
-cudaError_t make_tmap_2d_plain(CUtensorMap *m, const void *base, CUtensorMapDataType dtype,
-                               int elem_bytes, uint64_t rows, uint64_t cols,
-                               uint64_t pitch_elems, uint32_t box_rows, uint32_t box_cols);
 
 // Host: `planes` stacked row-major rows x cols matrices (plane pitch
 // rows * pitch_elems elements) as one 3-D tensor map with box

@@ -28,8 +28,7 @@ bool load_encoder() {
 
 cudaError_t encode(CUtensorMap *m, const void *base, CUtensorMapDataType dtype, int elem_bytes,
                    int rank, const cuuint64_t *dims, const cuuint64_t *strides,
-                   const cuuint32_t *box,
-                   CUtensorMapSwizzle swizzle = CU_TENSOR_MAP_SWIZZLE_128B) {
+                   const cuuint32_t *box) {
   if (!load_encoder()) return cudaErrorNotSupported;
   // TMA requires a 16-byte aligned base and 16-byte multiple strides.
   if ((uintptr_t)base & 15) return cudaErrorInvalidValue;
@@ -38,7 +37,7 @@ cudaError_t encode(CUtensorMap *m, const void *base, CUtensorMapDataType dtype, 
   if (((uint64_t)box[0] * elem_bytes) & 15) return cudaErrorInvalidValue;
   cuuint32_t estr[5] = {1, 1, 1, 1, 1};
   CUresult r = g_encode(m, dtype, rank, const_cast<void *>(base), dims, strides, box, estr,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
@@ -52,15 +51,6 @@ cudaError_t make_tmap_2d(CUtensorMap *m, const void *base, CUtensorMapDataType d
   cuuint64_t strides[1] = {pitch_elems * (cuuint64_t)elem_bytes};
   cuuint32_t box[2] = {box_cols, box_rows};
   return encode(m, base, dtype, elem_bytes, 2, dims, strides, box);
-}
-
-cudaError_t make_tmap_2d_plain(CUtensorMap *m, const void *base, CUtensorMapDataType dtype,
-                               int elem_bytes, uint64_t rows, uint64_t cols,
-                               uint64_t pitch_elems, uint32_t box_rows, uint32_t box_cols) {
-  cuuint64_t dims[2] = {cols, rows};
-  cuuint64_t strides[1] = {pitch_elems * (cuuint64_t)elem_bytes};
-  cuuint32_t box[2] = {box_cols, box_rows};
-  return encode(m, base, dtype, elem_bytes, 2, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE);
 }
 
 cudaError_t make_tmap_3d(CUtensorMap *m, const void *base, CUtensorMapDataType dtype,
