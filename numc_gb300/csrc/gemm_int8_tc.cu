@@ -397,9 +397,11 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
     }
     const bool staged = cso == 1 && (rso & 3) == 0 && (reinterpret_cast<uintptr_t>(C) & 3) == 0;
     if (ok && row < M && rule != kRuleX86Packed) {
+      const bool rf = simt::clamp_row_full(row, M, rule);
+      const int ncut = simt::clamp_col_limit(N, rule);
 #pragma unroll
       for (int j = 0; j < CW; j++)
-        d[j] = simt::fold8(0, d[j], true, rule, SIGNED, row, n0 + cbase + j, M, N);
+        d[j] = simt::narrow_once(d[j], rf && n0 + cbase + j < ncut, SIGNED);
     }
     if (ok && staged) {   // warp-uniform
       uint8_t *stage = smem + kStages * STAGE_BYTES + kBarBytes + (warp - 2) * 1024;
@@ -728,9 +730,11 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
         }
       } else {
         if (row < M) {
+          const bool rf = simt::clamp_row_full(row, M, rule);
+          const int ncut = simt::clamp_col_limit(N, rule);
 #pragma unroll
           for (int j = 0; j < CW; j++)
-            d[j] = simt::fold8(0, d[j], true, rule, SIGNED, row, n0 + cbase + j, M, N);
+            d[j] = simt::narrow_once(d[j], rf && n0 + cbase + j < ncut, SIGNED);
         }
         pack_bytes<CW>(d, w);
       }

@@ -148,6 +148,27 @@ __device__ __forceinline__ bool clamp_full(int64_t i, int64_t j, int64_t M, int6
   return (i - ic) < (mc / MR) * MR && j < (N / NR) * NR;
 }
 
+// The clamp-once rules' final narrowing of a row's outputs, with the tile
+// class split into its row and column halves in 32-bit arithmetic
+// (dimensions below 2^31): for every column j of the row,
+// narrow_once(...)[j] == fold8(0, P[j], true, rule, ...) for the NEON,
+// AVX-512 and wrap rules.
+__device__ __forceinline__ int32_t narrow_once(int32_t P, bool full, bool is_signed) {
+  if (full) return is_signed ? sat_s8(P) : ((uint32_t)P > 255u ? 255 : P);
+  return wrap8(P, is_signed);
+}
+__device__ __forceinline__ bool clamp_row_full(int i, int M, int rule) {
+  if (rule != kRuleNeon && rule != kRuleAvx512) return false;
+  const int MC = rule == kRuleNeon ? 72 : 240, MR = rule == kRuleNeon ? 6 : 12;
+  const int ic = i / MC * MC, mc = min(MC, M - ic);
+  return i - ic < mc / MR * MR;
+}
+// Columns below this are inside full tiles (with a full row).
+__device__ __forceinline__ int clamp_col_limit(int N, int rule) {
+  const int NR = rule == kRuleNeon ? 8 : 16;
+  return N / NR * NR;
+}
+
 // One K-block end for element (i, j): fold the block's partial sum P into
 // the stored value d according to the rule.  `first` marks block 0.
 // x86 packed rule with the element's tile class known (`full`: inside a
