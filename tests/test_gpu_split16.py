@@ -220,3 +220,22 @@ def test_tile_widths_store_identical_bits(tmp_path, ctas):
     assert np.isfinite(res["128"]).all()
     np.testing.assert_array_equal(res["128"].view(np.uint32), res["256"].view(np.uint32))
     np.testing.assert_array_equal(res["64"].view(np.uint32), res["256"].view(np.uint32))
+
+
+def test_programmatic_dependent_launch_changes_no_bits(tmp_path):
+    """The GEMM launched with programmatic dependent launch after its
+    operand pass (the default) and without it (NUMC_CUDA_PDL=0) store the
+    same bits."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    res = {}
+    for pdl in ("0", "1"):
+        path = str(tmp_path / f"c{pdl}.npy")
+        r = subprocess.run([sys.executable, "-c", _TILE_SCRIPT, path],
+                           env=dict(os.environ, NUMC_CUDA_PDL=pdl), cwd=root,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        res[pdl] = np.load(path)
+    np.testing.assert_array_equal(res["0"].view(np.uint32), res["1"].view(np.uint32))
