@@ -1,23 +1,25 @@
 // int8 / uint8 GEMM on the tcgen05 tensor cores with numc's store rules —
 // the tensor path for numc's gemm_i8_avx2 / gemm_u8_avx2
-// (src/intrinsics/gemm_avx2.h:2741-2880, 2983-3125) and gemm_i8_neon.
+// (src/intrinsics/gemm_avx2.h:2741-2880, 2983-3125), gemm_i8_neon and
+// gemm_i8_avx512.
 //
 // 8-bit integers are exact in bfloat16 (|x| <= 255 needs 8 significant
 // bits), products are exact in FP32, and so is every partial sum below
 // 2^24: a 512-deep K block of int8 products stays below 512 * 128^2 = 2^23,
 // a 256-deep block of uint8 products below 256 * 255^2 < 2^24.  The MMA
-// warp therefore accumulates one numc K block (int8: 8 slabs of 64; uint8:
-// two chunks of 4 slabs) per TMEM buffer, and the accumulator warps turn
-// each block's exact sum P_b into numc's stored byte with the same rule
-// the CUDA-core kernel uses (simt::fold8: x86 packed saturation per block
-// and tile class, NEON clamp-once, or truncation).  Results are bit-exact.
+// warp accumulates numc's K blocks in TMEM chunks, and the accumulator
+// warps turn the chunk sums into numc's stored bytes with the rule the
+// CUDA-core kernel uses (x86 packed saturation per block and tile class,
+// NEON / AVX-512 clamp-once, or truncation).  Results are bit-exact.
 //
 // Passes: one convert launch writes A as bf16 (M x Kp, K-major) and B^T as
-// bf16 (N x Kp), K padded to 512 with zeros; then one output tile per CTA:
-// 128 x 64 (24 KiB TMA ring stages, 8 of them, 320 threads) or, once the
-// 128 x 128 tiles give every SM one, 128 x 128 (32 KiB stages, 6 of them,
-// 576 threads): a TMA warp, an MMA warp and accumulator warps of 32 columns
-// each, which store their 32 output bytes of a row as two 16-byte stores.
+// bf16 (N x Kp), K padded to 512 with zeros.  Then either the persistent
+// CTA-pair kernel (int8_pair_gemm: 256 x 256 tiles, from about 2048^3) or
+// one output tile per CTA (int8_tc_gemm): 128 x 64 (24 KiB TMA ring
+// stages, 8 of them, 320 threads) or, once the 128 x 128 tiles give every
+// SM one, 128 x 128 (32 KiB stages, 6 of them, 576 threads): a TMA warp, an
+// MMA warp and accumulator warps of 32 columns each.  Both store their
+// output bytes through a per-warp staging buffer, whole rows a store.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
