@@ -33,13 +33,17 @@
 //
 // Kernels: row/column absolute maxima (atomicMax on the bit patterns),
 // slicing into s K-major bf16 planes per operand (B transposed), and the
-// GEMM: one 128 x 128 output tile per CTA; warp 0 streams one (A_p, B_q)
-// 64-deep slab pair per ring stage with TMA; warp 1 issues 4 tcgen05.mma
-// (M = N = 128) per stage into one of four TMEM buffers (one buffer per
-// chunk); warps 2-17 (four per TMEM lane quarter, 32 columns each) fold
-// finished chunks into the int64 accumulators and store.  (A 128 x 64 tile
-// fetched each slab pair for half the MMA work: 16 % tensor-active, bound by
-// the L2 -> shared-memory operand traffic.)
+// GEMM.  The default (ozaki_pair_gemm): persistent clusters of two CTAs on
+// 256 x 128 output tiles, one (A_p, B_q) 64-deep slab pair per ring stage,
+// cta_group::2 MMAs into two TMEM chunk buffers, the int64 Horner
+// accumulators held in TMEM and each diagonal's chunk sums kept as exact
+// FP32 partials (see the kernel).  ozaki_gemm (NUMC_CUDA_OZAKI_CTAS=1): one
+// 128 x 128 output tile per CTA; warp 0 streams one slab pair per ring
+// stage with TMA; warp 1 issues 4 tcgen05.mma (M = N = 128) per stage into
+// one of four TMEM buffers (one buffer per chunk); warps 2-17 (four per
+// TMEM lane quarter, 32 columns each) fold finished chunks into int64
+// accumulators in registers and store.  Both are bound by the L2 -> shared
+// memory operand stream: every diagonal fetches its slab pairs again.
 // Non-finite inputs are flagged and their tiles recomputed with FP64 FMA
 // chains (numc's arithmetic).
 #include <cuda.h>
