@@ -689,7 +689,17 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
                 const float v0 = __uint_as_float(d16[q] << 16);
                 const float v1 = __uint_as_float(d16[q] & 0xffff0000u);
                 float f0, f1;
-                if constexpr (ALL_FULL) {   // d = sat(d + P)
+                if constexpr (ALL_FULL && SIGNED) {
+                  // d = clamp(d + P, -128, 127) on the pair in bfloat16: the
+                  // FP32 sums are exact integers, bfloat16 keeps those up to
+                  // 256 in magnitude exactly and rounds larger ones to values
+                  // past the same bound
+                  const __nv_bfloat162 c = __hmin2(
+                      __hmax2(__floats2bfloat162_rn(v0 + p0, v1 + p1), __float2bfloat162_rn(-128.0f)),
+                      __float2bfloat162_rn(127.0f));
+                  d16[q] = *reinterpret_cast<const uint32_t *>(&c);
+                  continue;
+                } else if constexpr (ALL_FULL) {   // d = sat(d + P)
                   f0 = sat8_f<SIGNED>(v0 + p0);
                   f1 = sat8_f<SIGNED>(v1 + p1);
                 } else {
