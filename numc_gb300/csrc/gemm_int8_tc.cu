@@ -352,14 +352,12 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
     const int cbase = group * CW;
     const uint32_t lane_off = (uint32_t)(quad * 32) << 16;
     int32_t d[CW], part[CW];
-    uint32_t fullmask = 0;   // x86 rule: columns inside numc's full 6x16 tiles
-    const bool row_full = simt::x86_row_full(row, M);
+    // x86 rule: columns inside numc's full 6x16 tiles
+    const uint32_t fullmask = rule == kRuleX86Packed && simt::x86_row_full(row, M)
+                                  ? (uint32_t)simt::x86_col_mask(n0 + cbase, N, CW)
+                                  : 0u;
 #pragma unroll
-    for (int j = 0; j < CW; j++) {
-      d[j] = 0;
-      if (rule == kRuleX86Packed && row_full && simt::x86_col_full(n0 + cbase + j, N))
-        fullmask |= 1u << j;
-    }
+    for (int j = 0; j < CW; j++) d[j] = 0;
     const int nchunks = num_kb / CHUNK;   // num_kb is a multiple of the block size
     bool ok = true;
     for (int chunk = 0; chunk < nchunks; chunk++) {
@@ -649,15 +647,12 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
       // the wrapped int32 sums
       int32_t d[X86 ? 1 : CW];
       uint32_t d16[X86 ? CW / 2 : 1];
-      uint64_t fullmask = 0;   // x86 rule: columns inside numc's full 6x16 tiles
-      const bool row_full = X86 && simt::x86_row_full(row, M);
+      // x86 rule: columns inside numc's full 6x16 tiles
+      const uint64_t fullmask =
+          X86 && simt::x86_row_full(row, M) ? simt::x86_col_mask(n0 + cbase, N, CW) : 0ull;
+      if constexpr (!X86) {
 #pragma unroll
-      for (int j = 0; j < CW; j++) {
-        if constexpr (X86) {
-          if (row_full && simt::x86_col_full(n0 + cbase + j, N)) fullmask |= 1ull << j;
-        } else {
-          d[j] = 0;
-        }
+        for (int j = 0; j < CW; j++) d[j] = 0;
       }
 #pragma unroll
       for (int q = 0; q < (X86 ? CW / 2 : 1); q++) d16[q] = 0;

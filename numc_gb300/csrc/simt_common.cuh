@@ -136,6 +136,21 @@ __device__ __forceinline__ bool x86_col_full(int j, int N) {
   const int jc = j / 4080 * 4080, nc = min(4080, N - jc);
   return j - jc < nc / 16 * 16;
 }
+// x86_col_full of columns j0 .. j0 + W - 1 (W <= 64) as a bit mask (bit c
+// for column j0 + c): the full columns of an NC block are a prefix of it,
+// and W columns touch at most two NC blocks.
+__device__ __forceinline__ uint64_t x86_col_mask(int j0, int N, int W) {
+  auto prefix = [](int64_t n) -> uint64_t {   // bits [0, n), n clamped to [0, 64]
+    return n <= 0 ? 0ull : n >= 64 ? ~0ull : (1ull << n) - 1;
+  };
+  const int jc0 = j0 / 4080 * 4080;
+  const int64_t end0 = jc0 + min(4080, N - jc0) / 16 * 16;   // first non-full column of block 0
+  const int64_t jc1 = (int64_t)jc0 + 4080;
+  const int64_t end1 = jc1 + (N > jc1 ? min((int64_t)4080, N - jc1) / 16 * 16 : 0);
+  uint64_t m = prefix(end0 - j0);
+  if (jc1 < (int64_t)j0 + W) m |= prefix(end1 - j0) & ~prefix(jc1 - j0);
+  return m & prefix(W);
+}
 // Full MR x NR tile of a clamp-once int8 path that blocks M by MC (a
 // multiple of MR) and N by NR from column 0: numc's NEON build (72, 6, 8;
 // gemm_neon.h:1509-1535) and its AVX-512 build (240, 12, 16;
