@@ -481,6 +481,16 @@ __device__ __forceinline__ float fold8_x86_f(float d, float P, bool first, bool 
   if constexpr (SIGNED) return x > 127.0f ? x - 256.0f : (x < -128.0f ? x + 256.0f : x);
   return x > 255.0f ? x - 256.0f : x;
 }
+// s0 = low bfloat16 of `pair` + p0, s1 = high + p1, in FP32 (one
+// mixed-precision add each: the bfloat16 operand is widened exactly).
+__device__ __forceinline__ void add_bf16_pair(uint32_t pair, float p0, float p1, float &s0,
+                                              float &s1) {
+  asm("{\n .reg .b16 lo, hi;\n mov.b32 {lo, hi}, %2;\n"
+      " add.rn.f32.bf16 %0, lo, %3;\n add.rn.f32.bf16 %1, hi, %4;\n}"
+      : "=f"(s0), "=f"(s1)
+      : "r"(pair), "f"(p0), "f"(p1));
+}
+
 // f integral in [-128, 255]: 1.5 x 2^23 + f has f mod 256 as its low
 // mantissa byte.
 __device__ __forceinline__ uint32_t f_to_bits(float f) { return __float_as_uint(f + 12582912.0f); }
@@ -689,8 +699,10 @@ int8_pair_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ C
                   // FP32 sums are exact integers, bfloat16 keeps those up to
                   // 256 in magnitude exactly and rounds larger ones to values
                   // past the same bound
+                  float s0, s1;
+                  add_bf16_pair(d16[q], p0, p1, s0, s1);
                   const __nv_bfloat162 c = __hmin2(
-                      __hmax2(__floats2bfloat162_rn(v0 + p0, v1 + p1), __float2bfloat162_rn(-128.0f)),
+                      __hmax2(__floats2bfloat162_rn(s0, s1), __float2bfloat162_rn(-128.0f)),
                       __float2bfloat162_rn(127.0f));
                   d16[q] = *reinterpret_cast<const uint32_t *>(&c);
                   continue;
