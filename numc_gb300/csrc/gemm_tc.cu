@@ -691,7 +691,8 @@ cudaError_t launch_split_pass(const SplitLayout &L, const SplitBufs &b, const Ge
 
 template <int BN, int STAGES, int PLANES, int FLUSH, bool F16, int CTAS>
 cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, const Gemm &g,
-                               unsigned long long gen, unsigned *status, cudaStream_t s) {
+                               unsigned long long gen, unsigned *status, cudaStream_t s,
+                               bool pdl) {
   using Cfg = SplitCfg<BN, STAGES, PLANES, FLUSH, CTAS>;
   CUtensorMap ta, tb;
   cudaError_t e;
@@ -717,17 +718,18 @@ cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, cons
   fb.bias = (const float *)g.bias;
   fb.bias_stride = g.bias_stride;
   const int num_kb = (int)(L.Kp / kBK);
-  // programmatic dependent launch: the GEMM sets up while the split pass ends
-  cudaLaunchAttribute pdl;
-  pdl.id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  pdl.val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+  // programmatic dependent launch: the GEMM sets up while the split pass
+  // ends (only when that pass is the previous work in the stream)
+  cudaLaunchAttribute pdl_attr;
+  pdl_attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  pdl_attr.val.programmaticStreamSerializationAllowed = pdl && pdl_enabled() ? 1 : 0;
   if (CTAS == 1) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)std::min(tiles_m * tiles_n, sm_count()));
     cfg.blockDim = dim3(Cfg::THREADS);
     cfg.dynamicSmemBytes = Cfg::SMEM;
     cfg.stream = s;
-    cfg.attrs = &pdl;
+    cfg.attrs = &pdl_attr;
     cfg.numAttrs = 1;
     e = cudaLaunchKernelEx(&cfg, kern, ta, tb, (float *)g.c, (int64_t)g.rso, (int64_t)g.cso,
                            (int)g.M, (int)g.N, num_kb, tiles_m, tiles_n, vec4, status, fb,
@@ -740,7 +742,7 @@ cudaError_t launch_gemm_status(const SplitLayout &L, const SplitBufs &bufs, cons
     attr[0].val.clusterDim.x = CTAS;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
-    attr[1] = pdl;
+    attr[1] = pdl_attr;
     cfg.blockDim = dim3(Cfg::THREADS);
     cfg.dynamicSmemBytes = Cfg::SMEM;
     cfg.stream = s;
@@ -809,26 +811,26 @@ int split_tile_width(const Gemm &g, int ctas) {
 template <int CTAS>
 cudaError_t launch_gemm_ctas(const SplitLayout &L, const SplitBufs &ws, const Gemm &g,
                              unsigned long long gen, unsigned *status, cudaStream_t s,
-                             int narrow) {
+                             int narrow, bool pdl) {
   constexpr int S2 = CTAS == 2 ? 3 : 2;   // stages of the 2-plane ring
   if (L.f16 && L.flush == kF16DefaultFlush && narrow == 64)
     // 64-column single-CTA tiles: 48 KiB stages
-    return launch_gemm_status<64, 4, 2, kF16DefaultFlush, true, 1>(L, ws, g, gen, status, s);
+    return launch_gemm_status<64, 4, 2, kF16DefaultFlush, true, 1>(L, ws, g, gen, status, s, pdl);
   if (L.f16 && L.flush == kF16DefaultFlush && narrow == 128)
     // 128-column tiles: 48 KiB (pair) or 64 KiB (single CTA) stages
     return launch_gemm_status<128, CTAS == 2 ? 4 : 3, 2, kF16DefaultFlush, true, CTAS>(
-        L, ws, g, gen, status, s);
+        L, ws, g, gen, status, s, pdl);
   if (L.f16) {
     switch (L.flush) {
-    case 1: return launch_gemm_status<256, S2, 2, 1, true, CTAS>(L, ws, g, gen, status, s);
-    case 2: return launch_gemm_status<256, S2, 2, 2, true, CTAS>(L, ws, g, gen, status, s);
-    case 4: return launch_gemm_status<256, S2, 2, 4, true, CTAS>(L, ws, g, gen, status, s);
-    default: return launch_gemm_status<256, S2, 2, 8, true, CTAS>(L, ws, g, gen, status, s);
+    case 1: return launch_gemm_status<256, S2, 2, 1, true, CTAS>(L, ws, g, gen, status, s, pdl);
+    case 2: return launch_gemm_status<256, S2, 2, 2, true, CTAS>(L, ws, g, gen, status, s, pdl);
+    case 4: return launch_gemm_status<256, S2, 2, 4, true, CTAS>(L, ws, g, gen, status, s, pdl);
+    default: return launch_gemm_status<256, S2, 2, 8, true, CTAS>(L, ws, g, gen, status, s, pdl);
     }
   }
   if (L.planes == 3)
-    return launch_gemm_status<128, CTAS == 2 ? 3 : 2, 3, 1, false, CTAS>(L, ws, g, gen, status, s);
-  return launch_gemm_status<256, S2, 2, 8, false, CTAS>(L, ws, g, gen, status, s);
+    return launch_gemm_status<128, CTAS == 2 ? 3 : 2, 3, 1, false, CTAS>(L, ws, g, gen, status, s, pdl);
+  return launch_gemm_status<256, S2, 2, 8, false, CTAS>(L, ws, g, gen, status, s, pdl);
 }
 
 // CTA pairs unless NUMC_CUDA_SPLIT_CTAS=1 asks for single CTAs (for hosts
@@ -846,13 +848,13 @@ int split_ctas() {
 // Small problems that take 128-column tiles run them on single CTAs
 // (measured on GB300 at 512^3 - 1536^3: 0.5-0.7 us faster than pairs).
 cudaError_t launch_gemm(const SplitLayout &L, const SplitBufs &ws, const Gemm &g, unsigned long long gen,
-                        unsigned *status, cudaStream_t s) {
+                        unsigned *status, cudaStream_t s, bool pdl = true) {
   const int ctas = split_ctas();
   const int width = split_tile_width(g, ctas);
   const int narrow = width < 256 ? width : 0;   // 0: the wide tiles
   if (ctas == 2 && !(narrow && L.f16 && L.flush == kF16DefaultFlush))
-    return launch_gemm_ctas<2>(L, ws, g, gen, status, s, narrow);
-  return launch_gemm_ctas<1>(L, ws, g, gen, status, s, narrow);
+    return launch_gemm_ctas<2>(L, ws, g, gen, status, s, narrow, pdl);
+  return launch_gemm_ctas<1>(L, ws, g, gen, status, s, narrow, pdl);
 }
 
 int planes_for(int passes) { return passes == 6 ? 3 : 2; }
@@ -958,7 +960,10 @@ cudaError_t split_pipe_gemm(const SplitPipe &p, int panel, int bpanel, const Gem
     return cudaErrorInvalidValue;
   unsigned *status = status_word();
   if (!status) return cudaErrorMemoryAllocation;
-  return launch_gemm(pipe_params(p), pipe_bufs(p, panel, bpanel, (char *)ws), g, gen, status, s);
+  // the pipeline orders this GEMM after its panels' splits with events on
+  // other streams: no programmatic launch
+  return launch_gemm(pipe_params(p), pipe_bufs(p, panel, bpanel, (char *)ws), g, gen, status, s,
+                     false);
 }
 
 namespace {
