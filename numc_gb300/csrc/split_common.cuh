@@ -368,7 +368,22 @@ __device__ __forceinline__ void fused_scale_split_rows(
   // Pass 1: the row's largest magnitude (float32 bits) and non-finite values.
   unsigned m = 0;
   bool bad = false;
-  if (live) {
+  // rows contiguous and 16-byte aligned: float4 loads, k = 4 sub + 64 i
+  const bool vec = along_k && (rs_row & 3) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+  if (live && vec) {
+    const int K4 = K & ~3;
+#pragma unroll 4
+    for (int k = 4 * sub; k < K4; k += 64) {
+      const float4 x = *reinterpret_cast<const float4 *>(p + k);
+      bad |= !isfinite(x.x) || !isfinite(x.y) || !isfinite(x.z) || !isfinite(x.w);
+      m = max(m, max(max(absbits(x.x), absbits(x.y)), max(absbits(x.z), absbits(x.w))));
+    }
+    for (int k = K4 + sub; k < K; k += 16) {   // the last K % 4 columns
+      const float x = p[k];
+      bad |= !isfinite(x);
+      m = max(m, absbits(x));
+    }
+  } else if (live) {
 #pragma unroll 8
     for (int k = sub; k < K; k += 16) {
       const float x = p[(int64_t)k * rs_k];
@@ -445,8 +460,13 @@ __device__ __forceinline__ void fused_scale_split_rows(
 #pragma unroll 2
     for (int k = 4 * q; k < Kp; k += 64) {
       float rem[4];
+      if (vec && k + 4 <= K) {
+        const float4 x = *reinterpret_cast<const float4 *>(p2 + k);
+        rem[0] = x.x; rem[1] = x.y; rem[2] = x.z; rem[3] = x.w;
+      } else {
 #pragma unroll
-      for (int t = 0; t < 4; t++) rem[t] = k + t < K ? p2[(int64_t)(k + t) * rs_k] : 0.0f;
+        for (int t = 0; t < 4; t++) rem[t] = k + t < K ? p2[(int64_t)(k + t) * rs_k] : 0.0f;
+      }
       convert_store(rem, k);
     }
   }
