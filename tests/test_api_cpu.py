@@ -198,3 +198,18 @@ def test_workspace_sizes(M, K, N):
     assert nc.workspace_size("float64", nc.ALGO_DMMA, 0, M, K, N) == 0
     # split products: at least the two 16-bit planes of both operands
     assert nc.workspace_size("float32", nc.ALGO_SPLIT_FP16, 0, M, K, N) >= 4 * (M + N) * _up(K, 64)
+
+
+def test_int8_tile_schedule_param():
+    """NUMC_CUDA_ALGO_TC_INT8's param is the profile plus 16 x the tile
+    schedule: every schedule shares the workspace layout; schedules past
+    NUMC_INT8_TILE_PAIR256 and unknown profiles are refused (workspace size 0)."""
+    M, K, N = 300, 1100, 520
+    base = nc.workspace_size("int8", nc.ALGO_TC_INT8, nc.INT8_X86_AVX2, M, K, N)
+    assert base > 0
+    for tile in (nc.INT8_TILE_AUTO, nc.INT8_TILE_SINGLE, nc.INT8_TILE_PAIR128,
+                 nc.INT8_TILE_PAIR256):
+        for prof in (nc.INT8_X86_AVX2, nc.INT8_ARM_NEON, nc.INT8_WRAP, nc.INT8_X86_AVX512):
+            assert nc.workspace_size("uint8", nc.ALGO_TC_INT8, prof + 16 * tile, M, K, N) == base
+    assert nc.workspace_size("int8", nc.ALGO_TC_INT8, 16 * 4, M, K, N) == 0
+    assert nc.workspace_size("int8", nc.ALGO_TC_INT8, 16 * 2 + 9, M, K, N) == 0
