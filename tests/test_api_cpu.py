@@ -213,3 +213,11 @@ def test_int8_tile_schedule_param():
             assert nc.workspace_size("uint8", nc.ALGO_TC_INT8, prof + 16 * tile, M, K, N) == base
     assert nc.workspace_size("int8", nc.ALGO_TC_INT8, 16 * 4, M, K, N) == 0
     assert nc.workspace_size("int8", nc.ALGO_TC_INT8, 16 * 2 + 9, M, K, N) == 0
+
+
+def test_ctx_device_usage_without_device_arrays():
+    with nc.Ctx() as ctx:
+        ctx.zeros((4, 4), "float32")
+        assert ctx.device_usage() == (0, 0, 0)
+    n = ctypes.c_size_t()
+    assert nc.lib().numc_cuda_ctx_device_usage(None, ctypes.byref(n), None, None) == nc.ERR_NULL
