@@ -194,3 +194,15 @@ def test_both_kernels_within_bound(tmp_path, ctas):
         hi, lo = oracle.dot2_f64(a, b, *np.divmod(np.arange(M * N), N))
         err = np.abs(got - (hi + lo).reshape(M, N))
         assert (err <= _bound(a, b, s)).all(), (ctas, M, float((err / _bound(a, b, s)).max()))
+
+
+def test_long_k_flushes_partial_sums_within_a_diagonal():
+    """K = 70000, s = 8: the last diagonals have more chunks (over 2048) than
+    the CTA-pair kernel's FP32 partial sums hold exactly, so they are folded
+    into the int64 accumulators mid-diagonal; the bound still holds."""
+    M, K, N = 130, 70000, 140
+    a, b = synth.operands("expspread", M, K, N, dtype="float64", seed=17)
+    got = _oz(a, b, 8)
+    hi, lo = oracle.dot2_f64(a, b, *np.divmod(np.arange(M * N), N))
+    err = np.abs(got - (hi + lo).reshape(M, N))
+    assert (err <= _bound(a, b, 8)).all(), float((err / _bound(a, b, 8)).max())
