@@ -256,9 +256,12 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
              int tiles_m, int tiles_n, int rule, unsigned *status, WaitCfg wc) {
   constexpr int kNumBuf = I8Cfg<kBN>::kNumBuf, kStages = I8Cfg<kBN>::kStages;
   constexpr int kAccWarps = I8Cfg<kBN>::kAccWarps;
-  // slabs per TMEM chunk: a whole 512-deep block for int8, half for uint8
-  constexpr int CHUNK = SIGNED ? kBlockK / kBK : kBlockK / kBK / 2;
-  constexpr int CHUNKS_PER_BLOCK = kBlockK / kBK / CHUNK;
+  // slabs per TMEM chunk: a whole 512-deep block, except for uint8 under
+  // the rules that need its exact sum (two 256-deep halves; the x86 rule
+  // decides every byte from a rounded sum past 2^24 as from the exact one,
+  // see int8_pair_gemm)
+  const int chunk_log2 = (SIGNED || rule == kRuleX86Packed) ? 3 : 2;
+  const int CHUNK = 1 << chunk_log2, CHUNKS_PER_BLOCK = (kBlockK / kBK) >> chunk_log2;
   constexpr uint32_t A_BYTES = kBM * kBK * 2, B_BYTES = kBN * kBK * 2;
   constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
   extern __shared__ uint8_t smem_raw[];
@@ -321,8 +324,8 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
     if (lane == 0) {
       constexpr uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
       for (int kb = 0; kb < num_kb; kb++) {
-        const int s = kb % kStages, chunk = kb / CHUNK, buf = chunk % kNumBuf;
-        const bool cstart = kb % CHUNK == 0, cend = kb % CHUNK == CHUNK - 1;
+        const int s = kb % kStages, chunk = kb >> chunk_log2, buf = chunk % kNumBuf;
+        const bool cstart = (kb & (CHUNK - 1)) == 0, cend = (kb & (CHUNK - 1)) == CHUNK - 1;
         if (cstart && chunk >= kNumBuf &&
             !tc::mbar_wait_bounded(tc::smem_u32(&tempty[buf]), ((chunk / kNumBuf) & 1) ^ 1,
                                    status, kStatusTimeoutMma, wc.limit_ns))
@@ -358,7 +361,7 @@ int8_tc_gemm(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUt
                                   : 0u;
 #pragma unroll
     for (int j = 0; j < CW; j++) d[j] = 0;
-    const int nchunks = num_kb / CHUNK;   // num_kb is a multiple of the block size
+    const int nchunks = num_kb >> chunk_log2;   // num_kb is a multiple of the block size
     bool ok = true;
     for (int chunk = 0; chunk < nchunks; chunk++) {
       const int buf = chunk % kNumBuf;

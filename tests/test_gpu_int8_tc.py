@@ -142,11 +142,13 @@ def test_unaligned_and_general_strides(dt):
 @pytest.mark.parametrize("dt", ["int8", "uint8"])
 @pytest.mark.parametrize("profile", [nc.INT8_X86_AVX2, nc.INT8_ARM_NEON, nc.INT8_X86_AVX512],
                          ids=["x86", "neon", "avx512"])
-def test_long_k_sums_past_2_31(dt, profile):
+@pytest.mark.parametrize("tile", [nc.INT8_TILE_SINGLE, nc.INT8_TILE_PAIR256],
+                         ids=["single", "pair256"])
+def test_long_k_sums_past_2_31(dt, profile, tile):
     """K = 140000 with every entry at the dtype's extreme: the exact int32
     sums pass 2^31 (the clamp-once rules narrow the wrapped sum), the x86
-    rule folds 274 blocks; the CTA-pair schedule against the oracle."""
+    rule folds 274 blocks (uint8 block sums past 2^24); against the oracle."""
     M, K, N = 260, 140000, 264
     a, b = synth.operands("extreme", M, K, N, dtype=dt, seed=21)
-    np.testing.assert_array_equal(_tc(a, b, profile, nc.INT8_TILE_PAIR256),
+    np.testing.assert_array_equal(_tc(a, b, profile, tile),
                                   oracle.matmul(a, b, ORACLE_PROFILE[profile]))
