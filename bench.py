@@ -487,6 +487,8 @@ def accuracy_summary(r):
         out["int8_1024_bitexact_neon_avx512_builds"] = all(
             v["bitexact_vs_numc"] for k, d in ints.items()
             if k.endswith("_neon") or k.endswith("_avx512") for v in d.values())
+        out["int8_4096_tensor_equals_simt"] = all(
+            ints[k]["tensor_equals_simt"] for k in ("int8_4096", "int8_4096_neon_rule") if k in ints)
     return out
 
 
@@ -802,9 +804,15 @@ def int_workload(nc, torch, synth, dev):
     ms_ = time_gemm(nc, torch, ta_, tb_, tc_, nc.ALGO_TC_INT8, nc.INT8_X86_AVX2, steps=20, warmup=2)
     ints["int8_4096"] = {"tensor_tops": 2.0 * 4096 ** 3 / ms_ / 1e9, "tensor_ms": ms_,
                          "simt_ms": ms_s, "tensor_equals_simt": bool(torch.equal(tc_, ref_))}
+    # the same under numc's NEON rule (the GB300 host's own numc build)
+    ms_s = time_gemm(nc, torch, ta_, tb_, tc_, nc.ALGO_SIMT, nc.INT8_ARM_NEON, steps=1, warmup=1)
+    ref_ = tc_.clone()
+    ms_ = time_gemm(nc, torch, ta_, tb_, tc_, nc.ALGO_TC_INT8, nc.INT8_ARM_NEON, steps=20, warmup=2)
+    ints["int8_4096_neon_rule"] = {"tensor_tops": 2.0 * 4096 ** 3 / ms_ / 1e9, "tensor_ms": ms_,
+                              "simt_ms": ms_s, "tensor_equals_simt": bool(torch.equal(tc_, ref_))}
     ints["timing"] = ("1024^3: device time per call from 50 calls in a CUDA graph (eager_ms: "
                       "the same calls issued one by one from Python, host overhead included); "
-                      "4096^3: CUDA events around 20 eager calls")
+                      "4096^3 (x86 and NEON rules): CUDA events around 20 eager calls")
     return ints
 
 
