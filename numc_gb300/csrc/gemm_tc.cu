@@ -147,6 +147,187 @@ void launch_split_planes(dim3 grid, cudaStream_t s, int mode, const float *src, 
                                                       flags, flag_rows, gen, maxbits);
 }
 
+// Which one-launch float16 scale-and-split kernels run (NUMC_CUDA_SPLIT_PASS,
+// a bit mask read once; default 3): bit 0 scale_split_rows for k-contiguous
+// operands (A), bit 1 scale_split_cols for rows-contiguous ones (B^T of a
+// row-major B); a clear bit runs the scale pass and the split pass instead.
+// Every setting writes the same planes, maxima and flags.
+int split_pass_kernels() {
+  static const int v = [] {
+    const char *e = getenv("NUMC_CUDA_SPLIT_PASS");
+    return e && e[0] >= '0' && e[0] <= '3' && !e[1] ? e[0] - '0' : 3;
+  }();
+  return v;
+}
+
+// Scale and split of k-contiguous, 16-byte aligned rows (read mode 1) with
+// Kp <= 1024 V: one row a block, each value read once (scale_split_row_regs).
+constexpr int kRowRegsMaxKp = 16384;
+
+template <int V>
+__global__ void __launch_bounds__(256)
+scale_split_rows(const float *__restrict__ src, int64_t rs_row, int64_t R, int K, int Kp,
+                 uint16_t *__restrict__ planes, unsigned long long *flags, int flag_rows,
+                 unsigned *__restrict__ maxbits, unsigned long long gen) {
+  tc::griddep_launch_dependents();   // the GEMM may launch and set up meanwhile
+  scale_split_row_regs<V>(src, rs_row, R, K, Kp, (int64_t)blockIdx.x, planes, flags, flag_rows,
+                          maxbits, gen);
+}
+
+// Scale and split of rows-contiguous operands (read mode 2: the columns of a
+// row-major B, as B^T's rows), each value read once and held in registers
+// while the row maxima are found.  A row's maximum needs all of K, more
+// than one CTA's registers hold, so a cluster of 8 CTAs takes 16 rows: CTA q
+// of the cluster holds k in [q Kc, (q + 1) Kc), Kc = Kp / 8, and the CTAs'
+// partial maxima are combined through distributed shared memory.  Thread t
+// holds rows 4 (t % 4) .. + 3 at NQ k-quads, k = 4 (t / 4 + 128 p) + 0..3:
+// a warp load covers 8 k x 64 contiguous bytes, a warp store 4 rows x 64
+// contiguous bytes of a plane.  Same arithmetic as split_tile<2, true>
+// after absmax_rows_f32.
+constexpr int kColCluster = 8, kColRows = 16, kColThreads = 512;
+
+template <int NQ>
+__global__ void __cluster_dims__(kColCluster, 1, 1) __launch_bounds__(kColThreads, 2)
+scale_split_cols(const float *__restrict__ src, int64_t rs_k, int64_t R, int64_t K, int Kp,
+                 uint16_t *__restrict__ planes, unsigned long long *flags, int flag_rows,
+                 unsigned *__restrict__ maxbits, unsigned long long gen) {
+  __shared__ unsigned red[kColThreads / 32][kColRows];
+  __shared__ unsigned pmax[kColRows], fmax[kColRows];
+  tc::griddep_launch_dependents();   // the GEMM may launch and set up meanwhile
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t q = tc::cluster_ctarank();
+  const int Kc = Kp / kColCluster;   // a multiple of 8: a k-quad is all in or all out
+  const int64_t r0 = (int64_t)(blockIdx.x / kColCluster) * kColRows;
+  const int cg = tid & 3;
+  const int64_t rr = r0 + 4 * cg, klo = (int64_t)q * Kc;
+  // v[p][t]: rows rr .. rr + 3 at k = klo + 4 (tid / 4 + 128 p) + t
+  float4 v[NQ][4];
+#pragma unroll
+  for (int p = 0; p < NQ; p++) {
+    const int kl = 4 * ((tid >> 2) + 128 * p);
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      const int64_t k = klo + kl + t;
+      v[p][t] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (kl < Kc && k < K) {
+        const float *ptr = src + k * rs_k + rr;
+        if (rr + 3 < R) {
+          v[p][t] = __ldcs(reinterpret_cast<const float4 *>(ptr));
+        } else {
+          if (rr < R) v[p][t].x = ptr[0];
+          if (rr + 1 < R) v[p][t].y = ptr[1];
+          if (rr + 2 < R) v[p][t].z = ptr[2];
+        }
+      }
+    }
+  }
+  unsigned m[4] = {0, 0, 0, 0};
+  bool bad = false;
+#pragma unroll
+  for (int p = 0; p < NQ; p++)
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      const float x[4] = {v[p][t].x, v[p][t].y, v[p][t].z, v[p][t].w};
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        bad |= !isfinite(x[j]);
+        m[j] = max(m[j], absbits(x[j]));
+      }
+    }
+#pragma unroll
+  for (int j = 0; j < 4; j++) {   // lanes of one row group: lane % 4 equal
+    m[j] = max(m[j], __shfl_xor_sync(0xffffffffu, m[j], 4));
+    m[j] = max(m[j], __shfl_xor_sync(0xffffffffu, m[j], 8));
+    m[j] = max(m[j], __shfl_xor_sync(0xffffffffu, m[j], 16));
+  }
+  if (lane < 4)
+#pragma unroll
+    for (int j = 0; j < 4; j++) red[warp][4 * lane + j] = m[j];
+  const int anybad = __syncthreads_or(bad);
+  if (tid < kColRows) {
+    unsigned mm = 0;
+#pragma unroll
+    for (int w = 0; w < kColThreads / 32; w++) mm = max(mm, red[w][tid]);
+    pmax[tid] = mm;
+  }
+  if (tid == 0 && anybad) flags[r0 / flag_rows] = gen;
+  __syncwarp();
+  tc::cluster_sync();   // every CTA's partial maxima written
+  if (tid < kColRows) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(&pmax[tid]);
+    unsigned mm = 0;
+#pragma unroll
+    for (uint32_t c = 0; c < kColCluster; c++)
+      mm = max(mm, tc::ld_shared_cluster_u32(tc::mapa_shared(a, c)));
+    fmax[tid] = mm;
+    if (q == 0 && r0 + tid < R) maxbits[r0 + tid] = mm;
+  }
+  __syncwarp();
+  tc::cluster_arrive();   // done reading the peers' partial maxima
+  __syncthreads();
+  const int64_t plane_elems = R * Kp;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const int64_t r = rr + j;
+    if (r >= R) break;
+    const int sexp = f16_scale_exp(fmax[4 * cg + j]);
+    uint16_t *dst = planes + r * Kp + klo;
+#pragma unroll
+    for (int p = 0; p < NQ; p++) {
+      const int kl = 4 * ((tid >> 2) + 128 * p);
+      if (kl >= Kc) continue;
+      const float rem[4] = {(&v[p][0].x)[j], (&v[p][1].x)[j], (&v[p][2].x)[j], (&v[p][3].x)[j]};
+      uint16_t out[2][4];
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        float x = isfinite(rem[t]) ? scale_pow2(rem[t], sexp) : 0.0f;   // |x| < 2^15
+#pragma unroll
+        for (int pl = 0; pl < 2; pl++) {
+          const __half h = __float2half_rn(x);
+          out[pl][t] = __half_as_ushort(h);
+          x -= __half2float(h);   // exact
+        }
+      }
+#pragma unroll
+      for (int pl = 0; pl < 2; pl++) {
+        uint2 w;
+        w.x = (uint32_t)out[pl][0] | ((uint32_t)out[pl][1] << 16);
+        w.y = (uint32_t)out[pl][2] | ((uint32_t)out[pl][3] << 16);
+        *reinterpret_cast<uint2 *>(dst + pl * plane_elems + kl) = w;
+      }
+    }
+  }
+  __syncwarp();
+  tc::cluster_wait();   // no CTA leaves while a peer may read its maxima
+}
+
+// Largest Kp scale_split_cols takes: NQ = 2 (32 values a thread; more
+// would not fit the 64 registers of two 512-thread CTAs an SM).
+constexpr int kColMaxKp = kColCluster * 512 * 2;
+
+// Launch scale_split_cols on R rows (false if its clusters cannot be
+// resident on this device: the caller runs the two passes instead).
+bool launch_split_cols(const float *src, int64_t rs_k, int64_t R, int64_t K, int64_t Kp,
+                       uint16_t *planes, unsigned long long *flags, int flag_rows,
+                       unsigned *maxbits, unsigned long long gen, cudaStream_t s,
+                       cudaError_t *err) {
+  const int64_t clusters = (R + kColRows - 1) / kColRows;
+  if (clusters * kColCluster >= (1ll << 31)) return false;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(clusters * kColCluster));
+  cfg.blockDim = dim3(kColThreads);
+  cfg.stream = s;
+  auto go = [&](auto kern, LaunchCache &lc) {
+    if (clusters_once(lc, (const void *)kern, cfg) <= 0) return false;
+    *err = cudaLaunchKernelEx(&cfg, kern, src, rs_k, R, K, (int)Kp, planes, flags, flag_rows,
+                              maxbits, gen);
+    return true;
+  };
+  static LaunchCache lc1, lc2;
+  if (Kp <= kColCluster * 512) return go(scale_split_cols<1>, lc1);
+  return go(scale_split_cols<2>, lc2);
+}
+
 // Both operands of one float16-plane split through fused_scale_split_rows:
 // blocks [0, a_blocks) take 16 rows of A each, the
 // rest 16 columns of B.  One launch replaces two zeroings of the maxima,
@@ -631,16 +812,42 @@ cudaError_t split_operand(const SplitLayout &L, const float *src, int64_t rs_row
                           int64_t R, int64_t K, uint16_t *planes, unsigned long long *flags,
                           int flag_rows, unsigned *maxbits, unsigned long long gen,
                           cudaStream_t s) {
+  const int mode = split_mode(src, rs_row, rs_k);
+  cudaError_t e = cudaSuccess;
+  if (L.f16 && mode == 2 && L.Kp <= kColMaxKp && (split_pass_kernels() & 2) &&
+      launch_split_cols(src, rs_k, R, K, L.Kp, planes, flags, flag_rows, maxbits, gen, s, &e)) {
+    if (e) return e;
+    count_launch(1);
+    return cudaGetLastError();
+  }
   const dim3 grid((unsigned)((L.Kp + kSplitK - 1) / kSplitK),
                   (unsigned)((R + kSplitRows - 1) / kSplitRows));
   if (grid.y > 65535) return cudaErrorInvalidConfiguration;
-  const int mode = split_mode(src, rs_row, rs_k);
-  if (L.f16) {
+  if (L.f16 && mode == 1 && L.Kp <= kRowRegsMaxKp && R < (1ll << 31) &&
+      (split_pass_kernels() & 1)) {
+    const unsigned blocks = (unsigned)R;
+    const int k = (int)K, kp = (int)L.Kp;
+    if (L.Kp <= 1024)
+      scale_split_rows<1><<<blocks, 256, 0, s>>>(src, rs_row, R, k, kp, planes, flags, flag_rows,
+                                                 maxbits, gen);
+    else if (L.Kp <= 2048)
+      scale_split_rows<2><<<blocks, 256, 0, s>>>(src, rs_row, R, k, kp, planes, flags, flag_rows,
+                                                 maxbits, gen);
+    else if (L.Kp <= 4096)
+      scale_split_rows<4><<<blocks, 256, 0, s>>>(src, rs_row, R, k, kp, planes, flags, flag_rows,
+                                                 maxbits, gen);
+    else if (L.Kp <= 8192)
+      scale_split_rows<8><<<blocks, 256, 0, s>>>(src, rs_row, R, k, kp, planes, flags, flag_rows,
+                                                 maxbits, gen);
+    else
+      scale_split_rows<16><<<blocks, 256, 0, s>>>(src, rs_row, R, k, kp, planes, flags,
+                                                  flag_rows, maxbits, gen);
+    count_launch(1);
+  } else if (L.f16) {
     const int amode = absmax_mode(mode, rs_k);
     const dim3 rg = absmax_grid(R, K, amode);
     if (rg.y > 65535) return cudaErrorInvalidConfiguration;
-    cudaError_t e = cudaMemsetAsync(maxbits, 0, (size_t)R * 4, s);
-    if (e != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(maxbits, 0, (size_t)R * 4, s))) return e;
     absmax_rows_f32<<<rg, 256, 0, s>>>(src, rs_row, rs_k, R, K, amode, maxbits);
     launch_split_planes<2, true>(grid, s, mode, src, rs_row, rs_k, R, K, L.Kp, planes, flags,
                                  flag_rows, gen, maxbits);

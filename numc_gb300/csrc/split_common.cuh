@@ -120,19 +120,22 @@ __device__ __forceinline__ void absmax_block(const float *__restrict__ src, int6
     const int64_t k0 = bk * kk;
     unsigned m[4] = {0, 0, 0, 0};
     if (r < R) {
-      const int64_t k1 = k0 + kk < K ? k0 + kk : K;
-      for (int64_t k = k0; k < k1; k++) {
-        const float *p = src + r + k * rs_k;
-        if (r + 3 < R) {
+      const int n = (int)((k0 + kk < K ? k0 + kk : K) - k0);
+      const float *p = src + r + k0 * rs_k;
+      if (r + 3 < R) {
+        // 8 independent 16-byte loads in flight a thread
+#pragma unroll 8
+        for (int k = 0; k < n; k++, p += rs_k) {
           const float4 v = *reinterpret_cast<const float4 *>(p);
           m[0] = max(m[0], absbits(v.x));
           m[1] = max(m[1], absbits(v.y));
           m[2] = max(m[2], absbits(v.z));
           m[3] = max(m[3], absbits(v.w));
-        } else {
+        }
+      } else {
+        for (int k = 0; k < n; k++, p += rs_k)
           for (int t = 0; t < 4; t++)
             if (r + t < R) m[t] = max(m[t], absbits(p[t]));
-        }
       }
     }
     for (int t = 0; t < 4; t++)
@@ -468,6 +471,93 @@ __device__ __forceinline__ void fused_scale_split_rows(
         for (int t = 0; t < 4; t++) rem[t] = k + t < K ? p2[(int64_t)(k + t) * rs_k] : 0.0f;
       }
       convert_store(rem, k);
+    }
+  }
+}
+
+// ---- one k-contiguous row per block, held in registers -----------------------
+//
+// Scale and split of row `r` of an operand whose rows are contiguous along k
+// and 16-byte aligned (split read mode 1), by a 256-thread block: thread t
+// loads k = 4 t + 1024 i, i < V, as float4 (V * 1024 >= Kp), the block
+// reduces the row's largest magnitude, and the same registers are converted
+// to the two float16 planes — each float32 read from HBM once, no second
+// read and no shared-memory staging.  Writes maxbits[r] directly and, for a
+// non-finite value, flags[r / flag_rows] = gen.  Same arithmetic as
+// split_tile<2, true> after absmax_rows_f32, so the planes are the same bits.
+template <int V>
+__device__ __forceinline__ void scale_split_row_regs(const float *__restrict__ src,
+                                                     int64_t rs_row, int64_t R, int K, int Kp,
+                                                     int64_t r, uint16_t *__restrict__ planes,
+                                                     unsigned long long *flags, int flag_rows,
+                                                     unsigned *__restrict__ maxbits,
+                                                     unsigned long long gen) {
+  __shared__ unsigned wmax[8], wbad[8];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const float *row = src + r * rs_row;
+  float4 v[V];
+  unsigned m = 0;
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < V; i++) {
+    const int k = 4 * tid + 1024 * i;
+    v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (k + 4 <= K) {
+      v[i] = __ldcs(reinterpret_cast<const float4 *>(row + k));
+    } else if (k < K) {
+      v[i].x = row[k];
+      if (k + 1 < K) v[i].y = row[k + 1];
+      if (k + 2 < K) v[i].z = row[k + 2];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < V; i++) {
+    bad |= !isfinite(v[i].x) || !isfinite(v[i].y) || !isfinite(v[i].z) || !isfinite(v[i].w);
+    m = max(m, max(max(absbits(v[i].x), absbits(v[i].y)), max(absbits(v[i].z), absbits(v[i].w))));
+  }
+  m = __reduce_max_sync(0xffffffffu, m);
+  const unsigned b = __any_sync(0xffffffffu, bad);
+  if (lane == 0) {
+    wmax[warp] = m;
+    wbad[warp] = b;
+  }
+  __syncthreads();
+  m = wmax[0];
+  unsigned anybad = wbad[0];
+#pragma unroll
+  for (int w = 1; w < 8; w++) {
+    m = max(m, wmax[w]);
+    anybad |= wbad[w];
+  }
+  if (tid == 0) {
+    maxbits[r] = m;
+    if (anybad) flags[r / flag_rows] = gen;
+  }
+  const int sexp = f16_scale_exp(m);
+  const int64_t plane_elems = R * Kp;
+  uint16_t *dst = planes + r * Kp;
+#pragma unroll
+  for (int i = 0; i < V; i++) {
+    const int k = 4 * tid + 1024 * i;
+    if (k >= Kp) continue;
+    const float rem[4] = {v[i].x, v[i].y, v[i].z, v[i].w};
+    uint16_t out[2][4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      float x = isfinite(rem[t]) ? scale_pow2(rem[t], sexp) : 0.0f;   // |x| < 2^15
+#pragma unroll
+      for (int pl = 0; pl < 2; pl++) {
+        const __half h = __float2half_rn(x);
+        out[pl][t] = __half_as_ushort(h);
+        x -= __half2float(h);   // exact
+      }
+    }
+#pragma unroll
+    for (int pl = 0; pl < 2; pl++) {
+      uint2 w;
+      w.x = (uint32_t)out[pl][0] | ((uint32_t)out[pl][1] << 16);
+      w.y = (uint32_t)out[pl][2] | ((uint32_t)out[pl][3] << 16);
+      *reinterpret_cast<uint2 *>(dst + pl * plane_elems + k) = w;
     }
   }
 }

@@ -222,6 +222,64 @@ def test_tile_widths_store_identical_bits(tmp_path, ctas):
     np.testing.assert_array_equal(res["64"].view(np.uint32), res["256"].view(np.uint32))
 
 
+_LAYOUT_SCRIPT = r"""
+import sys
+import numpy as np, torch
+import numc_gb300 as nc
+from numc_gb300 import synth
+out = []
+for (M, K, N), kind, special in [((300, 1027, 260), "normal", False),
+                                 ((513, 4097, 200), "illscaled", False),
+                                 ((64, 8197, 96), "uniform", False),
+                                 ((256, 8192, 128), "normal", False),
+                                 ((130, 2048, 72), "normal", True),
+                                 ((40, 1500, 33), "illscaled", True)]:
+    a, b = synth.operands(kind, M, K, N, dtype="float32", seed=M + K)
+    if special:
+        a[3, 17] = np.inf
+        a[70 % M, K - 1] = np.nan
+        a[5, :] = 0.0
+        b[K // 2, 9] = -np.inf
+        b[:, 11] = 0.0
+    # A as a view with a row stride padded to a multiple of 4 floats: rows
+    # k-contiguous and 16-byte aligned even where K is not a multiple of 4
+    pa = torch.zeros((M, (K + 3) // 4 * 4 + 4), device="cuda")
+    pa[:, :K] = torch.from_numpy(a).cuda()
+    tb = torch.from_numpy(b).cuda()
+    for algo in (nc.ALGO_SPLIT_FP16, nc.ALGO_SPLIT_BF16):
+        for ta in (torch.from_numpy(a).cuda(), pa[:, :K]):
+            c = torch.full((M, N), float("nan"), device="cuda")
+            nc.gemm(ta, tb, c, algo=algo)
+            nc.check_status()
+            out.append(c.cpu().numpy().ravel())
+np.save(sys.argv[1], np.concatenate(out))
+"""
+
+
+def test_split_pass_layouts_write_same_planes(tmp_path):
+    """The one-launch scale-and-split kernels (NUMC_CUDA_SPLIT_PASS bit 0:
+    each k-contiguous row of A held in registers; bit 1: the columns of a
+    row-major B held in the registers of a cluster of 8 CTAs) write the
+    same planes, maxima and non-finite flags as the scale pass followed by
+    the split pass: identical output bits, with ragged K and N, K up to and
+    above 8192, padded row strides, infinities, NaNs and zero rows and
+    columns, and bfloat16 planes unchanged."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    res = {}
+    for v in ("0", "1", "2", "3"):
+        path = str(tmp_path / f"c{v}.npy")
+        r = subprocess.run([sys.executable, "-c", _LAYOUT_SCRIPT, path],
+                           env=dict(os.environ, NUMC_CUDA_SPLIT_PASS=v), cwd=root,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        res[v] = np.load(path)
+    for v in ("1", "2", "3"):
+        np.testing.assert_array_equal(res["0"].view(np.uint32), res[v].view(np.uint32))
+
+
 def test_programmatic_dependent_launch_changes_no_bits(tmp_path):
     """The GEMM launched with programmatic dependent launch after its
     operand pass (the default) and without it (NUMC_CUDA_PDL=0) store the
