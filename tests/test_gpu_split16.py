@@ -222,18 +222,14 @@ def test_tile_widths_store_identical_bits(tmp_path, ctas):
     np.testing.assert_array_equal(res["64"].view(np.uint32), res["256"].view(np.uint32))
 
 
-_LAYOUT_SCRIPT = r"""
-import sys
-import numpy as np, torch
-import numc_gb300 as nc
-from numc_gb300 import synth
-out = []
-for (M, K, N), kind, special in [((300, 1027, 260), "normal", False),
-                                 ((513, 4097, 200), "illscaled", False),
-                                 ((64, 8197, 96), "uniform", False),
-                                 ((256, 8192, 128), "normal", False),
-                                 ((130, 2048, 72), "normal", True),
-                                 ((40, 1500, 33), "illscaled", True)]:
+# (M, K, N), input kind, with special values
+_LAYOUT_CASES = [((300, 1027, 260), "normal", False), ((513, 4097, 200), "illscaled", False),
+                 ((64, 8197, 96), "uniform", False), ((256, 8192, 128), "normal", False),
+                 ((130, 2048, 72), "normal", True), ((40, 1500, 33), "illscaled", True)]
+
+
+def _layout_operands(shape, kind, special):
+    M, K, N = shape
     a, b = synth.operands(kind, M, K, N, dtype="float32", seed=M + K)
     if special:
         a[3, 17] = np.inf
@@ -241,15 +237,32 @@ for (M, K, N), kind, special in [((300, 1027, 260), "normal", False),
         a[5, :] = 0.0
         b[K // 2, 9] = -np.inf
         b[:, 11] = 0.0
+    return a, b
+
+
+_LAYOUT_SCRIPT = r"""
+import sys
+import numpy as np, torch
+import numc_gb300 as nc
+sys.path.insert(0, "tests")
+from test_gpu_split16 import _LAYOUT_CASES, _layout_operands
+out = []
+for shape, kind, special in _LAYOUT_CASES:
+    M, K, N = shape
+    a, b = _layout_operands(shape, kind, special)
     # A as a view with a row stride padded to a multiple of 4 floats: rows
     # k-contiguous and 16-byte aligned even where K is not a multiple of 4
     pa = torch.zeros((M, (K + 3) // 4 * 4 + 4), device="cuda")
     pa[:, :K] = torch.from_numpy(a).cuda()
     tb = torch.from_numpy(b).cuda()
+    # column-major views: A's rows contiguous (A split like a row-major B),
+    # B's columns contiguous along k (B split like a row-major A)
+    ta_t = torch.from_numpy(np.ascontiguousarray(a.T)).cuda().t()
+    tb_t = torch.from_numpy(np.ascontiguousarray(b.T)).cuda().t()
     for algo in (nc.ALGO_SPLIT_FP16, nc.ALGO_SPLIT_BF16):
-        for ta in (torch.from_numpy(a).cuda(), pa[:, :K]):
+        for ta, tbb in ((torch.from_numpy(a).cuda(), tb), (pa[:, :K], tb), (ta_t, tb_t)):
             c = torch.full((M, N), float("nan"), device="cuda")
-            nc.gemm(ta, tb, c, algo=algo)
+            nc.gemm(ta, tbb, c, algo=algo)
             nc.check_status()
             out.append(c.cpu().numpy().ravel())
 np.save(sys.argv[1], np.concatenate(out))
@@ -258,12 +271,14 @@ np.save(sys.argv[1], np.concatenate(out))
 
 def test_split_pass_layouts_write_same_planes(tmp_path):
     """The one-launch scale-and-split kernels (NUMC_CUDA_SPLIT_PASS bit 0:
-    each k-contiguous row of A held in registers; bit 1: the columns of a
-    row-major B held in the registers of a cluster of 8 CTAs) write the
-    same planes, maxima and non-finite flags as the scale pass followed by
-    the split pass: identical output bits, with ragged K and N, K up to and
-    above 8192, padded row strides, infinities, NaNs and zero rows and
-    columns, and bfloat16 planes unchanged."""
+    each k-contiguous row held in registers; bit 1: rows-contiguous operands
+    — a row-major B, a column-major A — held in the registers of a cluster
+    of 8 CTAs) write the same planes, maxima and non-finite flags as the
+    scale pass followed by the split pass: identical output bits, with
+    ragged K and N, K up to and above 8192, padded row strides, column-major
+    operands, infinities, NaNs and zero rows and columns, and bfloat16
+    planes unchanged; the default's float16 results meet the error bound
+    against the oracle."""
     import os
     import subprocess
     import sys
@@ -278,6 +293,18 @@ def test_split_pass_layouts_write_same_planes(tmp_path):
         res[v] = np.load(path)
     for v in ("1", "2", "3"):
         np.testing.assert_array_equal(res["0"].view(np.uint32), res[v].view(np.uint32))
+    off = 0
+    for shape, kind, special in _LAYOUT_CASES:
+        M, K, N = shape
+        a, b = _layout_operands(shape, kind, special)
+        want = None if special else oracle.matmul(a, b)
+        for algo in ("fp16", "bf16"):
+            for _ in range(3):
+                got = res["3"][off:off + M * N].reshape(M, N)
+                off += M * N
+                if algo == "fp16" and want is not None:
+                    assert rel_err_vs_scale(got, want, a, b) <= bound(K), (shape, kind)
+    assert off == res["3"].size
 
 
 def test_programmatic_dependent_launch_changes_no_bits(tmp_path):
