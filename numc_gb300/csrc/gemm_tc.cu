@@ -816,9 +816,14 @@ cudaError_t split_operand(const SplitLayout &L, const float *src, int64_t rs_row
   cudaError_t e = cudaSuccess;
   if (L.f16 && mode == 2 && L.Kp <= kColMaxKp && (split_pass_kernels() & 2) &&
       launch_split_cols(src, rs_k, R, K, L.Kp, planes, flags, flag_rows, maxbits, gen, s, &e)) {
-    if (e) return e;
-    count_launch(1);
-    return cudaGetLastError();
+    if (e == cudaSuccess) {
+      count_launch(1);
+      return cudaGetLastError();
+    }
+    // a cluster launch refused at run time (a launch-configuration error,
+    // which does not stick to the context): the two passes below instead
+    cudaGetLastError();
+    e = cudaSuccess;
   }
   const dim3 grid((unsigned)((L.Kp + kSplitK - 1) / kSplitK),
                   (unsigned)((R + kSplitRows - 1) / kSplitRows));
